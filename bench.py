@@ -1,0 +1,382 @@
+"""Benchmark of the hashed-container hot path on the voxel-block map workload.
+
+Workload (one GPU): stdgpu::unordered_map<uint64_t, uint32_t> with capacity 2^28;
+2^27 unique voxel-block keys (packed int3, 21 bits per axis, the surface voxels
+of a union of 64 random spheres), values = insertion index.  One step is one
+pass of the hot path on device-resident inputs:
+
+    clear -> insert(2^27 value_type pairs) -> find(2^27 keys, 70% hits) -> erase(2^25 keys)
+
+value = (inserts + finds + erases) / step time, in Mops/s, with CUDA events on
+the stream the kernels run on.  Inputs (2 GiB of pairs, 1 GiB of queries) are
+larger than L2, so no flush is needed between steps.
+
+e2e: the same step through the C ABI with host buffers: every step copies its
+inputs host->device from pinned memory and the find results device->host.
+
+--impl reference: the reference's own CPU implementation (stdgpu 1.3.0,
+OpenMP backend, built under oracle/_ref) on a bounded sample of the same
+workload with all host threads; falls back to the oracle restatement when the
+reference library is not available.
+
+Multi-GPU (torchrun, N > 1): the path is not partitioned here; each rank runs
+an independent replica of the workload ("replicas only"), and value sums the
+ranks' operations over the slowest rank's time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "insert/find Mops/s & HBM-roofline %"
+UNIT = "Mops/s"
+CAPACITY_LOG2 = 28
+KEYS_LOG2 = 27
+HIT_FRAC = 0.7
+ERASE_FRAC = 0.25
+
+# Algorithmic bytes per operation (lower bound; one 128-byte group line per op):
+#   insert: 16 B value_type pair in + 128 B home group + one 32 B sector written back (key and value share it)
+#   find:   8 B key in + 4 B value + 1 B flag out + 128 B home group (the value sits in the same line)
+#   erase:  8 B key in + 128 B home group + one 32 B sector written back (the erased marker)
+BYTES_PER_OP = {"insert": 16 + 128 + 32, "find": 8 + 5 + 128, "erase": 8 + 128 + 32}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["native", "reference"], default="native")
+    p.add_argument("--keys-log2", type=int, default=KEYS_LOG2, help="2^k keys (default: the full workload)")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, max clock, throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in Path(self.path).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        busy = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(busy) if busy else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ CPU side
+
+def cpu_sample_run(threads: int, keys_log2: int = 20, reps: int = 1):
+    """Reference (or oracle restatement) on a bounded sample of the workload: returns (Mops/s, kind, sample)."""
+    import oracle as O
+    from stdgpu_gb300 import workloads as W
+
+    n = 1 << keys_log2
+    w = W.voxel_map(n, hit_frac=HIT_FRAC, erase_frac=ERASE_FRAC, seed=0)
+    kind = "reference" if O.ref_available() else "port"
+    if kind == "reference":
+        O.ref_set_threads(threads)
+        make = lambda: O.RefTable(O.MAP_U64_U32, 2 * n)
+    else:
+        threads = 1
+        make = lambda: O.PortTable(O.MAP_U64_U32, 2 * n)
+    best = None
+    for _ in range(reps):
+        t = make()
+        t0 = time.perf_counter()
+        t.insert(w.keys, w.values)
+        t1 = time.perf_counter()
+        t.find(w.queries)
+        t2 = time.perf_counter()
+        t.erase(w.erase)
+        t3 = time.perf_counter()
+        t.close()
+        ops = len(w.keys) + len(w.queries) + len(w.erase)
+        mops = ops / (t3 - t0) / 1e6
+        if best is None or mops > best[0]:
+            best = (mops, {"insert_s": t1 - t0, "find_s": t2 - t1, "erase_s": t3 - t2})
+    sample = (f"2^{keys_log2} voxel keys into capacity 2^{keys_log2 + 1} (same 0.5 load), 2^{keys_log2} finds "
+              f"(70% hits), {len(w.erase)} erases; insert+find+erase wall time, best of {reps}")
+    return best[0], kind, threads, sample, best[1]
+
+
+def reference_arm(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    vals = []
+    detail = None
+    kind = sample = None
+    for i in range(args.warmup + args.steps):
+        mops, kind, used, sample, detail = cpu_sample_run(threads, keys_log2=18, reps=1)
+        if i >= args.warmup:
+            vals.append(mops)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+        "config": {"workload": "voxel-block unordered_map<uint64_t,uint32_t>, capacity 2^28, 2^27 keys; "
+                               "insert, find (70% hits), erase 25%", "sampled": True},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "phases_s": detail,
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ GPU side
+
+def native_arm(args):
+    import torch
+    import stdgpu_gb300 as sg
+    from stdgpu_gb300 import workloads as W
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    n = 1 << args.keys_log2
+    cap = 1 << (args.keys_log2 + 1)
+    w = W.voxel_map(n, hit_frac=HIT_FRAC, erase_frac=ERASE_FRAC, seed=0)
+    n_q, n_e = len(w.queries), len(w.erase)
+
+    # value_type array: pair<const uint64_t, uint32_t> = 16 bytes (key, value, 4 bytes padding)
+    pairs_np = np.zeros((n, 2), np.uint64)
+    pairs_np[:, 0] = w.keys
+    pairs_np[:, 1] = w.values.astype(np.uint64)
+    to_dev = lambda a: torch.from_numpy(a.view(np.int64)).to(dev)
+    pairs = to_dev(pairs_np.reshape(-1))
+    queries = to_dev(w.queries)
+    erase = to_dev(w.erase)
+    out_vals = torch.empty(n_q, dtype=torch.int32, device=dev)
+    out_found = torch.empty(n_q, dtype=torch.uint8, device=dev)
+
+    table = sg.unordered_map.createDeviceObject(cap, key="u64", mapped="u32")
+    lib = sg.load()
+    from ctypes import c_void_p
+    h = table._h
+    stream = torch.cuda.current_stream(dev)
+    sp = c_void_p(stream.cuda_stream)
+
+    def call(status, what):
+        if status != 0:
+            raise RuntimeError(f"{what} failed with status {status}")
+
+    def step(ev=None):
+        if ev is not None:
+            ev[0].record(stream)
+        call(lib.sg_unordered_clear(h, sp), "clear")
+        if ev is not None:
+            ev[1].record(stream)
+        call(lib.sg_unordered_insert(h, c_void_p(pairs.data_ptr()), n, None, sp), "insert")
+        if ev is not None:
+            ev[2].record(stream)
+        call(lib.sg_unordered_find(h, c_void_p(queries.data_ptr()), n_q, c_void_p(out_vals.data_ptr()),
+                                   c_void_p(out_found.data_ptr()), sp), "find")
+        if ev is not None:
+            ev[3].record(stream)
+        call(lib.sg_unordered_erase(h, c_void_p(erase.data_ptr()), n_e, None, sp), "erase")
+        if ev is not None:
+            ev[4].record(stream)
+
+    # correctness guard on the timed configuration (one untimed pass)
+    step()
+    torch.cuda.synchronize(dev)
+    size = table.size()
+    found = int(out_found.sum())
+    expect_found = int(w.query_hit.sum())
+    if size != n - n_e or found != expect_found:
+        raise RuntimeError(f"wrong results: size {size} (want {n - n_e}), found {found} (want {expect_found})")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize(dev)
+    if ws > 1:
+        torch.distributed.barrier()
+
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    launches0 = sg.kernel_launch_count()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(5)] for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    t_start.record(stream)
+    for k in range(args.steps):
+        step(evs[k])
+    t_end.record(stream)
+    torch.cuda.synchronize(dev)
+    launches = sg.kernel_launch_count() - launches0
+    clocks = sampler.stop()
+    total_ms = t_start.elapsed_time(t_end)
+    phase_ms = {name: [evs[k][i].elapsed_time(evs[k][i + 1]) for k in range(args.steps)]
+                for i, name in enumerate(["clear", "insert", "find", "erase"])}
+    ms_per_step = total_ms / args.steps
+    if ws > 1:
+        t = torch.tensor([ms_per_step], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_per_step = float(t.item())
+    ops_per_step = n + n_q + n_e
+    value = ops_per_step * ws / (ms_per_step * 1e-3) / 1e6
+
+    # ---------------- e2e: host buffers through the C ABI, copies inside the timed region
+    e2e = None
+    if not args.no_e2e:
+        pairs_h = torch.from_numpy(pairs_np.reshape(-1).view(np.int64)).pin_memory()
+        queries_h = torch.from_numpy(w.queries.view(np.int64)).pin_memory()
+        erase_h = torch.from_numpy(w.erase.view(np.int64)).pin_memory()
+        vals_h = torch.empty(n_q, dtype=torch.int32).pin_memory()
+        found_h = torch.empty(n_q, dtype=torch.uint8).pin_memory()
+
+        def e2e_step():
+            pairs.copy_(pairs_h, non_blocking=True)
+            queries.copy_(queries_h, non_blocking=True)
+            erase.copy_(erase_h, non_blocking=True)
+            step()
+            vals_h.copy_(out_vals, non_blocking=True)
+            found_h.copy_(out_found, non_blocking=True)
+
+        for _ in range(args.warmup):
+            e2e_step()
+        torch.cuda.synchronize(dev)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        e2e_ms = a.elapsed_time(b) / args.steps
+        if int(found_h.sum()) != expect_found:
+            raise RuntimeError("e2e results wrong")
+        h2d = pairs_h.numel() * 8 + queries_h.numel() * 8 + erase_h.numel() * 8
+        d2h = vals_h.numel() * 4 + found_h.numel()
+        e2e = {"value": ops_per_step * ws / (e2e_ms * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms}
+
+    # ---------------- roofline of the dominant kernel
+    med = {k: statistics.median(v) for k, v in phase_ms.items()}
+    counts = {"insert": n, "find": n_q, "erase": n_e}
+    dominant = max(["insert", "find", "erase"], key=lambda k: med[k])
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    alg_bytes = BYTES_PER_OP[dominant] * counts[dominant]
+    achieved = alg_bytes / (med[dominant] * 1e-3) / 1e9
+    traffic = None
+    tf = ROOT / "profiles" / "dram_traffic.json"
+    if tf.exists():
+        try:
+            traffic = json.loads(tf.read_text()).get(dominant)
+        except (ValueError, AttributeError):
+            traffic = None
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": dominant, "peak_source": peak_src,
+                "bytes_per_op": BYTES_PER_OP[dominant],
+                "per_kernel": {k: {"ms": med[k], "mops": counts[k] / (med[k] * 1e-3) / 1e6,
+                                   "gbs": BYTES_PER_OP[k] * counts[k] / (med[k] * 1e-3) / 1e9,
+                                   "frac": BYTES_PER_OP[k] * counts[k] / (med[k] * 1e-3) / 1e9 / peak}
+                               for k in counts}}
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        mops, kind, used, sample, _ = cpu_sample_run(1, keys_log2=21, reps=1)
+        cpu = {"value": mops, "unit": UNIT, "cores": used, "kind": kind, "sample": sample}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": f"voxel-block unordered_map<uint64_t,uint32_t>, capacity 2^{args.keys_log2 + 1}, "
+                                   f"2^{args.keys_log2} keys; clear+insert+find(70% hits)+erase(25%) per step",
+                       "capacity": cap, "keys": n, "finds": n_q, "erases": n_e, "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "inputs larger than L2 (no flush)"},
+            "phases_ms": med,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    sg.unordered_base.destroyDeviceObject(table)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        native_arm(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,236 @@
+/*
+ * stdgpu_gb300 -- C ABI of the GB300 (sm_103a) hashed-container path.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, `void*` for a CUDA stream
+ * (a cudaStream_t; NULL = the legacy default stream).  Every data pointer is a
+ * DEVICE pointer owned by the caller.  Calls are stream-ordered and
+ * asynchronous unless they return a host value through an out-parameter (those
+ * synchronise the given stream).  Distinct handles may be used concurrently on
+ * distinct streams; one handle must not be used from two host threads at once.
+ *
+ * Errors are returned as sg_status codes; no entry point aborts the process
+ * (the reference calls std::terminate on CUDA errors,
+ * src/stdgpu/cuda/impl/error.h:41-56).  Device-side conditions that the
+ * reference only printf()s (a refused insert into a full table, a bounded wait
+ * that ran out) are counted on the device and reported by the next call that
+ * synchronises (sg_unordered_size, sg_unordered_valid, ...).
+ *
+ * Each entry point cites the reference interface it replaces (paths relative
+ * to the stdgpu 1.3.0 source tree).
+ */
+#ifndef STDGPU_GB300_H
+#define STDGPU_GB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SG_API __attribute__((visibility("default")))
+#else
+#define SG_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum sg_status
+{
+    SG_OK = 0,
+    SG_ERR_FULL = 1,             /* inserts were refused because the table / container was full */
+    SG_ERR_BAD_ARG = 2,          /* null handle, negative size, unknown kind, size above a limit */
+    SG_ERR_OOM = 3,              /* device allocation failed */
+    SG_ERR_BUDGET = 4,           /* refused by an HBM budget (serving / batched entry points) */
+    SG_ERR_RETRY_EXHAUSTED = 5,  /* a bounded device wait or retry loop gave up */
+    SG_ERR_CUDA = 6,             /* a CUDA runtime call failed */
+    SG_ERR_NO_DEVICE = 7         /* no usable sm_103 device */
+} sg_status;
+
+/* Container kinds: key type and mapped type of unordered_set<Key> / unordered_map<Key,T>.
+ * The element layout in device memory is that of the reference's value_type:
+ * Key for sets, stdgpu::pair<const Key, T> for maps (src/stdgpu/unordered_map.cuh:80,
+ * src/stdgpu/unordered_set.cuh:69), i.e. key at offset 0 and T at its natural alignment. */
+typedef enum sg_kind
+{
+    SG_SET_U32 = 0,     /* unordered_set<uint32_t>            element  4 B */
+    SG_SET_U64 = 1,     /* unordered_set<uint64_t>            element  8 B */
+    SG_MAP_U64_U32 = 2, /* unordered_map<uint64_t, uint32_t>  element 16 B */
+    SG_MAP_U64_U64 = 3, /* unordered_map<uint64_t, uint64_t>  element 16 B */
+    SG_MAP_U32_U32 = 4, /* unordered_map<uint32_t, uint32_t>  element  8 B */
+    SG_MAP_U32_U64 = 5  /* unordered_map<uint32_t, uint64_t>  element 16 B */
+} sg_kind;
+
+typedef struct sg_unordered sg_unordered;
+
+/* Geometry of a table.  bucket_count / excess_count / max_size follow the reference's
+ * createDeviceObject (src/stdgpu/impl/unordered_base_detail.cuh:1264-1273); the rest
+ * describes this implementation's storage. */
+typedef struct sg_geometry
+{
+    int64_t capacity;        /* as passed to create */
+    int64_t bucket_count;    /* bucket_count()   unordered_base_detail.cuh:1141-1146 */
+    int64_t excess_count;    /* expected_collisions(bucket_count, capacity) + 1 */
+    int64_t max_size;        /* max_size() = total_count = bucket_count + excess_count */
+    int64_t num_groups;      /* 128-byte probe groups */
+    int32_t slot_bytes;      /* sizeof(value_type) */
+    int32_t slots_per_group; /* 128 / slot_bytes */
+    int64_t storage_bytes;   /* device bytes held by the table */
+} sg_geometry;
+
+/* Device view of a table for native device calls (include/stdgpu_gb300/device.cuh).
+ * Plain data; copy it by value into kernels. */
+typedef struct sg_unordered_view
+{
+    void* slots;             /* (num_groups + 1) * 128 bytes; the last group holds the two out-of-band keys */
+    void* header;            /* device counters */
+    int64_t num_groups;
+    int64_t total_count;     /* max_size(); slots at or above this index are never used */
+    int64_t bucket_count;
+    int32_t bucket_bits;     /* log2(bucket_count) */
+    int32_t kind;
+} sg_unordered_view;
+
+/* ---------------- unordered_set / unordered_map ---------------- */
+
+/* createDeviceObject(capacity): src/stdgpu/impl/unordered_base_detail.cuh:1254-1308,
+ * src/stdgpu/impl/unordered_map_detail.cuh:397-419.  capacity > 0 and max_size() < 2^31
+ * (the reference's 32-bit index_t, src/stdgpu/cstddef.h:42-59). */
+SG_API sg_status sg_unordered_create(int32_t kind, int64_t capacity, void* stream, sg_unordered** out);
+
+/* destroyDeviceObject: src/stdgpu/impl/unordered_base_detail.cuh:1310-1348 */
+SG_API sg_status sg_unordered_destroy(sg_unordered* table);
+
+/* insert(begin, end) with begin pointing at value_type elements:
+ * src/stdgpu/impl/unordered_base_detail.cuh:996-1017 (per element :967-994).
+ * out_inserted (nullable): per element 1 if this element was inserted, else 0. */
+SG_API sg_status sg_unordered_insert(sg_unordered* table, const void* values, int64_t n, uint8_t* out_inserted,
+                              void* stream);
+
+/* Same as sg_unordered_insert with keys and mapped values in two arrays (mapped ignored for sets). */
+SG_API sg_status sg_unordered_insert_kv(sg_unordered* table, const void* keys, const void* mapped, int64_t n,
+                                 uint8_t* out_inserted, void* stream);
+
+/* erase(begin, end) over keys: src/stdgpu/impl/unordered_base_detail.cuh:1045-1066 (per key :1019-1043).
+ * out_erased (nullable): per key 1 if this call erased it, else 0. */
+SG_API sg_status sg_unordered_erase(sg_unordered* table, const void* keys, int64_t n, uint8_t* out_erased, void* stream);
+
+/* Bulk form of the device-only find(key): src/stdgpu/impl/unordered_base_detail.cuh:619-682.
+ * out_mapped (nullable; maps only): the mapped value of each found key (untouched when absent).
+ * out_found (nullable): 1 when the key is present. */
+SG_API sg_status sg_unordered_find(sg_unordered* table, const void* keys, int64_t n, void* out_mapped, uint8_t* out_found,
+                            void* stream);
+
+/* Bulk form of the device-only contains(key) / count(key): unordered_base_detail.cuh:595-617, 684-706. */
+SG_API sg_status sg_unordered_contains(sg_unordered* table, const void* keys, int64_t n, uint8_t* out_flags, void* stream);
+
+/* size(): src/stdgpu/impl/unordered_base_detail.cuh:1121-1132 (synchronises the stream). */
+SG_API sg_status sg_unordered_size(sg_unordered* table, void* stream, int64_t* out_size);
+
+/* Device-side conditions the reference only printf()s (unordered_base_detail.cuh:769-772): the number of
+ * inserts refused for lack of a free slot since the last call (then reset) and the number of erased slots
+ * awaiting reuse.  Returns SG_ERR_FULL when refusals were counted.  Synchronises.  Outputs nullable. */
+SG_API sg_status sg_unordered_status(sg_unordered* table, void* stream, int64_t* out_refused, int64_t* out_tombstones);
+
+/* clear(): src/stdgpu/impl/unordered_base_detail.cuh:1220-1252 */
+SG_API sg_status sg_unordered_clear(sg_unordered* table, void* stream);
+
+/* valid(): src/stdgpu/impl/unordered_base_detail.cuh:1192-1218 -- the same invariants restated for
+ * this layout: every stored key is found at its own slot by its probe sequence (reachable, unique),
+ * unused tail slots are untouched, and size() equals the number of stored keys. */
+SG_API sg_status sg_unordered_valid(sg_unordered* table, void* stream, int32_t* out_valid);
+
+/* device_range(): src/stdgpu/impl/unordered_base_detail.cuh:160-208.  Writes the slot indices of all
+ * stored elements to out_slots (capacity >= max_size() + 2 entries) and their count to *out_n
+ * (synchronises).  Element i of the range is ((value_type*)view.slots)[out_slots[i]]. */
+SG_API sg_status sg_unordered_device_range(sg_unordered* table, int32_t* out_slots, void* stream, int64_t* out_n);
+
+/* Copy all stored keys (and mapped values for maps; nullable) out, in slot order.  *out_n gets the count. */
+SG_API sg_status sg_unordered_range_copy(sg_unordered* table, void* out_keys, void* out_mapped, void* stream,
+                                  int64_t* out_n);
+
+/* bucket(key) (host-callable): src/stdgpu/impl/unordered_base_detail.cuh:547-564 -- fibonacci hashing of the
+ * identity hash (src/stdgpu/impl/functional_detail.h:60-80).  key points to one key of the table's key type. */
+SG_API sg_status sg_unordered_bucket(const sg_unordered* table, const void* key, int64_t* out_bucket);
+
+/* bucket_count(), max_size(), max_load_factor() plus storage facts. */
+SG_API sg_status sg_unordered_geometry(const sg_unordered* table, sg_geometry* out);
+
+/* Device view for native device-side find / contains / insert / emplace / erase. */
+SG_API sg_status sg_unordered_view_of(const sg_unordered* table, sg_unordered_view* out);
+
+/* Geometry of createDeviceObject(capacity) without creating a table. */
+SG_API sg_status sg_unordered_geometry_for(int32_t kind, int64_t capacity, sg_geometry* out);
+
+/* ---------------- vector<T> (T = 4 or 8 bytes) ---------------- */
+
+typedef struct sg_vector sg_vector;
+
+typedef struct sg_vector_view
+{
+    void* data;
+    void* size; /* device int64 counter; may exceed capacity transiently, size() clamps (vector_detail.cuh:484-511) */
+    int64_t capacity;
+    int32_t elem_bytes;
+    int32_t pad;
+} sg_vector_view;
+
+/* vector::createDeviceObject(capacity): src/stdgpu/impl/vector_detail.cuh (createDeviceObject) */
+SG_API sg_status sg_vector_create(int32_t elem_bytes, int64_t capacity, sg_vector** out);
+SG_API sg_status sg_vector_destroy(sg_vector* vec);
+/* Bulk form of the device push_back (src/stdgpu/impl/vector_detail.cuh:181-238): element i is pushed when
+ * pred == NULL or pred[i] != 0.  out_pushed (nullable) gets 1 for each element that was stored. */
+SG_API sg_status sg_vector_push_back(sg_vector* vec, const void* values, const uint8_t* pred, int64_t n,
+                              uint8_t* out_pushed, void* stream);
+/* size() (clamped to [0, capacity]): src/stdgpu/impl/vector_detail.cuh:484-511 */
+SG_API sg_status sg_vector_size(sg_vector* vec, void* stream, int64_t* out_size);
+/* clear() */
+SG_API sg_status sg_vector_clear(sg_vector* vec, void* stream);
+SG_API sg_status sg_vector_view_of(const sg_vector* vec, sg_vector_view* out);
+
+/* ---------------- deque<T> (T = 4 or 8 bytes), push_back / pop_front ---------------- */
+
+typedef struct sg_deque sg_deque;
+
+typedef struct sg_deque_view
+{
+    void* data;
+    void* seq;      /* per-slot turn counter of the ring (uint32) */
+    void* counters; /* device {size, begin, end, error} */
+    int64_t capacity;
+    int32_t elem_bytes;
+    int32_t pad;
+} sg_deque_view;
+
+/* deque::createDeviceObject(capacity): src/stdgpu/impl/deque_detail.cuh (createDeviceObject) */
+SG_API sg_status sg_deque_create(int32_t elem_bytes, int64_t capacity, sg_deque** out);
+SG_API sg_status sg_deque_destroy(sg_deque* dq);
+/* Mixed launch: element i does push_back(values[i]) when is_push[i] != 0, else pop_front().
+ * deque_detail.cuh:202-258 (push_back) and :388-446 (pop_front).  out_popped / out_ok nullable.
+ * is_push == NULL means all push_back. */
+SG_API sg_status sg_deque_ops(sg_deque* dq, const uint8_t* is_push, const void* values, int64_t n, void* out_popped,
+                       uint8_t* out_ok, void* stream);
+/* size() (clamped): src/stdgpu/impl/deque_detail.cuh:486-520; SG_ERR_RETRY_EXHAUSTED if a wait gave up */
+SG_API sg_status sg_deque_size(sg_deque* dq, void* stream, int64_t* out_size);
+/* Copy the stored elements front to back to out (device) and return their count (synchronises). */
+SG_API sg_status sg_deque_copy_out(sg_deque* dq, void* out, void* stream, int64_t* out_n);
+SG_API sg_status sg_deque_clear(sg_deque* dq, void* stream);
+SG_API sg_status sg_deque_view_of(const sg_deque* dq, sg_deque_view* out);
+
+/* ---------------- bitset<unsigned int>::count ---------------- */
+
+/* bitset::count(): src/stdgpu/impl/bitset_detail.cuh:388-404 with count_block_bits :130-160.
+ * blocks: ceil(nbits / 32) 32-bit blocks, bit i = bit (i % 32) of blocks[i / 32]; bits at or above
+ * nbits in the last block are masked off.  Synchronises and returns the count. */
+SG_API sg_status sg_bitset_count(const uint32_t* blocks, int64_t nbits, void* stream, int64_t* out_count);
+
+/* ---------------- library ---------------- */
+
+/* Number of kernels this library has launched since load (all entry points). */
+SG_API int64_t sg_kernel_launch_count(void);
+/* Human-readable text for a status. */
+SG_API const char* sg_status_string(sg_status status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STDGPU_GB300_H */

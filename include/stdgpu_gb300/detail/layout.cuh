@@ -1,0 +1,225 @@
+// Storage layout of the GB300 hash table, shared by the library kernels and by the
+// native device API (include/stdgpu_gb300/device.cuh).
+//
+// Slots hold the reference's value_type byte for byte (Key for sets,
+// stdgpu::pair<const Key, T> for maps; src/stdgpu/unordered_map.cuh:80,
+// src/stdgpu/unordered_set.cuh:69), packed into 128-byte probe groups:
+// 32 slots of 4 B, 16 of 8 B or 8 of 16 B.  A key's home group comes from the
+// reference's own bucket(key) (fibonacci hashing of the identity hash,
+// src/stdgpu/impl/unordered_base_detail.cuh:56-85, :547-564) scaled from
+// bucket_count buckets onto num_groups groups, so keys that share a reference
+// bucket share a home group.  Probing is linear over whole groups.
+//
+// The key word of a slot carries its state: all-ones = never used (EMPTY),
+// all-ones minus one = erased (TOMB), anything else = a stored key.  Keys equal
+// to those two values are stored out of band in the two slots of the extra
+// group after the last probe group, with their presence in the device header,
+// so every key value of the type is accepted, as in the reference.
+//
+// Slots at index >= total_count (the reference's max_size()) in the last probe
+// group are set to TOMB at creation and never claimed, so a table holds at most
+// max_size() probed keys, as the reference does.
+#ifndef STDGPU_GB300_DETAIL_LAYOUT_CUH
+#define STDGPU_GB300_DETAIL_LAYOUT_CUH
+
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define SG_HD __host__ __device__ __forceinline__
+#define SG_D __device__ __forceinline__
+#else
+#define SG_HD inline
+#define SG_D inline
+#endif
+
+namespace sg
+{
+namespace detail
+{
+
+constexpr int kGroupBytes = 128;
+constexpr int kTileLanes = 8; // lanes cooperating on one probe group, 16 B each
+
+// Device-resident counters of one table.
+struct table_header
+{
+    unsigned long long size;       // stored elements, out-of-band keys included
+    unsigned long long refused;    // inserts refused because no slot was free (reported, then reset)
+    unsigned long long tombstones; // erased slots not yet reused
+    unsigned int special_state[2]; // out-of-band keys EMPTY-valued [0] / TOMB-valued [1]: 0 absent, 1 present, 2 writing
+    unsigned int error;            // sticky error bits (kErr*)
+    unsigned int pad0;
+    unsigned long long count;      // per-call scratch counter (valid / range)
+    unsigned long long pad1[2];
+};
+
+constexpr unsigned int kErrRetry = 1u;      // a CAS retry loop gave up
+constexpr unsigned int kErrIndex = 2u;      // an index outside the table was computed (never expected)
+
+// Kind traits: Key, mapped type and where they sit in a slot.
+template <int KIND>
+struct kind_traits;
+
+struct no_value
+{
+};
+
+template <>
+struct kind_traits<0> // unordered_set<uint32_t>
+{
+    using key_type = uint32_t;
+    using mapped_type = uint32_t; // unused
+    static constexpr bool is_map = false;
+    static constexpr int slot_bytes = 4;
+    static constexpr int val_offset = 0;
+};
+template <>
+struct kind_traits<1> // unordered_set<uint64_t>
+{
+    using key_type = uint64_t;
+    using mapped_type = uint64_t; // unused
+    static constexpr bool is_map = false;
+    static constexpr int slot_bytes = 8;
+    static constexpr int val_offset = 0;
+};
+template <>
+struct kind_traits<2> // unordered_map<uint64_t, uint32_t>
+{
+    using key_type = uint64_t;
+    using mapped_type = uint32_t;
+    static constexpr bool is_map = true;
+    static constexpr int slot_bytes = 16;
+    static constexpr int val_offset = 8;
+};
+template <>
+struct kind_traits<3> // unordered_map<uint64_t, uint64_t>
+{
+    using key_type = uint64_t;
+    using mapped_type = uint64_t;
+    static constexpr bool is_map = true;
+    static constexpr int slot_bytes = 16;
+    static constexpr int val_offset = 8;
+};
+template <>
+struct kind_traits<4> // unordered_map<uint32_t, uint32_t>
+{
+    using key_type = uint32_t;
+    using mapped_type = uint32_t;
+    static constexpr bool is_map = true;
+    static constexpr int slot_bytes = 8;
+    static constexpr int val_offset = 4;
+};
+template <>
+struct kind_traits<5> // unordered_map<uint32_t, uint64_t>
+{
+    using key_type = uint32_t;
+    using mapped_type = uint64_t;
+    static constexpr bool is_map = true;
+    static constexpr int slot_bytes = 16;
+    static constexpr int val_offset = 8;
+};
+
+template <int KIND>
+struct kind_consts
+{
+    using K = typename kind_traits<KIND>::key_type;
+    using V = typename kind_traits<KIND>::mapped_type;
+    static constexpr int slot_bytes = kind_traits<KIND>::slot_bytes;
+    static constexpr int slots_per_group = kGroupBytes / slot_bytes;
+    static constexpr int slots_per_lane = 16 / slot_bytes; // slots in one lane's 16-byte share of a group
+    static constexpr K empty_key = static_cast<K>(~static_cast<K>(0));
+    static constexpr K tomb_key = static_cast<K>(~static_cast<K>(0) - 1);
+};
+
+SG_HD int slot_bytes_of_kind(int kind)
+{
+    return kind == 0 ? 4 : (kind == 1 || kind == 4) ? 8 : 16;
+}
+
+// fibonacci_hashing(hash, 2^bits): src/stdgpu/impl/unordered_base_detail.cuh:56-85
+SG_HD uint64_t fibonacci_bucket(uint64_t hash, int bits)
+{
+    if (bits <= 0)
+    {
+        return 0;
+    }
+    const unsigned drop = 64u - static_cast<unsigned>(bits);
+    const uint64_t improved = hash ^ (hash >> drop);
+    return (improved * 11400714819323198485ull) >> drop;
+}
+
+// Home probe group of a reference bucket.
+SG_HD int64_t group_of_bucket(uint64_t bucket, int bits, int64_t num_groups)
+{
+    return static_cast<int64_t>((bucket * static_cast<uint64_t>(num_groups)) >> bits);
+}
+
+SG_HD int64_t next_group(int64_t g, int64_t num_groups)
+{
+    return (g + 1 == num_groups) ? 0 : g + 1;
+}
+
+// Extract sub-slot s (0 .. slots_per_lane-1) of a lane's 16-byte share.
+template <int KIND>
+SG_HD typename kind_consts<KIND>::K key_in_lane(const uint4& d, int s)
+{
+    using K = typename kind_consts<KIND>::K;
+    constexpr int sb = kind_consts<KIND>::slot_bytes;
+    if constexpr (sb == 4)
+    {
+        return static_cast<K>(s == 0 ? d.x : s == 1 ? d.y : s == 2 ? d.z : d.w);
+    }
+    else if constexpr (sb == 8)
+    {
+        if constexpr (sizeof(K) == 8)
+        {
+            return s == 0 ? (static_cast<uint64_t>(d.y) << 32 | d.x) : (static_cast<uint64_t>(d.w) << 32 | d.z);
+        }
+        else
+        {
+            return static_cast<K>(s == 0 ? d.x : d.z);
+        }
+    }
+    else
+    {
+        if constexpr (sizeof(K) == 8)
+        {
+            return static_cast<uint64_t>(d.y) << 32 | d.x;
+        }
+        else
+        {
+            return static_cast<K>(d.x);
+        }
+    }
+}
+
+template <int KIND>
+SG_HD typename kind_consts<KIND>::V value_in_lane(const uint4& d, int s)
+{
+    using V = typename kind_consts<KIND>::V;
+    constexpr int sb = kind_consts<KIND>::slot_bytes;
+    if constexpr (!kind_traits<KIND>::is_map)
+    {
+        return V{};
+    }
+    else if constexpr (sb == 8) // pair<u32,u32>
+    {
+        return static_cast<V>(s == 0 ? d.y : d.w);
+    }
+    else // 16-byte pair, value at offset 8
+    {
+        if constexpr (sizeof(V) == 8)
+        {
+            return static_cast<uint64_t>(d.w) << 32 | d.z;
+        }
+        else
+        {
+            return static_cast<V>(d.z);
+        }
+    }
+}
+
+} // namespace detail
+} // namespace sg
+
+#endif

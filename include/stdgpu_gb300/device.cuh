@@ -1,0 +1,299 @@
+// Native device-side calls on a table, for use inside a caller's own kernels
+// (the reference's device member functions find / contains / count / insert /
+// emplace / erase, src/stdgpu/impl/unordered_base_detail.cuh:619-706, 958-994,
+// 1019-1043).  One calling thread per key; each call reads whole 128-byte probe
+// groups with 16-byte loads through L2.
+//
+// Concurrency within one launch:
+//  * insert / emplace claim only never-used slots (compare-and-swap on the key
+//    word), so inserts may run concurrently with each other and with erase:
+//    a key is stored at most once and exactly one of several concurrent inserts
+//    of the same key reports success.  Erased slots are reclaimed by the bulk
+//    insert entry point (sg_unordered_insert), which runs alone on a table.
+//  * erase marks the slot erased (compare-and-swap key -> erased marker);
+//    exactly one of several concurrent erases of a key reports success.
+//  * find run concurrently with an insert of the same key may see the key
+//    before its mapped value is stored; the reference orders the two with its
+//    per-slot lock.  Separate finds from inserts of the same keys by a launch
+//    boundary when the mapped value matters.
+#ifndef STDGPU_GB300_DEVICE_CUH
+#define STDGPU_GB300_DEVICE_CUH
+
+#include <stdint.h>
+
+#include "../stdgpu_gb300.h"
+#include "detail/layout.cuh"
+
+namespace sg
+{
+
+template <int KIND>
+struct unordered_ref
+{
+    using C = detail::kind_consts<KIND>;
+    using key_type = typename C::K;
+    using mapped_type = typename C::V;
+    static constexpr int G = C::slots_per_group;
+    static constexpr int SPL = C::slots_per_lane;
+
+    sg_unordered_view v;
+
+    __device__ __forceinline__ detail::table_header*
+    header() const
+    {
+        return static_cast<detail::table_header*>(v.header);
+    }
+
+    __device__ __forceinline__ char*
+    slot_ptr(int64_t slot) const
+    {
+        return static_cast<char*>(v.slots) + slot * C::slot_bytes;
+    }
+
+    __device__ __forceinline__ const uint4*
+    group_ptr(int64_t g) const
+    {
+        return reinterpret_cast<const uint4*>(static_cast<const char*>(v.slots) + g * detail::kGroupBytes);
+    }
+
+    // bucket(key): the reference's fibonacci hashing of the identity hash
+    __device__ __forceinline__ int64_t
+    bucket(key_type key) const
+    {
+        return static_cast<int64_t>(detail::fibonacci_bucket(static_cast<uint64_t>(key), v.bucket_bits));
+    }
+
+    __device__ __forceinline__ int64_t
+    home_group(key_type key) const
+    {
+        return detail::group_of_bucket(detail::fibonacci_bucket(static_cast<uint64_t>(key), v.bucket_bits),
+                                       v.bucket_bits,
+                                       v.num_groups);
+    }
+
+    __device__ __forceinline__ static bool
+    is_special(key_type key)
+    {
+        return key >= C::tomb_key;
+    }
+
+    __device__ __forceinline__ int64_t
+    special_slot(key_type key) const
+    {
+        return v.num_groups * G + (key == C::empty_key ? 0 : 1);
+    }
+
+    // Slot index of key, or -1.  Stops at the first group holding a never-used slot.
+    __device__ int64_t
+    find_slot(key_type key) const
+    {
+        if (is_special(key))
+        {
+            const int s = key == C::empty_key ? 0 : 1;
+            unsigned st = *reinterpret_cast<volatile unsigned*>(&header()->special_state[s]);
+            return st == 1u ? special_slot(key) : -1;
+        }
+        int64_t g = home_group(key);
+        for (int64_t probes = 0; probes < v.num_groups; ++probes)
+        {
+            const uint4* p = group_ptr(g);
+            bool any_empty = false;
+#pragma unroll
+            for (int l = 0; l < detail::kTileLanes; ++l)
+            {
+                const uint4 d = __ldcg(p + l);
+#pragma unroll
+                for (int s = 0; s < SPL; ++s)
+                {
+                    const key_type k = detail::key_in_lane<KIND>(d, s);
+                    if (k == key)
+                    {
+                        return g * G + l * SPL + s;
+                    }
+                    any_empty |= (k == C::empty_key);
+                }
+            }
+            if (any_empty)
+            {
+                return -1;
+            }
+            g = detail::next_group(g, v.num_groups);
+        }
+        return -1;
+    }
+
+    __device__ __forceinline__ bool
+    contains(key_type key) const
+    {
+        return find_slot(key) >= 0;
+    }
+
+    __device__ __forceinline__ int64_t
+    count(key_type key) const
+    {
+        return contains(key) ? 1 : 0;
+    }
+
+    // find(key): true and *out = mapped value when present (maps); sets ignore out.
+    __device__ bool
+    find(key_type key, mapped_type* out) const
+    {
+        const int64_t s = find_slot(key);
+        if (s < 0)
+        {
+            return false;
+        }
+        if constexpr (detail::kind_traits<KIND>::is_map)
+        {
+            if (out != nullptr)
+            {
+                *out = __ldcg(reinterpret_cast<const mapped_type*>(slot_ptr(s) + detail::kind_traits<KIND>::val_offset));
+            }
+        }
+        return true;
+    }
+
+    // insert(value) / emplace(key, mapped): true when this call stored the key.
+    __device__ bool
+    insert(key_type key, mapped_type mapped = mapped_type{}) const
+    {
+        if (is_special(key))
+        {
+            const int s = key == C::empty_key ? 0 : 1;
+            if (atomicCAS(&header()->special_state[s], 0u, 2u) != 0u)
+            {
+                return false;
+            }
+            store_slot(special_slot(key), key, mapped);
+            __threadfence();
+            atomicExch(&header()->special_state[s], 1u);
+            atomicAdd(&header()->size, 1ull);
+            return true;
+        }
+        int64_t g = home_group(key);
+        int64_t steps = 0;
+        const int64_t limit = v.num_groups + 4096;
+        while (steps++ < limit)
+        {
+            const uint4* p = group_ptr(g);
+            int64_t target = -1;
+#pragma unroll
+            for (int l = 0; l < detail::kTileLanes; ++l)
+            {
+                const uint4 d = __ldcg(p + l);
+#pragma unroll
+                for (int s = 0; s < SPL; ++s)
+                {
+                    const key_type k = detail::key_in_lane<KIND>(d, s);
+                    if (k == key)
+                    {
+                        return false;
+                    }
+                    if (target < 0 && k == C::empty_key)
+                    {
+                        target = g * G + l * SPL + s;
+                    }
+                }
+            }
+            if (target < 0)
+            {
+                g = detail::next_group(g, v.num_groups);
+                if (steps > v.num_groups)
+                {
+                    break;
+                }
+                continue;
+            }
+            const key_type old = cas_key(target, C::empty_key, key);
+            if (old == C::empty_key)
+            {
+                if constexpr (detail::kind_traits<KIND>::is_map)
+                {
+                    *reinterpret_cast<volatile mapped_type*>(slot_ptr(target) + detail::kind_traits<KIND>::val_offset) =
+                            mapped;
+                }
+                atomicAdd(&header()->size, 1ull);
+                return true;
+            }
+            if (old == key)
+            {
+                return false;
+            }
+            // lost the slot to another key: rescan the same group
+        }
+        atomicAdd(&header()->refused, 1ull);
+        return false;
+    }
+
+    __device__ __forceinline__ bool
+    emplace(key_type key, mapped_type mapped = mapped_type{}) const
+    {
+        return insert(key, mapped);
+    }
+
+    // erase(key): 1 when this call removed the key, else 0.
+    __device__ int64_t
+    erase(key_type key) const
+    {
+        if (is_special(key))
+        {
+            const int s = key == C::empty_key ? 0 : 1;
+            if (atomicCAS(&header()->special_state[s], 1u, 0u) == 1u)
+            {
+                atomicAdd(&header()->size, ~0ull);
+                return 1;
+            }
+            return 0;
+        }
+        const int64_t slot = find_slot(key);
+        if (slot < 0)
+        {
+            return 0;
+        }
+        if (cas_key(slot, key, C::tomb_key) == key)
+        {
+            atomicAdd(&header()->size, ~0ull);
+            atomicAdd(&header()->tombstones, 1ull);
+            return 1;
+        }
+        return 0;
+    }
+
+    __device__ __forceinline__ key_type
+    cas_key(int64_t slot, key_type expected, key_type desired) const
+    {
+        if constexpr (sizeof(key_type) == 8)
+        {
+            return static_cast<key_type>(atomicCAS(reinterpret_cast<unsigned long long*>(slot_ptr(slot)),
+                                                   static_cast<unsigned long long>(expected),
+                                                   static_cast<unsigned long long>(desired)));
+        }
+        else
+        {
+            return static_cast<key_type>(atomicCAS(reinterpret_cast<unsigned int*>(slot_ptr(slot)),
+                                                   static_cast<unsigned int>(expected),
+                                                   static_cast<unsigned int>(desired)));
+        }
+    }
+
+    __device__ __forceinline__ void
+    store_slot(int64_t slot, key_type key, mapped_type mapped) const
+    {
+        *reinterpret_cast<volatile key_type*>(slot_ptr(slot)) = key;
+        if constexpr (detail::kind_traits<KIND>::is_map)
+        {
+            *reinterpret_cast<volatile mapped_type*>(slot_ptr(slot) + detail::kind_traits<KIND>::val_offset) = mapped;
+        }
+    }
+};
+
+using unordered_set_u32_ref = unordered_ref<SG_SET_U32>;
+using unordered_set_u64_ref = unordered_ref<SG_SET_U64>;
+using unordered_map_u64_u32_ref = unordered_ref<SG_MAP_U64_U32>;
+using unordered_map_u64_u64_ref = unordered_ref<SG_MAP_U64_U64>;
+using unordered_map_u32_u32_ref = unordered_ref<SG_MAP_U32_U32>;
+using unordered_map_u32_u64_ref = unordered_ref<SG_MAP_U32_U64>;
+
+} // namespace sg
+
+#endif

@@ -1,0 +1,349 @@
+"""Oracle -- test infrastructure only (the checker, never the thing measured or shipped).
+
+Two CPU implementations with one interface:
+
+* ``PortTable`` / ``port_*``: the plain-C restatement in ``oracle/port.c``.
+* ``RefTable`` / ``ref_*``: the reference library itself (stdgpu 1.3.0, OpenMP
+  backend) through ``oracle/ref_driver.cpp``; available where
+  ``oracle/build_oracle.py`` could build ``oracle/_ref/libsgref.so``.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py`` (its CPU-baseline
+leg and its reference arm) may import this package.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, byref, c_int, c_int64, c_uint8, c_void_p
+from pathlib import Path
+
+import numpy as np
+
+from . import build_oracle
+
+HERE = Path(__file__).resolve().parent
+
+# container kinds, numbered as in include/stdgpu_gb300.h
+SET_U32, SET_U64, MAP_U64_U32, MAP_U64_U64, MAP_U32_U32, MAP_U32_U64 = range(6)
+KEY_DTYPE = {SET_U32: np.uint32, SET_U64: np.uint64, MAP_U64_U32: np.uint64, MAP_U64_U64: np.uint64,
+             MAP_U32_U32: np.uint32, MAP_U32_U64: np.uint32}
+VAL_DTYPE = {SET_U32: None, SET_U64: None, MAP_U64_U32: np.uint32, MAP_U64_U64: np.uint64,
+             MAP_U32_U32: np.uint32, MAP_U32_U64: np.uint64}
+
+_port = None
+_ref = None
+
+
+def _p(a: np.ndarray | None) -> c_void_p:
+    return c_void_p(0) if a is None else c_void_p(a.ctypes.data)
+
+
+def port_lib() -> ctypes.CDLL:
+    global _port
+    if _port is None:
+        _port = ctypes.CDLL(str(build_oracle.build_port()))
+        L = _port
+        L.port_create.restype = c_void_p
+        L.port_create.argtypes = [c_int64]
+        L.port_destroy.argtypes = [c_void_p]
+        for f in ("port_size", "port_bucket_count", "port_max_size", "port_range", "port_bucket",
+                  "port_bucket_size", "port_fibonacci_hashing", "port_expected_collisions",
+                  "port_vector_push_back", "port_deque_ops", "port_bitset_count"):
+            getattr(L, f).restype = c_int64
+        L.port_size.argtypes = [c_void_p]
+        L.port_bucket_count.argtypes = [c_void_p]
+        L.port_max_size.argtypes = [c_void_p]
+        L.port_bucket.argtypes = [c_void_p, ctypes.c_uint64]
+        L.port_bucket_size.argtypes = [c_void_p, c_int64]
+        L.port_fibonacci_hashing.argtypes = [ctypes.c_uint64, c_int64]
+        L.port_expected_collisions.argtypes = [c_int64, c_int64]
+        L.port_geometry.argtypes = [c_int64, POINTER(c_int64), POINTER(c_int64), POINTER(c_int64)]
+        L.port_insert_bulk.argtypes = [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]
+        L.port_erase_bulk.argtypes = [c_void_p, c_void_p, c_int64, c_void_p]
+        L.port_find_bulk.argtypes = [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]
+        L.port_clear.argtypes = [c_void_p]
+        L.port_valid.argtypes = [c_void_p]
+        L.port_range.argtypes = [c_void_p, c_void_p, c_void_p]
+        L.port_vector_push_back.argtypes = [c_int64, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]
+        L.port_deque_ops.argtypes = [c_int64, c_void_p, c_int64, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
+                                     c_void_p]
+        L.port_bitset_count.argtypes = [c_void_p, c_int64]
+    return _port
+
+
+def ref_available() -> bool:
+    try:
+        ref_lib()
+        return True
+    except (OSError, RuntimeError):
+        return False
+
+
+def ref_lib() -> ctypes.CDLL:
+    global _ref
+    if _ref is None:
+        so = build_oracle.build_reference()
+        if so is None:
+            raise RuntimeError("reference library not available (no staged reference tree)")
+        L = ctypes.CDLL(str(so))
+        L.sgref_create.restype = c_void_p
+        L.sgref_create.argtypes = [c_int, c_int64]
+        L.sgref_destroy.argtypes = [c_void_p]
+        L.sgref_insert.argtypes = [c_void_p, c_void_p, c_void_p, c_int64]
+        L.sgref_insert_flags.argtypes = [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]
+        L.sgref_erase.argtypes = [c_void_p, c_void_p, c_int64]
+        L.sgref_erase_flags.argtypes = [c_void_p, c_void_p, c_int64, c_void_p]
+        L.sgref_find.argtypes = [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]
+        L.sgref_contains.argtypes = [c_void_p, c_void_p, c_int64, c_void_p]
+        L.sgref_size.restype = c_int64
+        L.sgref_size.argtypes = [c_void_p]
+        L.sgref_valid.argtypes = [c_void_p]
+        L.sgref_clear.argtypes = [c_void_p]
+        L.sgref_range.restype = c_int64
+        L.sgref_range.argtypes = [c_void_p, c_void_p, c_void_p]
+        L.sgref_bucket.restype = c_int64
+        L.sgref_bucket.argtypes = [c_void_p, c_void_p]
+        L.sgref_geometry.argtypes = [c_void_p, POINTER(c_int64), POINTER(c_int64)]
+        L.sgref_set_threads.argtypes = [c_int]
+        L.sgref_vector_push_back.restype = c_int64
+        L.sgref_vector_push_back.argtypes = [c_int64, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]
+        L.sgref_deque_ops.restype = c_int64
+        L.sgref_deque_ops.argtypes = [c_int64, c_void_p, c_int64, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
+                                      c_void_p]
+        L.sgref_bitset_count.restype = c_int64
+        L.sgref_bitset_count.argtypes = [c_void_p, c_int64]
+        _ref = L
+    return _ref
+
+
+def ref_set_threads(n: int) -> None:
+    ref_lib().sgref_set_threads(int(n))
+
+
+def ref_max_threads() -> int:
+    return int(ref_lib().sgref_max_threads())
+
+
+class _TableBase:
+    """Common numpy-facing surface of the two oracles."""
+
+    kind: int
+
+    def _keys(self, keys) -> np.ndarray:
+        return np.ascontiguousarray(keys, dtype=KEY_DTYPE[self.kind])
+
+    def _vals(self, vals, n) -> np.ndarray | None:
+        vd = VAL_DTYPE[self.kind]
+        if vd is None:
+            return None
+        if vals is None:
+            return np.zeros(n, dtype=vd)
+        return np.ascontiguousarray(vals, dtype=vd)
+
+
+class PortTable(_TableBase):
+    """unordered_set / unordered_map restated in C (oracle/port.c); keys and values carried as uint64."""
+
+    def __init__(self, kind: int, capacity: int):
+        self.kind = kind
+        self.L = port_lib()
+        self.h = c_void_p(self.L.port_create(int(capacity)))
+
+    def close(self):
+        if self.h:
+            self.L.port_destroy(self.h)
+            self.h = c_void_p(0)
+
+    __del__ = close
+
+    def insert(self, keys, vals=None, flags: bool = False):
+        k = self._keys(keys).astype(np.uint64)
+        v = self._vals(vals, len(k))
+        v64 = None if v is None else v.astype(np.uint64)
+        f = np.zeros(len(k), np.uint8) if flags else None
+        self.L.port_insert_bulk(self.h, _p(k), _p(v64), len(k), _p(f))
+        return f
+
+    def erase(self, keys, flags: bool = False):
+        k = self._keys(keys).astype(np.uint64)
+        f = np.zeros(len(k), np.uint8) if flags else None
+        self.L.port_erase_bulk(self.h, _p(k), len(k), _p(f))
+        return f
+
+    def find(self, keys):
+        k = self._keys(keys).astype(np.uint64)
+        v = np.zeros(len(k), np.uint64)
+        f = np.zeros(len(k), np.uint8)
+        self.L.port_find_bulk(self.h, _p(k), len(k), _p(v), _p(f))
+        vd = VAL_DTYPE[self.kind]
+        return (v.astype(vd) if vd is not None else None), f
+
+    def contains(self, keys):
+        return self.find(keys)[1]
+
+    def size(self) -> int:
+        return int(self.L.port_size(self.h))
+
+    def valid(self) -> bool:
+        return bool(self.L.port_valid(self.h))
+
+    def clear(self):
+        self.L.port_clear(self.h)
+
+    def bucket(self, key: int) -> int:
+        return int(self.L.port_bucket(self.h, int(key)))
+
+    def bucket_size(self, n: int) -> int:
+        return int(self.L.port_bucket_size(self.h, int(n)))
+
+    def geometry(self) -> tuple[int, int]:
+        return int(self.L.port_bucket_count(self.h)), int(self.L.port_max_size(self.h))
+
+    def range(self):
+        n_max = self.geometry()[1]
+        k = np.zeros(n_max, np.uint64)
+        v = np.zeros(n_max, np.uint64)
+        n = int(self.L.port_range(self.h, _p(k), _p(v)))
+        vd = VAL_DTYPE[self.kind]
+        return k[:n].astype(KEY_DTYPE[self.kind]), (v[:n].astype(vd) if vd is not None else None)
+
+
+class RefTable(_TableBase):
+    """The reference's own unordered_set / unordered_map (OpenMP backend) behind the same surface."""
+
+    def __init__(self, kind: int, capacity: int):
+        self.kind = kind
+        self.L = ref_lib()
+        self.h = c_void_p(self.L.sgref_create(kind, int(capacity)))
+        if not self.h:
+            raise ValueError("unknown kind")
+
+    def close(self):
+        if self.h:
+            self.L.sgref_destroy(self.h)
+            self.h = c_void_p(0)
+
+    __del__ = close
+
+    def insert(self, keys, vals=None, flags: bool = False):
+        k = self._keys(keys)
+        v = self._vals(vals, len(k))
+        if flags:
+            f = np.zeros(len(k), np.uint8)
+            self.L.sgref_insert_flags(self.h, _p(k), _p(v), len(k), _p(f))
+            return f
+        self.L.sgref_insert(self.h, _p(k), _p(v), len(k))
+        return None
+
+    def erase(self, keys, flags: bool = False):
+        k = self._keys(keys)
+        if flags:
+            f = np.zeros(len(k), np.uint8)
+            self.L.sgref_erase_flags(self.h, _p(k), len(k), _p(f))
+            return f
+        self.L.sgref_erase(self.h, _p(k), len(k))
+        return None
+
+    def find(self, keys):
+        k = self._keys(keys)
+        vd = VAL_DTYPE[self.kind]
+        v = np.zeros(len(k), vd) if vd is not None else None
+        f = np.zeros(len(k), np.uint8)
+        self.L.sgref_find(self.h, _p(k), len(k), _p(v), _p(f))
+        return v, f
+
+    def contains(self, keys):
+        k = self._keys(keys)
+        f = np.zeros(len(k), np.uint8)
+        self.L.sgref_contains(self.h, _p(k), len(k), _p(f))
+        return f
+
+    def size(self) -> int:
+        return int(self.L.sgref_size(self.h))
+
+    def valid(self) -> bool:
+        return bool(self.L.sgref_valid(self.h))
+
+    def clear(self):
+        self.L.sgref_clear(self.h)
+
+    def bucket(self, key: int) -> int:
+        k = np.array([key], dtype=KEY_DTYPE[self.kind])
+        return int(self.L.sgref_bucket(self.h, _p(k)))
+
+    def geometry(self) -> tuple[int, int]:
+        b, m = c_int64(), c_int64()
+        self.L.sgref_geometry(self.h, byref(b), byref(m))
+        return b.value, m.value
+
+    def range(self):
+        n_max = self.geometry()[1]
+        k = np.zeros(n_max, KEY_DTYPE[self.kind])
+        vd = VAL_DTYPE[self.kind]
+        v = np.zeros(n_max, vd) if vd is not None else None
+        n = int(self.L.sgref_range(self.h, _p(k), _p(v)))
+        return k[:n], (v[:n] if v is not None else None)
+
+
+def port_geometry(capacity: int) -> tuple[int, int, int]:
+    b, e, t = c_int64(), c_int64(), c_int64()
+    port_lib().port_geometry(int(capacity), byref(b), byref(e), byref(t))
+    return b.value, e.value, t.value
+
+
+def port_fibonacci_hashing(h: int, bucket_count: int) -> int:
+    return int(port_lib().port_fibonacci_hashing(int(h), int(bucket_count)))
+
+
+def port_vector_push_back(capacity: int, values, pred=None):
+    """Returns (size, pushed flags, contents)."""
+    v = np.ascontiguousarray(values, dtype=np.uint64)
+    p = None if pred is None else np.ascontiguousarray(pred, dtype=np.uint8)
+    pushed = np.zeros(len(v), np.uint8)
+    out = np.zeros(max(capacity, 1), np.uint64)
+    n = int(port_lib().port_vector_push_back(int(capacity), _p(v), _p(p), len(v), _p(pushed), _p(out)))
+    return n, pushed, out[:n]
+
+
+def ref_vector_push_back(capacity: int, values, pred=None):
+    v = np.ascontiguousarray(values, dtype=np.uint32)
+    p = None if pred is None else np.ascontiguousarray(pred, dtype=np.uint8)
+    pushed = np.zeros(len(v), np.uint8)
+    out = np.zeros(max(capacity, 1), np.uint32)
+    n = int(ref_lib().sgref_vector_push_back(int(capacity), _p(v), _p(p), len(v), _p(pushed), _p(out)))
+    return n, pushed, out[:n]
+
+
+def port_deque_ops(capacity: int, init, is_push, values):
+    """Returns (size, popped, ok, remaining front-to-back)."""
+    i = np.ascontiguousarray(init, dtype=np.uint64)
+    ip = np.ascontiguousarray(is_push, dtype=np.uint8)
+    v = np.ascontiguousarray(values, dtype=np.uint64)
+    popped = np.zeros(len(v), np.uint64)
+    ok = np.zeros(len(v), np.uint8)
+    rem = np.zeros(max(capacity, 1), np.uint64)
+    n = int(port_lib().port_deque_ops(int(capacity), _p(i), len(i), _p(ip), _p(v), len(v), _p(popped), _p(ok),
+                                      _p(rem)))
+    return n, popped, ok, rem[:n]
+
+
+def ref_deque_ops(capacity: int, init, is_push, values):
+    i = np.ascontiguousarray(init, dtype=np.uint64)
+    ip = np.ascontiguousarray(is_push, dtype=np.uint8)
+    v = np.ascontiguousarray(values, dtype=np.uint64)
+    popped = np.zeros(len(v), np.uint64)
+    ok = np.zeros(len(v), np.uint8)
+    rem = np.zeros(max(capacity, 1), np.uint64)
+    n = int(ref_lib().sgref_deque_ops(int(capacity), _p(i), len(i), _p(ip), _p(v), len(v), _p(popped), _p(ok),
+                                      _p(rem)))
+    return n, popped, ok, rem[:n]
+
+
+def port_bitset_count(words, nbits: int) -> int:
+    w = np.ascontiguousarray(words, dtype=np.uint32)
+    return int(port_lib().port_bitset_count(_p(w), int(nbits)))
+
+
+def ref_bitset_count(words, nbits: int) -> int:
+    w = np.ascontiguousarray(words, dtype=np.uint32)
+    return int(ref_lib().sgref_bitset_count(_p(w), int(nbits)))

@@ -1,0 +1,87 @@
+"""Builds the product library ``stdgpu_gb300/_lib/libstdgpu_gb300.so`` for sm_103a.
+
+Plain ``nvcc`` (no CMake, no torch extension machinery): one object per
+translation unit, compiled in parallel, linked into one shared library with a
+C ABI (``include/stdgpu_gb300.h``).  The same recipe runs on x86_64 and on the
+aarch64 GPU host.
+"""
+
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+ROOT = PKG.parent
+CSRC = PKG / "csrc"
+OUT = PKG / "_lib"
+INCLUDE = ROOT / "include"
+LIB_NAME = "libstdgpu_gb300.so"
+
+# translation units of the product library
+SOURCES = ["unordered.cu", "containers.cu"]
+
+ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
+              "-Xcompiler", "-fvisibility=hidden"]
+
+
+def nvcc() -> str:
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    p = Path(cuda) / "bin" / "nvcc"
+    return str(p) if p.exists() else (shutil.which("nvcc") or "nvcc")
+
+
+def _run(cmd: list[str]) -> str:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return r.stdout + r.stderr
+
+
+def _deps() -> list[Path]:
+    return list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.rglob("*.h")) + \
+        list(INCLUDE.rglob("*.cuh")) + [Path(__file__)]
+
+
+def library_path() -> Path:
+    return OUT / LIB_NAME
+
+
+def is_current() -> bool:
+    lib = library_path()
+    if not lib.exists():
+        return False
+    t = lib.stat().st_mtime
+    return all(p.stat().st_mtime <= t for p in _deps())
+
+
+def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
+    """Compile every translation unit for sm_103a and link the shared library."""
+    if not force and is_current():
+        return library_path()
+    OUT.mkdir(exist_ok=True)
+    extra = ["-Xptxas", "-v"] if verbose_ptxas else []
+    cmds = []
+    objs = []
+    for src in SOURCES:
+        obj = OUT / (Path(src).stem + ".o")
+        objs.append(obj)
+        cmds.append([nvcc(), *ARCH_FLAGS, *NVCC_FLAGS, *extra, "-I", str(INCLUDE), "-I", str(CSRC),
+                     "-c", str(CSRC / src), "-o", str(obj)])
+    with ThreadPoolExecutor(max_workers=len(cmds)) as ex:
+        logs = list(ex.map(_run, cmds))
+    tmp = OUT / (LIB_NAME + ".tmp")
+    _run([nvcc(), *ARCH_FLAGS, "-shared", "-o", str(tmp), *[str(o) for o in objs], "-lcudart"])
+    os.replace(tmp, library_path())
+    if verbose_ptxas:
+        (OUT / "ptxas.log").write_text("\n".join(logs))
+    return library_path()
+
+
+if __name__ == "__main__":
+    import sys
+    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv))

@@ -1,0 +1,335 @@
+"""Python host mirror of the reference containers on the hot path.
+
+Names and argument meaning follow the reference's C++ API
+(``stdgpu::unordered_map`` / ``unordered_set`` / ``vector`` / ``deque`` /
+``bitset::count``, src/stdgpu/*.cuh); every call goes through the C ABI of the
+native library (``include/stdgpu_gb300.h``).  Device buffers are torch CUDA
+tensors used purely as memory: keys and values are 4- or 8-byte integers and
+are passed bit for bit (an int64 tensor carries uint64 keys).
+"""
+
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_int32, c_int64, c_void_p
+
+import torch
+
+from . import _native as N
+
+_KEY_BYTES = {N.SET_U32: 4, N.SET_U64: 8, N.MAP_U64_U32: 8, N.MAP_U64_U64: 8, N.MAP_U32_U32: 4, N.MAP_U32_U64: 4}
+_MAPPED_BYTES = {N.SET_U32: 0, N.SET_U64: 0, N.MAP_U64_U32: 4, N.MAP_U64_U64: 8, N.MAP_U32_U32: 4,
+                 N.MAP_U32_U64: 8}
+_INT_DTYPE = {4: torch.int32, 8: torch.int64}
+
+KINDS = {("u32", None): N.SET_U32, ("u64", None): N.SET_U64, ("u64", "u32"): N.MAP_U64_U32,
+         ("u64", "u64"): N.MAP_U64_U64, ("u32", "u32"): N.MAP_U32_U32, ("u32", "u64"): N.MAP_U32_U64}
+
+
+def _stream(stream) -> c_void_p:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return c_void_p(stream.cuda_stream)
+
+
+def _ptr(t: torch.Tensor | None) -> c_void_p:
+    if t is None:
+        return c_void_p(0)
+    if not t.is_cuda:
+        raise ValueError("device tensor expected")
+    if not t.is_contiguous():
+        raise ValueError("contiguous tensor expected")
+    return c_void_p(t.data_ptr())
+
+
+def _as_bits(t: torch.Tensor, nbytes: int, what: str) -> torch.Tensor:
+    if t.element_size() != nbytes:
+        raise ValueError(f"{what}: {nbytes}-byte elements expected, got {t.dtype}")
+    return t.contiguous()
+
+
+class unordered_base:
+    """Shared implementation of unordered_set / unordered_map (src/stdgpu/impl/unordered_base.cuh:56-583)."""
+
+    def __init__(self, handle: int, kind: int):
+        self._h = c_void_p(handle)
+        self.kind = kind
+        self.key_bytes = _KEY_BYTES[kind]
+        self.mapped_bytes = _MAPPED_BYTES[kind]
+        g = N.sg_geometry()
+        N.check(N.load().sg_unordered_geometry(self._h, byref(g)), "geometry")
+        self._geom = g
+
+    # ---- create / destroy: unordered_base_detail.cuh:1254-1348
+    @classmethod
+    def _create(cls, kind: int, capacity: int, stream=None):
+        lib = N.load()
+        h = c_void_p()
+        N.check(lib.sg_unordered_create(kind, int(capacity), _stream(stream), byref(h)), "createDeviceObject")
+        return cls(h.value, kind)
+
+    @staticmethod
+    def destroyDeviceObject(obj: "unordered_base") -> None:
+        if obj._h:
+            N.check(N.load().sg_unordered_destroy(obj._h), "destroyDeviceObject")
+            obj._h = c_void_p(0)
+
+    # ---- geometry: unordered_base_detail.cuh:1134-1176
+    def bucket_count(self) -> int:
+        return self._geom.bucket_count
+
+    def max_size(self) -> int:
+        return self._geom.max_size
+
+    def max_load_factor(self) -> float:
+        return 1.0
+
+    def geometry(self) -> N.sg_geometry:
+        return self._geom
+
+    def load_factor(self, stream=None) -> float:
+        # float division as in unordered_base_detail.cuh:1155-1160
+        import numpy as np
+        return float(np.float32(self.size(stream)) / np.float32(self.bucket_count()))
+
+    def bucket(self, key: int) -> int:
+        kb = self.key_bytes
+        buf = (ctypes.c_uint32 if kb == 4 else ctypes.c_uint64)(int(key) & ((1 << (8 * kb)) - 1))
+        out = c_int64()
+        N.check(N.load().sg_unordered_bucket(self._h, ctypes.cast(byref(buf), c_void_p), byref(out)), "bucket")
+        return out.value
+
+    # ---- bulk operations
+    def insert(self, keys: torch.Tensor, mapped: torch.Tensor | None = None, *, flags: torch.Tensor | None = None,
+               stream=None) -> None:
+        """insert(begin, end) over keys (+ mapped values for maps): unordered_base_detail.cuh:996-1017."""
+        keys = _as_bits(keys, self.key_bytes, "keys")
+        if self.mapped_bytes:
+            if mapped is None:
+                raise ValueError("mapped values required for a map")
+            mapped = _as_bits(mapped, self.mapped_bytes, "mapped")
+        else:
+            mapped = None
+        N.check(N.load().sg_unordered_insert_kv(self._h, _ptr(keys), _ptr(mapped), keys.numel(), _ptr(flags),
+                                                _stream(stream)), "insert")
+
+    def insert_values(self, values: torch.Tensor, n: int, *, flags: torch.Tensor | None = None, stream=None) -> None:
+        """insert(begin, end) over a value_type array (raw bytes, n elements of slot_bytes)."""
+        if values.numel() * values.element_size() < n * self._geom.slot_bytes:
+            raise ValueError("values buffer too small")
+        N.check(N.load().sg_unordered_insert(self._h, _ptr(values), int(n), _ptr(flags), _stream(stream)), "insert")
+
+    def erase(self, keys: torch.Tensor, *, flags: torch.Tensor | None = None, stream=None) -> None:
+        """erase(begin, end): unordered_base_detail.cuh:1045-1066."""
+        keys = _as_bits(keys, self.key_bytes, "keys")
+        N.check(N.load().sg_unordered_erase(self._h, _ptr(keys), keys.numel(), _ptr(flags), _stream(stream)),
+                "erase")
+
+    def contains(self, keys: torch.Tensor, stream=None) -> torch.Tensor:
+        keys = _as_bits(keys, self.key_bytes, "keys")
+        out = torch.empty(keys.numel(), dtype=torch.uint8, device=keys.device)
+        N.check(N.load().sg_unordered_contains(self._h, _ptr(keys), keys.numel(), _ptr(out), _stream(stream)),
+                "contains")
+        return out
+
+    def count(self, keys: torch.Tensor, stream=None) -> torch.Tensor:
+        return self.contains(keys, stream)
+
+    def find(self, keys: torch.Tensor, stream=None) -> tuple[torch.Tensor | None, torch.Tensor]:
+        keys = _as_bits(keys, self.key_bytes, "keys")
+        found = torch.empty(keys.numel(), dtype=torch.uint8, device=keys.device)
+        vals = None
+        if self.mapped_bytes:
+            vals = torch.zeros(keys.numel(), dtype=_INT_DTYPE[self.mapped_bytes], device=keys.device)
+        N.check(N.load().sg_unordered_find(self._h, _ptr(keys), keys.numel(), _ptr(vals), _ptr(found),
+                                           _stream(stream)), "find")
+        return vals, found
+
+    def size(self, stream=None) -> int:
+        out = c_int64()
+        N.check(N.load().sg_unordered_size(self._h, _stream(stream), byref(out)), "size")
+        return out.value
+
+    def status(self, stream=None) -> tuple[int, int, int]:
+        """(status code, refused inserts since the last call, erased slots awaiting reuse)."""
+        refused, tombs = c_int64(), c_int64()
+        st = N.load().sg_unordered_status(self._h, _stream(stream), byref(refused), byref(tombs))
+        N.check(st, "status", allow=(N.SG_ERR_FULL,))
+        return st, refused.value, tombs.value
+
+    def empty(self, stream=None) -> bool:
+        return self.size(stream) == 0
+
+    def full(self, stream=None) -> bool:
+        return self.size(stream) == self.max_size()
+
+    def clear(self, stream=None) -> None:
+        N.check(N.load().sg_unordered_clear(self._h, _stream(stream)), "clear")
+
+    def valid(self, stream=None) -> bool:
+        out = c_int32()
+        N.check(N.load().sg_unordered_valid(self._h, _stream(stream), byref(out)), "valid")
+        return bool(out.value)
+
+    def device_range(self, stream=None) -> torch.Tensor:
+        """Slot indices of all stored elements (device_range(): unordered_base_detail.cuh:160-208)."""
+        out = torch.empty(self.max_size() + 2, dtype=torch.int32, device="cuda")
+        n = c_int64()
+        N.check(N.load().sg_unordered_device_range(self._h, _ptr(out), _stream(stream), byref(n)), "device_range")
+        return out[: n.value]
+
+    def range_copy(self, stream=None) -> tuple[torch.Tensor, torch.Tensor | None]:
+        """(keys, mapped) of all stored elements, in slot order."""
+        cap = self.max_size() + 2
+        keys = torch.empty(cap, dtype=_INT_DTYPE[self.key_bytes], device="cuda")
+        vals = torch.empty(cap, dtype=_INT_DTYPE[self.mapped_bytes], device="cuda") if self.mapped_bytes else None
+        n = c_int64()
+        N.check(N.load().sg_unordered_range_copy(self._h, _ptr(keys), _ptr(vals), _stream(stream), byref(n)),
+                "range_copy")
+        return keys[: n.value], (vals[: n.value] if vals is not None else None)
+
+    def view(self) -> N.sg_unordered_view:
+        v = N.sg_unordered_view()
+        N.check(N.load().sg_unordered_view_of(self._h, byref(v)), "view")
+        return v
+
+
+class unordered_set(unordered_base):
+    """stdgpu::unordered_set<Key> for Key = uint32_t / uint64_t (src/stdgpu/unordered_set.cuh:61-65)."""
+
+    @classmethod
+    def createDeviceObject(cls, capacity: int, key: str = "u64", stream=None) -> "unordered_set":
+        return cls._create(KINDS[(key, None)], capacity, stream)
+
+
+class unordered_map(unordered_base):
+    """stdgpu::unordered_map<Key, T> for 4/8-byte integer Key and T (src/stdgpu/unordered_map.cuh:70-75)."""
+
+    @classmethod
+    def createDeviceObject(cls, capacity: int, key: str = "u64", mapped: str = "u32",
+                           stream=None) -> "unordered_map":
+        return cls._create(KINDS[(key, mapped)], capacity, stream)
+
+
+def geometry_for(kind: int, capacity: int) -> N.sg_geometry:
+    g = N.sg_geometry()
+    N.check(N.load().sg_unordered_geometry_for(kind, int(capacity), byref(g)), "geometry_for")
+    return g
+
+
+class vector:
+    """stdgpu::vector<T> (T = 4 or 8 bytes): push_back, size, clear (src/stdgpu/vector.cuh)."""
+
+    def __init__(self, handle: int, elem_bytes: int, capacity: int):
+        self._h = c_void_p(handle)
+        self.elem_bytes = elem_bytes
+        self._capacity = capacity
+
+    @classmethod
+    def createDeviceObject(cls, capacity: int, elem_bytes: int = 4) -> "vector":
+        h = c_void_p()
+        N.check(N.load().sg_vector_create(elem_bytes, int(capacity), byref(h)), "vector::createDeviceObject")
+        return cls(h.value, elem_bytes, capacity)
+
+    @staticmethod
+    def destroyDeviceObject(v: "vector") -> None:
+        if v._h:
+            N.check(N.load().sg_vector_destroy(v._h), "vector::destroyDeviceObject")
+            v._h = c_void_p(0)
+
+    def capacity(self) -> int:
+        return self._capacity
+
+    def push_back(self, values: torch.Tensor, pred: torch.Tensor | None = None, *,
+                  flags: torch.Tensor | None = None, stream=None) -> None:
+        values = _as_bits(values, self.elem_bytes, "values")
+        N.check(N.load().sg_vector_push_back(self._h, _ptr(values), _ptr(pred), values.numel(), _ptr(flags),
+                                             _stream(stream)), "push_back")
+
+    def size(self, stream=None) -> int:
+        out = c_int64()
+        N.check(N.load().sg_vector_size(self._h, _stream(stream), byref(out)), "vector::size")
+        return out.value
+
+    def clear(self, stream=None) -> None:
+        N.check(N.load().sg_vector_clear(self._h, _stream(stream)), "vector::clear")
+
+    def data(self) -> torch.Tensor:
+        v = N.sg_vector_view()
+        N.check(N.load().sg_vector_view_of(self._h, byref(v)), "vector::data")
+        n = self.size()
+        return _tensor_from_ptr(v.data, n, self.elem_bytes)
+
+
+class deque:
+    """stdgpu::deque<T> (T = 4 or 8 bytes): push_back / pop_front (src/stdgpu/deque.cuh)."""
+
+    def __init__(self, handle: int, elem_bytes: int, capacity: int):
+        self._h = c_void_p(handle)
+        self.elem_bytes = elem_bytes
+        self._capacity = capacity
+
+    @classmethod
+    def createDeviceObject(cls, capacity: int, elem_bytes: int = 8) -> "deque":
+        h = c_void_p()
+        N.check(N.load().sg_deque_create(elem_bytes, int(capacity), byref(h)), "deque::createDeviceObject")
+        return cls(h.value, elem_bytes, capacity)
+
+    @staticmethod
+    def destroyDeviceObject(d: "deque") -> None:
+        if d._h:
+            N.check(N.load().sg_deque_destroy(d._h), "deque::destroyDeviceObject")
+            d._h = c_void_p(0)
+
+    def ops(self, is_push: torch.Tensor | None, values: torch.Tensor, *, stream=None):
+        """One launch: element i push_back(values[i]) if is_push[i] else pop_front().  Returns (popped, ok)."""
+        values = _as_bits(values, self.elem_bytes, "values")
+        n = values.numel()
+        popped = torch.zeros(n, dtype=_INT_DTYPE[self.elem_bytes], device=values.device)
+        ok = torch.zeros(n, dtype=torch.uint8, device=values.device)
+        N.check(N.load().sg_deque_ops(self._h, _ptr(is_push), _ptr(values), n, _ptr(popped), _ptr(ok),
+                                      _stream(stream)), "deque::ops")
+        return popped, ok
+
+    def size(self, stream=None) -> int:
+        out = c_int64()
+        N.check(N.load().sg_deque_size(self._h, _stream(stream), byref(out)), "deque::size")
+        return out.value
+
+    def to_tensor(self, stream=None) -> torch.Tensor:
+        out = torch.empty(max(self._capacity, 1), dtype=_INT_DTYPE[self.elem_bytes], device="cuda")
+        n = c_int64()
+        N.check(N.load().sg_deque_copy_out(self._h, _ptr(out), _stream(stream), byref(n)), "deque::copy_out")
+        return out[: n.value]
+
+    def clear(self, stream=None) -> None:
+        N.check(N.load().sg_deque_clear(self._h, _stream(stream)), "deque::clear")
+
+
+def bitset_count(blocks: torch.Tensor, nbits: int, stream=None) -> int:
+    """bitset<unsigned int>::count() over raw 32-bit blocks (src/stdgpu/impl/bitset_detail.cuh:388-404)."""
+    blocks = _as_bits(blocks, 4, "blocks")
+    if blocks.numel() * 32 < nbits:
+        raise ValueError("blocks too short for nbits")
+    out = c_int64()
+    N.check(N.load().sg_bitset_count(_ptr(blocks), int(nbits), _stream(stream), byref(out)), "bitset::count")
+    return out.value
+
+
+def kernel_launch_count() -> int:
+    return int(N.load().sg_kernel_launch_count())
+
+
+class _DeviceArray:
+    """Zero-copy description of a raw device buffer (CUDA array interface)."""
+
+    def __init__(self, ptr: int, n: int, elem_bytes: int):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<i%d" % elem_bytes, "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
+def _tensor_from_ptr(ptr: int, n: int, elem_bytes: int) -> torch.Tensor:
+    """Copy n elements from a raw device pointer into a new tensor."""
+    if n == 0:
+        return torch.empty(0, dtype=_INT_DTYPE[elem_bytes], device="cuda")
+    return torch.as_tensor(_DeviceArray(ptr, n, elem_bytes), device="cuda").clone()

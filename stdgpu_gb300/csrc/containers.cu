@@ -1,0 +1,765 @@
+// vector<T>::push_back, deque<T>::push_back / pop_front and bitset::count for GB300.
+//
+// vector / deque replace the reference's per-element global atomic plus slot
+// spin lock (src/stdgpu/impl/vector_detail.cuh:181-238,
+// src/stdgpu/impl/deque_detail.cuh:202-258, 388-446) with one warp-aggregated
+// reservation per warp: the lanes that push ballot, the lowest one adds the
+// warp's count to the shared counter and every lane takes its rank.
+//
+// The deque is a ring of tickets: push k and pop k use slot k mod capacity; a
+// per-slot turn counter (the k-th push stores k+1 after writing the element,
+// the k-th pop stores k+capacity after reading it) orders a pop after the push
+// of the same ticket and a push after the pop one lap earlier.  Those waits are
+// bounded: a wait that runs out sets an error bit and the operation reports
+// failure instead of spinning on.
+//
+// bitset::count (src/stdgpu/impl/bitset_detail.cuh:388-404, count_block_bits
+// :130-160) is a two-pass reduction: 16-byte loads and popc per thread, one
+// partial per block, then one block sums the partials.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <new>
+
+#include "sg_internal.cuh"
+#include "stdgpu_gb300.h"
+#include "stdgpu_gb300/detail/layout.cuh"
+
+namespace sg
+{
+namespace detail
+{
+
+constexpr int kCThreads = 256;
+constexpr unsigned int kDequeErrWait = 1u;
+constexpr long long kWaitLimit = 1ll << 22; // polls of a ring slot before giving up (about 1-2 s with backoff)
+
+struct deque_counters
+{
+    long long size;
+    unsigned long long begin;
+    unsigned long long end;
+    unsigned int error;
+    unsigned int pad;
+};
+
+SG_D unsigned
+lanemask_lt()
+{
+    unsigned m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+template <typename T>
+SG_D T
+ld_stream(const T* p)
+{
+    return __ldcs(p);
+}
+
+// ---------------------------------------------------------------- vector
+
+template <typename T>
+__global__ void __launch_bounds__(kCThreads)
+k_vector_push_back(T* data, long long* size, int64_t cap, const T* values, const uint8_t* pred, int64_t n,
+                   uint8_t* out_pushed)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t base = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) & ~int64_t{ 31 }; base < n;
+         base += stride)
+    {
+        const int64_t i = base + lane;
+        const bool in = i < n;
+        const bool want = in && (pred == nullptr || pred[i] != 0);
+        const unsigned mask = __ballot_sync(0xffffffffu, want);
+        long long slot0 = -1;
+        if (mask != 0u)
+        {
+            const int leader = __ffs(mask) - 1;
+            if (lane == leader)
+            {
+                // preemptive full() check, then one reservation for the warp (vector_detail.cuh:186-195)
+                const long long cur = *reinterpret_cast<volatile long long*>(size);
+                slot0 = cur >= cap ? -1 : atomicAdd(reinterpret_cast<unsigned long long*>(size),
+                                                    static_cast<unsigned long long>(__popc(mask)));
+            }
+            slot0 = __shfl_sync(0xffffffffu, slot0, leader);
+        }
+        const long long pos = slot0 + __popc(mask & lanemask_lt());
+        const bool ok = want && slot0 >= 0 && pos < cap;
+        if (ok)
+        {
+            data[pos] = ld_stream(values + i);
+        }
+        if (in && out_pushed != nullptr)
+        {
+            out_pushed[i] = static_cast<uint8_t>(ok);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- deque
+
+SG_D bool
+wait_turn(const unsigned* seq, unsigned want, unsigned* error)
+{
+    long long polls = 0;
+    unsigned backoff = 32;
+    while (true)
+    {
+        unsigned cur;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(seq) : "memory");
+        if (cur == want)
+        {
+            return true;
+        }
+        if (++polls > kWaitLimit)
+        {
+            atomicOr(error, kDequeErrWait);
+            return false;
+        }
+        __nanosleep(backoff);
+        backoff = backoff < 256 ? backoff * 2 : 256;
+    }
+}
+
+SG_D void
+store_turn(unsigned* seq, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(seq), "r"(v) : "memory");
+}
+
+// Mixed launch: element i pushes values[i] when is_push[i] != 0 (or is_push == NULL), else pops.
+template <typename T>
+__global__ void __launch_bounds__(kCThreads)
+k_deque_ops(T* data, unsigned* seq, deque_counters* c, int64_t cap, const uint8_t* is_push, const T* values,
+            int64_t n, T* out_popped, uint8_t* out_ok)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t base = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) & ~int64_t{ 31 }; base < n;
+         base += stride)
+    {
+        const int64_t i = base + lane;
+        const bool in = i < n;
+        const bool push = in && (is_push == nullptr || is_push[i] != 0);
+        const bool pop = in && !push;
+        const unsigned pmask = __ballot_sync(0xffffffffu, push);
+        const unsigned qmask = __ballot_sync(0xffffffffu, pop);
+        long long push_ok = 0, pop_ok = 0;
+        unsigned long long push_t0 = 0, pop_t0 = 0;
+        if (lane == 0)
+        {
+            const long long pc = __popc(pmask);
+            const long long qc = __popc(qmask);
+            if (pc > 0)
+            {
+                // push_back: reserve against the capacity (deque_detail.cuh:207-217), undo the overshoot
+                const long long cur = *reinterpret_cast<volatile long long*>(&c->size);
+                if (cur < cap)
+                {
+                    const long long old = static_cast<long long>(
+                            atomicAdd(reinterpret_cast<unsigned long long*>(&c->size), static_cast<unsigned long long>(pc)));
+                    long long room = cap - old;
+                    push_ok = room <= 0 ? 0 : (room < pc ? room : pc);
+                    if (push_ok < pc)
+                    {
+                        atomicAdd(reinterpret_cast<unsigned long long*>(&c->size),
+                                  static_cast<unsigned long long>(-(pc - push_ok)));
+                    }
+                    if (push_ok > 0)
+                    {
+                        push_t0 = atomicAdd(&c->end, static_cast<unsigned long long>(push_ok));
+                    }
+                }
+            }
+            if (qc > 0)
+            {
+                // pop_front: reserve against the current size (deque_detail.cuh:393-404), undo the overshoot
+                const long long cur = *reinterpret_cast<volatile long long*>(&c->size);
+                if (cur > 0)
+                {
+                    const long long old = static_cast<long long>(
+                            atomicAdd(reinterpret_cast<unsigned long long*>(&c->size), static_cast<unsigned long long>(-qc)));
+                    pop_ok = old <= 0 ? 0 : (old < qc ? old : qc);
+                    if (pop_ok < qc)
+                    {
+                        atomicAdd(reinterpret_cast<unsigned long long*>(&c->size),
+                                  static_cast<unsigned long long>(qc - pop_ok));
+                    }
+                    if (pop_ok > 0)
+                    {
+                        pop_t0 = atomicAdd(&c->begin, static_cast<unsigned long long>(pop_ok));
+                    }
+                }
+            }
+        }
+        push_ok = __shfl_sync(0xffffffffu, push_ok, 0);
+        pop_ok = __shfl_sync(0xffffffffu, pop_ok, 0);
+        push_t0 = __shfl_sync(0xffffffffu, push_t0, 0);
+        pop_t0 = __shfl_sync(0xffffffffu, pop_t0, 0);
+        bool ok = false;
+        if (push)
+        {
+            const long long r = __popc(pmask & lanemask_lt());
+            if (r < push_ok)
+            {
+                const unsigned long long tk = push_t0 + static_cast<unsigned long long>(r);
+                const int64_t pos = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
+                if (wait_turn(seq + pos, static_cast<unsigned>(tk), &c->error))
+                {
+                    data[pos] = values[i];
+                    store_turn(seq + pos, static_cast<unsigned>(tk + 1));
+                    ok = true;
+                }
+            }
+        }
+        else if (pop)
+        {
+            const long long r = __popc(qmask & lanemask_lt());
+            if (r < pop_ok)
+            {
+                const unsigned long long tk = pop_t0 + static_cast<unsigned long long>(r);
+                const int64_t pos = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
+                if (wait_turn(seq + pos, static_cast<unsigned>(tk + 1), &c->error))
+                {
+                    const T v = *reinterpret_cast<volatile T*>(data + pos);
+                    store_turn(seq + pos, static_cast<unsigned>(tk + static_cast<unsigned long long>(cap)));
+                    if (out_popped != nullptr)
+                    {
+                        out_popped[i] = v;
+                    }
+                    ok = true;
+                }
+            }
+        }
+        if (in && out_ok != nullptr)
+        {
+            out_ok[i] = static_cast<uint8_t>(ok);
+        }
+    }
+}
+
+__global__ void
+k_deque_reset(unsigned* seq, deque_counters* c, int64_t cap)
+{
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < cap; i += stride)
+    {
+        seq[i] = static_cast<unsigned>(i);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        c->size = 0;
+        c->begin = 0;
+        c->end = 0;
+        c->error = 0;
+    }
+}
+
+template <typename T>
+__global__ void
+k_deque_copy_out(const T* data, const deque_counters* c, int64_t cap, T* out)
+{
+    const long long n = c->size;
+    const unsigned long long b = c->begin;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    {
+        out[i] = data[(b + static_cast<unsigned long long>(i)) % static_cast<unsigned long long>(cap)];
+    }
+}
+
+// ---------------------------------------------------------------- bitset::count
+
+constexpr int kCountThreads = 512;
+
+__global__ void __launch_bounds__(kCountThreads)
+k_bitset_count(const uint32_t* blocks, int64_t nbits, unsigned long long* partials)
+{
+    const int64_t nwords = (nbits + 31) / 32;
+    const int64_t full_words = nbits / 32; // words with all 32 bits counted
+    const bool aligned = (reinterpret_cast<uintptr_t>(blocks) & 15u) == 0;
+    const int64_t nvec = aligned ? full_words / 4 : 0;
+    const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    unsigned long long sum = 0;
+    const uint4* v4 = reinterpret_cast<const uint4*>(blocks);
+    // 4 independent 16-byte loads in flight per thread
+    int64_t k = tid;
+    for (; k + 3 * stride < nvec; k += 4 * stride)
+    {
+        const uint4 a = __ldcs(v4 + k);
+        const uint4 b = __ldcs(v4 + k + stride);
+        const uint4 c = __ldcs(v4 + k + 2 * stride);
+        const uint4 d = __ldcs(v4 + k + 3 * stride);
+        sum += __popc(a.x) + __popc(a.y) + __popc(a.z) + __popc(a.w);
+        sum += __popc(b.x) + __popc(b.y) + __popc(b.z) + __popc(b.w);
+        sum += __popc(c.x) + __popc(c.y) + __popc(c.z) + __popc(c.w);
+        sum += __popc(d.x) + __popc(d.y) + __popc(d.z) + __popc(d.w);
+    }
+    for (; k < nvec; k += stride)
+    {
+        const uint4 a = __ldcs(v4 + k);
+        sum += __popc(a.x) + __popc(a.y) + __popc(a.z) + __popc(a.w);
+    }
+    // remaining full words, then the masked tail word (count_block_bits::block_mask)
+    for (int64_t w = nvec * 4 + tid; w < nwords; w += stride)
+    {
+        uint32_t x = blocks[w];
+        if (w >= full_words)
+        {
+            const int rem = static_cast<int>(nbits - w * 32);
+            x &= (1u << rem) - 1u;
+        }
+        sum += __popc(x);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    }
+    __shared__ unsigned long long red[kCountThreads / 32];
+    if ((threadIdx.x & 31) == 0)
+    {
+        red[threadIdx.x >> 5] = sum;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        unsigned long long s = 0;
+        for (int w = 0; w < kCountThreads / 32; ++w)
+        {
+            s += red[w];
+        }
+        partials[blockIdx.x] = s;
+    }
+}
+
+__global__ void __launch_bounds__(1024)
+k_sum_partials(const unsigned long long* partials, int n, unsigned long long* out)
+{
+    unsigned long long s = 0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+    {
+        s += partials[i];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+    }
+    __shared__ unsigned long long red[32];
+    if ((threadIdx.x & 31) == 0)
+    {
+        red[threadIdx.x >> 5] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        unsigned long long t = 0;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w)
+        {
+            t += red[w];
+        }
+        *out = t;
+    }
+}
+
+int
+count_grid()
+{
+    static const int g = persistent_grid(k_bitset_count, kCountThreads);
+    return g;
+}
+
+} // namespace detail
+} // namespace sg
+
+using namespace sg::detail;
+
+struct sg_vector
+{
+    int32_t elem_bytes;
+    int64_t capacity;
+    void* data;
+    long long* size;
+    long long* host;
+};
+
+struct sg_deque
+{
+    int32_t elem_bytes;
+    int64_t capacity;
+    void* data;
+    unsigned* seq;
+    deque_counters* counters;
+    deque_counters* host;
+};
+
+namespace
+{
+
+// Per-device scratch of bitset::count: one partial per block plus the result word.
+struct count_scratch
+{
+    unsigned long long* partials = nullptr;
+    unsigned long long* host = nullptr;
+    int blocks = 0;
+};
+
+std::mutex g_count_mutex;
+count_scratch g_count_scratch[64];
+
+} // namespace
+
+extern "C" {
+
+sg_status
+sg_vector_create(int32_t elem_bytes, int64_t capacity, sg_vector** out)
+{
+    if (out == nullptr || (elem_bytes != 4 && elem_bytes != 8) || capacity <= 0)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    *out = nullptr;
+    auto* v = new (std::nothrow) sg_vector{};
+    if (v == nullptr)
+    {
+        return SG_ERR_OOM;
+    }
+    v->elem_bytes = elem_bytes;
+    v->capacity = capacity;
+    cudaError_t e = cudaMalloc(&v->data, static_cast<size_t>(capacity) * elem_bytes);
+    if (e == cudaSuccess)
+    {
+        e = cudaMalloc(&v->size, sizeof(long long));
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaMemset(v->size, 0, sizeof(long long));
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaMallocHost(&v->host, sizeof(long long));
+    }
+    if (e != cudaSuccess)
+    {
+        sg_vector_destroy(v);
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? SG_ERR_OOM : SG_ERR_CUDA;
+    }
+    *out = v;
+    return SG_OK;
+}
+
+sg_status
+sg_vector_destroy(sg_vector* v)
+{
+    if (v == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    cudaDeviceSynchronize();
+    cudaFree(v->data);
+    cudaFree(v->size);
+    if (v->host != nullptr)
+    {
+        cudaFreeHost(v->host);
+    }
+    delete v;
+    return SG_OK;
+}
+
+sg_status
+sg_vector_push_back(sg_vector* v, const void* values, const uint8_t* pred, int64_t n, uint8_t* out_pushed,
+                    void* stream)
+{
+    if (v == nullptr || n < 0 || (n > 0 && values == nullptr))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    cudaStream_t s = as_stream(stream);
+    if (v->elem_bytes == 4)
+    {
+        static const int mg = persistent_grid(k_vector_push_back<uint32_t>, kCThreads);
+        k_vector_push_back<uint32_t><<<grid_for(n, kCThreads, mg), kCThreads, 0, s>>>(
+                static_cast<uint32_t*>(v->data), v->size, v->capacity, static_cast<const uint32_t*>(values), pred, n,
+                out_pushed);
+    }
+    else
+    {
+        static const int mg = persistent_grid(k_vector_push_back<unsigned long long>, kCThreads);
+        k_vector_push_back<unsigned long long><<<grid_for(n, kCThreads, mg), kCThreads, 0, s>>>(
+                static_cast<unsigned long long*>(v->data), v->size, v->capacity,
+                static_cast<const unsigned long long*>(values), pred, n, out_pushed);
+    }
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+}
+
+sg_status
+sg_vector_size(sg_vector* v, void* stream, int64_t* out_size)
+{
+    if (v == nullptr || out_size == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    cudaStream_t s = as_stream(stream);
+    SG_CUDA_TRY(cudaMemcpyAsync(v->host, v->size, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    SG_CUDA_TRY(cudaStreamSynchronize(s));
+    long long x = *v->host;
+    *out_size = x < 0 ? 0 : (x > v->capacity ? v->capacity : x);
+    return SG_OK;
+}
+
+sg_status
+sg_vector_clear(sg_vector* v, void* stream)
+{
+    if (v == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    SG_CUDA_TRY(cudaMemsetAsync(v->size, 0, sizeof(long long), as_stream(stream)));
+    return SG_OK;
+}
+
+sg_status
+sg_vector_view_of(const sg_vector* v, sg_vector_view* out)
+{
+    if (v == nullptr || out == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    out->data = v->data;
+    out->size = v->size;
+    out->capacity = v->capacity;
+    out->elem_bytes = v->elem_bytes;
+    out->pad = 0;
+    return SG_OK;
+}
+
+sg_status
+sg_deque_create(int32_t elem_bytes, int64_t capacity, sg_deque** out)
+{
+    if (out == nullptr || (elem_bytes != 4 && elem_bytes != 8) || capacity <= 0 || capacity >= (int64_t{ 1 } << 31))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    *out = nullptr;
+    auto* d = new (std::nothrow) sg_deque{};
+    if (d == nullptr)
+    {
+        return SG_ERR_OOM;
+    }
+    d->elem_bytes = elem_bytes;
+    d->capacity = capacity;
+    cudaError_t e = cudaMalloc(&d->data, static_cast<size_t>(capacity) * elem_bytes);
+    if (e == cudaSuccess)
+    {
+        e = cudaMalloc(&d->seq, static_cast<size_t>(capacity) * sizeof(unsigned));
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaMalloc(&d->counters, sizeof(deque_counters));
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaMallocHost(&d->host, sizeof(deque_counters));
+    }
+    if (e != cudaSuccess)
+    {
+        sg_deque_destroy(d);
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? SG_ERR_OOM : SG_ERR_CUDA;
+    }
+    sg_status st = sg_deque_clear(d, nullptr);
+    if (st != SG_OK)
+    {
+        sg_deque_destroy(d);
+        return st;
+    }
+    *out = d;
+    return SG_OK;
+}
+
+sg_status
+sg_deque_destroy(sg_deque* d)
+{
+    if (d == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    cudaDeviceSynchronize();
+    cudaFree(d->data);
+    cudaFree(d->seq);
+    cudaFree(d->counters);
+    if (d->host != nullptr)
+    {
+        cudaFreeHost(d->host);
+    }
+    delete d;
+    return SG_OK;
+}
+
+sg_status
+sg_deque_clear(sg_deque* d, void* stream)
+{
+    if (d == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    cudaStream_t s = as_stream(stream);
+    static const int mg = persistent_grid(k_deque_reset, kCThreads);
+    k_deque_reset<<<grid_for(d->capacity, kCThreads, mg), kCThreads, 0, s>>>(d->seq, d->counters, d->capacity);
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+}
+
+sg_status
+sg_deque_ops(sg_deque* d, const uint8_t* is_push, const void* values, int64_t n, void* out_popped, uint8_t* out_ok,
+             void* stream)
+{
+    if (d == nullptr || n < 0)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    cudaStream_t s = as_stream(stream);
+    if (d->elem_bytes == 4)
+    {
+        static const int mg = persistent_grid(k_deque_ops<uint32_t>, kCThreads);
+        k_deque_ops<uint32_t><<<grid_for(n, kCThreads, mg), kCThreads, 0, s>>>(
+                static_cast<uint32_t*>(d->data), d->seq, d->counters, d->capacity, is_push,
+                static_cast<const uint32_t*>(values), n, static_cast<uint32_t*>(out_popped), out_ok);
+    }
+    else
+    {
+        static const int mg = persistent_grid(k_deque_ops<unsigned long long>, kCThreads);
+        k_deque_ops<unsigned long long><<<grid_for(n, kCThreads, mg), kCThreads, 0, s>>>(
+                static_cast<unsigned long long*>(d->data), d->seq, d->counters, d->capacity, is_push,
+                static_cast<const unsigned long long*>(values), n, static_cast<unsigned long long*>(out_popped),
+                out_ok);
+    }
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+}
+
+sg_status
+sg_deque_size(sg_deque* d, void* stream, int64_t* out_size)
+{
+    if (d == nullptr || out_size == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    cudaStream_t s = as_stream(stream);
+    SG_CUDA_TRY(cudaMemcpyAsync(d->host, d->counters, sizeof(deque_counters), cudaMemcpyDeviceToHost, s));
+    SG_CUDA_TRY(cudaStreamSynchronize(s));
+    const long long x = d->host->size;
+    *out_size = x < 0 ? 0 : (x > d->capacity ? d->capacity : x);
+    return (d->host->error & kDequeErrWait) != 0u ? SG_ERR_RETRY_EXHAUSTED : SG_OK;
+}
+
+sg_status
+sg_deque_copy_out(sg_deque* d, void* out, void* stream, int64_t* out_n)
+{
+    if (d == nullptr || out == nullptr || out_n == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    cudaStream_t s = as_stream(stream);
+    int64_t n = 0;
+    sg_status st = sg_deque_size(d, stream, &n);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    if (n > 0)
+    {
+        const int grid = grid_for(n, kCThreads, 4096);
+        if (d->elem_bytes == 4)
+        {
+            k_deque_copy_out<uint32_t><<<grid, kCThreads, 0, s>>>(static_cast<const uint32_t*>(d->data), d->counters,
+                                                                  d->capacity, static_cast<uint32_t*>(out));
+        }
+        else
+        {
+            k_deque_copy_out<unsigned long long><<<grid, kCThreads, 0, s>>>(
+                    static_cast<const unsigned long long*>(d->data), d->counters, d->capacity,
+                    static_cast<unsigned long long*>(out));
+        }
+        SG_LAUNCH_CHECK();
+        SG_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    *out_n = n;
+    return SG_OK;
+}
+
+sg_status
+sg_deque_view_of(const sg_deque* d, sg_deque_view* out)
+{
+    if (d == nullptr || out == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    out->data = d->data;
+    out->seq = d->seq;
+    out->counters = d->counters;
+    out->capacity = d->capacity;
+    out->elem_bytes = d->elem_bytes;
+    out->pad = 0;
+    return SG_OK;
+}
+
+sg_status
+sg_bitset_count(const uint32_t* blocks, int64_t nbits, void* stream, int64_t* out_count)
+{
+    if (out_count == nullptr || nbits < 0 || (nbits > 0 && blocks == nullptr))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (nbits == 0)
+    {
+        *out_count = 0;
+        return SG_OK;
+    }
+    int dev = 0;
+    SG_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64)
+    {
+        return SG_ERR_NO_DEVICE;
+    }
+    cudaStream_t s = as_stream(stream);
+    std::lock_guard<std::mutex> lock(g_count_mutex);
+    count_scratch& sc = g_count_scratch[dev];
+    if (sc.partials == nullptr)
+    {
+        const int blocks_max = count_grid();
+        SG_CUDA_TRY(cudaMalloc(&sc.partials, static_cast<size_t>(blocks_max + 1) * sizeof(unsigned long long)));
+        SG_CUDA_TRY(cudaMallocHost(&sc.host, sizeof(unsigned long long)));
+        sc.blocks = blocks_max;
+    }
+    const int64_t nvec = (nbits + 127) / 128;
+    const int grid = grid_for(nvec, kCountThreads * 4, sc.blocks);
+    k_bitset_count<<<grid, kCountThreads, 0, s>>>(blocks, nbits, sc.partials);
+    SG_LAUNCH_CHECK();
+    k_sum_partials<<<1, 1024, 0, s>>>(sc.partials, grid, sc.partials + sc.blocks);
+    SG_LAUNCH_CHECK();
+    SG_CUDA_TRY(cudaMemcpyAsync(sc.host, sc.partials + sc.blocks, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                s));
+    SG_CUDA_TRY(cudaStreamSynchronize(s));
+    *out_count = static_cast<int64_t>(*sc.host);
+    return SG_OK;
+}
+
+} // extern "C"

@@ -1,0 +1,1592 @@
+// unordered_set / unordered_map for GB300 (sm_103a): bulk kernels and the C ABI.
+//
+// Replaces the reference's table core (src/stdgpu/impl/unordered_base.cuh,
+// src/stdgpu/impl/unordered_base_detail.cuh): a bucket array plus a linked
+// excess list guarded by per-slot spin locks becomes open addressing over
+// 128-byte probe groups (layout in include/stdgpu_gb300/detail/layout.cuh).
+//
+// Bulk kernels are warp-cooperative: a tile of 8 lanes owns one key at a time
+// and reads its whole probe group with one 16-byte load per lane; a warp holds
+// 32 keys (4 tiles x 8 keys) and issues the home-group loads of all 8 keys of a
+// tile before resolving any of them, so each warp keeps 32 random 128-byte
+// lines in flight.  Slots are claimed lock-free with one compare-and-swap on
+// the key word; counters are reduced per block and added once per block.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <new>
+
+#include "sg_internal.cuh"
+#include "stdgpu_gb300.h"
+#include "stdgpu_gb300/detail/layout.cuh"
+#include "stdgpu_gb300/device.cuh"
+
+namespace sg
+{
+namespace detail
+{
+
+std::atomic<long long> g_launches{ 0 };
+
+constexpr int kThreads = 256;
+constexpr int kRangeChunk = 2048; // slots per block in the compaction kernels (256 threads x 8 slots)
+
+struct dview
+{
+    char* slots;
+    table_header* hdr;
+    int64_t num_groups;
+    int64_t total;
+    int bits;
+};
+
+// ---------------------------------------------------------------- geometry
+
+// bit_ceil over size_t: src/stdgpu/impl/bit_detail.h:36-62
+inline uint64_t
+bit_ceil_u64(uint64_t x)
+{
+    uint64_t r = 1;
+    while (r < x && r != 0)
+    {
+        r <<= 1;
+    }
+    return r;
+}
+
+// createDeviceObject geometry: src/stdgpu/impl/unordered_base_detail.cuh:1264-1273 and
+// expected_collisions :34-48, evaluated with the same float / long double steps.
+inline void
+reference_geometry(int64_t capacity, int64_t* bucket_count, int64_t* excess_count)
+{
+    const float c = std::ceil(static_cast<float>(capacity) / 1.0F);
+    const uint64_t b = bit_ceil_u64(static_cast<uint64_t>(c));
+    const long double k = static_cast<long double>(b);
+    const long double n = static_cast<long double>(capacity);
+    const int64_t e = static_cast<int64_t>(std::ceil(n * (1.0L - std::pow(1.0L - (1.0L / k), n - 1.0L))));
+    *bucket_count = static_cast<int64_t>(b);
+    *excess_count = e + 1;
+}
+
+inline int
+log2_exact(int64_t x)
+{
+    int b = 0;
+    while ((int64_t{ 1 } << b) < x)
+    {
+        ++b;
+    }
+    return b;
+}
+
+// ---------------------------------------------------------------- device helpers
+
+SG_D uint4
+load_lane(const dview& t, int64_t g, int tl)
+{
+    return __ldcg(reinterpret_cast<const uint4*>(t.slots + g * kGroupBytes) + tl);
+}
+
+template <int KIND>
+SG_D int64_t
+home_of(const dview& t, typename kind_consts<KIND>::K key)
+{
+    return group_of_bucket(fibonacci_bucket(static_cast<uint64_t>(key), t.bits), t.bits, t.num_groups);
+}
+
+template <typename T>
+SG_D T
+tile_shfl(unsigned mask, T v, int src)
+{
+    return __shfl_sync(mask, v, src);
+}
+
+template <int KIND>
+SG_D typename kind_consts<KIND>::K
+cas_key(const dview& t, int64_t slot, typename kind_consts<KIND>::K expected, typename kind_consts<KIND>::K desired)
+{
+    using K = typename kind_consts<KIND>::K;
+    char* p = t.slots + slot * kind_consts<KIND>::slot_bytes;
+    if constexpr (sizeof(K) == 8)
+    {
+        return static_cast<K>(atomicCAS(reinterpret_cast<unsigned long long*>(p),
+                                        static_cast<unsigned long long>(expected),
+                                        static_cast<unsigned long long>(desired)));
+    }
+    else
+    {
+        return static_cast<K>(atomicCAS(reinterpret_cast<unsigned int*>(p),
+                                        static_cast<unsigned int>(expected),
+                                        static_cast<unsigned int>(desired)));
+    }
+}
+
+template <int KIND>
+SG_D void
+store_value(const dview& t, int64_t slot, typename kind_consts<KIND>::V v)
+{
+    if constexpr (kind_traits<KIND>::is_map)
+    {
+        using V = typename kind_consts<KIND>::V;
+        *reinterpret_cast<V*>(t.slots + slot * kind_consts<KIND>::slot_bytes + kind_traits<KIND>::val_offset) = v;
+    }
+}
+
+// Input element i: value_type array (AoS) or separate key / mapped arrays.
+template <int KIND, bool AOS>
+SG_D void
+load_input(const void* in0, const void* in1, int64_t i, typename kind_consts<KIND>::K& key,
+           typename kind_consts<KIND>::V& val)
+{
+    using K = typename kind_consts<KIND>::K;
+    using V = typename kind_consts<KIND>::V;
+    constexpr int sb = kind_consts<KIND>::slot_bytes;
+    if constexpr (AOS)
+    {
+        if constexpr (sb == 16)
+        {
+            const uint4 d = __ldcs(reinterpret_cast<const uint4*>(in0) + i);
+            key = key_in_lane<KIND>(d, 0);
+            val = value_in_lane<KIND>(d, 0);
+        }
+        else if constexpr (sb == 8)
+        {
+            const uint2 d = __ldcs(reinterpret_cast<const uint2*>(in0) + i);
+            const uint4 q = make_uint4(d.x, d.y, 0u, 0u);
+            key = key_in_lane<KIND>(q, 0);
+            val = value_in_lane<KIND>(q, 0);
+        }
+        else
+        {
+            key = static_cast<K>(__ldcs(reinterpret_cast<const unsigned int*>(in0) + i));
+            val = V{};
+        }
+    }
+    else
+    {
+        key = __ldcs(reinterpret_cast<const K*>(in0) + i);
+        if constexpr (kind_traits<KIND>::is_map)
+        {
+            val = in1 != nullptr ? __ldcs(reinterpret_cast<const V*>(in1) + i) : V{};
+        }
+        else
+        {
+            val = V{};
+        }
+    }
+}
+
+// Out-of-band keys (EMPTY- or TOMB-valued): presence in the header, storage in the tail group.
+template <int KIND>
+SG_D int
+special_insert(const dview& t, typename kind_consts<KIND>::K key, typename kind_consts<KIND>::V val)
+{
+    using C = kind_consts<KIND>;
+    const int s = key == C::empty_key ? 0 : 1;
+    if (atomicCAS(&t.hdr->special_state[s], 0u, 2u) != 0u)
+    {
+        return 0;
+    }
+    const int64_t slot = t.num_groups * C::slots_per_group + s;
+    *reinterpret_cast<typename C::K*>(t.slots + slot * C::slot_bytes) = key;
+    store_value<KIND>(t, slot, val);
+    __threadfence();
+    atomicExch(&t.hdr->special_state[s], 1u);
+    return 1;
+}
+
+template <int KIND>
+SG_D bool
+special_find(const dview& t, typename kind_consts<KIND>::K key, typename kind_consts<KIND>::V& val)
+{
+    using C = kind_consts<KIND>;
+    const int s = key == C::empty_key ? 0 : 1;
+    if (*reinterpret_cast<volatile unsigned*>(&t.hdr->special_state[s]) != 1u)
+    {
+        return false;
+    }
+    const int64_t slot = t.num_groups * C::slots_per_group + s;
+    if constexpr (kind_traits<KIND>::is_map)
+    {
+        val = *reinterpret_cast<const volatile typename C::V*>(t.slots + slot * C::slot_bytes +
+                                                               kind_traits<KIND>::val_offset);
+    }
+    return true;
+}
+
+template <int KIND>
+SG_D int
+special_erase(const dview& t, typename kind_consts<KIND>::K key)
+{
+    using C = kind_consts<KIND>;
+    const int s = key == C::empty_key ? 0 : 1;
+    return atomicCAS(&t.hdr->special_state[s], 1u, 0u) == 1u ? 1 : 0;
+}
+
+// Per-lane masks of the lane's sub-slots that hold `key`, EMPTY, or a reusable TOMB.
+template <int KIND, bool WANT_TOMB>
+SG_D void
+lane_masks(const uint4& d, typename kind_consts<KIND>::K key, int64_t first_slot, int64_t total, unsigned& m_match,
+           unsigned& m_empty, unsigned& m_tomb)
+{
+    using C = kind_consts<KIND>;
+    m_match = 0;
+    m_empty = 0;
+    m_tomb = 0;
+#pragma unroll
+    for (int s = 0; s < C::slots_per_lane; ++s)
+    {
+        const typename C::K k = key_in_lane<KIND>(d, s);
+        m_match |= static_cast<unsigned>(k == key) << s;
+        m_empty |= static_cast<unsigned>(k == C::empty_key) << s;
+        if constexpr (WANT_TOMB)
+        {
+            m_tomb |= static_cast<unsigned>(k == C::tomb_key && first_slot + s < total) << s;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- tile operations
+// All 8 lanes of a tile call these together with the same key; d is this lane's
+// 16-byte share of the key's home group.  tbase = first lane of the tile.
+
+// Returns 1 inserted, 0 already present, 2 refused (no free slot in the whole table), 3 retry limit.
+template <int KIND, bool REUSE>
+SG_D int
+tile_insert(const dview& t, typename kind_consts<KIND>::K key, typename kind_consts<KIND>::V val, uint4 d,
+            unsigned tmask, int tbase, int tl, unsigned long long& tombs_reused)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    constexpr int G = C::slots_per_group;
+    constexpr int SPL = C::slots_per_lane;
+    const int64_t home = home_of<KIND>(t, key);
+    int64_t g = home;
+    int64_t free_slot = -1; // first reusable erased slot seen along the probe sequence
+    int64_t probes = 0;
+    int retries = 0;
+    while (true)
+    {
+        unsigned m_match, m_empty, m_tomb;
+        const int64_t first = g * G + tl * SPL;
+        lane_masks<KIND, REUSE>(d, key, first, t.total, m_match, m_empty, m_tomb);
+        if (__ballot_sync(tmask, m_match != 0u) != 0u)
+        {
+            return 0;
+        }
+        if constexpr (REUSE)
+        {
+            if (free_slot < 0)
+            {
+                const unsigned bt = __ballot_sync(tmask, m_tomb != 0u);
+                if (bt != 0u)
+                {
+                    const int owner = __ffs(bt) - 1;
+                    const unsigned om = __shfl_sync(tmask, m_tomb, owner);
+                    free_slot = g * G + (owner - tbase) * SPL + (__ffs(om) - 1);
+                }
+            }
+        }
+        const unsigned be = __ballot_sync(tmask, m_empty != 0u);
+        if (be != 0u)
+        {
+            int64_t target;
+            K expected;
+            if (REUSE && free_slot >= 0)
+            {
+                target = free_slot;
+                expected = C::tomb_key;
+            }
+            else
+            {
+                const int owner = __ffs(be) - 1;
+                const unsigned om = __shfl_sync(tmask, m_empty, owner);
+                target = g * G + (owner - tbase) * SPL + (__ffs(om) - 1);
+                expected = C::empty_key;
+            }
+            K old = expected;
+            if (tl == 0)
+            {
+                old = cas_key<KIND>(t, target, expected, key);
+                if (old == expected)
+                {
+                    store_value<KIND>(t, target, val);
+                    if (expected == C::tomb_key)
+                    {
+                        ++tombs_reused;
+                    }
+                }
+            }
+            old = __shfl_sync(tmask, old, tbase);
+            if (old == expected)
+            {
+                return 1;
+            }
+            if (old == key)
+            {
+                return 0;
+            }
+            // Another key took the slot: rescan from the slot's group (every earlier group was
+            // seen without a free slot, and free slots only disappear during an insert launch).
+            if (++retries > 65536)
+            {
+                return 3;
+            }
+            {
+                const int64_t tg = target / G;
+                probes = tg >= home ? tg - home : tg + t.num_groups - home;
+                g = tg;
+            }
+            free_slot = -1;
+            d = load_lane(t, g, tl);
+            continue;
+        }
+        if (++probes >= t.num_groups)
+        {
+            if (REUSE && free_slot >= 0)
+            {
+                // no never-used slot anywhere: claim the erased slot seen first
+                K old = C::tomb_key;
+                if (tl == 0)
+                {
+                    old = cas_key<KIND>(t, free_slot, C::tomb_key, key);
+                    if (old == C::tomb_key)
+                    {
+                        store_value<KIND>(t, free_slot, val);
+                        ++tombs_reused;
+                    }
+                }
+                old = __shfl_sync(tmask, old, tbase);
+                if (old == C::tomb_key)
+                {
+                    return 1;
+                }
+                if (old == key)
+                {
+                    return 0;
+                }
+                if (++retries > 65536)
+                {
+                    return 3;
+                }
+                g = free_slot / G;
+                probes = g >= home ? g - home : g + t.num_groups - home;
+                free_slot = -1;
+                d = load_lane(t, g, tl);
+                continue;
+            }
+            return 2;
+        }
+        g = next_group(g, t.num_groups);
+        d = load_lane(t, g, tl);
+    }
+}
+
+// Returns the slot holding key (and its mapped value via val), or -1.
+template <int KIND>
+SG_D int64_t
+tile_find(const dview& t, typename kind_consts<KIND>::K key, uint4 d, unsigned tmask, int tbase, int tl,
+          typename kind_consts<KIND>::V& val)
+{
+    using C = kind_consts<KIND>;
+    constexpr int G = C::slots_per_group;
+    constexpr int SPL = C::slots_per_lane;
+    int64_t g = home_of<KIND>(t, key);
+    for (int64_t probes = 0; probes < t.num_groups; ++probes)
+    {
+        unsigned m_match, m_empty, m_tomb;
+        lane_masks<KIND, false>(d, key, 0, 0, m_match, m_empty, m_tomb);
+        const unsigned bm = __ballot_sync(tmask, m_match != 0u);
+        if (bm != 0u)
+        {
+            const int owner = __ffs(bm) - 1;
+            const int s = __ffs(__shfl_sync(tmask, m_match, owner)) - 1;
+            typename C::V mine{};
+            if constexpr (kind_traits<KIND>::is_map)
+            {
+                mine = value_in_lane<KIND>(d, s);
+            }
+            val = __shfl_sync(tmask, mine, owner);
+            return g * G + (owner - tbase) * SPL + s;
+        }
+        if (__ballot_sync(tmask, m_empty != 0u) != 0u)
+        {
+            return -1;
+        }
+        g = next_group(g, t.num_groups);
+        d = load_lane(t, g, tl);
+    }
+    return -1;
+}
+
+// ---------------------------------------------------------------- block reduction of counters
+
+template <int N>
+SG_D void
+block_add(unsigned long long (&v)[N], unsigned long long* const (&dst)[N])
+{
+    __shared__ unsigned long long red[N][kThreads / 32];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+    {
+        unsigned long long x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            x += __shfl_xor_sync(0xffffffffu, x, o);
+        }
+        if (lane == 0)
+        {
+            red[k][warp] = x;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < N)
+    {
+        unsigned long long s = 0;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w)
+        {
+            s += red[threadIdx.x][w];
+        }
+        if (s != 0 && dst[threadIdx.x] != nullptr)
+        {
+            atomicAdd(dst[threadIdx.x], s);
+        }
+    }
+}
+
+// ---------------------------------------------------------------- kernels
+
+// Fills every slot with the never-used marker and the slots at or above total_count with the erased
+// marker; resets the header.  clear(): unordered_base_detail.cuh:1220-1252 (one launch instead of four).
+template <int KIND>
+__global__ void __launch_bounds__(kThreads)
+k_init(dview t)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    constexpr int G = C::slots_per_group;
+    const int64_t lanes_total = (t.num_groups + 1) * kTileLanes; // 16-byte units, tail group included
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    uint4* base = reinterpret_cast<uint4*>(t.slots);
+    for (int64_t u = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; u < lanes_total; u += stride)
+    {
+        const int64_t first = u * C::slots_per_lane;
+        if (first + C::slots_per_lane <= t.total || first >= t.num_groups * G)
+        {
+            base[u] = make_uint4(~0u, ~0u, ~0u, ~0u);
+        }
+        else
+        {
+            uint4 d = make_uint4(~0u, ~0u, ~0u, ~0u);
+            char* bytes = reinterpret_cast<char*>(&d);
+            for (int s = 0; s < C::slots_per_lane; ++s)
+            {
+                if (first + s >= t.total)
+                {
+                    *reinterpret_cast<K*>(bytes + s * C::slot_bytes) = C::tomb_key;
+                }
+            }
+            base[u] = d;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+        t.hdr->size = 0;
+        t.hdr->refused = 0;
+        t.hdr->tombstones = 0;
+        t.hdr->special_state[0] = 0;
+        t.hdr->special_state[1] = 0;
+        t.hdr->error = 0;
+        t.hdr->count = 0;
+    }
+}
+
+// Bulk insert: src/stdgpu/impl/unordered_base_detail.cuh:996-1017 (insert_value :470-495).
+template <int KIND, bool AOS>
+__global__ void __launch_bounds__(kThreads)
+k_insert(dview t, const void* in0, const void* in1, int64_t n, uint8_t* out_flags)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    const int lane = threadIdx.x & 31;
+    const int tbase = lane & ~7;
+    const int tl = lane & 7;
+    const unsigned tmask = 0xFFu << tbase;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    unsigned long long cnt[3] = { 0, 0, 0 }; // inserted, refused, erased slots reused
+    unsigned long long retry = 0;
+    for (int64_t base = warp * 32; base < n; base += nwarps * 32)
+    {
+        const int64_t i = base + lane;
+        const bool valid = i < n;
+        K key = C::empty_key;
+        V val{};
+        if (valid)
+        {
+            load_input<KIND, AOS>(in0, in1, i, key, val);
+        }
+        const bool special = valid && key >= C::tomb_key;
+        int res = 0;
+        if (special)
+        {
+            res = special_insert<KIND>(t, key, val);
+        }
+        const bool probe = valid && !special;
+        uint4 pre[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+        {
+            const K kj = tile_shfl(tmask, key, tbase + j);
+            const bool pj = __shfl_sync(tmask, probe, tbase + j);
+            if (pj)
+            {
+                pre[j] = load_lane(t, home_of<KIND>(t, kj), tl);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+        {
+            const K kj = tile_shfl(tmask, key, tbase + j);
+            const V vj = tile_shfl(tmask, val, tbase + j);
+            const bool pj = __shfl_sync(tmask, probe, tbase + j);
+            if (pj)
+            {
+                const int r = tile_insert<KIND, true>(t, kj, vj, pre[j], tmask, tbase, tl, cnt[2]);
+                if (tl == j)
+                {
+                    res = r;
+                }
+            }
+        }
+        if (valid)
+        {
+            cnt[0] += (res == 1);
+            cnt[1] += (res == 2);
+            retry += (res == 3);
+            if (out_flags != nullptr)
+            {
+                out_flags[i] = static_cast<uint8_t>(res == 1);
+            }
+        }
+    }
+    if (retry != 0)
+    {
+        atomicOr(&t.hdr->error, kErrRetry);
+    }
+    // size += inserted; refused += refused; tombstones -= reused
+    unsigned long long neg_reused = 0ull - cnt[2];
+    unsigned long long v[3] = { cnt[0], cnt[1], neg_reused };
+    unsigned long long* const dst[3] = { &t.hdr->size, &t.hdr->refused, &t.hdr->tombstones };
+    block_add<3>(v, dst);
+}
+
+// Bulk erase: src/stdgpu/impl/unordered_base_detail.cuh:1045-1066 (erase_from_key :497-522).
+template <int KIND>
+__global__ void __launch_bounds__(kThreads)
+k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    const int lane = threadIdx.x & 31;
+    const int tbase = lane & ~7;
+    const int tl = lane & 7;
+    const unsigned tmask = 0xFFu << tbase;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    unsigned long long erased = 0, erased_oob = 0;
+    for (int64_t base = warp * 32; base < n; base += nwarps * 32)
+    {
+        const int64_t i = base + lane;
+        const bool valid = i < n;
+        K key = valid ? __ldcs(reinterpret_cast<const K*>(keys) + i) : C::empty_key;
+        const bool special = valid && key >= C::tomb_key;
+        int res = 0;
+        if (special)
+        {
+            res = special_erase<KIND>(t, key);
+            erased_oob += static_cast<unsigned long long>(res);
+        }
+        const bool probe = valid && !special;
+        uint4 pre[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+        {
+            const K kj = tile_shfl(tmask, key, tbase + j);
+            if (__shfl_sync(tmask, probe, tbase + j))
+            {
+                pre[j] = load_lane(t, home_of<KIND>(t, kj), tl);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+        {
+            const K kj = tile_shfl(tmask, key, tbase + j);
+            if (__shfl_sync(tmask, probe, tbase + j))
+            {
+                V dummy{};
+                const int64_t slot = tile_find<KIND>(t, kj, pre[j], tmask, tbase, tl, dummy);
+                int r = 0;
+                if (slot >= 0)
+                {
+                    K old = kj;
+                    if (tl == 0)
+                    {
+                        old = cas_key<KIND>(t, slot, kj, C::tomb_key);
+                    }
+                    old = __shfl_sync(tmask, old, tbase);
+                    r = old == kj ? 1 : 0;
+                }
+                if (tl == j)
+                {
+                    res = r;
+                }
+            }
+        }
+        if (valid)
+        {
+            erased += static_cast<unsigned long long>(res);
+            if (out_flags != nullptr)
+            {
+                out_flags[i] = static_cast<uint8_t>(res);
+            }
+        }
+    }
+    unsigned long long v[2] = { 0ull - erased, erased - erased_oob };
+    unsigned long long* const dst[2] = { &t.hdr->size, &t.hdr->tombstones };
+    block_add<2>(v, dst);
+}
+
+// Bulk find / contains (device-only find/contains in the reference, :619-706).
+template <int KIND, bool WANT_VALUES>
+__global__ void __launch_bounds__(kThreads)
+k_find(dview t, const void* keys, int64_t n, void* out_vals, uint8_t* out_found)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    const int lane = threadIdx.x & 31;
+    const int tbase = lane & ~7;
+    const int tl = lane & 7;
+    const unsigned tmask = 0xFFu << tbase;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t base = warp * 32; base < n; base += nwarps * 32)
+    {
+        const int64_t i = base + lane;
+        const bool valid = i < n;
+        K key = valid ? __ldcs(reinterpret_cast<const K*>(keys) + i) : C::empty_key;
+        const bool special = valid && key >= C::tomb_key;
+        bool found = false;
+        V val{};
+        if (special)
+        {
+            found = special_find<KIND>(t, key, val);
+        }
+        const bool probe = valid && !special;
+        uint4 pre[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+        {
+            const K kj = tile_shfl(tmask, key, tbase + j);
+            if (__shfl_sync(tmask, probe, tbase + j))
+            {
+                pre[j] = load_lane(t, home_of<KIND>(t, kj), tl);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+        {
+            const K kj = tile_shfl(tmask, key, tbase + j);
+            if (__shfl_sync(tmask, probe, tbase + j))
+            {
+                V vj{};
+                const int64_t slot = tile_find<KIND>(t, kj, pre[j], tmask, tbase, tl, vj);
+                if (tl == j)
+                {
+                    found = slot >= 0;
+                    val = vj;
+                }
+            }
+        }
+        if (valid)
+        {
+            if (out_found != nullptr)
+            {
+                __stcs(out_found + i, static_cast<uint8_t>(found));
+            }
+            if constexpr (WANT_VALUES && kind_traits<KIND>::is_map)
+            {
+                if (found && out_vals != nullptr)
+                {
+                    __stcs(reinterpret_cast<V*>(out_vals) + i, val);
+                }
+            }
+        }
+    }
+}
+
+// valid(): every stored key is found at its own slot by its probe sequence, unused tail slots still hold
+// the erased marker, and the stored-key count plus out-of-band keys equals size().
+template <int KIND>
+__global__ void __launch_bounds__(kThreads)
+k_valid(dview t, sg_unordered_view v, unsigned long long* bad)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    constexpr int G = C::slots_per_group;
+    unordered_ref<KIND> ref{ v };
+    const int64_t nslots = t.num_groups * G;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    unsigned long long live = 0, wrong = 0;
+    for (int64_t s = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; s < nslots; s += stride)
+    {
+        const K k = __ldcg(reinterpret_cast<const K*>(t.slots + s * C::slot_bytes));
+        if (s >= t.total)
+        {
+            wrong += (k != C::tomb_key);
+            continue;
+        }
+        if (k == C::empty_key || k == C::tomb_key)
+        {
+            continue;
+        }
+        ++live;
+        wrong += (ref.find_slot(k) != s);
+    }
+    unsigned long long vv[2] = { live, wrong };
+    unsigned long long* const dst[2] = { &t.hdr->count, bad };
+    block_add<2>(vv, dst);
+}
+
+// Compaction, pass 1: live slots per chunk of kRangeChunk slots.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads)
+k_range_count(dview t, unsigned int* chunk_counts)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    const int64_t c = blockIdx.x;
+    const int64_t first = c * kRangeChunk;
+    const int64_t limit = t.total;
+    unsigned int live = 0;
+#pragma unroll
+    for (int r = 0; r < kRangeChunk / kThreads; ++r)
+    {
+        const int64_t s = first + r * kThreads + threadIdx.x;
+        if (s < limit)
+        {
+            const K k = __ldcg(reinterpret_cast<const K*>(t.slots + s * C::slot_bytes));
+            live += (k != C::empty_key && k != C::tomb_key);
+        }
+    }
+    __shared__ unsigned int red[kThreads / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        live += __shfl_xor_sync(0xffffffffu, live, o);
+    }
+    if ((threadIdx.x & 31) == 0)
+    {
+        red[threadIdx.x >> 5] = live;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        unsigned int s = 0;
+        for (int w = 0; w < kThreads / 32; ++w)
+        {
+            s += red[w];
+        }
+        chunk_counts[c] = s;
+    }
+}
+
+// Compaction, pass 2: exclusive scan of the chunk counts (one block), then the out-of-band keys are
+// appended after the probed ones; the total lands in hdr->count.
+__global__ void __launch_bounds__(1024)
+k_range_scan(unsigned int* chunk_counts, int64_t nchunks, table_header* hdr, int32_t* out_slots,
+             int64_t special_base, int want_slots)
+{
+    __shared__ unsigned long long part[1024];
+    const int64_t per = (nchunks + blockDim.x - 1) / blockDim.x;
+    const int64_t lo = threadIdx.x * per;
+    const int64_t hi = lo + per < nchunks ? lo + per : nchunks;
+    unsigned long long s = 0;
+    for (int64_t c = lo; c < hi; ++c)
+    {
+        s += chunk_counts[c];
+    }
+    part[threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        unsigned long long run = 0;
+        for (int w = 0; w < static_cast<int>(blockDim.x); ++w)
+        {
+            const unsigned long long x = part[w];
+            part[w] = run;
+            run += x;
+        }
+        unsigned long long total = run;
+        for (int sp = 0; sp < 2; ++sp)
+        {
+            if (hdr->special_state[sp] == 1u)
+            {
+                if (want_slots && out_slots != nullptr)
+                {
+                    out_slots[total] = static_cast<int32_t>(special_base + sp);
+                }
+                ++total;
+            }
+        }
+        hdr->count = total;
+    }
+    __syncthreads();
+    unsigned long long run = part[threadIdx.x];
+    for (int64_t c = lo; c < hi; ++c)
+    {
+        const unsigned int x = chunk_counts[c];
+        chunk_counts[c] = static_cast<unsigned int>(run);
+        run += x;
+    }
+}
+
+// Compaction, pass 3: write slot indices (or keys / mapped values) of live slots in slot order.
+template <int KIND, bool SLOTS>
+__global__ void __launch_bounds__(kThreads)
+k_range_write(dview t, const unsigned int* chunk_offsets, int32_t* out_slots, void* out_keys, void* out_vals)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    const int64_t c = blockIdx.x;
+    const int64_t first = c * kRangeChunk;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    __shared__ unsigned int warp_base[kThreads / 32];
+    __shared__ unsigned int round_base;
+    if (threadIdx.x == 0)
+    {
+        round_base = chunk_offsets[c];
+    }
+    __syncthreads();
+    for (int r = 0; r < kRangeChunk / kThreads; ++r)
+    {
+        const int64_t s = first + r * kThreads + threadIdx.x;
+        bool live = false;
+        K k = C::empty_key;
+        if (s < t.total)
+        {
+            k = __ldcg(reinterpret_cast<const K*>(t.slots + s * C::slot_bytes));
+            live = (k != C::empty_key && k != C::tomb_key);
+        }
+        const unsigned b = __ballot_sync(0xffffffffu, live);
+        if (lane == 0)
+        {
+            warp_base[warp] = __popc(b);
+        }
+        __syncthreads();
+        unsigned int before = round_base;
+        for (int w = 0; w < warp; ++w)
+        {
+            before += warp_base[w];
+        }
+        if (live)
+        {
+            const unsigned int pos = before + __popc(b & ((1u << lane) - 1u));
+            if constexpr (SLOTS)
+            {
+                out_slots[pos] = static_cast<int32_t>(s);
+            }
+            else
+            {
+                if (out_keys != nullptr)
+                {
+                    reinterpret_cast<K*>(out_keys)[pos] = k;
+                }
+                if constexpr (kind_traits<KIND>::is_map)
+                {
+                    if (out_vals != nullptr)
+                    {
+                        reinterpret_cast<V*>(out_vals)[pos] = *reinterpret_cast<const V*>(
+                                t.slots + s * C::slot_bytes + kind_traits<KIND>::val_offset);
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+        {
+            unsigned int add = 0;
+            for (int w = 0; w < kThreads / 32; ++w)
+            {
+                add += warp_base[w];
+            }
+            round_base += add;
+        }
+        __syncthreads();
+    }
+}
+
+// Appends the out-of-band keys (keys / mapped values) after the probed ones.
+template <int KIND>
+__global__ void
+k_range_specials(dview t, const unsigned int* chunk_offsets, int64_t nchunks, const unsigned int* last_count,
+                 void* out_keys, void* out_vals)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    unsigned long long pos = static_cast<unsigned long long>(chunk_offsets[nchunks - 1]) + *last_count;
+    for (int sp = 0; sp < 2; ++sp)
+    {
+        if (t.hdr->special_state[sp] == 1u)
+        {
+            const int64_t slot = t.num_groups * C::slots_per_group + sp;
+            if (out_keys != nullptr)
+            {
+                reinterpret_cast<K*>(out_keys)[pos] = sp == 0 ? C::empty_key : C::tomb_key;
+            }
+            if constexpr (kind_traits<KIND>::is_map)
+            {
+                if (out_vals != nullptr)
+                {
+                    reinterpret_cast<V*>(out_vals)[pos] =
+                            *reinterpret_cast<const V*>(t.slots + slot * C::slot_bytes + kind_traits<KIND>::val_offset);
+                }
+            }
+            ++pos;
+        }
+    }
+}
+
+} // namespace detail
+} // namespace sg
+
+// ====================================================================== host side
+
+using namespace sg::detail;
+
+struct sg_unordered
+{
+    int32_t kind;
+    int32_t slot_bytes;
+    int64_t capacity;
+    int64_t bucket_count;
+    int64_t excess_count;
+    int64_t total;
+    int64_t num_groups;
+    int bits;
+    char* slots;
+    table_header* hdr;
+    unsigned int* chunk_counts; // compaction scratch: one count per kRangeChunk slots, plus one
+    int64_t nchunks;
+    unsigned long long* host_hdr; // pinned mirror for synchronous reads
+    int device;
+};
+
+namespace
+{
+
+bool
+kind_ok(int32_t kind)
+{
+    return kind >= SG_SET_U32 && kind <= SG_MAP_U32_U64;
+}
+
+dview
+view_of(const sg_unordered* t)
+{
+    return dview{ t->slots, t->hdr, t->num_groups, t->total, t->bits };
+}
+
+sg_unordered_view
+public_view(const sg_unordered* t)
+{
+    sg_unordered_view v{};
+    v.slots = t->slots;
+    v.header = t->hdr;
+    v.num_groups = t->num_groups;
+    v.total_count = t->total;
+    v.bucket_count = t->bucket_count;
+    v.bucket_bits = t->bits;
+    v.kind = t->kind;
+    return v;
+}
+
+void
+fill_geometry(int32_t kind, int64_t capacity, sg_geometry* g)
+{
+    int64_t b = 0, e = 0;
+    reference_geometry(capacity, &b, &e);
+    const int sb = slot_bytes_of_kind(kind);
+    const int spg = kGroupBytes / sb;
+    g->capacity = capacity;
+    g->bucket_count = b;
+    g->excess_count = e;
+    g->max_size = b + e;
+    g->num_groups = (g->max_size + spg - 1) / spg;
+    g->slot_bytes = sb;
+    g->slots_per_group = spg;
+    const int64_t nchunks = (g->max_size + kRangeChunk - 1) / kRangeChunk;
+    g->storage_bytes = (g->num_groups + 1) * kGroupBytes + static_cast<int64_t>(sizeof(table_header)) +
+                       (nchunks + 1) * 4;
+}
+
+// Kernel dispatch over the six kinds.
+template <template <int> class F, typename... Args>
+sg_status
+dispatch(int32_t kind, Args&&... args)
+{
+    switch (kind)
+    {
+        case 0:
+            return F<0>::run(args...);
+        case 1:
+            return F<1>::run(args...);
+        case 2:
+            return F<2>::run(args...);
+        case 3:
+            return F<3>::run(args...);
+        case 4:
+            return F<4>::run(args...);
+        case 5:
+            return F<5>::run(args...);
+        default:
+            return SG_ERR_BAD_ARG;
+    }
+}
+
+template <int KIND>
+struct do_init
+{
+    static sg_status
+    run(sg_unordered* t, cudaStream_t s)
+    {
+        static const int max_grid = persistent_grid(k_init<KIND>, kThreads);
+        const int64_t units = (t->num_groups + 1) * kTileLanes;
+        k_init<KIND><<<grid_for(units, kThreads, max_grid), kThreads, 0, s>>>(view_of(t));
+        SG_LAUNCH_CHECK();
+        return SG_OK;
+    }
+};
+
+template <int KIND>
+struct do_insert
+{
+    static sg_status
+    run(sg_unordered* t, const void* in0, const void* in1, bool aos, int64_t n, uint8_t* flags, cudaStream_t s)
+    {
+        if (aos)
+        {
+            static const int max_grid = persistent_grid(k_insert<KIND, true>, kThreads);
+            k_insert<KIND, true><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), in0, in1, n, flags);
+        }
+        else
+        {
+            static const int max_grid = persistent_grid(k_insert<KIND, false>, kThreads);
+            k_insert<KIND, false><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), in0, in1, n, flags);
+        }
+        SG_LAUNCH_CHECK();
+        return SG_OK;
+    }
+};
+
+template <int KIND>
+struct do_erase
+{
+    static sg_status
+    run(sg_unordered* t, const void* keys, int64_t n, uint8_t* flags, cudaStream_t s)
+    {
+        static const int max_grid = persistent_grid(k_erase<KIND>, kThreads);
+        k_erase<KIND><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n, flags);
+        SG_LAUNCH_CHECK();
+        return SG_OK;
+    }
+};
+
+template <int KIND>
+struct do_find
+{
+    static sg_status
+    run(sg_unordered* t, const void* keys, int64_t n, void* vals, uint8_t* found, cudaStream_t s)
+    {
+        if (vals != nullptr)
+        {
+            static const int max_grid = persistent_grid(k_find<KIND, true>, kThreads);
+            k_find<KIND, true><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n, vals, found);
+        }
+        else
+        {
+            static const int max_grid = persistent_grid(k_find<KIND, false>, kThreads);
+            k_find<KIND, false><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n, vals, found);
+        }
+        SG_LAUNCH_CHECK();
+        return SG_OK;
+    }
+};
+
+template <int KIND>
+struct do_valid
+{
+    static sg_status
+    run(sg_unordered* t, unsigned long long* bad, cudaStream_t s)
+    {
+        static const int max_grid = persistent_grid(k_valid<KIND>, kThreads);
+        const int64_t nslots = t->num_groups * (kGroupBytes / t->slot_bytes);
+        k_valid<KIND><<<grid_for(nslots, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), public_view(t), bad);
+        SG_LAUNCH_CHECK();
+        return SG_OK;
+    }
+};
+
+template <int KIND>
+struct do_range
+{
+    static sg_status
+    run(sg_unordered* t, int32_t* out_slots, void* out_keys, void* out_vals, cudaStream_t s)
+    {
+        const int64_t nch = t->nchunks;
+        k_range_count<KIND><<<static_cast<unsigned>(nch), kThreads, 0, s>>>(view_of(t), t->chunk_counts);
+        SG_LAUNCH_CHECK();
+        // keep the last chunk's count for the tail append before the scan overwrites it
+        SG_CUDA_TRY(cudaMemcpyAsync(t->chunk_counts + nch, t->chunk_counts + nch - 1, sizeof(unsigned int),
+                                    cudaMemcpyDeviceToDevice, s));
+        const int64_t special_base = t->num_groups * (kGroupBytes / t->slot_bytes);
+        k_range_scan<<<1, 1024, 0, s>>>(t->chunk_counts, nch, t->hdr, out_slots, special_base, out_slots != nullptr);
+        SG_LAUNCH_CHECK();
+        if (out_slots != nullptr)
+        {
+            k_range_write<KIND, true><<<static_cast<unsigned>(nch), kThreads, 0, s>>>(view_of(t), t->chunk_counts,
+                                                                                      out_slots, nullptr, nullptr);
+            SG_LAUNCH_CHECK();
+        }
+        else
+        {
+            k_range_write<KIND, false><<<static_cast<unsigned>(nch), kThreads, 0, s>>>(view_of(t), t->chunk_counts,
+                                                                                       nullptr, out_keys, out_vals);
+            SG_LAUNCH_CHECK();
+            k_range_specials<KIND><<<1, 1, 0, s>>>(view_of(t), t->chunk_counts, nch, t->chunk_counts + nch, out_keys,
+                                                   out_vals);
+            SG_LAUNCH_CHECK();
+        }
+        return SG_OK;
+    }
+};
+
+sg_status
+read_header(sg_unordered* t, cudaStream_t s)
+{
+    SG_CUDA_TRY(cudaMemcpyAsync(t->host_hdr, t->hdr, sizeof(table_header), cudaMemcpyDeviceToHost, s));
+    SG_CUDA_TRY(cudaStreamSynchronize(s));
+    return SG_OK;
+}
+
+const table_header&
+host_header(const sg_unordered* t)
+{
+    return *reinterpret_cast<const table_header*>(t->host_hdr);
+}
+
+} // namespace
+
+extern "C" {
+
+sg_status
+sg_unordered_geometry_for(int32_t kind, int64_t capacity, sg_geometry* out)
+{
+    if (!kind_ok(kind) || capacity <= 0 || out == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    fill_geometry(kind, capacity, out);
+    if (out->max_size >= (int64_t{ 1 } << 31))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    return SG_OK;
+}
+
+sg_status
+sg_unordered_create(int32_t kind, int64_t capacity, void* stream, sg_unordered** out)
+{
+    if (out == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    *out = nullptr;
+    sg_geometry g{};
+    sg_status st = sg_unordered_geometry_for(kind, capacity, &g);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+    {
+        return SG_ERR_NO_DEVICE;
+    }
+    auto* t = new (std::nothrow) sg_unordered{};
+    if (t == nullptr)
+    {
+        return SG_ERR_OOM;
+    }
+    t->kind = kind;
+    t->slot_bytes = g.slot_bytes;
+    t->capacity = capacity;
+    t->bucket_count = g.bucket_count;
+    t->excess_count = g.excess_count;
+    t->total = g.max_size;
+    t->num_groups = g.num_groups;
+    t->bits = log2_exact(g.bucket_count);
+    t->nchunks = (t->total + kRangeChunk - 1) / kRangeChunk;
+    t->device = dev;
+    cudaError_t e = cudaMalloc(&t->slots, static_cast<size_t>((t->num_groups + 1) * kGroupBytes));
+    if (e == cudaSuccess)
+    {
+        e = cudaMalloc(&t->hdr, sizeof(table_header));
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaMalloc(&t->chunk_counts, static_cast<size_t>(t->nchunks + 1) * sizeof(unsigned int));
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaMallocHost(&t->host_hdr, sizeof(table_header));
+    }
+    if (e != cudaSuccess)
+    {
+        sg_unordered_destroy(t);
+        cudaGetLastError();
+        return e == cudaErrorMemoryAllocation ? SG_ERR_OOM : SG_ERR_CUDA;
+    }
+    st = dispatch<do_init>(kind, t, as_stream(stream));
+    if (st != SG_OK)
+    {
+        sg_unordered_destroy(t);
+        return st;
+    }
+    *out = t;
+    return SG_OK;
+}
+
+sg_status
+sg_unordered_destroy(sg_unordered* t)
+{
+    if (t == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    cudaError_t e = cudaSuccess;
+    if (t->slots != nullptr || t->hdr != nullptr)
+    {
+        e = cudaDeviceSynchronize();
+    }
+    if (t->slots != nullptr)
+    {
+        cudaFree(t->slots);
+    }
+    if (t->hdr != nullptr)
+    {
+        cudaFree(t->hdr);
+    }
+    if (t->chunk_counts != nullptr)
+    {
+        cudaFree(t->chunk_counts);
+    }
+    if (t->host_hdr != nullptr)
+    {
+        cudaFreeHost(t->host_hdr);
+    }
+    delete t;
+    return e == cudaSuccess ? SG_OK : SG_ERR_CUDA;
+}
+
+sg_status
+sg_unordered_insert(sg_unordered* t, const void* values, int64_t n, uint8_t* out_inserted, void* stream)
+{
+    if (t == nullptr || n < 0 || (n > 0 && values == nullptr))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    return dispatch<do_insert>(t->kind, t, values, nullptr, true, n, out_inserted, as_stream(stream));
+}
+
+sg_status
+sg_unordered_insert_kv(sg_unordered* t, const void* keys, const void* mapped, int64_t n, uint8_t* out_inserted,
+                       void* stream)
+{
+    if (t == nullptr || n < 0 || (n > 0 && keys == nullptr))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    return dispatch<do_insert>(t->kind, t, keys, mapped, false, n, out_inserted, as_stream(stream));
+}
+
+sg_status
+sg_unordered_erase(sg_unordered* t, const void* keys, int64_t n, uint8_t* out_erased, void* stream)
+{
+    if (t == nullptr || n < 0 || (n > 0 && keys == nullptr))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    return dispatch<do_erase>(t->kind, t, keys, n, out_erased, as_stream(stream));
+}
+
+sg_status
+sg_unordered_find(sg_unordered* t, const void* keys, int64_t n, void* out_mapped, uint8_t* out_found, void* stream)
+{
+    if (t == nullptr || n < 0 || (n > 0 && keys == nullptr))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    const bool is_map = t->kind >= SG_MAP_U64_U32;
+    return dispatch<do_find>(t->kind, t, keys, n, is_map ? out_mapped : nullptr, out_found, as_stream(stream));
+}
+
+sg_status
+sg_unordered_contains(sg_unordered* t, const void* keys, int64_t n, uint8_t* out_flags, void* stream)
+{
+    if (t == nullptr || n < 0 || (n > 0 && (keys == nullptr || out_flags == nullptr)))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    return dispatch<do_find>(t->kind, t, keys, n, nullptr, out_flags, as_stream(stream));
+}
+
+sg_status
+sg_unordered_size(sg_unordered* t, void* stream, int64_t* out_size)
+{
+    if (t == nullptr || out_size == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    sg_status st = read_header(t, as_stream(stream));
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    *out_size = static_cast<int64_t>(host_header(t).size);
+    return (host_header(t).error & kErrRetry) != 0u ? SG_ERR_RETRY_EXHAUSTED : SG_OK;
+}
+
+sg_status
+sg_unordered_status(sg_unordered* t, void* stream, int64_t* out_refused, int64_t* out_tombstones)
+{
+    if (t == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    sg_status st = read_header(t, as_stream(stream));
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    const table_header& h = host_header(t);
+    if (out_refused != nullptr)
+    {
+        *out_refused = static_cast<int64_t>(h.refused);
+    }
+    if (out_tombstones != nullptr)
+    {
+        *out_tombstones = static_cast<int64_t>(h.tombstones);
+    }
+    if (h.refused != 0)
+    {
+        SG_CUDA_TRY(cudaMemsetAsync(&t->hdr->refused, 0, sizeof(unsigned long long), as_stream(stream)));
+        return SG_ERR_FULL;
+    }
+    return (h.error & kErrRetry) != 0u ? SG_ERR_RETRY_EXHAUSTED : SG_OK;
+}
+
+sg_status
+sg_unordered_clear(sg_unordered* t, void* stream)
+{
+    if (t == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    return dispatch<do_init>(t->kind, t, as_stream(stream));
+}
+
+sg_status
+sg_unordered_valid(sg_unordered* t, void* stream, int32_t* out_valid)
+{
+    if (t == nullptr || out_valid == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    cudaStream_t s = as_stream(stream);
+    // hdr->count accumulates live slots; pad1[0] accumulates violations
+    SG_CUDA_TRY(cudaMemsetAsync(&t->hdr->count, 0, 3 * sizeof(unsigned long long), s));
+    sg_status st = dispatch<do_valid>(t->kind, t, &t->hdr->pad1[0], s);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    st = read_header(t, s);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    const table_header& h = host_header(t);
+    unsigned long long specials = 0;
+    bool ok = true;
+    for (int sp = 0; sp < 2; ++sp)
+    {
+        ok = ok && (h.special_state[sp] <= 1u);
+        specials += (h.special_state[sp] == 1u);
+    }
+    ok = ok && h.pad1[0] == 0 && (h.count + specials == h.size);
+    *out_valid = ok ? 1 : 0;
+    return SG_OK;
+}
+
+sg_status
+sg_unordered_device_range(sg_unordered* t, int32_t* out_slots, void* stream, int64_t* out_n)
+{
+    if (t == nullptr || out_slots == nullptr || out_n == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    cudaStream_t s = as_stream(stream);
+    sg_status st = dispatch<do_range>(t->kind, t, out_slots, nullptr, nullptr, s);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    st = read_header(t, s);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    *out_n = static_cast<int64_t>(host_header(t).count);
+    return SG_OK;
+}
+
+sg_status
+sg_unordered_range_copy(sg_unordered* t, void* out_keys, void* out_mapped, void* stream, int64_t* out_n)
+{
+    if (t == nullptr || out_n == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    cudaStream_t s = as_stream(stream);
+    const bool is_map = t->kind >= SG_MAP_U64_U32;
+    sg_status st = dispatch<do_range>(t->kind, t, nullptr, out_keys, is_map ? out_mapped : nullptr, s);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    st = read_header(t, s);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    *out_n = static_cast<int64_t>(host_header(t).count);
+    return SG_OK;
+}
+
+sg_status
+sg_unordered_bucket(const sg_unordered* t, const void* key, int64_t* out_bucket)
+{
+    if (t == nullptr || key == nullptr || out_bucket == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    uint64_t k = 0;
+    if (t->kind == SG_SET_U32 || t->kind == SG_MAP_U32_U32 || t->kind == SG_MAP_U32_U64)
+    {
+        k = *static_cast<const uint32_t*>(key);
+    }
+    else
+    {
+        k = *static_cast<const uint64_t*>(key);
+    }
+    *out_bucket = static_cast<int64_t>(fibonacci_bucket(k, t->bits));
+    return SG_OK;
+}
+
+sg_status
+sg_unordered_geometry(const sg_unordered* t, sg_geometry* out)
+{
+    if (t == nullptr || out == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    fill_geometry(t->kind, t->capacity, out);
+    return SG_OK;
+}
+
+sg_status
+sg_unordered_view_of(const sg_unordered* t, sg_unordered_view* out)
+{
+    if (t == nullptr || out == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    *out = public_view(t);
+    return SG_OK;
+}
+
+int64_t
+sg_kernel_launch_count(void)
+{
+    return g_launches.load(std::memory_order_relaxed);
+}
+
+const char*
+sg_status_string(sg_status s)
+{
+    switch (s)
+    {
+        case SG_OK:
+            return "ok";
+        case SG_ERR_FULL:
+            return "container full: elements were refused";
+        case SG_ERR_BAD_ARG:
+            return "bad argument";
+        case SG_ERR_OOM:
+            return "device allocation failed";
+        case SG_ERR_BUDGET:
+            return "refused by the memory budget";
+        case SG_ERR_RETRY_EXHAUSTED:
+            return "a bounded device wait or retry gave up";
+        case SG_ERR_CUDA:
+            return "CUDA runtime error";
+        case SG_ERR_NO_DEVICE:
+            return "no usable device";
+        default:
+            return "unknown status";
+    }
+}
+
+} // extern "C"

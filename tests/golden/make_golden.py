@@ -1,0 +1,180 @@
+"""Regenerates the golden fixtures in tests/golden/ by running the reference library itself.
+
+The reference (stdgpu 1.3.0) ships no golden vectors; its tests check structure
+(valid(), counts against closed forms).  These fixtures record what the
+reference's own OpenMP build answers on small seeded inputs, run with one
+thread so that every per-element outcome is deterministic:
+
+* geometry.npz       createDeviceObject(capacity) -> bucket_count, max_size
+* buckets.npz        bucket(key) for several table sizes and key patterns
+* table_<kind>.npz   insert (with duplicates) / find / erase / final contents per container kind
+* refusal.npz        inserts into tiny tables until refusal (capacity 1..8)
+* vector.npz, deque.npz, bitset.npz
+
+Usage (needs the reference tree; see oracle/build_oracle.py):
+    python tests/golden/make_golden.py
+"""
+
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+
+import oracle as O  # noqa: E402
+
+OUT = Path(__file__).resolve().parent
+
+GEOMETRY_CAPACITIES = [1, 2, 3, 4, 5, 7, 8, 9, 15, 16, 17, 31, 33, 63, 100, 127, 128, 129, 1000, 1023, 1025,
+                       4096, 10000, 65535, 65536, 65537, 100000, 131072, 1 << 20, (1 << 20) + 1, 1 << 21]
+
+
+def geometry():
+    caps, bcs, mss = [], [], []
+    for c in GEOMETRY_CAPACITIES:
+        t = O.RefTable(O.SET_U32, c)
+        b, m = t.geometry()
+        t.close()
+        caps.append(c)
+        bcs.append(b)
+        mss.append(m)
+    np.savez_compressed(OUT / "geometry.npz", capacity=np.array(caps, np.int64), bucket_count=np.array(bcs, np.int64),
+                        max_size=np.array(mss, np.int64))
+
+
+def buckets():
+    rng = np.random.default_rng(7)
+    keys = np.concatenate([
+        np.arange(0, 64, dtype=np.uint64),
+        np.array([2**32 - 1, 2**32 - 2, 2**32, 2**63, 2**64 - 1, 2**64 - 2, 11400714819323198485], np.uint64),
+        rng.integers(0, 2**64 - 1, size=200, dtype=np.uint64),
+    ])
+    out = {"keys": keys}
+    for cap in [1, 2, 3, 100, 1000, 100000, 1 << 21]:
+        t = O.RefTable(O.SET_U64, cap)
+        out[f"bucket_{cap}"] = np.array([t.bucket(int(k)) for k in keys], np.int64)
+        out[f"bucket_count_{cap}"] = np.array(t.geometry()[0], np.int64)
+        t.close()
+    np.savez_compressed(OUT / "buckets.npz", **out)
+
+
+def table_scenario(kind: int, seed: int):
+    rng = np.random.default_rng(100 + seed)
+    kd, vd = O.KEY_DTYPE[kind], O.VAL_DTYPE[kind]
+    cap = 5000
+    n = 4000
+    hi = 2**32 - 1 if kd == np.uint32 else 2**64 - 1
+    base = rng.integers(0, hi, size=n // 2, dtype=np.uint64)
+    keys = np.concatenate([base, base[rng.integers(0, len(base), size=n - len(base))]])  # ~half duplicates
+    keys = keys[rng.permutation(n)]
+    # out-of-band values: the all-ones key and its neighbour are ordinary keys in the reference
+    keys[:3] = [hi, hi - 1, 0]
+    keys = keys.astype(kd)
+    vals = None
+    if vd is not None:
+        # the generator gives every repeated key the same value
+        vals = (O_mix(keys.astype(np.uint64)) & np.uint64(np.iinfo(vd).max)).astype(vd)
+    t = O.RefTable(kind, cap)
+    ins_flags = t.insert(keys, vals, flags=True)
+    size_after_insert = t.size()
+    queries = np.concatenate([keys[rng.integers(0, n, size=n)], rng.integers(0, hi, size=n, dtype=np.uint64).astype(kd),
+                              np.array([hi, hi - 1], np.uint64).astype(kd)])
+    fvals, found = t.find(queries)
+    erase = np.concatenate([keys[rng.integers(0, n, size=n // 2)],
+                            rng.integers(0, hi, size=n // 4, dtype=np.uint64).astype(kd)])
+    erase_flags = t.erase(erase, flags=True)
+    size_after_erase = t.size()
+    valid = t.valid()
+    rk, rv = t.range()
+    order = np.argsort(rk)
+    out = dict(capacity=np.array(cap), keys=keys, insert_flags=ins_flags, size_after_insert=np.array(size_after_insert),
+               queries=queries, found=found, erase=erase, erase_flags=erase_flags,
+               size_after_erase=np.array(size_after_erase), valid=np.array(valid), final_keys=rk[order])
+    if vd is not None:
+        out["values"] = vals
+        out["found_values"] = np.where(found == 1, fvals, 0).astype(vd)
+        out["final_values"] = rv[order]
+    t.close()
+    np.savez_compressed(OUT / f"table_{kind}.npz", **out)
+
+
+def O_mix(x: np.ndarray) -> np.ndarray:
+    z = x.copy()
+    with np.errstate(over="ignore"):
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def refusal():
+    """Sequential single-key inserts into tiny tables: which ones the reference refuses."""
+    rng = np.random.default_rng(3)
+    out = {}
+    for cap in [1, 2, 3, 4, 5, 8]:
+        keys = rng.integers(0, 1 << 40, size=4 * cap + 4, dtype=np.uint64)
+        t = O.RefTable(O.SET_U64, cap)
+        flags = np.array([t.insert(keys[i:i + 1], None, flags=True)[0] for i in range(len(keys))], np.uint8)
+        out[f"keys_{cap}"] = keys
+        out[f"flags_{cap}"] = flags
+        out[f"size_{cap}"] = np.array(t.size())
+        out[f"max_size_{cap}"] = np.array(t.geometry()[1])
+        t.close()
+    np.savez_compressed(OUT / "refusal.npz", **out)
+
+
+def vector():
+    rng = np.random.default_rng(5)
+    n = 5000
+    values = rng.integers(0, 2**32 - 1, size=n, dtype=np.uint64).astype(np.uint32)
+    pred = (rng.random(n) < 0.3).astype(np.uint8)
+    out = {"values": values, "pred": pred}
+    for cap in [100, 1000, 5000]:
+        size, pushed, contents = O.ref_vector_push_back(cap, values, pred)
+        out[f"size_{cap}"] = np.array(size)
+        out[f"pushed_{cap}"] = pushed
+        out[f"contents_{cap}"] = contents
+    np.savez_compressed(OUT / "vector.npz", **out)
+
+
+def deque():
+    rng = np.random.default_rng(6)
+    cap = 1000
+    init = rng.integers(0, 2**63, size=600, dtype=np.uint64)
+    n = 3000
+    is_push = (rng.random(n) < 0.5).astype(np.uint8)
+    values = rng.integers(0, 2**63, size=n, dtype=np.uint64)
+    size, popped, ok, rem = O.ref_deque_ops(cap, init, is_push, values)
+    np.savez_compressed(OUT / "deque.npz", capacity=np.array(cap), init=init, is_push=is_push, values=values,
+                        size=np.array(size), popped=popped, ok=ok, remaining=rem)
+
+
+def bitset():
+    rng = np.random.default_rng(8)
+    out = {}
+    for nbits in [1, 31, 32, 33, 1000, 4096, 100003]:
+        words = rng.integers(0, 2**32, size=(nbits + 31) // 32, dtype=np.uint64).astype(np.uint32)
+        out[f"words_{nbits}"] = words
+        out[f"count_{nbits}"] = np.array(O.ref_bitset_count(words, nbits))
+    np.savez_compressed(OUT / "bitset.npz", **out)
+
+
+def main():
+    O.ref_set_threads(1)
+    geometry()
+    buckets()
+    for kind in range(6):
+        table_scenario(kind, kind)
+    refusal()
+    vector()
+    deque()
+    bitset()
+    print("fixtures written to", OUT)
+
+
+if __name__ == "__main__":
+    main()
