@@ -107,7 +107,10 @@ class StdgpuError(RuntimeError):
 
 
 def library_path() -> Path:
-    return _build.library_path()
+    """The in-tree library, or the file named by $STDGPU_GB300_LIB (a separately built copy)."""
+    import os
+    override = os.environ.get("STDGPU_GB300_LIB")
+    return Path(override) if override else _build.library_path()
 
 
 def load(build_if_missing: bool = True) -> ctypes.CDLL:
@@ -116,7 +119,10 @@ def load(build_if_missing: bool = True) -> ctypes.CDLL:
     if _lib is not None:
         return _lib
     path = library_path()
-    if not path.exists() or (build_if_missing and not _build.is_current()):
+    import os
+    if os.environ.get("STDGPU_GB300_LIB"):
+        build_if_missing = False
+    elif not path.exists() or (build_if_missing and not _build.is_current()):
         if not build_if_missing:
             raise RuntimeError(f"stdgpu_gb300 native library missing: {path}")
         _build.build()

@@ -53,7 +53,7 @@ def library_path() -> Path:
 
 def is_current() -> bool:
     lib = library_path()
-    if not lib.exists():
+    if not lib.exists() or os.environ.get("STDGPU_GB300_NVCC_FLAGS"):
         return False
     t = lib.stat().st_mtime
     return all(p.stat().st_mtime <= t for p in _deps())
@@ -65,6 +65,8 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
         return library_path()
     OUT.mkdir(exist_ok=True)
     extra = ["-Xptxas", "-v"] if verbose_ptxas else []
+    # optional extra compiler flags, e.g. -DSG_BULK_MIN_BLOCKS=3
+    extra += os.environ.get("STDGPU_GB300_NVCC_FLAGS", "").split()
     cmds = []
     objs = []
     for src in SOURCES:

@@ -5,12 +5,12 @@
 // excess list guarded by per-slot spin locks becomes open addressing over
 // 128-byte probe groups (layout in include/stdgpu_gb300/detail/layout.cuh).
 //
-// Bulk kernels are warp-cooperative: a tile of 8 lanes owns one key at a time
-// and reads its whole probe group with one 16-byte load per lane; a warp holds
-// 32 keys (4 tiles x 8 keys) and issues the home-group loads of all 8 keys of a
-// tile before resolving any of them, so each warp keeps 32 random 128-byte
-// lines in flight.  Slots are claimed lock-free with one compare-and-swap on
-// the key word; counters are reduced per block and added once per block.
+// Bulk kernels are tile-cooperative: 4 lanes own one key and read its
+// 128-byte probe group as one request (one 32-byte sector per lane, 256-bit
+// loads through L2); a warp holds 32 keys and each tile issues the home-group
+// loads of its 4 keys before resolving them.  Slots are claimed lock-free with
+// one compare-and-swap on the key word; counters are reduced per block and
+// added once per block.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -31,14 +31,21 @@ namespace detail
 std::atomic<long long> g_launches{ 0 };
 
 constexpr int kThreads = 256;
+
+// Resident blocks per SM the bulk kernels are compiled for (register budget 65536 / (256 * N)).
+#ifndef SG_BULK_MIN_BLOCKS
+#define SG_BULK_MIN_BLOCKS 4
+#endif
 constexpr int kRangeChunk = 2048; // slots per block in the compaction kernels (256 threads x 8 slots)
 
+// Kernel view of a table.  Group and slot indices fit 32 bits (max_size() < 2^31), so the hot paths
+// index in 32-bit arithmetic and widen only to form addresses.
 struct dview
 {
     char* slots;
     table_header* hdr;
-    int64_t num_groups;
-    int64_t total;
+    uint32_t num_groups;
+    uint32_t total;
     int bits;
 };
 
@@ -83,32 +90,27 @@ log2_exact(int64_t x)
 
 // ---------------------------------------------------------------- device helpers
 
-SG_D uint4
-load_lane(const dview& t, int64_t g, int tl)
-{
-    return __ldcg(reinterpret_cast<const uint4*>(t.slots + g * kGroupBytes) + tl);
-}
-
+// Home group: the reference's bucket(key) scaled from 2^bits buckets onto num_groups groups.
 template <int KIND>
-SG_D int64_t
+SG_D uint32_t
 home_of(const dview& t, typename kind_consts<KIND>::K key)
 {
-    return group_of_bucket(fibonacci_bucket(static_cast<uint64_t>(key), t.bits), t.bits, t.num_groups);
+    const uint32_t b = static_cast<uint32_t>(fibonacci_bucket(static_cast<uint64_t>(key), t.bits));
+    return static_cast<uint32_t>((static_cast<uint64_t>(b) * t.num_groups) >> t.bits);
 }
 
-template <typename T>
-SG_D T
-tile_shfl(unsigned mask, T v, int src)
+SG_D uint32_t
+next_group32(uint32_t g, uint32_t num_groups)
 {
-    return __shfl_sync(mask, v, src);
+    return g + 1 == num_groups ? 0u : g + 1;
 }
 
 template <int KIND>
 SG_D typename kind_consts<KIND>::K
-cas_key(const dview& t, int64_t slot, typename kind_consts<KIND>::K expected, typename kind_consts<KIND>::K desired)
+cas_key(const dview& t, uint32_t slot, typename kind_consts<KIND>::K expected, typename kind_consts<KIND>::K desired)
 {
     using K = typename kind_consts<KIND>::K;
-    char* p = t.slots + slot * kind_consts<KIND>::slot_bytes;
+    char* p = t.slots + static_cast<uint64_t>(slot) * kind_consts<KIND>::slot_bytes;
     if constexpr (sizeof(K) == 8)
     {
         return static_cast<K>(atomicCAS(reinterpret_cast<unsigned long long*>(p),
@@ -125,12 +127,13 @@ cas_key(const dview& t, int64_t slot, typename kind_consts<KIND>::K expected, ty
 
 template <int KIND>
 SG_D void
-store_value(const dview& t, int64_t slot, typename kind_consts<KIND>::V v)
+store_value(const dview& t, uint32_t slot, typename kind_consts<KIND>::V v)
 {
     if constexpr (kind_traits<KIND>::is_map)
     {
         using V = typename kind_consts<KIND>::V;
-        *reinterpret_cast<V*>(t.slots + slot * kind_consts<KIND>::slot_bytes + kind_traits<KIND>::val_offset) = v;
+        *reinterpret_cast<V*>(t.slots + static_cast<uint64_t>(slot) * kind_consts<KIND>::slot_bytes +
+                              kind_traits<KIND>::val_offset) = v;
     }
 }
 
@@ -189,8 +192,8 @@ special_insert(const dview& t, typename kind_consts<KIND>::K key, typename kind_
     {
         return 0;
     }
-    const int64_t slot = t.num_groups * C::slots_per_group + s;
-    *reinterpret_cast<typename C::K*>(t.slots + slot * C::slot_bytes) = key;
+    const uint32_t slot = t.num_groups * C::slots_per_group + s;
+    *reinterpret_cast<typename C::K*>(t.slots + static_cast<uint64_t>(slot) * C::slot_bytes) = key;
     store_value<KIND>(t, slot, val);
     __threadfence();
     atomicExch(&t.hdr->special_state[s], 1u);
@@ -207,7 +210,7 @@ special_find(const dview& t, typename kind_consts<KIND>::K key, typename kind_co
     {
         return false;
     }
-    const int64_t slot = t.num_groups * C::slots_per_group + s;
+    const uint64_t slot = static_cast<uint64_t>(t.num_groups) * C::slots_per_group + s;
     if constexpr (kind_traits<KIND>::is_map)
     {
         val = *reinterpret_cast<const volatile typename C::V*>(t.slots + slot * C::slot_bytes +
@@ -225,54 +228,140 @@ special_erase(const dview& t, typename kind_consts<KIND>::K key)
     return atomicCAS(&t.hdr->special_state[s], 1u, 0u) == 1u ? 1 : 0;
 }
 
-// Per-lane masks of the lane's sub-slots that hold `key`, EMPTY, or a reusable TOMB.
+// ---------------------------------------------------------------- tile probing
+// A tile of 4 lanes owns one key at a time.  Lane q of the tile reads sector q (bytes 32q..32q+31) of
+// the key's 128-byte probe group with one 256-bit load, so each group costs one 128-byte request and a
+// warp instruction covers 8 keys.  Measured on GB300 over an 8 GB buffer, random 128-byte lines read
+// this way reach 36-38 G lines/s, against 21-25 G with 8 lanes x 16 B and 10-12 G with one thread
+// issuing 4 x 32 B.
+
+constexpr int kTile = 4;
+
+SG_D void
+load_sector(const dview& t, uint32_t g, int q, uint32_t (&w)[8])
+{
+    const char* p = t.slots + (static_cast<uint64_t>(g) << 7) + 32 * q;
+    asm volatile("ld.global.cg.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
+                 : "l"(p));
+}
+
+template <int KIND>
+struct sector_consts
+{
+    static constexpr int slot_words = kind_consts<KIND>::slot_bytes / 4;
+    static constexpr int slots = 32 / kind_consts<KIND>::slot_bytes; // slots per 32-byte sector
+};
+
+template <int KIND>
+SG_D typename kind_consts<KIND>::K
+sector_key(const uint32_t (&w)[8], int s)
+{
+    using K = typename kind_consts<KIND>::K;
+    constexpr int sw = sector_consts<KIND>::slot_words;
+    if constexpr (sizeof(K) == 8)
+    {
+        return static_cast<uint64_t>(w[sw * s + 1]) << 32 | w[sw * s];
+    }
+    else
+    {
+        return static_cast<K>(w[sw * s]);
+    }
+}
+
+template <int KIND>
+SG_D typename kind_consts<KIND>::V
+sector_value(const uint32_t (&w)[8], int s)
+{
+    using V = typename kind_consts<KIND>::V;
+    constexpr int sw = sector_consts<KIND>::slot_words;
+    constexpr int off = kind_traits<KIND>::val_offset / 4;
+    if constexpr (!kind_traits<KIND>::is_map)
+    {
+        return V{};
+    }
+    else if constexpr (sizeof(V) == 8)
+    {
+        return static_cast<uint64_t>(w[sw * s + off + 1]) << 32 | w[sw * s + off];
+    }
+    else
+    {
+        return static_cast<V>(w[sw * s + off]);
+    }
+}
+
+// Bit s set when sector slot s holds key / is never-used / is erased and below total (reusable).
 template <int KIND, bool WANT_TOMB>
 SG_D void
-lane_masks(const uint4& d, typename kind_consts<KIND>::K key, int64_t first_slot, int64_t total, unsigned& m_match,
-           unsigned& m_empty, unsigned& m_tomb)
+sector_masks(const uint32_t (&w)[8], typename kind_consts<KIND>::K key, uint32_t first_slot, uint32_t total,
+             unsigned& m_match, unsigned& m_empty, unsigned& m_tomb)
 {
     using C = kind_consts<KIND>;
+    constexpr int S = sector_consts<KIND>::slots;
     m_match = 0;
     m_empty = 0;
     m_tomb = 0;
 #pragma unroll
-    for (int s = 0; s < C::slots_per_lane; ++s)
+    for (int s = 0; s < S; ++s)
     {
-        const typename C::K k = key_in_lane<KIND>(d, s);
+        const typename C::K k = sector_key<KIND>(w, s);
         m_match |= static_cast<unsigned>(k == key) << s;
         m_empty |= static_cast<unsigned>(k == C::empty_key) << s;
         if constexpr (WANT_TOMB)
         {
-            m_tomb |= static_cast<unsigned>(k == C::tomb_key && first_slot + s < total) << s;
+            m_tomb |= static_cast<unsigned>(k == C::tomb_key) << s;
+        }
+    }
+    if constexpr (WANT_TOMB)
+    {
+        // slots at or above total_count are never claimed
+        if (first_slot + S > total)
+        {
+            m_tomb &= first_slot >= total ? 0u : ((1u << (total - first_slot)) - 1u);
         }
     }
 }
 
-// ---------------------------------------------------------------- tile operations
-// All 8 lanes of a tile call these together with the same key; d is this lane's
-// 16-byte share of the key's home group.  tbase = first lane of the tile.
+template <int KIND>
+SG_D typename kind_consts<KIND>::V
+select_sector_value(const uint32_t (&w)[8], unsigned one_hot)
+{
+    typename kind_consts<KIND>::V v{};
+#pragma unroll
+    for (int s = 0; s < sector_consts<KIND>::slots; ++s)
+    {
+        if (one_hot & (1u << s))
+        {
+            v = sector_value<KIND>(w, s);
+        }
+    }
+    return v;
+}
 
-// Returns 1 inserted, 0 already present, 2 refused (no free slot in the whole table), 3 retry limit.
+// Insert of one key by one tile (all 4 lanes call it with the same key; w is this lane's sector of the
+// key's home group).  Returns 1 inserted, 0 already present, 2 refused (no free slot in the table),
+// 3 retry limit.  With REUSE, erased slots are claimed too: the tile scans to the first group holding a
+// never-used slot (so a copy of the key stored beyond an erased slot is seen) and claims the first free
+// slot of the probe sequence.  Free slots only disappear during an insert launch, so two inserts of one
+// key cannot both succeed: each has read every slot before the one it claims.
 template <int KIND, bool REUSE>
 SG_D int
-tile_insert(const dview& t, typename kind_consts<KIND>::K key, typename kind_consts<KIND>::V val, uint4 d,
-            unsigned tmask, int tbase, int tl, unsigned long long& tombs_reused)
+tile_insert(const dview& t, typename kind_consts<KIND>::K key, typename kind_consts<KIND>::V val, uint32_t home,
+            uint32_t (&w)[8], unsigned tmask, int tbase, int q, unsigned long long& tombs_reused)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
-    constexpr int G = C::slots_per_group;
-    constexpr int SPL = C::slots_per_lane;
-    const int64_t home = home_of<KIND>(t, key);
-    int64_t g = home;
-    int64_t free_slot = -1; // first reusable erased slot seen along the probe sequence
-    int64_t probes = 0;
+    constexpr uint32_t G = C::slots_per_group;
+    constexpr uint32_t S = sector_consts<KIND>::slots;
+    uint32_t g = home;
+    int32_t free_slot = -1;
+    uint32_t probes = 0;
     int retries = 0;
     while (true)
     {
-        unsigned m_match, m_empty, m_tomb;
-        const int64_t first = g * G + tl * SPL;
-        lane_masks<KIND, REUSE>(d, key, first, t.total, m_match, m_empty, m_tomb);
-        if (__ballot_sync(tmask, m_match != 0u) != 0u)
+        unsigned mm, me, mt;
+        sector_masks<KIND, REUSE>(w, key, g * G + q * S, t.total, mm, me, mt);
+        if (__ballot_sync(tmask, mm != 0u) != 0u)
         {
             return 0;
         }
@@ -280,143 +369,109 @@ tile_insert(const dview& t, typename kind_consts<KIND>::K key, typename kind_con
         {
             if (free_slot < 0)
             {
-                const unsigned bt = __ballot_sync(tmask, m_tomb != 0u);
+                const unsigned bt = __ballot_sync(tmask, mt != 0u);
                 if (bt != 0u)
                 {
                     const int owner = __ffs(bt) - 1;
-                    const unsigned om = __shfl_sync(tmask, m_tomb, owner);
-                    free_slot = g * G + (owner - tbase) * SPL + (__ffs(om) - 1);
+                    free_slot = static_cast<int32_t>(g * G + (owner - tbase) * S +
+                                                     (__ffs(__shfl_sync(tmask, mt, owner)) - 1));
                 }
             }
         }
-        const unsigned be = __ballot_sync(tmask, m_empty != 0u);
-        if (be != 0u)
+        const unsigned be = __ballot_sync(tmask, me != 0u);
+        bool claim = be != 0u;
+        if (!claim && ++probes >= t.num_groups)
         {
-            int64_t target;
-            K expected;
-            if (REUSE && free_slot >= 0)
+            if (!(REUSE && free_slot >= 0))
             {
-                target = free_slot;
-                expected = C::tomb_key;
+                return 2;
             }
-            else
-            {
-                const int owner = __ffs(be) - 1;
-                const unsigned om = __shfl_sync(tmask, m_empty, owner);
-                target = g * G + (owner - tbase) * SPL + (__ffs(om) - 1);
-                expected = C::empty_key;
-            }
-            K old = expected;
-            if (tl == 0)
-            {
-                old = cas_key<KIND>(t, target, expected, key);
-                if (old == expected)
-                {
-                    store_value<KIND>(t, target, val);
-                    if (expected == C::tomb_key)
-                    {
-                        ++tombs_reused;
-                    }
-                }
-            }
-            old = __shfl_sync(tmask, old, tbase);
-            if (old == expected)
-            {
-                return 1;
-            }
-            if (old == key)
-            {
-                return 0;
-            }
-            // Another key took the slot: rescan from the slot's group (every earlier group was
-            // seen without a free slot, and free slots only disappear during an insert launch).
-            if (++retries > 65536)
-            {
-                return 3;
-            }
-            {
-                const int64_t tg = target / G;
-                probes = tg >= home ? tg - home : tg + t.num_groups - home;
-                g = tg;
-            }
-            free_slot = -1;
-            d = load_lane(t, g, tl);
+            claim = true; // no never-used slot anywhere: take the first erased slot seen
+        }
+        if (!claim)
+        {
+            g = next_group32(g, t.num_groups);
+            load_sector(t, g, q, w);
             continue;
         }
-        if (++probes >= t.num_groups)
+        uint32_t target;
+        K expected;
+        if (REUSE && free_slot >= 0)
         {
-            if (REUSE && free_slot >= 0)
-            {
-                // no never-used slot anywhere: claim the erased slot seen first
-                K old = C::tomb_key;
-                if (tl == 0)
-                {
-                    old = cas_key<KIND>(t, free_slot, C::tomb_key, key);
-                    if (old == C::tomb_key)
-                    {
-                        store_value<KIND>(t, free_slot, val);
-                        ++tombs_reused;
-                    }
-                }
-                old = __shfl_sync(tmask, old, tbase);
-                if (old == C::tomb_key)
-                {
-                    return 1;
-                }
-                if (old == key)
-                {
-                    return 0;
-                }
-                if (++retries > 65536)
-                {
-                    return 3;
-                }
-                g = free_slot / G;
-                probes = g >= home ? g - home : g + t.num_groups - home;
-                free_slot = -1;
-                d = load_lane(t, g, tl);
-                continue;
-            }
-            return 2;
+            target = static_cast<uint32_t>(free_slot);
+            expected = C::tomb_key;
         }
-        g = next_group(g, t.num_groups);
-        d = load_lane(t, g, tl);
+        else
+        {
+            const int owner = __ffs(be) - 1;
+            target = g * G + (owner - tbase) * S + (__ffs(__shfl_sync(tmask, me, owner)) - 1);
+            expected = C::empty_key;
+        }
+        K old = expected;
+        if (q == 0)
+        {
+            old = cas_key<KIND>(t, target, expected, key);
+            if (old == expected)
+            {
+                store_value<KIND>(t, target, val);
+                tombs_reused += (expected == C::tomb_key);
+            }
+        }
+        old = __shfl_sync(tmask, old, tbase);
+        if (old == expected)
+        {
+            return 1;
+        }
+        if (old == key)
+        {
+            return 0;
+        }
+        // another key took the slot: rescan from the slot's group (every earlier group was seen without
+        // a free slot)
+        if (++retries > 65536)
+        {
+            return 3;
+        }
+        g = target / G;
+        probes = g >= home ? g - home : g + t.num_groups - home;
+        free_slot = -1;
+        load_sector(t, g, q, w);
     }
 }
 
-// Returns the slot holding key (and its mapped value via val), or -1.
+// Slot of key (mapped value broadcast to the tile through val), or -1.  Stops at the first group
+// holding a never-used slot.
 template <int KIND>
-SG_D int64_t
-tile_find(const dview& t, typename kind_consts<KIND>::K key, uint4 d, unsigned tmask, int tbase, int tl,
-          typename kind_consts<KIND>::V& val)
+SG_D int32_t
+tile_find(const dview& t, typename kind_consts<KIND>::K key, uint32_t home, uint32_t (&w)[8], unsigned tmask,
+          int tbase, int q, typename kind_consts<KIND>::V& val)
 {
-    using C = kind_consts<KIND>;
-    constexpr int G = C::slots_per_group;
-    constexpr int SPL = C::slots_per_lane;
-    int64_t g = home_of<KIND>(t, key);
-    for (int64_t probes = 0; probes < t.num_groups; ++probes)
+    constexpr uint32_t G = kind_consts<KIND>::slots_per_group;
+    constexpr uint32_t S = sector_consts<KIND>::slots;
+    uint32_t g = home;
+    for (uint32_t probes = 0; probes < t.num_groups; ++probes)
     {
-        unsigned m_match, m_empty, m_tomb;
-        lane_masks<KIND, false>(d, key, 0, 0, m_match, m_empty, m_tomb);
-        const unsigned bm = __ballot_sync(tmask, m_match != 0u);
+        unsigned mm, me, mt;
+        sector_masks<KIND, false>(w, key, 0, 0, mm, me, mt);
+        const unsigned bm = __ballot_sync(tmask, mm != 0u);
         if (bm != 0u)
         {
             const int owner = __ffs(bm) - 1;
-            const int s = __ffs(__shfl_sync(tmask, m_match, owner)) - 1;
-            typename C::V mine{};
+            typename kind_consts<KIND>::V mine{};
             if constexpr (kind_traits<KIND>::is_map)
             {
-                mine = value_in_lane<KIND>(d, s);
+                mine = select_sector_value<KIND>(w, mm);
             }
             val = __shfl_sync(tmask, mine, owner);
-            return g * G + (owner - tbase) * SPL + s;
+            const int s = __ffs(__shfl_sync(tmask, mm, owner)) - 1;
+            return static_cast<int32_t>(g * G + (owner - tbase) * S + s);
         }
-        if (__ballot_sync(tmask, m_empty != 0u) != 0u)
+        if (__ballot_sync(tmask, me != 0u) != 0u)
         {
             return -1;
         }
-        g = next_group(g, t.num_groups);
-        d = load_lane(t, g, tl);
+        g = next_group32(g, t.num_groups);
+        load_sector(t, g, q, w);
     }
     return -1;
 }
@@ -470,7 +525,7 @@ k_init(dview t)
     using C = kind_consts<KIND>;
     using K = typename C::K;
     constexpr int G = C::slots_per_group;
-    const int64_t lanes_total = (t.num_groups + 1) * kTileLanes; // 16-byte units, tail group included
+    const int64_t lanes_total = (t.num_groups + 1) * (kGroupBytes / 16); // 16-byte units, tail group included
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     uint4* base = reinterpret_cast<uint4*>(t.slots);
     for (int64_t u = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; u < lanes_total; u += stride)
@@ -506,25 +561,37 @@ k_init(dview t)
     }
 }
 
+// Lanes of a warp: tiles of 4; the warp holds 32 keys (one per lane, loaded coalesced) and each tile
+// resolves the 4 keys of its own lanes in 4 rounds, after issuing the home-group loads of all 4.
+struct tile_lanes
+{
+    int lane, tbase, q;
+    unsigned tmask;
+    SG_D tile_lanes()
+    {
+        lane = threadIdx.x & 31;
+        tbase = lane & ~(kTile - 1);
+        q = lane & (kTile - 1);
+        tmask = 0xFu << tbase;
+    }
+};
+
 // Bulk insert: src/stdgpu/impl/unordered_base_detail.cuh:996-1017 (insert_value :470-495).
+// Each tile loads the home groups of its 4 keys, then inserts them one after another.
 template <int KIND, bool AOS>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
 k_insert(dview t, const void* in0, const void* in1, int64_t n, uint8_t* out_flags)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
     using V = typename C::V;
-    const int lane = threadIdx.x & 31;
-    const int tbase = lane & ~7;
-    const int tl = lane & 7;
-    const unsigned tmask = 0xFFu << tbase;
+    const tile_lanes L;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
-    unsigned long long cnt[3] = { 0, 0, 0 }; // inserted, refused, erased slots reused
-    unsigned long long retry = 0;
+    unsigned long long n_ins = 0, n_ref = 0, n_reused = 0, n_retry = 0;
     for (int64_t base = warp * 32; base < n; base += nwarps * 32)
     {
-        const int64_t i = base + lane;
+        const int64_t i = base + L.lane;
         const bool valid = i < n;
         K key = C::empty_key;
         V val{};
@@ -533,80 +600,77 @@ k_insert(dview t, const void* in0, const void* in1, int64_t n, uint8_t* out_flag
             load_input<KIND, AOS>(in0, in1, i, key, val);
         }
         const bool special = valid && key >= C::tomb_key;
-        int res = 0;
-        if (special)
-        {
-            res = special_insert<KIND>(t, key, val);
-        }
+        int res = special ? special_insert<KIND>(t, key, val) : 0;
         const bool probe = valid && !special;
-        uint4 pre[8];
+        const unsigned pmask = __ballot_sync(L.tmask, probe) >> L.tbase;
+        uint32_t pre[kTile][8];
+        uint32_t hr[kTile];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int r = 0; r < kTile; ++r)
         {
-            const K kj = tile_shfl(tmask, key, tbase + j);
-            const bool pj = __shfl_sync(tmask, probe, tbase + j);
-            if (pj)
+            hr[r] = home_of<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r));
+            if (pmask & (1u << r))
             {
-                pre[j] = load_lane(t, home_of<KIND>(t, kj), tl);
+                load_sector(t, hr[r], L.q, pre[r]);
             }
         }
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int r = 0; r < kTile; ++r)
         {
-            const K kj = tile_shfl(tmask, key, tbase + j);
-            const V vj = tile_shfl(tmask, val, tbase + j);
-            const bool pj = __shfl_sync(tmask, probe, tbase + j);
-            if (pj)
+            const K kr = __shfl_sync(L.tmask, key, L.tbase + r);
+            const V vr = __shfl_sync(L.tmask, val, L.tbase + r);
+            if (pmask & (1u << r))
             {
-                const int r = tile_insert<KIND, true>(t, kj, vj, pre[j], tmask, tbase, tl, cnt[2]);
-                if (tl == j)
+                const int x = tile_insert<KIND, true>(t, kr, vr, hr[r], pre[r], L.tmask, L.tbase, L.q, n_reused);
+                if (L.q == r)
                 {
-                    res = r;
+                    res = x;
                 }
             }
         }
         if (valid)
         {
-            cnt[0] += (res == 1);
-            cnt[1] += (res == 2);
-            retry += (res == 3);
+            n_ins += (res == 1);
+            n_ref += (res == 2);
+            n_retry += (res == 3);
             if (out_flags != nullptr)
             {
                 out_flags[i] = static_cast<uint8_t>(res == 1);
             }
         }
     }
-    if (retry != 0)
+    if (n_retry != 0)
     {
         atomicOr(&t.hdr->error, kErrRetry);
     }
     // size += inserted; refused += refused; tombstones -= reused
-    unsigned long long neg_reused = 0ull - cnt[2];
-    unsigned long long v[3] = { cnt[0], cnt[1], neg_reused };
+    unsigned long long v[3] = { n_ins, n_ref, 0ull - n_reused };
     unsigned long long* const dst[3] = { &t.hdr->size, &t.hdr->refused, &t.hdr->tombstones };
     block_add<3>(v, dst);
 }
 
 // Bulk erase: src/stdgpu/impl/unordered_base_detail.cuh:1045-1066 (erase_from_key :497-522).
+// Tiles locate the 4 keys of their lanes; then every lane swaps its own key's slot to the erased
+// marker (32 compare-and-swaps in flight per warp).
 template <int KIND>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
 k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
     using V = typename C::V;
-    const int lane = threadIdx.x & 31;
-    const int tbase = lane & ~7;
-    const int tl = lane & 7;
-    const unsigned tmask = 0xFFu << tbase;
+    const tile_lanes L;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     unsigned long long erased = 0, erased_oob = 0;
-    for (int64_t base = warp * 32; base < n; base += nwarps * 32)
+    int64_t base = warp * 32;
+    K key = base + L.lane < n ? __ldcs(reinterpret_cast<const K*>(keys) + base + L.lane) : C::empty_key;
+    for (; base < n; base += nwarps * 32)
     {
-        const int64_t i = base + lane;
+        const int64_t i = base + L.lane;
         const bool valid = i < n;
-        K key = valid ? __ldcs(reinterpret_cast<const K*>(keys) + i) : C::empty_key;
+        const K next_key =
+                i + nwarps * 32 < n ? __ldcs(reinterpret_cast<const K*>(keys) + i + nwarps * 32) : C::empty_key;
         const bool special = valid && key >= C::tomb_key;
         int res = 0;
         if (special)
@@ -615,40 +679,36 @@ k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags)
             erased_oob += static_cast<unsigned long long>(res);
         }
         const bool probe = valid && !special;
-        uint4 pre[8];
+        const unsigned pmask = __ballot_sync(L.tmask, probe) >> L.tbase;
+        uint32_t pre[kTile][8];
+        uint32_t hr[kTile];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int r = 0; r < kTile; ++r)
         {
-            const K kj = tile_shfl(tmask, key, tbase + j);
-            if (__shfl_sync(tmask, probe, tbase + j))
+            hr[r] = home_of<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r));
+            if (pmask & (1u << r))
             {
-                pre[j] = load_lane(t, home_of<KIND>(t, kj), tl);
+                load_sector(t, hr[r], L.q, pre[r]);
             }
         }
+        int32_t my_slot = -1;
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int r = 0; r < kTile; ++r)
         {
-            const K kj = tile_shfl(tmask, key, tbase + j);
-            if (__shfl_sync(tmask, probe, tbase + j))
+            if (pmask & (1u << r))
             {
                 V dummy{};
-                const int64_t slot = tile_find<KIND>(t, kj, pre[j], tmask, tbase, tl, dummy);
-                int r = 0;
-                if (slot >= 0)
+                const int32_t slot = tile_find<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r), hr[r], pre[r],
+                                                     L.tmask, L.tbase, L.q, dummy);
+                if (L.q == r)
                 {
-                    K old = kj;
-                    if (tl == 0)
-                    {
-                        old = cas_key<KIND>(t, slot, kj, C::tomb_key);
-                    }
-                    old = __shfl_sync(tmask, old, tbase);
-                    r = old == kj ? 1 : 0;
-                }
-                if (tl == j)
-                {
-                    res = r;
+                    my_slot = slot;
                 }
             }
+        }
+        if (probe && my_slot >= 0)
+        {
+            res = cas_key<KIND>(t, static_cast<uint32_t>(my_slot), key, C::tomb_key) == key ? 1 : 0;
         }
         if (valid)
         {
@@ -658,7 +718,9 @@ k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags)
                 out_flags[i] = static_cast<uint8_t>(res);
             }
         }
+        key = next_key;
     }
+    // size -= erased; tombstones += erased probed keys
     unsigned long long v[2] = { 0ull - erased, erased - erased_oob };
     unsigned long long* const dst[2] = { &t.hdr->size, &t.hdr->tombstones };
     block_add<2>(v, dst);
@@ -666,53 +728,48 @@ k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags)
 
 // Bulk find / contains (device-only find/contains in the reference, :619-706).
 template <int KIND, bool WANT_VALUES>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
 k_find(dview t, const void* keys, int64_t n, void* out_vals, uint8_t* out_found)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
     using V = typename C::V;
-    const int lane = threadIdx.x & 31;
-    const int tbase = lane & ~7;
-    const int tl = lane & 7;
-    const unsigned tmask = 0xFFu << tbase;
+    const tile_lanes L;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     for (int64_t base = warp * 32; base < n; base += nwarps * 32)
     {
-        const int64_t i = base + lane;
+        const int64_t i = base + L.lane;
         const bool valid = i < n;
-        K key = valid ? __ldcs(reinterpret_cast<const K*>(keys) + i) : C::empty_key;
+        const K key = valid ? __ldcs(reinterpret_cast<const K*>(keys) + i) : C::empty_key;
         const bool special = valid && key >= C::tomb_key;
-        bool found = false;
         V val{};
-        if (special)
-        {
-            found = special_find<KIND>(t, key, val);
-        }
+        bool found = special ? special_find<KIND>(t, key, val) : false;
         const bool probe = valid && !special;
-        uint4 pre[8];
+        const unsigned pmask = __ballot_sync(L.tmask, probe) >> L.tbase;
+        uint32_t pre[kTile][8];
+        uint32_t hr[kTile];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int r = 0; r < kTile; ++r)
         {
-            const K kj = tile_shfl(tmask, key, tbase + j);
-            if (__shfl_sync(tmask, probe, tbase + j))
+            hr[r] = home_of<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r));
+            if (pmask & (1u << r))
             {
-                pre[j] = load_lane(t, home_of<KIND>(t, kj), tl);
+                load_sector(t, hr[r], L.q, pre[r]);
             }
         }
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int r = 0; r < kTile; ++r)
         {
-            const K kj = tile_shfl(tmask, key, tbase + j);
-            if (__shfl_sync(tmask, probe, tbase + j))
+            if (pmask & (1u << r))
             {
-                V vj{};
-                const int64_t slot = tile_find<KIND>(t, kj, pre[j], tmask, tbase, tl, vj);
-                if (tl == j)
+                V vr{};
+                const int32_t slot = tile_find<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r), hr[r], pre[r],
+                                                     L.tmask, L.tbase, L.q, vr);
+                if (L.q == r)
                 {
                     found = slot >= 0;
-                    val = vj;
+                    val = vr;
                 }
             }
         }
@@ -743,7 +800,7 @@ k_valid(dview t, sg_unordered_view v, unsigned long long* bad)
     using K = typename C::K;
     constexpr int G = C::slots_per_group;
     unordered_ref<KIND> ref{ v };
-    const int64_t nslots = t.num_groups * G;
+    const int64_t nslots = static_cast<int64_t>(t.num_groups) * G;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     unsigned long long live = 0, wrong = 0;
     for (int64_t s = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; s < nslots; s += stride)
@@ -950,7 +1007,7 @@ k_range_specials(dview t, const unsigned int* chunk_offsets, int64_t nchunks, co
     {
         if (t.hdr->special_state[sp] == 1u)
         {
-            const int64_t slot = t.num_groups * C::slots_per_group + sp;
+            const int64_t slot = static_cast<int64_t>(t.num_groups) * C::slots_per_group + sp;
             if (out_keys != nullptr)
             {
                 reinterpret_cast<K*>(out_keys)[pos] = sp == 0 ? C::empty_key : C::tomb_key;
@@ -1005,7 +1062,7 @@ kind_ok(int32_t kind)
 dview
 view_of(const sg_unordered* t)
 {
-    return dview{ t->slots, t->hdr, t->num_groups, t->total, t->bits };
+    return dview{ t->slots, t->hdr, static_cast<uint32_t>(t->num_groups), static_cast<uint32_t>(t->total), t->bits };
 }
 
 sg_unordered_view
@@ -1072,7 +1129,7 @@ struct do_init
     run(sg_unordered* t, cudaStream_t s)
     {
         static const int max_grid = persistent_grid(k_init<KIND>, kThreads);
-        const int64_t units = (t->num_groups + 1) * kTileLanes;
+        const int64_t units = (t->num_groups + 1) * (kGroupBytes / 16);
         k_init<KIND><<<grid_for(units, kThreads, max_grid), kThreads, 0, s>>>(view_of(t));
         SG_LAUNCH_CHECK();
         return SG_OK;
