@@ -222,6 +222,20 @@ SG_API sg_status sg_deque_view_of(const sg_deque* dq, sg_deque_view* out);
  * nbits in the last block are masked off.  Synchronises and returns the count. */
 SG_API sg_status sg_bitset_count(const uint32_t* blocks, int64_t nbits, void* stream, int64_t* out_count);
 
+/* Allocation-free form of sg_bitset_count.  It has no counterpart in the reference.
+ * For callers that must not allocate device memory: code that runs while a CUDA graph is being captured
+ * in global mode (where cudaMalloc fails), processes whose device memory is owned by another allocator
+ * with a budget fixed up front, and latency-critical paths that cannot take an allocation's implicit
+ * synchronisation.  sg_bitset_count allocates its per-block partial sums on first use; this entry point
+ * keeps them in a fixed array compiled into the library instead (64 KiB, present on every GPU that
+ * loads the library until the process exits) and calls no allocator.  The count is written to
+ * out_count, which is DEVICE memory owned by the caller; the call is asynchronous on `stream`.
+ * Limit: nbits <= 2^34 (2 GiB of blocks); larger inputs return SG_ERR_BAD_ARG.  All calls on a device
+ * share the array, so two calls whose kernels overlap on the GPU (unordered streams) race and give
+ * wrong counts: order them on one stream or with events.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call before any stream capture. */
+SG_API sg_status sg_bitset_count_noalloc(const uint32_t* blocks, int64_t nbits, int64_t* out_count, void* stream);
+
 /* ---------------- library ---------------- */
 
 /* Number of kernels this library has launched since load (all entry points). */

@@ -92,6 +92,7 @@ SIGNATURES = {
     "sg_deque_clear": (c_int32, [c_void_p, c_void_p]),
     "sg_deque_view_of": (c_int32, [c_void_p, POINTER(sg_deque_view)]),
     "sg_bitset_count": (c_int32, [c_void_p, c_int64, c_void_p, POINTER(c_int64)]),
+    "sg_bitset_count_noalloc": (c_int32, [c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_kernel_launch_count": (c_int64, []),
     "sg_status_string": (c_char_p, [c_int32]),
 }

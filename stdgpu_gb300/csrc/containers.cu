@@ -376,6 +376,72 @@ count_grid()
     return g;
 }
 
+// ---------------------------------------------------------------- allocation-free bitset::count
+// The same count with its scratch in a fixed array compiled into the library instead of memory the
+// library allocates: one partial sum per CTA, each CTA owning a fixed chunk of the blocks, so the
+// array's length bounds the largest input.  The array lives in every GPU that loads the library until
+// the process exits; all calls on a device share it, so calls that overlap on the GPU race.
+
+constexpr int kNoAllocPartials = 8192;                                   // 64 KiB of partial sums
+constexpr int64_t kNoAllocChunkWords = 65536;                            // 32-bit blocks per CTA (256 KiB)
+constexpr int64_t kNoAllocMaxBits = kNoAllocPartials * kNoAllocChunkWords * 32; // 2^34 bits
+
+static __device__ __align__(256) unsigned long long g_noalloc_partials[kNoAllocPartials];
+
+__global__ void __launch_bounds__(kCountThreads)
+k_bitset_count_chunked(const uint32_t* blocks, int64_t nbits, unsigned long long* partials)
+{
+    const int64_t nwords = (nbits + 31) / 32;
+    const int64_t full_words = nbits / 32;
+    const int64_t lo = static_cast<int64_t>(blockIdx.x) * kNoAllocChunkWords;
+    const int64_t hi = lo + kNoAllocChunkWords < nwords ? lo + kNoAllocChunkWords : nwords;
+    unsigned long long sum = 0;
+    const bool aligned = (reinterpret_cast<uintptr_t>(blocks) & 15u) == 0;
+    int64_t w = lo;
+    if (aligned)
+    {
+        // whole 16-byte vectors of full words inside the chunk
+        const int64_t vhi = lo + ((min(hi, full_words) - lo) / 4) * 4;
+        const uint4* v4 = reinterpret_cast<const uint4*>(blocks + lo);
+        const int64_t nv = (vhi - lo) / 4;
+        for (int64_t k = threadIdx.x; k < nv; k += blockDim.x)
+        {
+            const uint4 a = __ldcs(v4 + k);
+            sum += __popc(a.x) + __popc(a.y) + __popc(a.z) + __popc(a.w);
+        }
+        w = vhi;
+    }
+    for (int64_t x = w + threadIdx.x; x < hi; x += blockDim.x)
+    {
+        uint32_t b = blocks[x];
+        if (x >= full_words)
+        {
+            b &= (1u << static_cast<int>(nbits - x * 32)) - 1u;
+        }
+        sum += __popc(b);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    }
+    __shared__ unsigned long long red[kCountThreads / 32];
+    if ((threadIdx.x & 31) == 0)
+    {
+        red[threadIdx.x >> 5] = sum;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+        unsigned long long t = 0;
+        for (int k = 0; k < kCountThreads / 32; ++k)
+        {
+            t += red[k];
+        }
+        partials[blockIdx.x] = t; // every entry the sum kernel reads is written by this call
+    }
+}
+
 } // namespace detail
 } // namespace sg
 
@@ -759,6 +825,75 @@ sg_bitset_count(const uint32_t* blocks, int64_t nbits, void* stream, int64_t* ou
                                 s));
     SG_CUDA_TRY(cudaStreamSynchronize(s));
     *out_count = static_cast<int64_t>(*sc.host);
+    return SG_OK;
+}
+
+} // extern "C"
+
+namespace
+{
+
+// Device address of the fixed scratch array, looked up once per device with that device current.
+std::mutex g_noalloc_mutex;
+unsigned long long* g_noalloc_ptr[64] = {};
+
+sg_status
+noalloc_scratch(unsigned long long** out)
+{
+    int dev = 0;
+    SG_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64)
+    {
+        return SG_ERR_NO_DEVICE;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (g_noalloc_ptr[dev] == nullptr)
+    {
+        void* p = nullptr;
+        // the symbol name in host code is a host-side stand-in; the kernels need its device address
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+        if (e != cudaSuccess || p == nullptr)
+        {
+            cudaGetLastError();
+            return SG_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = static_cast<unsigned long long*>(p);
+    }
+    *out = g_noalloc_ptr[dev];
+    return SG_OK;
+}
+
+} // namespace
+
+extern "C" {
+
+sg_status
+sg_bitset_count_noalloc(const uint32_t* blocks, int64_t nbits, int64_t* out_count, void* stream)
+{
+    if (out_count == nullptr || nbits < 0 || (nbits > 0 && blocks == nullptr))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (nbits > kNoAllocMaxBits)
+    {
+        return SG_ERR_BAD_ARG; // more chunks than the fixed scratch array holds partial sums for
+    }
+    unsigned long long* scratch = nullptr;
+    sg_status st = noalloc_scratch(&scratch);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    cudaStream_t s = as_stream(stream);
+    const int64_t nwords = (nbits + 31) / 32;
+    const int chunks = static_cast<int>((nwords + kNoAllocChunkWords - 1) / kNoAllocChunkWords);
+    if (chunks > 0)
+    {
+        k_bitset_count_chunked<<<chunks, kCountThreads, 0, s>>>(blocks, nbits, scratch);
+        SG_LAUNCH_CHECK();
+    }
+    k_sum_partials<<<1, 1024, 0, s>>>(scratch, chunks, reinterpret_cast<unsigned long long*>(out_count));
+    SG_LAUNCH_CHECK();
     return SG_OK;
 }
 
