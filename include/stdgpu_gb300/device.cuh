@@ -153,22 +153,23 @@ struct unordered_ref
         return true;
     }
 
-    // insert(value) / emplace(key, mapped): true when this call stored the key.
-    __device__ bool
-    insert(key_type key, mapped_type mapped = mapped_type{}) const
+    // insert(value) / emplace(key, mapped): the slot this call stored the key in, or -1 when the key
+    // was already present or no never-used slot was left (the reference returns (end(), false)).
+    __device__ int64_t
+    insert_slot(key_type key, mapped_type mapped = mapped_type{}) const
     {
         if (is_special(key))
         {
             const int s = key == C::empty_key ? 0 : 1;
             if (atomicCAS(&header()->special_state[s], 0u, 2u) != 0u)
             {
-                return false;
+                return -1;
             }
             store_slot(special_slot(key), key, mapped);
             __threadfence();
             atomicExch(&header()->special_state[s], 1u);
             atomicAdd(&header()->size, 1ull);
-            return true;
+            return special_slot(key);
         }
         int64_t g = home_group(key);
         int64_t steps = 0;
@@ -187,7 +188,7 @@ struct unordered_ref
                     const key_type k = detail::key_in_lane<KIND>(d, s);
                     if (k == key)
                     {
-                        return false;
+                        return -1;
                     }
                     if (target < 0 && k == C::empty_key)
                     {
@@ -213,16 +214,68 @@ struct unordered_ref
                             mapped;
                 }
                 atomicAdd(&header()->size, 1ull);
-                return true;
+                return target;
             }
             if (old == key)
             {
-                return false;
+                return -1;
             }
             // lost the slot to another key: rescan the same group
         }
         atomicAdd(&header()->refused, 1ull);
-        return false;
+        return -1;
+    }
+
+    __device__ __forceinline__ bool
+    insert(key_type key, mapped_type mapped = mapped_type{}) const
+    {
+        return insert_slot(key, mapped) >= 0;
+    }
+
+    // bucket_size(n): stored keys whose reference bucket is n (unordered_base_detail.cuh:566-593).  They
+    // all sit on the probe sequence of n's home group before its first group holding a never-used slot.
+    __device__ int64_t
+    bucket_size(int64_t n) const
+    {
+        int64_t g = detail::group_of_bucket(static_cast<uint64_t>(n), v.bucket_bits, v.num_groups);
+        int64_t c = 0;
+        for (int64_t probes = 0; probes < v.num_groups; ++probes)
+        {
+            const uint4* p = group_ptr(g);
+            bool any_empty = false;
+#pragma unroll
+            for (int l = 0; l < detail::kTileLanes; ++l)
+            {
+                const uint4 d = __ldcg(p + l);
+#pragma unroll
+                for (int s = 0; s < SPL; ++s)
+                {
+                    const key_type k = detail::key_in_lane<KIND>(d, s);
+                    if (k == C::empty_key)
+                    {
+                        any_empty = true;
+                    }
+                    else if (k != C::tomb_key && g * G + l * SPL + s < v.total_count && bucket(k) == n)
+                    {
+                        ++c;
+                    }
+                }
+            }
+            if (any_empty)
+            {
+                break;
+            }
+            g = detail::next_group(g, v.num_groups);
+        }
+        for (int s = 0; s < 2; ++s)
+        {
+            const key_type k = s == 0 ? C::empty_key : C::tomb_key;
+            if (*reinterpret_cast<volatile unsigned*>(&header()->special_state[s]) == 1u && bucket(k) == n)
+            {
+                ++c;
+            }
+        }
+        return c;
     }
 
     __device__ __forceinline__ bool

@@ -1,0 +1,509 @@
+// C++ host API with the reference's names over the C ABI of this library.
+//
+// A translation unit that used stdgpu's hashed containers
+// (src/stdgpu/unordered_map.cuh, src/stdgpu/unordered_set.cuh, src/stdgpu/vector.cuh,
+// src/stdgpu/deque.cuh, src/stdgpu/bitset.cuh) for 4/8-byte integer keys includes this header
+// instead and keeps its calls: createDeviceObject / destroyDeviceObject, bulk insert(begin, end) /
+// erase(begin, end), size / empty / full / max_size / bucket_count / load_factor / clear / valid /
+// device_range, and inside its own kernels the device members find / contains / count / insert /
+// emplace / erase / bucket / bucket_size.  Objects are shallow handles copied by value into kernels,
+// as in the reference (docs/api/object.md); exactly one destroyDeviceObject frees them.
+//
+// Errors: like the reference (src/stdgpu/cuda/impl/error.h:41-56), a failed call prints and
+// terminates by default; set stdgpu::gb300_error_handler to change that.
+#ifndef STDGPU_GB300_STDGPU_CUH
+#define STDGPU_GB300_STDGPU_CUH
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <exception>
+#include <type_traits>
+
+#include "../stdgpu_gb300.h"
+#include "device.cuh"
+
+namespace stdgpu
+{
+
+using index_t = std::int32_t; // the reference's default index type (src/stdgpu/cstddef.h:42-59)
+
+inline void (*gb300_error_handler)(sg_status, const char*) = [](sg_status st, const char* what) {
+    std::fprintf(stderr, "stdgpu_gb300: %s failed: %s\n", what, sg_status_string(st));
+    std::terminate();
+};
+
+namespace detail
+{
+inline void
+gb300_check(sg_status st, const char* what)
+{
+    if (st != SG_OK)
+    {
+        gb300_error_handler(st, what);
+    }
+}
+} // namespace detail
+
+// stdgpu::pair (src/stdgpu/utility.h); pair<const Key, T> has the reference's byte layout.
+template <typename T1, typename T2>
+struct pair
+{
+    T1 first;
+    T2 second;
+
+    pair() = default;
+    __host__ __device__ constexpr pair(const T1& a, const T2& b)
+      : first(a)
+      , second(b)
+    {
+    }
+};
+
+// Execution policies: the reference's execution::device plus a stream-carrying policy.
+namespace execution
+{
+struct device_policy
+{
+    cudaStream_t stream = nullptr;
+};
+inline constexpr device_policy device{};
+inline device_policy
+on(cudaStream_t s)
+{
+    return device_policy{ s };
+}
+} // namespace execution
+
+// Result of device_range(): stored elements addressed through slot indices, in slot order.
+template <typename T>
+struct device_indexed_range
+{
+    const std::int32_t* indices = nullptr;
+    index_t count = 0;
+    T* values = nullptr;
+
+    __host__ __device__ index_t
+    size() const
+    {
+        return count;
+    }
+    __device__ T&
+    operator[](index_t i) const
+    {
+        return values[indices[i]];
+    }
+};
+
+namespace detail
+{
+template <typename Key, typename T>
+struct gb300_kind;
+template <>
+struct gb300_kind<std::uint32_t, void> : std::integral_constant<int, SG_SET_U32>
+{
+};
+template <>
+struct gb300_kind<std::uint64_t, void> : std::integral_constant<int, SG_SET_U64>
+{
+};
+template <>
+struct gb300_kind<std::uint64_t, std::uint32_t> : std::integral_constant<int, SG_MAP_U64_U32>
+{
+};
+template <>
+struct gb300_kind<std::uint64_t, std::uint64_t> : std::integral_constant<int, SG_MAP_U64_U64>
+{
+};
+template <>
+struct gb300_kind<std::uint32_t, std::uint32_t> : std::integral_constant<int, SG_MAP_U32_U32>
+{
+};
+template <>
+struct gb300_kind<std::uint32_t, std::uint64_t> : std::integral_constant<int, SG_MAP_U32_U64>
+{
+};
+
+// Shared implementation of unordered_map / unordered_set (src/stdgpu/impl/unordered_base.cuh:56-583).
+template <typename Key, typename T, typename Value, typename Derived>
+class gb300_unordered
+{
+public:
+    static constexpr int kind = gb300_kind<Key, T>::value;
+    using key_type = Key;
+    using value_type = Value;
+    using index_type = index_t;
+    using iterator = value_type*;
+    using const_iterator = const value_type*;
+    using ref_type = sg::unordered_ref<kind>;
+
+    static_assert(sizeof(Value) == sg::detail::kind_consts<kind>::slot_bytes, "value_type layout");
+
+    // createDeviceObject(capacity): src/stdgpu/impl/unordered_base_detail.cuh:1254-1308
+    static Derived
+    createDeviceObject(const index_t& capacity)
+    {
+        return createDeviceObject(execution::device, capacity);
+    }
+
+    static Derived
+    createDeviceObject(execution::device_policy policy, const index_t& capacity)
+    {
+        Derived d;
+        gb300_check(sg_unordered_create(kind, capacity, policy.stream, &d._handle), "createDeviceObject");
+        gb300_check(sg_unordered_view_of(d._handle, &d._view), "createDeviceObject");
+        gb300_check(cudaMalloc(&d._range, sizeof(std::int32_t) * (d._view.total_count + 2)) == cudaSuccess
+                            ? SG_OK
+                            : SG_ERR_OOM,
+                    "createDeviceObject");
+        return d;
+    }
+
+    // destroyDeviceObject: src/stdgpu/impl/unordered_base_detail.cuh:1310-1348
+    static void
+    destroyDeviceObject(Derived& d)
+    {
+        destroyDeviceObject(execution::device, d);
+    }
+
+    static void
+    destroyDeviceObject(execution::device_policy, Derived& d)
+    {
+        if (d._handle != nullptr)
+        {
+            gb300_check(sg_unordered_destroy(d._handle), "destroyDeviceObject");
+            cudaFree(d._range);
+        }
+        d._handle = nullptr;
+        d._range = nullptr;
+        d._view = sg_unordered_view{};
+    }
+
+    // insert(begin, end) over value_type elements: unordered_base_detail.cuh:996-1017
+    void
+    insert(const value_type* begin, const value_type* end)
+    {
+        insert(execution::device, begin, end);
+    }
+
+    void
+    insert(execution::device_policy policy, const value_type* begin, const value_type* end)
+    {
+        gb300_check(sg_unordered_insert(_handle, begin, static_cast<int64_t>(end - begin), nullptr, policy.stream),
+                    "insert");
+    }
+
+    // erase(begin, end) over keys: unordered_base_detail.cuh:1045-1066
+    void
+    erase(const key_type* begin, const key_type* end)
+    {
+        erase(execution::device, begin, end);
+    }
+
+    void
+    erase(execution::device_policy policy, const key_type* begin, const key_type* end)
+    {
+        gb300_check(sg_unordered_erase(_handle, begin, static_cast<int64_t>(end - begin), nullptr, policy.stream),
+                    "erase");
+    }
+
+    // size() / empty() / full(): unordered_base_detail.cuh:1078-1132 (host side, synchronising)
+    index_t
+    size(execution::device_policy policy = execution::device) const
+    {
+        int64_t n = 0;
+        gb300_check(sg_unordered_size(_handle, policy.stream, &n), "size");
+        return static_cast<index_t>(n);
+    }
+
+    bool
+    empty(execution::device_policy policy = execution::device) const
+    {
+        return size(policy) == 0;
+    }
+
+    bool
+    full(execution::device_policy policy = execution::device) const
+    {
+        return size(policy) == max_size();
+    }
+
+    __host__ __device__ index_t
+    max_size() const noexcept
+    {
+        return static_cast<index_t>(_view.total_count);
+    }
+
+    __host__ __device__ index_t
+    bucket_count() const
+    {
+        return static_cast<index_t>(_view.bucket_count);
+    }
+
+    float
+    load_factor(execution::device_policy policy = execution::device) const
+    {
+        return static_cast<float>(size(policy)) / static_cast<float>(bucket_count());
+    }
+
+    __host__ __device__ float
+    max_load_factor() const
+    {
+        return 1.0F;
+    }
+
+    void
+    clear(execution::device_policy policy = execution::device)
+    {
+        gb300_check(sg_unordered_clear(_handle, policy.stream), "clear");
+    }
+
+    bool
+    valid(execution::device_policy policy = execution::device) const
+    {
+        if (_handle == nullptr)
+        {
+            return true; // an empty handle is valid, as in the reference
+        }
+        int32_t ok = 0;
+        gb300_check(sg_unordered_valid(_handle, policy.stream, &ok), "valid");
+        return ok != 0;
+    }
+
+    // device_range(): unordered_base_detail.cuh:160-208
+    device_indexed_range<value_type>
+    device_range(execution::device_policy policy = execution::device)
+    {
+        int64_t n = 0;
+        gb300_check(sg_unordered_device_range(_handle, _range, policy.stream, &n), "device_range");
+        return device_indexed_range<value_type>{ _range, static_cast<index_t>(n), begin_host() };
+    }
+
+    // bucket(key): host and device (unordered_base_detail.cuh:547-564)
+    __host__ __device__ index_t
+    bucket(const key_type& key) const
+    {
+        return static_cast<index_t>(sg::detail::fibonacci_bucket(static_cast<std::uint64_t>(key), _view.bucket_bits));
+    }
+
+    // ---- device members (unordered_base_detail.cuh:566-706, 958-1043)
+    __device__ iterator
+    begin() const
+    {
+        return static_cast<value_type*>(_view.slots);
+    }
+
+    __device__ iterator
+    end() const
+    {
+        return begin() + max_size();
+    }
+
+    __device__ index_t
+    bucket_size(index_t n) const
+    {
+        return static_cast<index_t>(ref_type{ _view }.bucket_size(n));
+    }
+
+    __device__ iterator
+    find(const key_type& key) const
+    {
+        const int64_t s = ref_type{ _view }.find_slot(key);
+        return s >= 0 ? begin() + s : end();
+    }
+
+    __device__ bool
+    contains(const key_type& key) const
+    {
+        return ref_type{ _view }.contains(key);
+    }
+
+    __device__ index_t
+    count(const key_type& key) const
+    {
+        return contains(key) ? 1 : 0;
+    }
+
+    __device__ index_t
+    erase(const key_type& key) const
+    {
+        return static_cast<index_t>(ref_type{ _view }.erase(key));
+    }
+
+    __host__ __device__ bool
+    is_null() const
+    {
+        return _view.slots == nullptr;
+    }
+
+protected:
+    __host__ __device__ value_type*
+    begin_host() const
+    {
+        return static_cast<value_type*>(_view.slots);
+    }
+
+    __device__ pair<iterator, bool>
+    insert_impl(const key_type& key, typename ref_type::mapped_type mapped) const
+    {
+        const int64_t s = ref_type{ _view }.insert_slot(key, mapped);
+        return s >= 0 ? pair<iterator, bool>(begin() + s, true) : pair<iterator, bool>(end(), false);
+    }
+
+    sg_unordered* _handle = nullptr;
+    sg_unordered_view _view{};
+    std::int32_t* _range = nullptr;
+};
+} // namespace detail
+
+// stdgpu::unordered_map<Key, T> for 4/8-byte unsigned integer Key and T.
+template <typename Key, typename T>
+class unordered_map : public detail::gb300_unordered<Key, T, pair<const Key, T>, unordered_map<Key, T>>
+{
+    using base = detail::gb300_unordered<Key, T, pair<const Key, T>, unordered_map<Key, T>>;
+    friend base;
+
+public:
+    using mapped_type = T;
+    using typename base::iterator;
+    using typename base::key_type;
+    using typename base::value_type;
+    using base::erase;
+    using base::insert;
+
+    // insert(value) / emplace(args...) (device): unordered_base_detail.cuh:958-994
+    __device__ pair<iterator, bool>
+    insert(const value_type& value) const
+    {
+        return this->insert_impl(value.first, value.second);
+    }
+
+    __device__ pair<iterator, bool>
+    emplace(const Key& key, const T& mapped) const
+    {
+        return this->insert_impl(key, mapped);
+    }
+};
+
+// stdgpu::unordered_set<Key> for 4/8-byte unsigned integer Key.
+template <typename Key>
+class unordered_set : public detail::gb300_unordered<Key, void, Key, unordered_set<Key>>
+{
+    using base = detail::gb300_unordered<Key, void, Key, unordered_set<Key>>;
+    friend base;
+
+public:
+    using typename base::iterator;
+    using typename base::key_type;
+    using typename base::value_type;
+    using base::erase;
+    using base::insert;
+
+    __device__ pair<iterator, bool>
+    insert(const value_type& key) const
+    {
+        return this->insert_impl(key, typename base::ref_type::mapped_type{});
+    }
+
+    __device__ pair<iterator, bool>
+    emplace(const Key& key) const
+    {
+        return this->insert_impl(key, typename base::ref_type::mapped_type{});
+    }
+};
+
+// stdgpu::vector<T>: bulk push_back and size (src/stdgpu/vector.cuh); device push_back is
+// warp-aggregated like the bulk kernel.
+template <typename T>
+class vector
+{
+    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+
+public:
+    static vector
+    createDeviceObject(const index_t& capacity)
+    {
+        vector v;
+        detail::gb300_check(sg_vector_create(sizeof(T), capacity, &v._handle), "vector::createDeviceObject");
+        detail::gb300_check(sg_vector_view_of(v._handle, &v._view), "vector::createDeviceObject");
+        return v;
+    }
+
+    static void
+    destroyDeviceObject(vector& v)
+    {
+        if (v._handle != nullptr)
+        {
+            detail::gb300_check(sg_vector_destroy(v._handle), "vector::destroyDeviceObject");
+        }
+        v._handle = nullptr;
+        v._view = sg_vector_view{};
+    }
+
+    index_t
+    size(execution::device_policy policy = execution::device) const
+    {
+        int64_t n = 0;
+        detail::gb300_check(sg_vector_size(_handle, policy.stream, &n), "vector::size");
+        return static_cast<index_t>(n);
+    }
+
+    __host__ __device__ index_t
+    capacity() const
+    {
+        return static_cast<index_t>(_view.capacity);
+    }
+
+    __host__ __device__ T*
+    data() const
+    {
+        return static_cast<T*>(_view.data);
+    }
+
+    // Device push_back (src/stdgpu/impl/vector_detail.cuh:181-238): the calling lanes that are active
+    // together reserve their positions with one atomic per warp.
+    __device__ bool
+    push_back(const T& element) const
+    {
+        const unsigned active = __activemask();
+        const int lane = threadIdx.x & 31;
+        const int leader = __ffs(active) - 1;
+        unsigned lt;
+        asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+        long long* size = static_cast<long long*>(_view.size);
+        long long base = -1;
+        if (lane == leader)
+        {
+            const long long cur = *reinterpret_cast<volatile long long*>(size);
+            base = cur >= _view.capacity ? -1
+                                         : static_cast<long long>(atomicAdd(reinterpret_cast<unsigned long long*>(size),
+                                                                            static_cast<unsigned long long>(__popc(active))));
+        }
+        base = __shfl_sync(active, base, leader);
+        const long long pos = base + __popc(active & lt);
+        if (base < 0 || pos >= _view.capacity)
+        {
+            return false;
+        }
+        data()[pos] = element;
+        return true;
+    }
+
+private:
+    sg_vector* _handle = nullptr;
+    sg_vector_view _view{};
+};
+
+// bitset::count() over raw blocks (src/stdgpu/impl/bitset_detail.cuh:388-404).
+inline std::int64_t
+bitset_count(const std::uint32_t* blocks, std::int64_t nbits, execution::device_policy policy = execution::device)
+{
+    std::int64_t n = 0;
+    detail::gb300_check(sg_bitset_count(blocks, nbits, policy.stream, &n), "bitset::count");
+    return n;
+}
+
+} // namespace stdgpu
+
+#endif

@@ -1,0 +1,320 @@
+// Scenarios of the reference's own unordered / vector tests (tests/stdgpu/unordered_datastructure.inc,
+// tests/stdgpu/vector.inc), written against the C++ API of include/stdgpu_gb300/stdgpu.cuh: native
+// device calls inside user kernels plus the host bulk calls.  Prints one line per check and ends with
+// "ALL PASS" when every check holds.
+#include <cstdint>
+#include <cstdio>
+#include <random>
+#include <unordered_set>
+#include <vector>
+
+#include <stdgpu_gb300/stdgpu.cuh>
+
+using map_t = stdgpu::unordered_map<std::uint64_t, std::uint32_t>;
+using set_t = stdgpu::unordered_set<std::uint64_t>;
+
+static int failures = 0;
+
+static void
+check(bool ok, const char* name)
+{
+    std::printf("%s %s\n", ok ? "PASS" : "FAIL", name);
+    if (!ok)
+    {
+        ++failures;
+    }
+}
+
+template <typename T>
+static T*
+to_device(const std::vector<T>& h)
+{
+    T* d = nullptr;
+    cudaMalloc(&d, sizeof(T) * (h.size() ? h.size() : 1));
+    cudaMemcpy(d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice);
+    return d;
+}
+
+template <typename T>
+static std::vector<T>
+to_host(const T* d, size_t n)
+{
+    std::vector<T> h(n);
+    cudaMemcpy(h.data(), d, sizeof(T) * n, cudaMemcpyDeviceToHost);
+    return h;
+}
+
+static std::vector<std::uint64_t>
+unique_keys(size_t n, std::uint64_t seed)
+{
+    std::mt19937_64 rng(seed);
+    std::unordered_set<std::uint64_t> s;
+    std::vector<std::uint64_t> out;
+    while (out.size() < n)
+    {
+        std::uint64_t k = rng() >> 1;
+        if (s.insert(k).second)
+        {
+            out.push_back(k);
+        }
+    }
+    return out;
+}
+
+__global__ void
+k_insert(map_t m, const std::uint64_t* keys, int n, int* inserted)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        inserted[i] = m.insert(stdgpu::pair<const std::uint64_t, std::uint32_t>(keys[i], static_cast<std::uint32_t>(i))).second;
+    }
+}
+
+__global__ void
+k_emplace(map_t m, const std::uint64_t* keys, int n, int* inserted)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        inserted[i] = m.emplace(keys[i], static_cast<std::uint32_t>(i)).second;
+    }
+}
+
+__global__ void
+k_erase(map_t m, const std::uint64_t* keys, int n, int* erased)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        erased[i] = m.erase(keys[i]);
+    }
+}
+
+__global__ void
+k_insert_and_erase(map_t m, const std::uint64_t* keys, int n, int* inserted, int* erased)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        inserted[i] = m.emplace(keys[i], 1u).second;
+        erased[i] = m.erase(keys[i]);
+    }
+}
+
+__global__ void
+k_insert_same(set_t s, std::uint64_t key, int n, int* inserted)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        inserted[i] = s.insert(key).second;
+    }
+}
+
+__global__ void
+k_find_values(map_t m, const std::uint64_t* keys, int n, int* ok)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        auto it = m.find(keys[i]);
+        ok[i] = (it != m.end() && it->first == keys[i] && it->second == static_cast<std::uint32_t>(i)) ? 1 : 0;
+    }
+}
+
+__global__ void
+k_count_sum(map_t m, const std::uint64_t* keys, int n, unsigned long long* sum)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        atomicAdd(sum, static_cast<unsigned long long>(m.count(keys[i])));
+    }
+}
+
+__global__ void
+k_bucket_size_sum(map_t m, unsigned long long* sum)
+{
+    int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < m.bucket_count())
+    {
+        atomicAdd(sum, static_cast<unsigned long long>(m.bucket_size(b)));
+    }
+}
+
+__global__ void
+k_range_sum(stdgpu::device_indexed_range<map_t::value_type> r, unsigned long long* sum)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < r.size())
+    {
+        atomicAdd(sum, static_cast<unsigned long long>(r[i].second));
+    }
+}
+
+__global__ void
+k_push_if(stdgpu::vector<std::uint32_t> v, int n, int* pushed)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && (i % 3) == 0)
+    {
+        pushed[i] = v.push_back(static_cast<std::uint32_t>(i));
+    }
+}
+
+static int
+sum_of(const int* d, int n)
+{
+    auto h = to_host(d, n);
+    int s = 0;
+    for (int x : h)
+    {
+        s += x;
+    }
+    return s;
+}
+
+int
+main()
+{
+    const int N = 100000;
+    const int threads = 256;
+    const int blocks = (N + threads - 1) / threads;
+    auto keys = unique_keys(N, 42);
+    std::uint64_t* d_keys = to_device(keys);
+    int* flags = nullptr;
+    int* flags2 = nullptr;
+    cudaMalloc(&flags, sizeof(int) * N);
+    cudaMalloc(&flags2, sizeof(int) * N);
+    unsigned long long* d_sum = nullptr;
+    cudaMalloc(&d_sum, sizeof(unsigned long long));
+
+    // insert_unique_parallel (unordered_datastructure.inc:1880)
+    {
+        map_t m = map_t::createDeviceObject(N);
+        k_insert<<<blocks, threads>>>(m, d_keys, N, flags);
+        check(sum_of(flags, N) == N, "insert_unique_parallel: every key inserted once");
+        check(m.size() == N && m.valid(), "insert_unique_parallel: size and valid");
+        k_find_values<<<blocks, threads>>>(m, d_keys, N, flags);
+        check(sum_of(flags, N) == N, "find returns the stored pair");
+        cudaMemset(d_sum, 0, sizeof(unsigned long long));
+        k_count_sum<<<blocks, threads>>>(m, d_keys, N, d_sum);
+        check(to_host(d_sum, 1)[0] == static_cast<unsigned long long>(N), "count_sum");
+        cudaMemset(d_sum, 0, sizeof(unsigned long long));
+        k_bucket_size_sum<<<(m.bucket_count() + threads - 1) / threads, threads>>>(m, d_sum);
+        check(to_host(d_sum, 1)[0] == static_cast<unsigned long long>(N), "bucket_size_sum");
+        auto r = m.device_range();
+        cudaMemset(d_sum, 0, sizeof(unsigned long long));
+        k_range_sum<<<(r.size() + threads - 1) / threads, threads>>>(r, d_sum);
+        check(r.size() == N && to_host(d_sum, 1)[0] == static_cast<unsigned long long>(N) * (N - 1) / 2,
+              "device_range covers every stored pair");
+        // erase_unique_parallel (unordered_datastructure.inc:1898)
+        k_erase<<<blocks, threads>>>(m, d_keys, N, flags);
+        check(sum_of(flags, N) == N && m.size() == 0 && m.empty() && m.valid(), "erase_unique_parallel");
+        // a second erase finds nothing
+        k_erase<<<blocks, threads>>>(m, d_keys, N, flags);
+        check(sum_of(flags, N) == 0, "erase of absent keys");
+        map_t::destroyDeviceObject(m);
+    }
+
+    // emplace_unique_parallel, then the bulk calls on the same object
+    {
+        map_t m = map_t::createDeviceObject(N);
+        k_emplace<<<blocks, threads>>>(m, d_keys, N, flags);
+        check(sum_of(flags, N) == N && m.size() == N, "emplace_unique_parallel");
+        k_emplace<<<blocks, threads>>>(m, d_keys, N, flags);
+        check(sum_of(flags, N) == 0 && m.size() == N, "emplace of present keys inserts nothing");
+        m.clear();
+        check(m.size() == 0 && m.valid(), "clear");
+        // bulk insert(begin, end) over value_type elements (unordered_base_detail.cuh:996-1017)
+        std::vector<map_t::value_type> values;
+        values.reserve(N);
+        for (int i = 0; i < N; ++i)
+        {
+            values.emplace_back(keys[i], static_cast<std::uint32_t>(i));
+        }
+        map_t::value_type* d_values = nullptr;
+        cudaMalloc(&d_values, sizeof(map_t::value_type) * N);
+        cudaMemcpy(d_values, values.data(), sizeof(map_t::value_type) * N, cudaMemcpyHostToDevice);
+        m.insert(d_values, d_values + N);
+        k_find_values<<<blocks, threads>>>(m, d_keys, N, flags);
+        check(m.size() == N && sum_of(flags, N) == N, "bulk insert(begin, end)");
+        m.erase(d_keys, d_keys + N / 2);
+        check(m.size() == N - N / 2 && m.valid(), "bulk erase(begin, end)");
+        cudaFree(d_values);
+        map_t::destroyDeviceObject(m);
+    }
+
+    // insert_and_erase_unique_parallel (unordered_datastructure.inc:2118)
+    {
+        const int n = 10000;
+        map_t m = map_t::createDeviceObject(N);
+        k_insert_and_erase<<<(n + threads - 1) / threads, threads>>>(m, d_keys, n, flags, flags2);
+        check(sum_of(flags, n) == n && sum_of(flags2, n) == n && m.size() == 0 && m.valid(),
+              "insert_and_erase_unique_parallel");
+        map_t::destroyDeviceObject(m);
+    }
+
+    // insert_parallel_while_one_free (unordered_datastructure.inc:1549): capacity 1 gives 2 slots
+    {
+        set_t s = set_t::createDeviceObject(1);
+        check(s.max_size() == 2 && s.bucket_count() == 1, "capacity 1 geometry");
+        k_insert_same<<<1, 1>>>(s, 11, 1, flags);
+        k_insert_same<<<blocks, threads>>>(s, 22, N, flags);
+        check(sum_of(flags, N) == 1 && s.size() == 2 && s.full() && s.valid(), "insert_parallel_while_one_free");
+        k_insert_same<<<blocks, threads>>>(s, 33, N, flags);
+        check(sum_of(flags, N) == 0 && s.size() == 2, "insert_multiple_while_full");
+        set_t::destroyDeviceObject(s);
+    }
+
+    // vector push_back from a user kernel (tests/stdgpu/vector.inc:404-512)
+    {
+        stdgpu::vector<std::uint32_t> v = stdgpu::vector<std::uint32_t>::createDeviceObject(N);
+        cudaMemset(flags, 0, sizeof(int) * N);
+        k_push_if<<<blocks, threads>>>(v, N, flags);
+        const int expected = (N + 2) / 3;
+        auto data = to_host(v.data(), expected);
+        long long sum = 0;
+        for (auto x : data)
+        {
+            sum += x;
+        }
+        long long want = 0;
+        for (int i = 0; i < N; i += 3)
+        {
+            want += i;
+        }
+        check(v.size() == expected && sum_of(flags, N) == expected && sum == want, "vector push_back in a kernel");
+        stdgpu::vector<std::uint32_t>::destroyDeviceObject(v);
+    }
+
+    // bitset count
+    {
+        std::vector<std::uint32_t> words(1000);
+        std::mt19937 rng(3);
+        long long want = 0;
+        for (auto& w : words)
+        {
+            w = rng();
+            want += __builtin_popcount(w);
+        }
+        std::uint32_t* d_words = to_device(words);
+        check(stdgpu::bitset_count(d_words, 32000) == want, "bitset count");
+        cudaFree(d_words);
+    }
+
+    cudaError_t e = cudaDeviceSynchronize();
+    check(e == cudaSuccess, "no CUDA error");
+    cudaFree(d_keys);
+    cudaFree(flags);
+    cudaFree(flags2);
+    cudaFree(d_sum);
+    if (failures == 0)
+    {
+        std::printf("ALL PASS\n");
+        return 0;
+    }
+    std::printf("%d FAILED\n", failures);
+    return 1;
+}

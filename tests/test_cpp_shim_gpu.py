@@ -1,0 +1,41 @@
+"""The C++ API with the reference's names (include/stdgpu_gb300/stdgpu.cuh), used by a program that
+runs the reference's own test scenarios with native device calls inside user kernels."""
+
+import subprocess
+from pathlib import Path
+
+import pytest
+
+import stdgpu_gb300
+from stdgpu_gb300 import build as B
+
+ROOT = Path(__file__).resolve().parents[1]
+SRC = ROOT / "tests" / "cpp" / "shim_test.cu"
+OUT = ROOT / "tests" / "cpp" / "_build"
+
+
+def _compile(flags=()):
+    OUT.mkdir(exist_ok=True)
+    lib = stdgpu_gb300.library_path()
+    exe = OUT / "shim_test"
+    cmd = [B.nvcc(), *B.ARCH_FLAGS, "-std=c++17", "-O2", *flags, "-I", str(ROOT / "include"), str(SRC),
+           "-L", str(lib.parent), "-lstdgpu_gb300", f"-Xlinker=-rpath={lib.parent}", "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_shim_compiles_for_sm103a():
+    """CPU part: the header compiles with the test program (no device needed)."""
+    stdgpu_gb300.load()
+    _compile()
+
+
+@pytest.mark.gpu
+def test_shim_reference_scenarios_on_gpu():
+    stdgpu_gb300.load()
+    exe = _compile()
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "ALL PASS" in r.stdout
