@@ -64,6 +64,8 @@ def parse():
     p.add_argument("--keys-log2", type=int, default=KEYS_LOG2, help="2^k keys (default: the full workload)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--workload", choices=["voxel", "batched"], default="voxel",
+                   help="voxel: the headline map workload; batched: 4096 small sets, batched vs plain calls")
     return p.parse_args()
 
 
@@ -370,10 +372,25 @@ def native_arm(args):
         torch.distributed.destroy_process_group()
 
 
+def batched_arm(args):
+    """Many small tables: plain per-table calls vs one batched launch vs a CUDA graph (one GPU)."""
+    from stdgpu_gb300 import batch_bench
+    r = batch_bench.run(steps=args.steps, warmup=args.warmup)
+    line = {"metric": "many-small-tables clear+insert+contains Mops/s", "value": r["graph_mops"], "unit": UNIT,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["graph_ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": "4096 unordered_set<uint64_t>, lognormal counts (median 2048, sigma 1.5, "
+                                   "64..262144), capacity bit_ceil(2 count), contains 50% hits"},
+            "batched": r}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == "batched":
+        batched_arm(args)
     else:
         native_arm(args)
 

@@ -160,6 +160,43 @@ SG_API sg_status sg_unordered_view_of(const sg_unordered* table, sg_unordered_vi
 /* Geometry of createDeviceObject(capacity) without creating a table. */
 SG_API sg_status sg_unordered_geometry_for(int32_t kind, int64_t capacity, sg_geometry* out);
 
+/* ---------------- batched many-table objects (no counterpart in the reference) ---------------- */
+
+/* Thousands of independent unordered_set / unordered_map objects of one kind and uneven capacities,
+ * each with the geometry and behaviour of a single table, stored in one device arena.  Every batched
+ * operation takes the keys of all tables concatenated, table t owning elements [offsets[t],
+ * offsets[t+1]) of the input (offsets: DEVICE array of n_tables + 1 int64), and runs as one
+ * persistent launch over (table, 32-key range) tiles.  No host work depends on the sizes, so a
+ * sequence of batched calls can be captured in a CUDA graph. */
+typedef struct sg_table_batch sg_table_batch;
+
+/* capacities: HOST array of n_tables capacities (createDeviceObject(capacity) of each table). */
+SG_API sg_status sg_batch_create(int32_t kind, int32_t n_tables, const int64_t* capacities, void* stream,
+                                 sg_table_batch** out);
+SG_API sg_status sg_batch_destroy(sg_table_batch* batch);
+/* Launch shape of the walking kernels: threads per block (128, 256, 512), resident blocks per SM
+ * (0 = as many as fit), tiles each warp takes per step (1..64). */
+SG_API sg_status sg_batch_configure(sg_table_batch* batch, int32_t threads_per_block, int32_t blocks_per_sm,
+                                    int32_t tiles_per_step);
+/* clear() of every table */
+SG_API sg_status sg_batch_clear(sg_table_batch* batch, void* stream);
+/* insert(begin, end) per table over value_type elements / over keys and mapped values */
+SG_API sg_status sg_batch_insert(sg_table_batch* batch, const void* values, const int64_t* offsets,
+                                 uint8_t* out_inserted, void* stream);
+SG_API sg_status sg_batch_insert_kv(sg_table_batch* batch, const void* keys, const void* mapped,
+                                    const int64_t* offsets, uint8_t* out_inserted, void* stream);
+SG_API sg_status sg_batch_erase(sg_table_batch* batch, const void* keys, const int64_t* offsets,
+                                uint8_t* out_erased, void* stream);
+SG_API sg_status sg_batch_find(sg_table_batch* batch, const void* keys, const int64_t* offsets, void* out_mapped,
+                               uint8_t* out_found, void* stream);
+SG_API sg_status sg_batch_contains(sg_table_batch* batch, const void* keys, const int64_t* offsets,
+                                   uint8_t* out_flags, void* stream);
+/* size() of every table into a HOST array of n_tables (synchronises). */
+SG_API sg_status sg_batch_sizes(sg_table_batch* batch, void* stream, int64_t* out_sizes);
+/* Device view of table t for native device calls. */
+SG_API sg_status sg_batch_view_of(const sg_table_batch* batch, int32_t table, sg_unordered_view* out);
+SG_API sg_status sg_batch_info(const sg_table_batch* batch, int64_t* out_storage_bytes, int32_t* out_n_tables);
+
 /* ---------------- vector<T> (T = 4 or 8 bytes) ---------------- */
 
 typedef struct sg_vector sg_vector;

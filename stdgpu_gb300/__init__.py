@@ -11,6 +11,7 @@ from .containers import (  # noqa: F401
     deque,
     geometry_for,
     kernel_launch_count,
+    table_batch,
     unordered_base,
     unordered_map,
     unordered_set,

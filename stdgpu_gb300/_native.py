@@ -78,6 +78,18 @@ SIGNATURES = {
     "sg_unordered_geometry": (c_int32, [c_void_p, POINTER(sg_geometry)]),
     "sg_unordered_view_of": (c_int32, [c_void_p, POINTER(sg_unordered_view)]),
     "sg_unordered_geometry_for": (c_int32, [c_int32, c_int64, POINTER(sg_geometry)]),
+    "sg_batch_create": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, POINTER(c_void_p)]),
+    "sg_batch_destroy": (c_int32, [c_void_p]),
+    "sg_batch_configure": (c_int32, [c_void_p, c_int32, c_int32, c_int32]),
+    "sg_batch_clear": (c_int32, [c_void_p, c_void_p]),
+    "sg_batch_insert": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sg_batch_insert_kv": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sg_batch_erase": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sg_batch_find": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sg_batch_contains": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "sg_batch_sizes": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "sg_batch_view_of": (c_int32, [c_void_p, c_int32, POINTER(sg_unordered_view)]),
+    "sg_batch_info": (c_int32, [c_void_p, POINTER(c_int64), POINTER(c_int32)]),
     "sg_vector_create": (c_int32, [c_int32, c_int64, POINTER(c_void_p)]),
     "sg_vector_destroy": (c_int32, [c_void_p]),
     "sg_vector_push_back": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),

@@ -217,6 +217,118 @@ def geometry_for(kind: int, capacity: int) -> N.sg_geometry:
     return g
 
 
+class table_batch:
+    """Many independent unordered_set / unordered_map objects of one kind in one device arena.
+
+    Operations take the keys of all tables concatenated with per-table offsets (a device int64 tensor
+    of n_tables + 1 entries) and run as one persistent launch; a sequence of them can be captured in a
+    CUDA graph.  No counterpart in the reference: it batches what the reference does with one
+    createDeviceObject and one bulk call per table.
+    """
+
+    def __init__(self, handle: int, kind: int, n_tables: int):
+        self._h = c_void_p(handle)
+        self.kind = kind
+        self.n_tables = n_tables
+        self.key_bytes = _KEY_BYTES[kind]
+        self.mapped_bytes = _MAPPED_BYTES[kind]
+
+    @classmethod
+    def createDeviceObjects(cls, capacities, key: str = "u64", mapped: str | None = None,
+                            stream=None, tuning: dict | None = None) -> "table_batch":
+        import numpy as np
+        kind = KINDS[(key, mapped)]
+        caps = np.ascontiguousarray(np.asarray(capacities, dtype=np.int64))
+        h = c_void_p()
+        N.check(N.load().sg_batch_create(kind, len(caps), c_void_p(caps.ctypes.data), _stream(stream), byref(h)),
+                "batch::createDeviceObjects")
+        b = cls(h.value, kind, len(caps))
+        cfg = tuning if tuning is not None else load_batch_tuning()
+        if cfg:
+            b.configure(cfg["threads_per_block"], cfg["blocks_per_sm"], cfg["tiles_per_step"])
+        return b
+
+    @staticmethod
+    def destroyDeviceObjects(b: "table_batch") -> None:
+        if b._h:
+            N.check(N.load().sg_batch_destroy(b._h), "batch::destroyDeviceObjects")
+            b._h = c_void_p(0)
+
+    def configure(self, threads_per_block: int, blocks_per_sm: int, tiles_per_step: int) -> None:
+        N.check(N.load().sg_batch_configure(self._h, threads_per_block, blocks_per_sm, tiles_per_step),
+                "batch::configure")
+
+    def clear(self, stream=None) -> None:
+        N.check(N.load().sg_batch_clear(self._h, _stream(stream)), "batch::clear")
+
+    def insert(self, keys: torch.Tensor, offsets: torch.Tensor, mapped: torch.Tensor | None = None, *,
+               flags: torch.Tensor | None = None, stream=None) -> None:
+        keys = _as_bits(keys, self.key_bytes, "keys")
+        if self.mapped_bytes:
+            mapped = _as_bits(mapped, self.mapped_bytes, "mapped")
+        N.check(N.load().sg_batch_insert_kv(self._h, _ptr(keys), _ptr(mapped if self.mapped_bytes else None),
+                                            _ptr(_offsets(offsets)), _ptr(flags), _stream(stream)), "batch::insert")
+
+    def erase(self, keys: torch.Tensor, offsets: torch.Tensor, *, flags: torch.Tensor | None = None,
+              stream=None) -> None:
+        keys = _as_bits(keys, self.key_bytes, "keys")
+        N.check(N.load().sg_batch_erase(self._h, _ptr(keys), _ptr(_offsets(offsets)), _ptr(flags), _stream(stream)),
+                "batch::erase")
+
+    def contains(self, keys: torch.Tensor, offsets: torch.Tensor, out: torch.Tensor | None = None,
+                 stream=None) -> torch.Tensor:
+        keys = _as_bits(keys, self.key_bytes, "keys")
+        if out is None:
+            out = torch.empty(keys.numel(), dtype=torch.uint8, device=keys.device)
+        N.check(N.load().sg_batch_contains(self._h, _ptr(keys), _ptr(_offsets(offsets)), _ptr(out),
+                                           _stream(stream)), "batch::contains")
+        return out
+
+    def find(self, keys: torch.Tensor, offsets: torch.Tensor, stream=None):
+        keys = _as_bits(keys, self.key_bytes, "keys")
+        found = torch.empty(keys.numel(), dtype=torch.uint8, device=keys.device)
+        vals = torch.zeros(keys.numel(), dtype=_INT_DTYPE[self.mapped_bytes], device=keys.device) \
+            if self.mapped_bytes else None
+        N.check(N.load().sg_batch_find(self._h, _ptr(keys), _ptr(_offsets(offsets)), _ptr(vals), _ptr(found),
+                                       _stream(stream)), "batch::find")
+        return vals, found
+
+    def sizes(self, stream=None):
+        import numpy as np
+        out = np.zeros(self.n_tables, dtype=np.int64)
+        N.check(N.load().sg_batch_sizes(self._h, _stream(stream), c_void_p(out.ctypes.data)), "batch::sizes")
+        return out
+
+    def view(self, table: int) -> N.sg_unordered_view:
+        v = N.sg_unordered_view()
+        N.check(N.load().sg_batch_view_of(self._h, int(table), byref(v)), "batch::view")
+        return v
+
+    def storage_bytes(self) -> int:
+        b = c_int64()
+        N.check(N.load().sg_batch_info(self._h, byref(b), None), "batch::info")
+        return b.value
+
+
+def _offsets(offsets: torch.Tensor) -> torch.Tensor:
+    if offsets.dtype != torch.int64 or not offsets.is_cuda:
+        raise ValueError("offsets: device int64 tensor of n_tables + 1 entries expected")
+    return offsets.contiguous()
+
+
+def load_batch_tuning() -> dict | None:
+    """Launch shape chosen by stdgpu_gb300/autotune.py on a GB300, if recorded."""
+    import json
+    from pathlib import Path
+    f = Path(__file__).resolve().parent / "tuning" / "batch.json"
+    if f.exists():
+        try:
+            return json.loads(f.read_text())["best"]
+        except (ValueError, KeyError):
+            return None
+    return None
+
+
 class vector:
     """stdgpu::vector<T> (T = 4 or 8 bytes): push_back, size, clear (src/stdgpu/vector.cuh)."""
 

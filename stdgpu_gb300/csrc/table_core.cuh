@@ -1,0 +1,705 @@
+// Device-side building blocks of the table kernels (probe groups, tile probing, counters), shared by the
+// single-table entry points (unordered.cu) and the batched many-table entry points (batch.cu).
+#ifndef SG_TABLE_CORE_CUH
+#define SG_TABLE_CORE_CUH
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "stdgpu_gb300/detail/layout.cuh"
+
+namespace sg
+{
+namespace detail
+{
+
+constexpr int kThreads = 256;
+
+// Resident blocks per SM the bulk kernels are compiled for (register budget 65536 / (256 * N)).
+#ifndef SG_BULK_MIN_BLOCKS
+#define SG_BULK_MIN_BLOCKS 4
+#endif
+constexpr int kRangeChunk = 2048; // slots per block in the compaction kernels (256 threads x 8 slots)
+
+// Kernel view of a table.  Group and slot indices fit 32 bits (max_size() < 2^31), so the hot paths
+// index in 32-bit arithmetic and widen only to form addresses.
+struct dview
+{
+    char* slots;
+    table_header* hdr;
+    uint32_t num_groups;
+    uint32_t total;
+    int bits;
+};
+
+// ---------------------------------------------------------------- geometry
+
+// bit_ceil over size_t: src/stdgpu/impl/bit_detail.h:36-62
+inline uint64_t
+bit_ceil_u64(uint64_t x)
+{
+    uint64_t r = 1;
+    while (r < x && r != 0)
+    {
+        r <<= 1;
+    }
+    return r;
+}
+
+// createDeviceObject geometry: src/stdgpu/impl/unordered_base_detail.cuh:1264-1273 and
+// expected_collisions :34-48, evaluated with the same float / long double steps.
+inline void
+reference_geometry(int64_t capacity, int64_t* bucket_count, int64_t* excess_count)
+{
+    const float c = std::ceil(static_cast<float>(capacity) / 1.0F);
+    const uint64_t b = bit_ceil_u64(static_cast<uint64_t>(c));
+    const long double k = static_cast<long double>(b);
+    const long double n = static_cast<long double>(capacity);
+    const int64_t e = static_cast<int64_t>(std::ceil(n * (1.0L - std::pow(1.0L - (1.0L / k), n - 1.0L))));
+    *bucket_count = static_cast<int64_t>(b);
+    *excess_count = e + 1;
+}
+
+inline int
+log2_exact(int64_t x)
+{
+    int b = 0;
+    while ((int64_t{ 1 } << b) < x)
+    {
+        ++b;
+    }
+    return b;
+}
+
+// ---------------------------------------------------------------- device helpers
+
+// Home group: the reference's bucket(key) scaled from 2^bits buckets onto num_groups groups.
+template <int KIND>
+SG_D uint32_t
+home_of(const dview& t, typename kind_consts<KIND>::K key)
+{
+    const uint32_t b = static_cast<uint32_t>(fibonacci_bucket(static_cast<uint64_t>(key), t.bits));
+    return static_cast<uint32_t>((static_cast<uint64_t>(b) * t.num_groups) >> t.bits);
+}
+
+SG_D uint32_t
+next_group32(uint32_t g, uint32_t num_groups)
+{
+    return g + 1 == num_groups ? 0u : g + 1;
+}
+
+template <int KIND>
+SG_D typename kind_consts<KIND>::K
+cas_key(const dview& t, uint32_t slot, typename kind_consts<KIND>::K expected, typename kind_consts<KIND>::K desired)
+{
+    using K = typename kind_consts<KIND>::K;
+    char* p = t.slots + static_cast<uint64_t>(slot) * kind_consts<KIND>::slot_bytes;
+    if constexpr (sizeof(K) == 8)
+    {
+        return static_cast<K>(atomicCAS(reinterpret_cast<unsigned long long*>(p),
+                                        static_cast<unsigned long long>(expected),
+                                        static_cast<unsigned long long>(desired)));
+    }
+    else
+    {
+        return static_cast<K>(atomicCAS(reinterpret_cast<unsigned int*>(p),
+                                        static_cast<unsigned int>(expected),
+                                        static_cast<unsigned int>(desired)));
+    }
+}
+
+template <int KIND>
+SG_D void
+store_value(const dview& t, uint32_t slot, typename kind_consts<KIND>::V v)
+{
+    if constexpr (kind_traits<KIND>::is_map)
+    {
+        using V = typename kind_consts<KIND>::V;
+        *reinterpret_cast<V*>(t.slots + static_cast<uint64_t>(slot) * kind_consts<KIND>::slot_bytes +
+                              kind_traits<KIND>::val_offset) = v;
+    }
+}
+
+// Input element i: value_type array (AoS) or separate key / mapped arrays.
+template <int KIND, bool AOS>
+SG_D void
+load_input(const void* in0, const void* in1, int64_t i, typename kind_consts<KIND>::K& key,
+           typename kind_consts<KIND>::V& val)
+{
+    using K = typename kind_consts<KIND>::K;
+    using V = typename kind_consts<KIND>::V;
+    constexpr int sb = kind_consts<KIND>::slot_bytes;
+    if constexpr (AOS)
+    {
+        if constexpr (sb == 16)
+        {
+            const uint4 d = __ldcs(reinterpret_cast<const uint4*>(in0) + i);
+            key = key_in_lane<KIND>(d, 0);
+            val = value_in_lane<KIND>(d, 0);
+        }
+        else if constexpr (sb == 8)
+        {
+            const uint2 d = __ldcs(reinterpret_cast<const uint2*>(in0) + i);
+            const uint4 q = make_uint4(d.x, d.y, 0u, 0u);
+            key = key_in_lane<KIND>(q, 0);
+            val = value_in_lane<KIND>(q, 0);
+        }
+        else
+        {
+            key = static_cast<K>(__ldcs(reinterpret_cast<const unsigned int*>(in0) + i));
+            val = V{};
+        }
+    }
+    else
+    {
+        key = __ldcs(reinterpret_cast<const K*>(in0) + i);
+        if constexpr (kind_traits<KIND>::is_map)
+        {
+            val = in1 != nullptr ? __ldcs(reinterpret_cast<const V*>(in1) + i) : V{};
+        }
+        else
+        {
+            val = V{};
+        }
+    }
+}
+
+// Out-of-band keys (EMPTY- or TOMB-valued): presence in the header, storage in the tail group.
+template <int KIND>
+SG_D int
+special_insert(const dview& t, typename kind_consts<KIND>::K key, typename kind_consts<KIND>::V val)
+{
+    using C = kind_consts<KIND>;
+    const int s = key == C::empty_key ? 0 : 1;
+    if (atomicCAS(&t.hdr->special_state[s], 0u, 2u) != 0u)
+    {
+        return 0;
+    }
+    const uint32_t slot = t.num_groups * C::slots_per_group + s;
+    *reinterpret_cast<typename C::K*>(t.slots + static_cast<uint64_t>(slot) * C::slot_bytes) = key;
+    store_value<KIND>(t, slot, val);
+    __threadfence();
+    atomicExch(&t.hdr->special_state[s], 1u);
+    return 1;
+}
+
+template <int KIND>
+SG_D bool
+special_find(const dview& t, typename kind_consts<KIND>::K key, typename kind_consts<KIND>::V& val)
+{
+    using C = kind_consts<KIND>;
+    const int s = key == C::empty_key ? 0 : 1;
+    if (*reinterpret_cast<volatile unsigned*>(&t.hdr->special_state[s]) != 1u)
+    {
+        return false;
+    }
+    const uint64_t slot = static_cast<uint64_t>(t.num_groups) * C::slots_per_group + s;
+    if constexpr (kind_traits<KIND>::is_map)
+    {
+        val = *reinterpret_cast<const volatile typename C::V*>(t.slots + slot * C::slot_bytes +
+                                                               kind_traits<KIND>::val_offset);
+    }
+    return true;
+}
+
+template <int KIND>
+SG_D int
+special_erase(const dview& t, typename kind_consts<KIND>::K key)
+{
+    using C = kind_consts<KIND>;
+    const int s = key == C::empty_key ? 0 : 1;
+    return atomicCAS(&t.hdr->special_state[s], 1u, 0u) == 1u ? 1 : 0;
+}
+
+// ---------------------------------------------------------------- tile probing
+// A tile of 4 lanes owns one key at a time.  Lane q of the tile reads sector q (bytes 32q..32q+31) of
+// the key's 128-byte probe group with one 256-bit load, so each group costs one 128-byte request and a
+// warp instruction covers 8 keys.  Measured on GB300 over an 8 GB buffer, random 128-byte lines read
+// this way reach 36-38 G lines/s, against 21-25 G with 8 lanes x 16 B and 10-12 G with one thread
+// issuing 4 x 32 B.
+
+constexpr int kTile = 4;
+
+SG_D void
+load_sector(const dview& t, uint32_t g, int q, uint32_t (&w)[8])
+{
+    const char* p = t.slots + (static_cast<uint64_t>(g) << 7) + 32 * q;
+    asm volatile("ld.global.cg.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(w[0]), "=r"(w[1]), "=r"(w[2]), "=r"(w[3]), "=r"(w[4]), "=r"(w[5]), "=r"(w[6]), "=r"(w[7])
+                 : "l"(p));
+}
+
+template <int KIND>
+struct sector_consts
+{
+    static constexpr int slot_words = kind_consts<KIND>::slot_bytes / 4;
+    static constexpr int slots = 32 / kind_consts<KIND>::slot_bytes; // slots per 32-byte sector
+};
+
+template <int KIND>
+SG_D typename kind_consts<KIND>::K
+sector_key(const uint32_t (&w)[8], int s)
+{
+    using K = typename kind_consts<KIND>::K;
+    constexpr int sw = sector_consts<KIND>::slot_words;
+    if constexpr (sizeof(K) == 8)
+    {
+        return static_cast<uint64_t>(w[sw * s + 1]) << 32 | w[sw * s];
+    }
+    else
+    {
+        return static_cast<K>(w[sw * s]);
+    }
+}
+
+template <int KIND>
+SG_D typename kind_consts<KIND>::V
+sector_value(const uint32_t (&w)[8], int s)
+{
+    using V = typename kind_consts<KIND>::V;
+    constexpr int sw = sector_consts<KIND>::slot_words;
+    constexpr int off = kind_traits<KIND>::val_offset / 4;
+    if constexpr (!kind_traits<KIND>::is_map)
+    {
+        return V{};
+    }
+    else if constexpr (sizeof(V) == 8)
+    {
+        return static_cast<uint64_t>(w[sw * s + off + 1]) << 32 | w[sw * s + off];
+    }
+    else
+    {
+        return static_cast<V>(w[sw * s + off]);
+    }
+}
+
+// Bit s set when sector slot s holds key / is never-used / is erased and below total (reusable).
+template <int KIND, bool WANT_TOMB>
+SG_D void
+sector_masks(const uint32_t (&w)[8], typename kind_consts<KIND>::K key, uint32_t first_slot, uint32_t total,
+             unsigned& m_match, unsigned& m_empty, unsigned& m_tomb)
+{
+    using C = kind_consts<KIND>;
+    constexpr int S = sector_consts<KIND>::slots;
+    m_match = 0;
+    m_empty = 0;
+    m_tomb = 0;
+#pragma unroll
+    for (int s = 0; s < S; ++s)
+    {
+        const typename C::K k = sector_key<KIND>(w, s);
+        m_match |= static_cast<unsigned>(k == key) << s;
+        m_empty |= static_cast<unsigned>(k == C::empty_key) << s;
+        if constexpr (WANT_TOMB)
+        {
+            m_tomb |= static_cast<unsigned>(k == C::tomb_key) << s;
+        }
+    }
+    if constexpr (WANT_TOMB)
+    {
+        // slots at or above total_count are never claimed
+        if (first_slot + S > total)
+        {
+            m_tomb &= first_slot >= total ? 0u : ((1u << (total - first_slot)) - 1u);
+        }
+    }
+}
+
+template <int KIND>
+SG_D typename kind_consts<KIND>::V
+select_sector_value(const uint32_t (&w)[8], unsigned one_hot)
+{
+    typename kind_consts<KIND>::V v{};
+#pragma unroll
+    for (int s = 0; s < sector_consts<KIND>::slots; ++s)
+    {
+        if (one_hot & (1u << s))
+        {
+            v = sector_value<KIND>(w, s);
+        }
+    }
+    return v;
+}
+
+// Insert of one key by one tile (all 4 lanes call it with the same key; w is this lane's sector of the
+// key's home group).  Returns 1 inserted, 0 already present, 2 refused (no free slot in the table),
+// 3 retry limit.  With REUSE, erased slots are claimed too: the tile scans to the first group holding a
+// never-used slot (so a copy of the key stored beyond an erased slot is seen) and claims the first free
+// slot of the probe sequence.  Free slots only disappear during an insert launch, so two inserts of one
+// key cannot both succeed: each has read every slot before the one it claims.
+template <int KIND, bool REUSE>
+SG_D int
+tile_insert(const dview& t, typename kind_consts<KIND>::K key, typename kind_consts<KIND>::V val, uint32_t home,
+            uint32_t (&w)[8], unsigned tmask, int tbase, int q, unsigned long long& tombs_reused)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    constexpr uint32_t G = C::slots_per_group;
+    constexpr uint32_t S = sector_consts<KIND>::slots;
+    uint32_t g = home;
+    int32_t free_slot = -1;
+    uint32_t probes = 0;
+    int retries = 0;
+    while (true)
+    {
+        unsigned mm, me, mt;
+        sector_masks<KIND, REUSE>(w, key, g * G + q * S, t.total, mm, me, mt);
+        if (__ballot_sync(tmask, mm != 0u) != 0u)
+        {
+            return 0;
+        }
+        if constexpr (REUSE)
+        {
+            if (free_slot < 0)
+            {
+                const unsigned bt = __ballot_sync(tmask, mt != 0u);
+                if (bt != 0u)
+                {
+                    const int owner = __ffs(bt) - 1;
+                    free_slot = static_cast<int32_t>(g * G + (owner - tbase) * S +
+                                                     (__ffs(__shfl_sync(tmask, mt, owner)) - 1));
+                }
+            }
+        }
+        const unsigned be = __ballot_sync(tmask, me != 0u);
+        bool claim = be != 0u;
+        if (!claim && ++probes >= t.num_groups)
+        {
+            if (!(REUSE && free_slot >= 0))
+            {
+                return 2;
+            }
+            claim = true; // no never-used slot anywhere: take the first erased slot seen
+        }
+        if (!claim)
+        {
+            g = next_group32(g, t.num_groups);
+            load_sector(t, g, q, w);
+            continue;
+        }
+        uint32_t target;
+        K expected;
+        if (REUSE && free_slot >= 0)
+        {
+            target = static_cast<uint32_t>(free_slot);
+            expected = C::tomb_key;
+        }
+        else
+        {
+            const int owner = __ffs(be) - 1;
+            target = g * G + (owner - tbase) * S + (__ffs(__shfl_sync(tmask, me, owner)) - 1);
+            expected = C::empty_key;
+        }
+        K old = expected;
+        if (q == 0)
+        {
+            old = cas_key<KIND>(t, target, expected, key);
+            if (old == expected)
+            {
+                store_value<KIND>(t, target, val);
+                tombs_reused += (expected == C::tomb_key);
+            }
+        }
+        old = __shfl_sync(tmask, old, tbase);
+        if (old == expected)
+        {
+            return 1;
+        }
+        if (old == key)
+        {
+            return 0;
+        }
+        // another key took the slot: rescan from the slot's group (every earlier group was seen without
+        // a free slot)
+        if (++retries > 65536)
+        {
+            return 3;
+        }
+        g = target / G;
+        probes = g >= home ? g - home : g + t.num_groups - home;
+        free_slot = -1;
+        load_sector(t, g, q, w);
+    }
+}
+
+// Slot of key (mapped value broadcast to the tile through val), or -1.  Stops at the first group
+// holding a never-used slot.
+template <int KIND>
+SG_D int32_t
+tile_find(const dview& t, typename kind_consts<KIND>::K key, uint32_t home, uint32_t (&w)[8], unsigned tmask,
+          int tbase, int q, typename kind_consts<KIND>::V& val)
+{
+    constexpr uint32_t G = kind_consts<KIND>::slots_per_group;
+    constexpr uint32_t S = sector_consts<KIND>::slots;
+    uint32_t g = home;
+    for (uint32_t probes = 0; probes < t.num_groups; ++probes)
+    {
+        unsigned mm, me, mt;
+        sector_masks<KIND, false>(w, key, 0, 0, mm, me, mt);
+        const unsigned bm = __ballot_sync(tmask, mm != 0u);
+        if (bm != 0u)
+        {
+            const int owner = __ffs(bm) - 1;
+            typename kind_consts<KIND>::V mine{};
+            if constexpr (kind_traits<KIND>::is_map)
+            {
+                mine = select_sector_value<KIND>(w, mm);
+            }
+            val = __shfl_sync(tmask, mine, owner);
+            const int s = __ffs(__shfl_sync(tmask, mm, owner)) - 1;
+            return static_cast<int32_t>(g * G + (owner - tbase) * S + s);
+        }
+        if (__ballot_sync(tmask, me != 0u) != 0u)
+        {
+            return -1;
+        }
+        g = next_group32(g, t.num_groups);
+        load_sector(t, g, q, w);
+    }
+    return -1;
+}
+
+// ---------------------------------------------------------------- block reduction of counters
+
+template <int N>
+SG_D void
+block_add(unsigned long long (&v)[N], unsigned long long* const (&dst)[N])
+{
+    __shared__ unsigned long long red[N][kThreads / 32];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+    {
+        unsigned long long x = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+        {
+            x += __shfl_xor_sync(0xffffffffu, x, o);
+        }
+        if (lane == 0)
+        {
+            red[k][warp] = x;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < N)
+    {
+        unsigned long long s = 0;
+        for (int w = 0; w < static_cast<int>(blockDim.x >> 5); ++w)
+        {
+            s += red[threadIdx.x][w];
+        }
+        if (s != 0 && dst[threadIdx.x] != nullptr)
+        {
+            atomicAdd(dst[threadIdx.x], s);
+        }
+    }
+}
+
+// Lanes of a warp: tiles of 4; the warp holds 32 keys (one per lane, loaded coalesced) and each tile
+// resolves the 4 keys of its own lanes in 4 rounds, after issuing the home-group loads of all 4.
+struct tile_lanes
+{
+    int lane, tbase, q;
+    unsigned tmask;
+    SG_D tile_lanes()
+    {
+        lane = threadIdx.x & 31;
+        tbase = lane & ~(kTile - 1);
+        q = lane & (kTile - 1);
+        tmask = 0xFu << tbase;
+    }
+};
+
+
+// Counts of one lane over the steps it ran.
+struct step_counts
+{
+    unsigned long long done = 0;    // inserted / erased
+    unsigned long long refused = 0; // inserts refused: no free slot left
+    unsigned long long reused = 0;  // erased slots claimed by inserts
+    unsigned long long oob = 0;     // erased out-of-band keys
+    unsigned long long retry = 0;   // retry limit reached
+};
+
+// One warp step over 32 consecutive elements (lane l owns element i; valid when i is in range), all
+// on table t.  Each tile loads the home groups of its 4 keys, then inserts them one after another.
+template <int KIND, bool AOS>
+SG_D void
+insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in1, int64_t i, bool valid,
+            uint8_t* out_flags, step_counts& c)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    K key = C::empty_key;
+    V val{};
+    if (valid)
+    {
+        load_input<KIND, AOS>(in0, in1, i, key, val);
+    }
+    const bool special = valid && key >= C::tomb_key;
+    int res = special ? special_insert<KIND>(t, key, val) : 0;
+    const bool probe = valid && !special;
+    const unsigned pmask = __ballot_sync(L.tmask, probe) >> L.tbase;
+    uint32_t pre[kTile][8];
+    uint32_t hr[kTile];
+#pragma unroll
+    for (int r = 0; r < kTile; ++r)
+    {
+        hr[r] = home_of<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r));
+        if (pmask & (1u << r))
+        {
+            load_sector(t, hr[r], L.q, pre[r]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kTile; ++r)
+    {
+        const K kr = __shfl_sync(L.tmask, key, L.tbase + r);
+        const V vr = __shfl_sync(L.tmask, val, L.tbase + r);
+        if (pmask & (1u << r))
+        {
+            const int x = tile_insert<KIND, true>(t, kr, vr, hr[r], pre[r], L.tmask, L.tbase, L.q, c.reused);
+            if (L.q == r)
+            {
+                res = x;
+            }
+        }
+    }
+    if (valid)
+    {
+        c.done += (res == 1);
+        c.refused += (res == 2);
+        c.retry += (res == 3);
+        if (out_flags != nullptr)
+        {
+            out_flags[i] = static_cast<uint8_t>(res == 1);
+        }
+    }
+}
+
+// Erase step: tiles locate the 4 keys of their lanes, then every lane swaps its own key's slot to the
+// erased marker.
+template <int KIND>
+SG_D void
+erase_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool valid, uint8_t* out_flags,
+           step_counts& c)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    const K key = valid ? __ldcs(reinterpret_cast<const K*>(keys) + i) : C::empty_key;
+    const bool special = valid && key >= C::tomb_key;
+    int res = 0;
+    if (special)
+    {
+        res = special_erase<KIND>(t, key);
+        c.oob += static_cast<unsigned long long>(res);
+    }
+    const bool probe = valid && !special;
+    const unsigned pmask = __ballot_sync(L.tmask, probe) >> L.tbase;
+    uint32_t pre[kTile][8];
+    uint32_t hr[kTile];
+#pragma unroll
+    for (int r = 0; r < kTile; ++r)
+    {
+        hr[r] = home_of<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r));
+        if (pmask & (1u << r))
+        {
+            load_sector(t, hr[r], L.q, pre[r]);
+        }
+    }
+    int32_t my_slot = -1;
+#pragma unroll
+    for (int r = 0; r < kTile; ++r)
+    {
+        if (pmask & (1u << r))
+        {
+            V dummy{};
+            const int32_t slot = tile_find<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r), hr[r], pre[r], L.tmask,
+                                                 L.tbase, L.q, dummy);
+            if (L.q == r)
+            {
+                my_slot = slot;
+            }
+        }
+    }
+    if (probe && my_slot >= 0)
+    {
+        res = cas_key<KIND>(t, static_cast<uint32_t>(my_slot), key, C::tomb_key) == key ? 1 : 0;
+    }
+    if (valid)
+    {
+        c.done += static_cast<unsigned long long>(res);
+        if (out_flags != nullptr)
+        {
+            out_flags[i] = static_cast<uint8_t>(res);
+        }
+    }
+}
+
+// Find / contains step.
+template <int KIND, bool WANT_VALUES>
+SG_D void
+find_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool valid, void* out_vals,
+          uint8_t* out_found)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    const K key = valid ? __ldcs(reinterpret_cast<const K*>(keys) + i) : C::empty_key;
+    const bool special = valid && key >= C::tomb_key;
+    V val{};
+    bool found = special ? special_find<KIND>(t, key, val) : false;
+    const bool probe = valid && !special;
+    const unsigned pmask = __ballot_sync(L.tmask, probe) >> L.tbase;
+    uint32_t pre[kTile][8];
+    uint32_t hr[kTile];
+#pragma unroll
+    for (int r = 0; r < kTile; ++r)
+    {
+        hr[r] = home_of<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r));
+        if (pmask & (1u << r))
+        {
+            load_sector(t, hr[r], L.q, pre[r]);
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kTile; ++r)
+    {
+        if (pmask & (1u << r))
+        {
+            V vr{};
+            const int32_t slot = tile_find<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r), hr[r], pre[r], L.tmask,
+                                                 L.tbase, L.q, vr);
+            if (L.q == r)
+            {
+                found = slot >= 0;
+                val = vr;
+            }
+        }
+    }
+    if (valid)
+    {
+        if (out_found != nullptr)
+        {
+            __stcs(out_found + i, static_cast<uint8_t>(found));
+        }
+        if constexpr (WANT_VALUES && kind_traits<KIND>::is_map)
+        {
+            if (found && out_vals != nullptr)
+            {
+                __stcs(reinterpret_cast<V*>(out_vals) + i, val);
+            }
+        }
+    }
+}
+
+} // namespace detail
+} // namespace sg
+
+#endif
