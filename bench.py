@@ -64,8 +64,10 @@ def parse():
     p.add_argument("--keys-log2", type=int, default=KEYS_LOG2, help="2^k keys (default: the full workload)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["voxel", "batched"], default="voxel",
-                   help="voxel: the headline map workload; batched: 4096 small sets, batched vs plain calls")
+    p.add_argument("--workload", choices=["voxel", "batched", "serve"], default="voxel",
+                   help="voxel: the headline map workload; batched: 4096 small sets, batched vs plain calls; "
+                        "serve: request stream over 256 resident maps, continuous batching vs serial calls")
+    p.add_argument("--requests", type=int, default=600, help="serve workload: number of requests")
     return p.parse_args()
 
 
@@ -385,10 +387,27 @@ def batched_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def serve_arm(args):
+    """Request stream over 256 resident maps: the native server vs serial plain calls (one GPU)."""
+    from stdgpu_gb300 import serve_bench
+    r = serve_bench.run(n_requests=args.requests)
+    small = serve_bench.run(n_requests=4 * args.requests, min_n=1 << 10, max_n=1 << 14)
+    line = {"metric": "served request stream keys/s and p50/p99 latency", "value": r["saturated"]["server_keys_per_s"],
+            "unit": "keys/s", "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64", "data": "synthetic",
+            "config": {"workload": "256 unordered_map<uint64_t,uint64_t>, capacity log-uniform 2^16..2^24; requests "
+                                   "insert 40% / find 50% / erase 10%, log-uniform 1K..4M keys, Zipf(0.99) over 2^30; "
+                                   "HBM budget 120 GB"},
+            "serve": r, "serve_small_requests": small}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == "serve":
+        serve_arm(args)
     elif args.workload == "batched":
         batched_arm(args)
     else:

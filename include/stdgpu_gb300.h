@@ -197,6 +197,76 @@ SG_API sg_status sg_batch_sizes(sg_table_batch* batch, void* stream, int64_t* ou
 SG_API sg_status sg_batch_view_of(const sg_table_batch* batch, int32_t table, sg_unordered_view* out);
 SG_API sg_status sg_batch_info(const sg_table_batch* batch, int64_t* out_storage_bytes, int32_t* out_n_tables);
 
+/* ---------------- served request stream (no counterpart in the reference) ---------------- */
+
+/* A scheduler thread keeps tables of one kind resident and executes submitted requests with
+ * continuous batching: each free launch slot takes, from every table with pending requests and
+ * nothing in flight, its run of consecutive same-operation requests; all runs of one operation share
+ * one segmented launch, and the launches of a wave run on different streams.  Requests on one table
+ * execute in submission order.  Tables are admitted, and grown (rehashed to twice the capacity)
+ * before an insert run would pass 85 % of max_size(), only while the HBM budget allows; otherwise
+ * the table admission or the request is refused with SG_ERR_BUDGET -- nothing spills to host memory.
+ * Within one run of same-operation requests the per-key inserted / erased flags of a key repeated in
+ * several requests may fall on any of them (as for duplicates within one bulk call). */
+typedef struct sg_server sg_server;
+
+typedef enum sg_server_op
+{
+    SG_SERVER_INSERT = 0,
+    SG_SERVER_FIND = 1,
+    SG_SERVER_ERASE = 2
+} sg_server_op;
+
+typedef struct sg_request
+{
+    int32_t table;      /* table id given to sg_server_admit_table */
+    int32_t op;         /* sg_server_op */
+    int64_t n;          /* keys */
+    const void* keys;   /* DEVICE, n keys; must stay valid until the request completes */
+    const void* mapped; /* DEVICE, n mapped values for inserts into maps (nullable) */
+    void* out_mapped;   /* DEVICE, n mapped values written by finds on maps (nullable) */
+    uint8_t* out_flags; /* DEVICE, n flags: inserted / found / erased (nullable) */
+} sg_request;
+
+typedef struct sg_server_stats
+{
+    int64_t requests_done;
+    int64_t keys_done;
+    double p50_us;     /* request latency, submission to completion */
+    double p99_us;
+    double max_us;
+    double keys_per_s; /* keys of completed requests over first submission .. last completion */
+    int64_t launches;
+    int64_t waves;
+    int64_t refused_budget;
+    int64_t rehashes;
+    int64_t hbm_used_bytes;
+} sg_server_stats;
+
+SG_API sg_status sg_server_create(int32_t kind, int64_t hbm_budget_bytes, int32_t n_streams, int32_t n_slots,
+                                  sg_server** out);
+/* Waits for requests in flight, then frees every table. */
+SG_API sg_status sg_server_destroy(sg_server* server);
+/* createDeviceObject(capacity) for table id `table`, if the budget allows (else SG_ERR_BUDGET). */
+SG_API sg_status sg_server_admit_table(sg_server* server, int32_t table, int64_t capacity);
+/* Waits for the table's requests, then destroyDeviceObject. */
+SG_API sg_status sg_server_drop_table(sg_server* server, int32_t table);
+/* Non-blocking; returns a ticket. */
+SG_API sg_status sg_server_submit(sg_server* server, const sg_request* request, int64_t* out_ticket);
+/* Submits n requests in order in one call (one ticket each). */
+SG_API sg_status sg_server_submit_many(sg_server* server, const sg_request* requests, int32_t n, int64_t* out_tickets);
+/* While paused, submitted requests queue and no new launch starts (launches in flight finish);
+ * resuming lets the queued requests coalesce into the next waves. */
+SG_API sg_status sg_server_set_paused(sg_server* server, int32_t paused);
+/* Waits (timeout_ms < 0: no limit) for a ticket; out_request_status: SG_OK or SG_ERR_BUDGET (refused). */
+SG_API sg_status sg_server_wait(sg_server* server, int64_t ticket, int32_t timeout_ms, sg_status* out_request_status);
+/* Waits for every submitted request. */
+SG_API sg_status sg_server_drain(sg_server* server, int32_t timeout_ms);
+SG_API sg_status sg_server_get_stats(sg_server* server, sg_server_stats* out);
+/* Waits for the table's requests, then size(). */
+SG_API sg_status sg_server_table_size(sg_server* server, int32_t table, int64_t* out_size);
+SG_API sg_status sg_server_table_view(sg_server* server, int32_t table, sg_unordered_view* out);
+
 /* ---------------- vector<T> (T = 4 or 8 bytes) ---------------- */
 
 typedef struct sg_vector sg_vector;

@@ -59,6 +59,18 @@ class sg_deque_view(ctypes.Structure):
                 ("elem_bytes", c_int32), ("pad", c_int32)]
 
 
+class sg_request(ctypes.Structure):
+    _fields_ = [("table", c_int32), ("op", c_int32), ("n", c_int64), ("keys", c_void_p), ("mapped", c_void_p),
+                ("out_mapped", c_void_p), ("out_flags", c_void_p)]
+
+
+class sg_server_stats(ctypes.Structure):
+    _fields_ = [("requests_done", c_int64), ("keys_done", c_int64), ("p50_us", ctypes.c_double),
+                ("p99_us", ctypes.c_double), ("max_us", ctypes.c_double), ("keys_per_s", ctypes.c_double),
+                ("launches", c_int64), ("waves", c_int64), ("refused_budget", c_int64), ("rehashes", c_int64),
+                ("hbm_used_bytes", c_int64)]
+
+
 # name -> (restype, argtypes); every symbol the header declares
 SIGNATURES = {
     "sg_unordered_create": (c_int32, [c_int32, c_int64, c_void_p, POINTER(c_void_p)]),
@@ -90,6 +102,18 @@ SIGNATURES = {
     "sg_batch_sizes": (c_int32, [c_void_p, c_void_p, c_void_p]),
     "sg_batch_view_of": (c_int32, [c_void_p, c_int32, POINTER(sg_unordered_view)]),
     "sg_batch_info": (c_int32, [c_void_p, POINTER(c_int64), POINTER(c_int32)]),
+    "sg_server_create": (c_int32, [c_int32, c_int64, c_int32, c_int32, POINTER(c_void_p)]),
+    "sg_server_destroy": (c_int32, [c_void_p]),
+    "sg_server_admit_table": (c_int32, [c_void_p, c_int32, c_int64]),
+    "sg_server_drop_table": (c_int32, [c_void_p, c_int32]),
+    "sg_server_submit": (c_int32, [c_void_p, POINTER(sg_request), POINTER(c_int64)]),
+    "sg_server_submit_many": (c_int32, [c_void_p, POINTER(sg_request), c_int32, POINTER(c_int64)]),
+    "sg_server_set_paused": (c_int32, [c_void_p, c_int32]),
+    "sg_server_wait": (c_int32, [c_void_p, c_int64, c_int32, POINTER(c_int32)]),
+    "sg_server_drain": (c_int32, [c_void_p, c_int32]),
+    "sg_server_get_stats": (c_int32, [c_void_p, POINTER(sg_server_stats)]),
+    "sg_server_table_size": (c_int32, [c_void_p, c_int32, POINTER(c_int64)]),
+    "sg_server_table_view": (c_int32, [c_void_p, c_int32, POINTER(sg_unordered_view)]),
     "sg_vector_create": (c_int32, [c_int32, c_int64, POINTER(c_void_p)]),
     "sg_vector_destroy": (c_int32, [c_void_p]),
     "sg_vector_push_back": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),

@@ -1,0 +1,1061 @@
+// Served request stream over device-resident tables (no counterpart in the reference).
+//
+// A scheduler thread keeps tables resident in HBM and turns submitted insert / find / erase requests
+// into launches.  Continuous batching: whenever a launch slot is free, every table that has pending
+// requests and nothing in flight contributes its longest run of consecutive same-operation requests;
+// all runs of one operation go into one segmented launch (one segment per request), the launches of a
+// wave go to different streams, and requests that arrive while earlier waves are on the GPU join the
+// next wave.  A table stays busy until its wave completes, so every table sees its requests in
+// submission order.  Tables are admitted, and grown before an insert run that would pass 85 % of
+// max_size(), only while the HBM budget allows; otherwise the request is refused (SG_ERR_BUDGET)
+// rather than spilled.  Latency is measured per request from submission to completion.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstdint>
+#include <deque>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "sg_internal.cuh"
+#include "stdgpu_gb300.h"
+#include "table_core.cuh"
+
+namespace sg
+{
+namespace detail
+{
+
+// One request's share of a segmented launch.
+struct seg_desc
+{
+    dview view;
+    const void* in0;
+    const void* in1;
+    void* out_vals;
+    uint8_t* out_flags;
+    int64_t n;
+};
+
+constexpr int kSegThreads = 128;
+
+SG_D int32_t
+segment_of(const int64_t* prefix, int32_t nseg, int64_t x)
+{
+    int32_t t = 0;
+    if ((threadIdx.x & 31) == 0)
+    {
+        int32_t lo = 0, hi = nseg; // prefix[lo] <= x < prefix[hi]
+        while (hi - lo > 1)
+        {
+            const int32_t mid = (lo + hi) >> 1;
+            if (__ldg(prefix + mid) <= x)
+            {
+                lo = mid;
+            }
+            else
+            {
+                hi = mid;
+            }
+        }
+        t = lo;
+    }
+    return __shfl_sync(0xffffffffu, t, 0);
+}
+
+SG_D unsigned long long
+seg_warp_sum(unsigned long long v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    }
+    return v;
+}
+
+// OP: 0 insert (key / mapped arrays), 1 find, 2 erase.  prefix[s] = tiles before segment s.  Each warp
+// walks kSegTilesPerStep consecutive tiles at a time, looks the segment up again only when it crosses
+// a segment boundary, and adds its counts to the segment's table when it leaves the segment.
+constexpr int kSegTilesPerStep = 8;
+
+template <int KIND, int OP>
+__global__ void __launch_bounds__(kSegThreads)
+k_segments(const seg_desc* segs, const int64_t* prefix, int32_t nseg)
+{
+    const tile_lanes L;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    const int64_t tiles = __ldg(prefix + nseg);
+    for (int64_t x0 = warp * kSegTilesPerStep; x0 < tiles; x0 += nwarps * kSegTilesPerStep)
+    {
+        const int64_t x1 = x0 + kSegTilesPerStep < tiles ? x0 + kSegTilesPerStep : tiles;
+        int32_t s = segment_of(prefix, nseg, x0);
+        seg_desc d = segs[s];
+        int64_t s_begin = __ldg(prefix + s);
+        int64_t s_end = __ldg(prefix + s + 1);
+        step_counts c;
+        for (int64_t x = x0; x < x1; ++x)
+        {
+            if (x >= s_end)
+            {
+                // leaving segment s: flush its counts, move to the next non-empty segment
+                if constexpr (OP != 1)
+                {
+                    const unsigned long long dn = seg_warp_sum(c.done), rf = seg_warp_sum(c.refused),
+                                             ru = seg_warp_sum(c.reused), ob = seg_warp_sum(c.oob);
+                    if (L.lane == 0 && (dn | rf | ru) != 0)
+                    {
+                        if (OP == 0)
+                        {
+                            atomicAdd(&d.view.hdr->size, dn);
+                            atomicAdd(&d.view.hdr->refused, rf);
+                            atomicAdd(&d.view.hdr->tombstones, 0ull - ru);
+                        }
+                        else
+                        {
+                            atomicAdd(&d.view.hdr->size, 0ull - dn);
+                            atomicAdd(&d.view.hdr->tombstones, dn - ob);
+                        }
+                    }
+                    c = step_counts{};
+                }
+                s = segment_of(prefix, nseg, x);
+                d = segs[s];
+                s_begin = __ldg(prefix + s);
+                s_end = __ldg(prefix + s + 1);
+            }
+            const int64_t i = (x - s_begin) * 32 + L.lane;
+            const bool valid = i < d.n;
+            if constexpr (OP == 0)
+            {
+                insert_step<KIND, false>(d.view, L, d.in0, d.in1, i, valid, d.out_flags, c);
+            }
+            else if constexpr (OP == 1)
+            {
+                find_step<KIND, true>(d.view, L, d.in0, i, valid, d.out_vals, d.out_flags);
+            }
+            else
+            {
+                erase_step<KIND>(d.view, L, d.in0, i, valid, d.out_flags, c);
+            }
+        }
+        if constexpr (OP != 1)
+        {
+            const unsigned long long dn = seg_warp_sum(c.done), rf = seg_warp_sum(c.refused),
+                                     ru = seg_warp_sum(c.reused), ob = seg_warp_sum(c.oob);
+            if (L.lane == 0 && (dn | rf | ru) != 0)
+            {
+                if (OP == 0)
+                {
+                    atomicAdd(&d.view.hdr->size, dn);
+                    atomicAdd(&d.view.hdr->refused, rf);
+                    atomicAdd(&d.view.hdr->tombstones, 0ull - ru);
+                }
+                else
+                {
+                    atomicAdd(&d.view.hdr->size, 0ull - dn);
+                    atomicAdd(&d.view.hdr->tombstones, dn - ob);
+                }
+            }
+        }
+    }
+}
+
+template <int KIND>
+sg_status
+launch_segments(int op, const seg_desc* segs, const int64_t* prefix, int32_t nseg, int64_t tiles, int grid_cap,
+                cudaStream_t s)
+{
+    const int64_t want = (tiles * 32 / kSegTilesPerStep + kSegThreads - 1) / kSegThreads;
+    const int grid = static_cast<int>(want < grid_cap ? (want < 1 ? 1 : want) : grid_cap);
+    if (op == 0)
+    {
+        k_segments<KIND, 0><<<grid, kSegThreads, 0, s>>>(segs, prefix, nseg);
+    }
+    else if (op == 1)
+    {
+        k_segments<KIND, 1><<<grid, kSegThreads, 0, s>>>(segs, prefix, nseg);
+    }
+    else
+    {
+        k_segments<KIND, 2><<<grid, kSegThreads, 0, s>>>(segs, prefix, nseg);
+    }
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+}
+
+sg_status
+launch_segments_kind(int kind, int op, const seg_desc* segs, const int64_t* prefix, int32_t nseg, int64_t tiles,
+                     int grid_cap, cudaStream_t s)
+{
+    switch (kind)
+    {
+        case 0:
+            return launch_segments<0>(op, segs, prefix, nseg, tiles, grid_cap, s);
+        case 1:
+            return launch_segments<1>(op, segs, prefix, nseg, tiles, grid_cap, s);
+        case 2:
+            return launch_segments<2>(op, segs, prefix, nseg, tiles, grid_cap, s);
+        case 3:
+            return launch_segments<3>(op, segs, prefix, nseg, tiles, grid_cap, s);
+        case 4:
+            return launch_segments<4>(op, segs, prefix, nseg, tiles, grid_cap, s);
+        case 5:
+            return launch_segments<5>(op, segs, prefix, nseg, tiles, grid_cap, s);
+        default:
+            return SG_ERR_BAD_ARG;
+    }
+}
+
+} // namespace detail
+} // namespace sg
+
+using namespace sg::detail;
+
+namespace
+{
+
+using clock_type = std::chrono::steady_clock;
+
+constexpr int kSlotSegments = 4096;          // segments one launch slot can carry
+constexpr int64_t kDirectKeys = int64_t{ 1 } << 16; // requests this large run as their own single-table launch
+
+struct request_rec
+{
+    sg_request r{};
+    sg_status status = SG_OK;
+    clock_type::time_point t_submit;
+    clock_type::time_point t_done;
+    bool done = false;
+};
+
+struct table_rec
+{
+    sg_unordered* h = nullptr;
+    int64_t capacity = 0;
+    int64_t max_size = 0;
+    int64_t bytes = 0;
+    int64_t size_bound = 0; // upper bound of size(): exact after a check, plus keys inserted since
+    std::deque<int64_t> fifo;
+    bool busy = false;
+};
+
+// Device and pinned host memory of one in-flight launch group (a wave).
+struct launch_slot
+{
+    seg_desc* d_segs = nullptr;
+    int64_t* d_prefix = nullptr;
+    seg_desc* h_segs = nullptr;
+    int64_t* h_prefix = nullptr;
+    cudaEvent_t done = nullptr;
+    bool in_use = false;
+    std::vector<int64_t> tickets;
+    std::vector<int32_t> tables;
+};
+
+} // namespace
+
+struct sg_server
+{
+    int32_t kind = 0;
+    int64_t budget = 0;
+    int64_t used = 0;
+    int grid_cap = 0;
+    std::vector<cudaStream_t> streams;
+    int next_stream = 0;
+    std::vector<launch_slot> slots;
+    std::mutex m;
+    std::condition_variable cv_work;
+    std::condition_variable cv_done;
+    std::unordered_map<int32_t, table_rec> tables;
+    std::deque<request_rec> reqs; // index = ticket - ticket_base
+    int64_t ticket_base = 0;
+    std::vector<double> latencies_us;
+    int64_t keys_done = 0;
+    int64_t launches = 0;
+    int64_t waves = 0;
+    int64_t refused_budget = 0;
+    int64_t rehashes = 0;
+    clock_type::time_point t_first{}, t_last{};
+    bool any_done = false;
+    bool stop = false;
+    bool paused = false;
+    std::atomic<uint64_t> submissions{ 0 }; // bumped by every submit: wakes the scheduler's spin
+    std::thread worker;
+    int device = 0;
+
+    request_rec&
+    rec(int64_t ticket)
+    {
+        return reqs[static_cast<size_t>(ticket - ticket_base)];
+    }
+
+    void run();
+    bool complete_finished();
+    bool form_wave();
+    sg_status grow(table_rec& t, int64_t need);
+};
+
+namespace
+{
+
+int64_t
+table_bytes(int32_t kind, int64_t capacity, int64_t* max_size)
+{
+    sg_geometry g{};
+    if (sg_unordered_geometry_for(kind, capacity, &g) != SG_OK)
+    {
+        return -1;
+    }
+    *max_size = g.max_size;
+    return g.storage_bytes;
+}
+
+dview
+kernel_view(sg_unordered* h)
+{
+    sg_unordered_view v{};
+    sg_unordered_view_of(h, &v);
+    return dview{ static_cast<char*>(v.slots), static_cast<table_header*>(v.header),
+                  static_cast<uint32_t>(v.num_groups), static_cast<uint32_t>(v.total_count), v.bucket_bits };
+}
+
+} // namespace
+
+// Completes every wave whose event has fired.  Caller holds the lock.
+bool
+sg_server::complete_finished()
+{
+    bool any = false;
+    for (auto& sl : slots)
+    {
+        if (!sl.in_use || cudaEventQuery(sl.done) != cudaSuccess)
+        {
+            continue;
+        }
+        const auto now = clock_type::now();
+        for (int64_t tk : sl.tickets)
+        {
+            request_rec& r = rec(tk);
+            r.done = true;
+            r.t_done = now;
+            latencies_us.push_back(std::chrono::duration<double, std::micro>(now - r.t_submit).count());
+            keys_done += r.r.n;
+        }
+        for (int32_t t : sl.tables)
+        {
+            auto it = tables.find(t);
+            if (it != tables.end())
+            {
+                it->second.busy = false;
+            }
+        }
+        t_last = now;
+        sl.tickets.clear();
+        sl.tables.clear();
+        sl.in_use = false;
+        any = true;
+    }
+    return any;
+}
+
+// Grows table t (rehash into a table of twice the capacity, until `need` elements fit under 85 %
+// of max_size) when the budget allows.  Caller holds the lock; the table has nothing in flight.
+sg_status
+sg_server::grow(table_rec& t, int64_t need)
+{
+    int64_t cap = t.capacity;
+    int64_t ms = 0;
+    int64_t bytes = 0;
+    do
+    {
+        cap *= 2;
+        bytes = table_bytes(kind, cap, &ms);
+        if (bytes < 0)
+        {
+            return SG_ERR_BUDGET;
+        }
+    } while (need > ms * 85 / 100);
+    const int64_t elem = slot_bytes_of_kind(kind);
+    int64_t cur = 0;
+    sg_status st = sg_unordered_size(t.h, nullptr, &cur);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    const int64_t temp = (cur + 2) * 16;
+    if (used + bytes + temp > budget)
+    {
+        return SG_ERR_BUDGET;
+    }
+    sg_unordered* nh = nullptr;
+    st = sg_unordered_create(kind, cap, nullptr, &nh);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    void* keys = nullptr;
+    void* vals = nullptr;
+    if (cudaMalloc(&keys, static_cast<size_t>((cur + 2) * 8)) != cudaSuccess ||
+        cudaMalloc(&vals, static_cast<size_t>((cur + 2) * 8)) != cudaSuccess)
+    {
+        cudaFree(keys);
+        sg_unordered_destroy(nh);
+        cudaGetLastError();
+        return SG_ERR_OOM;
+    }
+    int64_t n = 0;
+    const bool is_map = kind >= SG_MAP_U64_U32;
+    st = sg_unordered_range_copy(t.h, keys, is_map ? vals : nullptr, nullptr, &n);
+    if (st == SG_OK && n > 0)
+    {
+        st = sg_unordered_insert_kv(nh, keys, is_map ? vals : nullptr, n, nullptr, nullptr);
+    }
+    if (st == SG_OK)
+    {
+        st = cudaDeviceSynchronize() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
+    }
+    cudaFree(keys);
+    cudaFree(vals);
+    (void)elem;
+    if (st != SG_OK)
+    {
+        sg_unordered_destroy(nh);
+        return st;
+    }
+    sg_unordered_destroy(t.h);
+    used += bytes - t.bytes;
+    t.h = nh;
+    t.capacity = cap;
+    t.max_size = ms;
+    t.bytes = bytes;
+    t.size_bound = n;
+    ++rehashes;
+    return SG_OK;
+}
+
+// Forms and launches one wave if a slot is free and some table has runnable requests.  Caller holds
+// the lock.
+bool
+sg_server::form_wave()
+{
+    launch_slot* sl = nullptr;
+    for (auto& s : slots)
+    {
+        if (!s.in_use)
+        {
+            sl = &s;
+            break;
+        }
+    }
+    if (sl == nullptr)
+    {
+        return false;
+    }
+    // runs[op] = (table, ticket) pairs, in table order then FIFO order
+    std::vector<std::pair<int32_t, int64_t>> runs[3];
+    int nseg = 0;
+    for (auto& kv : tables)
+    {
+        table_rec& t = kv.second;
+        if (t.busy || t.fifo.empty())
+        {
+            continue;
+        }
+        const int op = rec(t.fifo.front()).r.op;
+        int64_t run_keys = 0;
+        size_t take = 0;
+        while (take < t.fifo.size() && rec(t.fifo[take]).r.op == op && nseg + static_cast<int>(take) < kSlotSegments)
+        {
+            run_keys += rec(t.fifo[take]).r.n;
+            ++take;
+        }
+        if (take == 0)
+        {
+            continue;
+        }
+        if (op == SG_SERVER_INSERT && t.size_bound + run_keys > t.max_size * 85 / 100)
+        {
+            int64_t exact = 0;
+            if (sg_unordered_size(t.h, nullptr, &exact) == SG_OK)
+            {
+                t.size_bound = exact;
+            }
+            if (t.size_bound + run_keys > t.max_size * 85 / 100 && grow(t, t.size_bound + run_keys) != SG_OK)
+            {
+                // refuse the run rather than spill: these requests complete with SG_ERR_BUDGET
+                const auto now = clock_type::now();
+                for (size_t k = 0; k < take; ++k)
+                {
+                    request_rec& r = rec(t.fifo.front());
+                    r.status = SG_ERR_BUDGET;
+                    r.done = true;
+                    r.t_done = now;
+                    ++refused_budget;
+                    t.fifo.pop_front();
+                }
+                continue;
+            }
+        }
+        if (op == SG_SERVER_INSERT)
+        {
+            t.size_bound += run_keys;
+        }
+        for (size_t k = 0; k < take; ++k)
+        {
+            runs[op].push_back({ kv.first, t.fifo.front() });
+            t.fifo.pop_front();
+        }
+        nseg += static_cast<int>(take);
+        t.busy = true;
+        sl->tables.push_back(kv.first);
+    }
+    if (nseg == 0)
+    {
+        if (!sl->tables.empty())
+        {
+            sl->tables.clear();
+        }
+        cv_done.notify_all();
+        return false;
+    }
+    // large requests run as their own single-table launches; the rest are packed into one segmented
+    // launch per operation (descriptors: op 0 first, then 1, then 2)
+    std::vector<std::pair<int32_t, int64_t>> direct;
+    for (int op = 0; op < 3; ++op)
+    {
+        std::vector<std::pair<int32_t, int64_t>> packed;
+        for (const auto& tr : runs[op])
+        {
+            (rec(tr.second).r.n >= kDirectKeys ? direct : packed).push_back(tr);
+        }
+        runs[op].swap(packed);
+    }
+    int base = 0;
+    int op_first[3], op_count[3];
+    int64_t op_tiles[3];
+    for (int op = 0; op < 3; ++op)
+    {
+        op_first[op] = base;
+        op_count[op] = static_cast<int>(runs[op].size());
+        int64_t tiles = 0;
+        for (const auto& tr : runs[op])
+        {
+            const request_rec& r = rec(tr.second);
+            seg_desc& d = sl->h_segs[base];
+            d.view = kernel_view(tables[tr.first].h);
+            d.in0 = r.r.keys;
+            d.in1 = r.r.mapped;
+            d.out_vals = r.r.out_mapped;
+            d.out_flags = r.r.out_flags;
+            d.n = r.r.n;
+            sl->h_prefix[base + op] = tiles; // per-op prefix arrays are laid out back to back
+            tiles += (r.r.n + 31) / 32;
+            sl->tickets.push_back(tr.second);
+            ++base;
+        }
+        sl->h_prefix[base + op] = tiles;
+        op_tiles[op] = tiles;
+    }
+    cudaStream_t s0 = streams[next_stream];
+    next_stream = (next_stream + 1) % static_cast<int>(streams.size());
+    bool ok = cudaMemcpyAsync(sl->d_segs, sl->h_segs, sizeof(seg_desc) * base, cudaMemcpyHostToDevice, s0) ==
+                      cudaSuccess &&
+              cudaMemcpyAsync(sl->d_prefix, sl->h_prefix, sizeof(int64_t) * (base + 3), cudaMemcpyHostToDevice, s0) ==
+                      cudaSuccess;
+    cudaEvent_t staged = nullptr;
+    cudaEventCreateWithFlags(&staged, cudaEventDisableTiming);
+    cudaEventRecord(staged, s0);
+    std::vector<cudaStream_t> used_streams;
+    for (int op = 0; op < 3 && ok; ++op)
+    {
+        if (op_count[op] == 0)
+        {
+            continue;
+        }
+        cudaStream_t s = streams[next_stream];
+        next_stream = (next_stream + 1) % static_cast<int>(streams.size());
+        cudaStreamWaitEvent(s, staged, 0);
+        ok = launch_segments_kind(kind, op, sl->d_segs + op_first[op], sl->d_prefix + op_first[op] + op,
+                                  op_count[op], op_tiles[op], grid_cap, s) == SG_OK;
+        used_streams.push_back(s);
+        ++launches;
+    }
+    for (const auto& tr : direct)
+    {
+        if (!ok)
+        {
+            break;
+        }
+        const request_rec& r = rec(tr.second);
+        sg_unordered* h = tables[tr.first].h;
+        cudaStream_t s = streams[next_stream];
+        next_stream = (next_stream + 1) % static_cast<int>(streams.size());
+        sg_status st = SG_OK;
+        if (r.r.op == SG_SERVER_INSERT)
+        {
+            st = sg_unordered_insert_kv(h, r.r.keys, r.r.mapped, r.r.n, r.r.out_flags, s);
+        }
+        else if (r.r.op == SG_SERVER_FIND)
+        {
+            st = sg_unordered_find(h, r.r.keys, r.r.n, r.r.out_mapped, r.r.out_flags, s);
+        }
+        else
+        {
+            st = sg_unordered_erase(h, r.r.keys, r.r.n, r.r.out_flags, s);
+        }
+        ok = st == SG_OK;
+        sl->tickets.push_back(tr.second);
+        used_streams.push_back(s);
+        ++launches;
+    }
+    // the wave is done when every stream it used is done
+    for (cudaStream_t s : used_streams)
+    {
+        if (s != s0)
+        {
+            cudaEvent_t e = nullptr;
+            cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+            cudaEventRecord(e, s);
+            cudaStreamWaitEvent(s0, e, 0);
+            cudaEventDestroy(e);
+        }
+    }
+    cudaEventRecord(sl->done, s0);
+    cudaEventDestroy(staged);
+    sl->in_use = true;
+    ++waves;
+    if (!ok)
+    {
+        for (int64_t tk : sl->tickets)
+        {
+            rec(tk).status = SG_ERR_CUDA;
+        }
+    }
+    return true;
+}
+
+void
+sg_server::run()
+{
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lock(m);
+    while (true)
+    {
+        const bool finished = complete_finished();
+        if (finished)
+        {
+            cv_done.notify_all();
+        }
+        bool launched = false;
+        while (!paused && form_wave())
+        {
+            launched = true;
+        }
+        if (stop)
+        {
+            bool idle = true;
+            for (auto& s : slots)
+            {
+                idle = idle && !s.in_use;
+            }
+            if (idle)
+            {
+                break;
+            }
+        }
+        bool in_flight = false;
+        for (auto& s : slots)
+        {
+            in_flight = in_flight || s.in_use;
+        }
+        if (in_flight)
+        {
+            // Spin outside the lock until a wave completes or a request arrives; only this thread
+            // touches the slots' events.  After ~200 us of spinning, yield the core between polls.
+            const uint64_t seen = submissions.load(std::memory_order_acquire);
+            lock.unlock();
+            const auto t0 = clock_type::now();
+            while (true)
+            {
+                bool ready = false;
+                for (auto& sl : slots)
+                {
+                    if (sl.in_use && cudaEventQuery(sl.done) == cudaSuccess)
+                    {
+                        ready = true;
+                        break;
+                    }
+                }
+                if (ready || submissions.load(std::memory_order_acquire) != seen)
+                {
+                    break;
+                }
+                if (clock_type::now() - t0 > std::chrono::microseconds(200))
+                {
+                    std::this_thread::yield();
+                }
+            }
+            lock.lock();
+        }
+        else if (!launched)
+        {
+            cv_work.wait_for(lock, std::chrono::milliseconds(5));
+        }
+    }
+    cv_done.notify_all();
+}
+
+extern "C" {
+
+sg_status
+sg_server_create(int32_t kind, int64_t hbm_budget_bytes, int32_t n_streams, int32_t n_slots, sg_server** out)
+{
+    if (out == nullptr || kind < SG_SET_U32 || kind > SG_MAP_U32_U64 || hbm_budget_bytes <= 0 || n_streams < 1 ||
+        n_streams > 64 || n_slots < 1 || n_slots > 256)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    *out = nullptr;
+    auto* srv = new (std::nothrow) sg_server{};
+    if (srv == nullptr)
+    {
+        return SG_ERR_OOM;
+    }
+    srv->kind = kind;
+    srv->budget = hbm_budget_bytes;
+    cudaGetDevice(&srv->device);
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, srv->device);
+    srv->grid_cap = sms * 8;
+    srv->streams.resize(n_streams);
+    for (auto& s : srv->streams)
+    {
+        cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    }
+    srv->slots.resize(n_slots);
+    for (auto& sl : srv->slots)
+    {
+        if (cudaMalloc(&sl.d_segs, sizeof(seg_desc) * kSlotSegments) != cudaSuccess ||
+            cudaMalloc(&sl.d_prefix, sizeof(int64_t) * (kSlotSegments + 3)) != cudaSuccess ||
+            cudaMallocHost(&sl.h_segs, sizeof(seg_desc) * kSlotSegments) != cudaSuccess ||
+            cudaMallocHost(&sl.h_prefix, sizeof(int64_t) * (kSlotSegments + 3)) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess)
+        {
+            cudaGetLastError();
+            sg_server_destroy(srv);
+            return SG_ERR_OOM;
+        }
+    }
+    srv->worker = std::thread([srv] { srv->run(); });
+    *out = srv;
+    return SG_OK;
+}
+
+sg_status
+sg_server_destroy(sg_server* srv)
+{
+    if (srv == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    {
+        std::lock_guard<std::mutex> lock(srv->m);
+        srv->stop = true;
+    }
+    srv->cv_work.notify_all();
+    if (srv->worker.joinable())
+    {
+        srv->worker.join();
+    }
+    cudaDeviceSynchronize();
+    for (auto& kv : srv->tables)
+    {
+        sg_unordered_destroy(kv.second.h);
+    }
+    for (auto& sl : srv->slots)
+    {
+        cudaFree(sl.d_segs);
+        cudaFree(sl.d_prefix);
+        if (sl.h_segs != nullptr)
+        {
+            cudaFreeHost(sl.h_segs);
+        }
+        if (sl.h_prefix != nullptr)
+        {
+            cudaFreeHost(sl.h_prefix);
+        }
+        if (sl.done != nullptr)
+        {
+            cudaEventDestroy(sl.done);
+        }
+    }
+    for (auto& s : srv->streams)
+    {
+        cudaStreamDestroy(s);
+    }
+    delete srv;
+    return SG_OK;
+}
+
+sg_status
+sg_server_admit_table(sg_server* srv, int32_t table, int64_t capacity)
+{
+    if (srv == nullptr || table < 0 || capacity <= 0)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    std::lock_guard<std::mutex> lock(srv->m);
+    if (srv->tables.count(table) != 0)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    int64_t ms = 0;
+    const int64_t bytes = table_bytes(srv->kind, capacity, &ms);
+    if (bytes < 0)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (srv->used + bytes > srv->budget)
+    {
+        return SG_ERR_BUDGET;
+    }
+    table_rec t;
+    const sg_status st = sg_unordered_create(srv->kind, capacity, nullptr, &t.h);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess)
+    {
+        sg_unordered_destroy(t.h);
+        return SG_ERR_CUDA;
+    }
+    t.capacity = capacity;
+    t.max_size = ms;
+    t.bytes = bytes;
+    srv->used += bytes;
+    srv->tables.emplace(table, std::move(t));
+    return SG_OK;
+}
+
+sg_status
+sg_server_drop_table(sg_server* srv, int32_t table)
+{
+    if (srv == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    std::unique_lock<std::mutex> lock(srv->m);
+    auto it = srv->tables.find(table);
+    if (it == srv->tables.end())
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    srv->cv_done.wait(lock, [&] { return !it->second.busy && it->second.fifo.empty(); });
+    sg_unordered_destroy(it->second.h);
+    srv->used -= it->second.bytes;
+    srv->tables.erase(it);
+    return SG_OK;
+}
+
+sg_status
+sg_server_submit_many(sg_server* srv, const sg_request* reqs, int32_t n, int64_t* out_tickets)
+{
+    if (srv == nullptr || (n > 0 && (reqs == nullptr || out_tickets == nullptr)) || n < 0)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    for (int32_t k = 0; k < n; ++k)
+    {
+        const sg_request& r = reqs[k];
+        if (r.n < 0 || (r.n > 0 && r.keys == nullptr) || r.op < SG_SERVER_INSERT || r.op > SG_SERVER_ERASE)
+        {
+            return SG_ERR_BAD_ARG;
+        }
+    }
+    {
+        std::lock_guard<std::mutex> lock(srv->m);
+        if (srv->stop)
+        {
+            return SG_ERR_BAD_ARG;
+        }
+        for (int32_t k = 0; k < n; ++k)
+        {
+            if (srv->tables.find(reqs[k].table) == srv->tables.end())
+            {
+                return SG_ERR_BAD_ARG;
+            }
+        }
+        const auto now = clock_type::now();
+        for (int32_t k = 0; k < n; ++k)
+        {
+            const int64_t ticket = srv->ticket_base + static_cast<int64_t>(srv->reqs.size());
+            request_rec r;
+            r.r = reqs[k];
+            r.t_submit = now;
+            if (!srv->any_done)
+            {
+                srv->t_first = now;
+                srv->any_done = true;
+            }
+            if (reqs[k].n == 0)
+            {
+                r.done = true;
+                r.t_done = now;
+                srv->reqs.push_back(r);
+            }
+            else
+            {
+                srv->reqs.push_back(r);
+                srv->tables[reqs[k].table].fifo.push_back(ticket);
+            }
+            out_tickets[k] = ticket;
+        }
+    }
+    srv->submissions.fetch_add(1, std::memory_order_release);
+    srv->cv_work.notify_one();
+    return SG_OK;
+}
+
+sg_status
+sg_server_submit(sg_server* srv, const sg_request* req, int64_t* out_ticket)
+{
+    return sg_server_submit_many(srv, req, req != nullptr ? 1 : 0, out_ticket);
+}
+
+sg_status
+sg_server_set_paused(sg_server* srv, int32_t paused)
+{
+    if (srv == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    {
+        std::lock_guard<std::mutex> lock(srv->m);
+        srv->paused = paused != 0;
+    }
+    srv->cv_work.notify_all();
+    return SG_OK;
+}
+
+sg_status
+sg_server_wait(sg_server* srv, int64_t ticket, int32_t timeout_ms, sg_status* out_request_status)
+{
+    if (srv == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    std::unique_lock<std::mutex> lock(srv->m);
+    if (ticket < srv->ticket_base || ticket >= srv->ticket_base + static_cast<int64_t>(srv->reqs.size()))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    const bool ok = srv->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms < 0 ? 3600000 : timeout_ms),
+                                          [&] { return srv->rec(ticket).done; });
+    if (!ok)
+    {
+        return SG_ERR_RETRY_EXHAUSTED;
+    }
+    if (out_request_status != nullptr)
+    {
+        *out_request_status = srv->rec(ticket).status;
+    }
+    return SG_OK;
+}
+
+sg_status
+sg_server_drain(sg_server* srv, int32_t timeout_ms)
+{
+    if (srv == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    std::unique_lock<std::mutex> lock(srv->m);
+    const bool ok = srv->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms < 0 ? 3600000 : timeout_ms), [&] {
+        for (const auto& r : srv->reqs)
+        {
+            if (!r.done)
+            {
+                return false;
+            }
+        }
+        return true;
+    });
+    return ok ? SG_OK : SG_ERR_RETRY_EXHAUSTED;
+}
+
+sg_status
+sg_server_get_stats(sg_server* srv, sg_server_stats* out)
+{
+    if (srv == nullptr || out == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    std::lock_guard<std::mutex> lock(srv->m);
+    std::vector<double> v = srv->latencies_us;
+    std::sort(v.begin(), v.end());
+    auto pct = [&](double p) {
+        if (v.empty())
+        {
+            return 0.0;
+        }
+        size_t k = static_cast<size_t>(p * static_cast<double>(v.size() - 1) + 0.5);
+        return v[std::min(k, v.size() - 1)];
+    };
+    out->requests_done = static_cast<int64_t>(v.size());
+    out->keys_done = srv->keys_done;
+    out->p50_us = pct(0.50);
+    out->p99_us = pct(0.99);
+    out->max_us = v.empty() ? 0.0 : v.back();
+    const double span = srv->any_done ? std::chrono::duration<double>(srv->t_last - srv->t_first).count() : 0.0;
+    out->keys_per_s = span > 0 ? static_cast<double>(srv->keys_done) / span : 0.0;
+    out->launches = srv->launches;
+    out->waves = srv->waves;
+    out->refused_budget = srv->refused_budget;
+    out->rehashes = srv->rehashes;
+    out->hbm_used_bytes = srv->used;
+    return SG_OK;
+}
+
+sg_status
+sg_server_table_view(sg_server* srv, int32_t table, sg_unordered_view* out)
+{
+    if (srv == nullptr || out == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    std::lock_guard<std::mutex> lock(srv->m);
+    auto it = srv->tables.find(table);
+    if (it == srv->tables.end())
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    return sg_unordered_view_of(it->second.h, out);
+}
+
+sg_status
+sg_server_table_size(sg_server* srv, int32_t table, int64_t* out_size)
+{
+    if (srv == nullptr || out_size == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    std::unique_lock<std::mutex> lock(srv->m);
+    auto it = srv->tables.find(table);
+    if (it == srv->tables.end())
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    srv->cv_done.wait(lock, [&] { return !it->second.busy && it->second.fifo.empty(); });
+    return sg_unordered_size(it->second.h, nullptr, out_size);
+}
+
+} // extern "C"

@@ -1,0 +1,157 @@
+"""Served request stream workload: continuous batching vs serial plain calls (one GB300).
+
+256 live unordered_map<uint64_t, uint64_t> tables, capacity log-uniform in 2^16..2^24.  Each request
+picks a table uniformly and is an insert (40 %), find (50 %) or erase (10 %) of a log-uniform 1K..4M
+keys drawn Zipf(0.99) over a 2^30-rank universe per table (rank -> key by a seeded bijective 64-bit
+mix, salted per table); values are a hash of the key.  HBM budget 120 GB.  Measured:
+
+* saturated throughput: all requests submitted back to back, server vs serial plain calls (one
+  request at a time, each a C-ABI call on the table's own object followed by a stream sync);
+* latency under load: Poisson arrivals at a rate that keeps the device >= 80 % busy (80 % of the
+  server's saturated request rate), p50 / p99 of submission-to-completion for the server and for the
+  serial path fed the same arrivals.
+
+The serial path's tables are created at the capacity each table reaches in the server run, so it
+pays no rehash.
+"""
+
+from __future__ import annotations
+
+import time
+from ctypes import c_void_p
+
+import numpy as np
+import torch
+
+from . import _native as N
+from . import containers as C
+from . import server as S
+from . import workloads as W
+
+
+def zipf_ranks(rng, n, universe=2**30, s=0.99):
+    u = rng.random(n)
+    a = 1.0 - s
+    return np.floor((1.0 + u * (universe ** a - 1.0)) ** (1.0 / a)).astype(np.uint64)
+
+
+def make_stream(n_tables=256, n_requests=600, seed=0, min_n=1 << 10, max_n=1 << 22):
+    rng = np.random.default_rng(seed)
+    caps = np.exp(rng.uniform(np.log(2**16), np.log(2**24), size=n_tables)).astype(np.int64)
+    salts = W.mix64(np.arange(n_tables, dtype=np.uint64) + np.uint64(12345))
+    reqs = []
+    for _ in range(n_requests):
+        t = int(rng.integers(0, n_tables))
+        op = int(rng.choice([S.INSERT, S.FIND, S.ERASE], p=[0.4, 0.5, 0.1]))
+        n = int(np.exp(rng.uniform(np.log(min_n), np.log(max_n))))
+        keys = W.mix64(zipf_ranks(rng, n) ^ salts[t])
+        reqs.append((t, op, keys))
+    return caps, reqs
+
+
+def stage(reqs):
+    """Device buffers of every request (keys, values for inserts, outputs)."""
+    out = []
+    for t, op, keys in reqs:
+        k = torch.from_numpy(keys.view(np.int64)).cuda()
+        v = torch.from_numpy(W.mix64(keys).view(np.int64)).cuda() if op == S.INSERT else None
+        ov = torch.empty(len(keys), dtype=torch.int64, device="cuda") if op == S.FIND else None
+        of = torch.empty(len(keys), dtype=torch.uint8, device="cuda")
+        out.append((t, op, k, v, ov, of))
+    torch.cuda.synchronize()
+    return out
+
+
+def run_server(caps, staged, arrivals=None, budget=120 << 30):
+    srv = S.server(key="u64", mapped="u64", budget_bytes=budget, n_streams=8, n_slots=16)
+    for t, c in enumerate(caps):
+        if srv.admit(t, int(c)) != N.SG_OK:
+            raise RuntimeError("budget too small for the initial tables")
+    t0 = time.perf_counter()
+    if arrivals is None:
+        # every request is ready at once: one call submits them all
+        tickets = srv.submit_many(staged)
+    else:
+        tickets = []
+        for i, (t, op, k, v, ov, of) in enumerate(staged):
+            due = t0 + arrivals[i]
+            while time.perf_counter() < due:
+                pass
+            tickets.append(srv.submit(t, op, k, v, ov, of))
+    statuses = [srv.wait(tk) for tk in tickets]
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    final_caps = []
+    for t in range(len(caps)):
+        v = srv.table_view(t)
+        final_caps.append(int(v.bucket_count))
+    sizes = [srv.table_size(t) for t in range(len(caps))]
+    srv.close()
+    return wall, st, statuses, final_caps, sizes
+
+
+def run_serial(caps, staged, arrivals=None):
+    lib = N.load()
+    tables = [C.unordered_map.createDeviceObject(int(c), key="u64", mapped="u64") for c in caps]
+    stream = torch.cuda.current_stream()
+    sp = c_void_p(stream.cuda_stream)
+    torch.cuda.synchronize()
+    lat = []
+    t0 = time.perf_counter()
+    for i, (t, op, k, v, ov, of) in enumerate(staged):
+        arrive = t0 + (arrivals[i] if arrivals is not None else 0.0)
+        while arrivals is not None and time.perf_counter() < arrive:
+            pass
+        h = tables[t]._h
+        n = k.numel()
+        if op == S.INSERT:
+            lib.sg_unordered_insert_kv(h, c_void_p(k.data_ptr()), c_void_p(v.data_ptr()), n,
+                                       c_void_p(of.data_ptr()), sp)
+        elif op == S.FIND:
+            lib.sg_unordered_find(h, c_void_p(k.data_ptr()), n, c_void_p(ov.data_ptr()), c_void_p(of.data_ptr()), sp)
+        else:
+            lib.sg_unordered_erase(h, c_void_p(k.data_ptr()), n, c_void_p(of.data_ptr()), sp)
+        stream.synchronize()
+        lat.append((time.perf_counter() - arrive) * 1e6)
+    wall = time.perf_counter() - t0
+    sizes = [tb.size() for tb in tables]
+    for tb in tables:
+        C.unordered_base.destroyDeviceObject(tb)
+    return wall, np.array(lat), sizes
+
+
+def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22) -> dict:
+    caps, reqs = make_stream(n_requests=n_requests, seed=seed, min_n=min_n, max_n=max_n)
+    staged = stage(reqs)
+    keys_total = int(sum(len(r[2]) for r in reqs))
+    # saturated server (also gives the capacity each table grows to)
+    wall_srv, st_sat, statuses, final_caps, sizes_srv = run_server(caps, staged)
+    refused = sum(1 for s in statuses if s != N.SG_OK)
+    # serial plain calls on tables presized to the final capacities
+    wall_ser, lat_ser_sat, sizes_ser = run_serial(final_caps, staged)
+    # Poisson arrivals at `load` x the server's saturated request rate
+    rate = load * len(staged) / wall_srv
+    rng = np.random.default_rng(seed + 1)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(staged)))
+    wall_srv_l, st_load, _, _, _ = run_server(caps, staged, arrivals)
+    wall_ser_l, lat_ser_load, _ = run_serial(final_caps, staged, arrivals)
+    return {
+        "request_keys": [min_n, max_n],
+        "tables": len(caps), "requests": len(staged), "keys": keys_total,
+        "refused_requests": refused, "rehashes": st_sat["rehashes"], "hbm_used_bytes": st_sat["hbm_used_bytes"],
+        "saturated": {
+            "server_s": wall_srv, "serial_s": wall_ser,
+            "server_keys_per_s": keys_total / wall_srv, "serial_keys_per_s": keys_total / wall_ser,
+            "server_requests_per_s": len(staged) / wall_srv, "serial_requests_per_s": len(staged) / wall_ser,
+            "speedup": wall_ser / wall_srv, "waves": st_sat["waves"], "launches": st_sat["launches"],
+        },
+        "under_load": {
+            "arrival_rate_per_s": rate, "load_vs_server_capacity": load,
+            "server_p50_us": st_load["p50_us"], "server_p99_us": st_load["p99_us"],
+            "serial_p50_us": float(np.percentile(lat_ser_load, 50)),
+            "serial_p99_us": float(np.percentile(lat_ser_load, 99)),
+            "server_wall_s": wall_srv_l, "serial_wall_s": wall_ser_l,
+            "server_keys_per_s": keys_total / wall_srv_l, "serial_keys_per_s": keys_total / wall_ser_l,
+        },
+        "final_sizes_agree": bool(sizes_srv == sizes_ser),
+    }
