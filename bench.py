@@ -64,7 +64,7 @@ def parse():
     p.add_argument("--keys-log2", type=int, default=KEYS_LOG2, help="2^k keys (default: the full workload)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["voxel", "batched", "serve"], default="voxel",
+    p.add_argument("--workload", choices=["voxel", "batched", "serve", "large"], default="voxel",
                    help="voxel: the headline map workload; batched: 4096 small sets, batched vs plain calls; "
                         "serve: request stream over 256 resident maps, continuous batching vs serial calls")
     p.add_argument("--requests", type=int, default=600, help="serve workload: number of requests")
@@ -402,10 +402,26 @@ def serve_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def large_arm(args):
+    """Capacity-2^30 map at 0.5/0.75/0.9 load with Zipf batches, plus vector / deque / bitset (one GPU)."""
+    from stdgpu_gb300 import large_bench
+    r = large_bench.run(full=True)
+    line = {"metric": "large mixed workload Mops/s", "value": r["map"][-2]["find_mops"], "unit": UNIT, "n_gpus": 1,
+            "steps": 1, "warmup": 0, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic",
+            "config": {"workload": "unordered_map<uint64_t,uint32_t> capacity 2^30 at 0.5/0.75/0.9 load, 2^24-key Zipf(0.99) "
+                                   "insert/find batches over 2^34; vector push_back 2^28 threads 30%; deque 2^26 mixed "
+                                   "ops; bitset count 2^33 bits"},
+            "large": r}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == "large":
+        large_arm(args)
     elif args.workload == "serve":
         serve_arm(args)
     elif args.workload == "batched":

@@ -301,7 +301,7 @@ typedef struct sg_deque_view
 {
     void* data;
     void* seq;      /* per-slot turn counter of the ring (uint32) */
-    void* counters; /* device {size, begin, end, error} */
+    void* counters; /* device {int64 size, uint64 begin, uint64 end, uint32 error, uint32 pad, int64 avail} */
     int64_t capacity;
     int32_t elem_bytes;
     int32_t pad;

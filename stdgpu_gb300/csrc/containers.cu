@@ -2,9 +2,11 @@
 //
 // vector / deque replace the reference's per-element global atomic plus slot
 // spin lock (src/stdgpu/impl/vector_detail.cuh:181-238,
-// src/stdgpu/impl/deque_detail.cuh:202-258, 388-446) with one warp-aggregated
-// reservation per warp: the lanes that push ballot, the lowest one adds the
-// warp's count to the shared counter and every lane takes its rank.
+// src/stdgpu/impl/deque_detail.cuh:202-258, 388-446) with one reservation per
+// tile of 2048 elements: the warps ballot, one warp scans the counts, one
+// thread adds the tile's total to the shared counter and every element takes
+// its rank.  A counter that every warp hits once saturates near 0.5 G updates
+// a second on one address; once per tile it is no longer the bound.
 //
 // The deque is a ring of tickets: push k and pop k use slot k mod capacity; a
 // per-slot turn counter (the k-th push stores k+1 after writing the element,
@@ -35,6 +37,12 @@ constexpr int kCThreads = 256;
 constexpr unsigned int kDequeErrWait = 1u;
 constexpr long long kWaitLimit = 1ll << 22; // polls of a ring slot before giving up (about 1-2 s with backoff)
 
+// size guards the capacity: a push reservation adds to it first, a pop reservation subtracts from it
+// only after its tickets are claimed.  avail guards pop_front: a push reservation adds to it only after
+// its tickets are claimed, a pop reservation subtracts from it first.  So a pop is only reserved for a
+// ticket that a push has claimed, and a push only for a slot whose previous pop has been claimed; an
+// over-reservation is undone and can make a concurrent reservation fail near the bounds, never succeed
+// wrongly.  Both equal the element count when no launch is running.
 struct deque_counters
 {
     long long size;
@@ -42,6 +50,7 @@ struct deque_counters
     unsigned long long end;
     unsigned int error;
     unsigned int pad;
+    long long avail;
 };
 
 SG_D unsigned
@@ -59,6 +68,41 @@ ld_stream(const T* p)
     return __ldcs(p);
 }
 
+// ---------------------------------------------------------------- block reservations
+//
+// A block takes a tile of kItems x kCThreads elements, element tile + j * kCThreads + threadIdx.x being
+// item j of the thread.  Each warp ballots its items and writes one count per (item, warp) into shared
+// memory in element order; one warp scans the kItems * kWarps counts, so every element learns its rank
+// among the tile's selected elements and the tile makes one reservation on the shared counter.
+
+constexpr int kItems = 8;
+constexpr int kWarps = kCThreads / 32;
+constexpr int kCounts = kItems * kWarps; // 64: two per lane of the scanning warp
+constexpr int64_t kTileElems = int64_t{ kItems } * kCThreads;
+static_assert(kCounts == 64, "the scan gives each lane two counts");
+
+// Exclusive scan of cnt[0, 64) in place by one warp; returns the total to every lane.
+SG_D unsigned
+scan_counts(unsigned* cnt, int lane)
+{
+    const unsigned a = cnt[2 * lane];
+    const unsigned b = cnt[2 * lane + 1];
+    unsigned s = a + b;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1)
+    {
+        const unsigned t = __shfl_up_sync(0xffffffffu, s, d);
+        if (lane >= d)
+        {
+            s += t;
+        }
+    }
+    const unsigned excl = s - a - b;
+    cnt[2 * lane] = excl;
+    cnt[2 * lane + 1] = excl + a;
+    return __shfl_sync(0xffffffffu, s, 31);
+}
+
 // ---------------------------------------------------------------- vector
 
 template <typename T>
@@ -66,38 +110,62 @@ __global__ void __launch_bounds__(kCThreads)
 k_vector_push_back(T* data, long long* size, int64_t cap, const T* values, const uint8_t* pred, int64_t n,
                    uint8_t* out_pushed)
 {
+    __shared__ unsigned cnt[kCounts];
+    __shared__ long long s_base;
     const int lane = threadIdx.x & 31;
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t base = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) & ~int64_t{ 31 }; base < n;
-         base += stride)
+    const int warp = threadIdx.x >> 5;
+    for (int64_t tile = static_cast<int64_t>(blockIdx.x) * kTileElems; tile < n;
+         tile += static_cast<int64_t>(gridDim.x) * kTileElems)
     {
-        const int64_t i = base + lane;
-        const bool in = i < n;
-        const bool want = in && (pred == nullptr || pred[i] != 0);
-        const unsigned mask = __ballot_sync(0xffffffffu, want);
-        long long slot0 = -1;
-        if (mask != 0u)
+        unsigned masks[kItems];
+#pragma unroll
+        for (int j = 0; j < kItems; ++j)
         {
-            const int leader = __ffs(mask) - 1;
-            if (lane == leader)
+            const int64_t i = tile + j * kCThreads + threadIdx.x;
+            const bool want = i < n && (pred == nullptr || pred[i] != 0);
+            masks[j] = __ballot_sync(0xffffffffu, want);
+            if (lane == 0)
             {
-                // preemptive full() check, then one reservation for the warp (vector_detail.cuh:186-195)
-                const long long cur = *reinterpret_cast<volatile long long*>(size);
-                slot0 = cur >= cap ? -1 : atomicAdd(reinterpret_cast<unsigned long long*>(size),
-                                                    static_cast<unsigned long long>(__popc(mask)));
+                cnt[j * kWarps + warp] = __popc(masks[j]);
             }
-            slot0 = __shfl_sync(0xffffffffu, slot0, leader);
         }
-        const long long pos = slot0 + __popc(mask & lanemask_lt());
-        const bool ok = want && slot0 >= 0 && pos < cap;
-        if (ok)
+        __syncthreads();
+        if (warp == 0)
         {
-            data[pos] = ld_stream(values + i);
+            const unsigned total = scan_counts(cnt, lane);
+            if (lane == 0)
+            {
+                // preemptive full() check, then one reservation for the tile (vector_detail.cuh:186-195)
+                long long b = -1;
+                if (total > 0)
+                {
+                    const long long cur = *reinterpret_cast<volatile long long*>(size);
+                    b = cur >= cap ? -1
+                                   : static_cast<long long>(atomicAdd(reinterpret_cast<unsigned long long*>(size),
+                                                                      static_cast<unsigned long long>(total)));
+                }
+                s_base = b;
+            }
         }
-        if (in && out_pushed != nullptr)
+        __syncthreads();
+        const long long base = s_base;
+#pragma unroll
+        for (int j = 0; j < kItems; ++j)
         {
-            out_pushed[i] = static_cast<uint8_t>(ok);
+            const int64_t i = tile + j * kCThreads + threadIdx.x;
+            const bool want = (masks[j] >> lane) & 1u;
+            const long long pos = base + cnt[j * kWarps + warp] + __popc(masks[j] & lanemask_lt());
+            const bool ok = want && base >= 0 && pos < cap;
+            if (ok)
+            {
+                data[pos] = ld_stream(values + i);
+            }
+            if (i < n && out_pushed != nullptr)
+            {
+                out_pushed[i] = static_cast<uint8_t>(ok);
+            }
         }
+        __syncthreads(); // cnt and s_base are rewritten by the next tile
     }
 }
 
@@ -132,114 +200,147 @@ store_turn(unsigned* seq, unsigned v)
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(seq), "r"(v) : "memory");
 }
 
-// Mixed launch: element i pushes values[i] when is_push[i] != 0 (or is_push == NULL), else pops.
+SG_D long long
+atomic_add_ll(long long* p, long long v)
+{
+    return static_cast<long long>(
+            atomicAdd(reinterpret_cast<unsigned long long*>(p), static_cast<unsigned long long>(v)));
+}
+
+// Reserves up to `want` units of `counter` below `bound` (grow) or above zero (!grow): a preemptive read,
+// one add, and an undo of what did not fit (deque_detail.cuh:207-217 push_back, :393-404 pop_front).
+SG_D long long
+reserve(long long* counter, long long bound, long long want, bool grow)
+{
+    const long long cur = *reinterpret_cast<volatile long long*>(counter);
+    if (grow ? cur >= bound : cur <= 0)
+    {
+        return 0;
+    }
+    const long long old = atomic_add_ll(counter, grow ? want : -want);
+    const long long room = grow ? bound - old : old;
+    const long long take = room <= 0 ? 0 : (room < want ? room : want);
+    if (take < want)
+    {
+        atomic_add_ll(counter, grow ? take - want : want - take);
+    }
+    return take;
+}
+
+// Mixed launch: element i pushes values[i] when is_push[i] != 0 (or is_push == NULL), else pops.  Each
+// tile reserves its pushes and its pops once; the tile's pushes take consecutive tickets in element
+// order, and so do its pops.
 template <typename T>
 __global__ void __launch_bounds__(kCThreads)
 k_deque_ops(T* data, unsigned* seq, deque_counters* c, int64_t cap, const uint8_t* is_push, const T* values,
             int64_t n, T* out_popped, uint8_t* out_ok)
 {
+    __shared__ unsigned cpush[kCounts];
+    __shared__ unsigned cpop[kCounts];
+    __shared__ unsigned mpush[kCounts]; // the ballots, so the wait loop below indexes no local array
+    __shared__ unsigned mpop[kCounts];
+    __shared__ long long s_push_ok, s_pop_ok;
+    __shared__ unsigned long long s_push_t0, s_pop_t0;
     const int lane = threadIdx.x & 31;
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t base = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) & ~int64_t{ 31 }; base < n;
-         base += stride)
+    const int warp = threadIdx.x >> 5;
+    for (int64_t tile = static_cast<int64_t>(blockIdx.x) * kTileElems; tile < n;
+         tile += static_cast<int64_t>(gridDim.x) * kTileElems)
     {
-        const int64_t i = base + lane;
-        const bool in = i < n;
-        const bool push = in && (is_push == nullptr || is_push[i] != 0);
-        const bool pop = in && !push;
-        const unsigned pmask = __ballot_sync(0xffffffffu, push);
-        const unsigned qmask = __ballot_sync(0xffffffffu, pop);
-        long long push_ok = 0, pop_ok = 0;
-        unsigned long long push_t0 = 0, pop_t0 = 0;
-        if (lane == 0)
+#pragma unroll
+        for (int j = 0; j < kItems; ++j)
         {
-            const long long pc = __popc(pmask);
-            const long long qc = __popc(qmask);
-            if (pc > 0)
+            const int64_t i = tile + j * kCThreads + threadIdx.x;
+            const bool in = i < n;
+            const bool push = in && (is_push == nullptr || is_push[i] != 0);
+            const unsigned pm = __ballot_sync(0xffffffffu, push);
+            const unsigned qm = __ballot_sync(0xffffffffu, in && !push);
+            if (lane == 0)
             {
-                // push_back: reserve against the capacity (deque_detail.cuh:207-217), undo the overshoot
-                const long long cur = *reinterpret_cast<volatile long long*>(&c->size);
-                if (cur < cap)
-                {
-                    const long long old = static_cast<long long>(
-                            atomicAdd(reinterpret_cast<unsigned long long*>(&c->size), static_cast<unsigned long long>(pc)));
-                    long long room = cap - old;
-                    push_ok = room <= 0 ? 0 : (room < pc ? room : pc);
-                    if (push_ok < pc)
-                    {
-                        atomicAdd(reinterpret_cast<unsigned long long*>(&c->size),
-                                  static_cast<unsigned long long>(-(pc - push_ok)));
-                    }
-                    if (push_ok > 0)
-                    {
-                        push_t0 = atomicAdd(&c->end, static_cast<unsigned long long>(push_ok));
-                    }
-                }
+                cpush[j * kWarps + warp] = __popc(pm);
+                cpop[j * kWarps + warp] = __popc(qm);
+                mpush[j * kWarps + warp] = pm;
+                mpop[j * kWarps + warp] = qm;
             }
-            if (qc > 0)
+        }
+        __syncthreads();
+        if (warp < 2)
+        {
+            const bool grow = warp == 0;
+            const unsigned total = scan_counts(grow ? cpush : cpop, lane);
+            if (lane == 0)
             {
-                // pop_front: reserve against the current size (deque_detail.cuh:393-404), undo the overshoot
-                const long long cur = *reinterpret_cast<volatile long long*>(&c->size);
-                if (cur > 0)
+                const long long ok = total > 0 ? reserve(grow ? &c->size : &c->avail, cap, total, grow) : 0;
+                unsigned long long t0 = 0;
+                if (ok > 0)
                 {
-                    const long long old = static_cast<long long>(
-                            atomicAdd(reinterpret_cast<unsigned long long*>(&c->size), static_cast<unsigned long long>(-qc)));
-                    pop_ok = old <= 0 ? 0 : (old < qc ? old : qc);
-                    if (pop_ok < qc)
-                    {
-                        atomicAdd(reinterpret_cast<unsigned long long*>(&c->size),
-                                  static_cast<unsigned long long>(qc - pop_ok));
-                    }
-                    if (pop_ok > 0)
-                    {
-                        pop_t0 = atomicAdd(&c->begin, static_cast<unsigned long long>(pop_ok));
-                    }
+                    t0 = atomicAdd(grow ? &c->end : &c->begin, static_cast<unsigned long long>(ok));
+                    atomic_add_ll(grow ? &c->avail : &c->size, grow ? ok : -ok);
+                }
+                if (grow)
+                {
+                    s_push_ok = ok;
+                    s_push_t0 = t0;
+                }
+                else
+                {
+                    s_pop_ok = ok;
+                    s_pop_t0 = t0;
                 }
             }
         }
-        push_ok = __shfl_sync(0xffffffffu, push_ok, 0);
-        pop_ok = __shfl_sync(0xffffffffu, pop_ok, 0);
-        push_t0 = __shfl_sync(0xffffffffu, push_t0, 0);
-        pop_t0 = __shfl_sync(0xffffffffu, pop_t0, 0);
-        bool ok = false;
-        if (push)
+        __syncthreads();
+        const long long push_ok = s_push_ok;
+        const long long pop_ok = s_pop_ok;
+        const unsigned long long push_t0 = s_push_t0;
+        const unsigned long long pop_t0 = s_pop_t0;
+#pragma unroll 1
+        for (int j = 0; j < kItems; ++j)
         {
-            const long long r = __popc(pmask & lanemask_lt());
-            if (r < push_ok)
+            const int64_t i = tile + j * kCThreads + threadIdx.x;
+            const unsigned bit = 1u << lane;
+            const unsigned pm = mpush[j * kWarps + warp];
+            const unsigned qm = mpop[j * kWarps + warp];
+            bool ok = false;
+            if (pm & bit)
             {
-                const unsigned long long tk = push_t0 + static_cast<unsigned long long>(r);
-                const int64_t pos = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
-                if (wait_turn(seq + pos, static_cast<unsigned>(tk), &c->error))
+                const long long r = cpush[j * kWarps + warp] + __popc(pm & lanemask_lt());
+                if (r < push_ok)
                 {
-                    data[pos] = values[i];
-                    store_turn(seq + pos, static_cast<unsigned>(tk + 1));
-                    ok = true;
-                }
-            }
-        }
-        else if (pop)
-        {
-            const long long r = __popc(qmask & lanemask_lt());
-            if (r < pop_ok)
-            {
-                const unsigned long long tk = pop_t0 + static_cast<unsigned long long>(r);
-                const int64_t pos = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
-                if (wait_turn(seq + pos, static_cast<unsigned>(tk + 1), &c->error))
-                {
-                    const T v = *reinterpret_cast<volatile T*>(data + pos);
-                    store_turn(seq + pos, static_cast<unsigned>(tk + static_cast<unsigned long long>(cap)));
-                    if (out_popped != nullptr)
+                    const unsigned long long tk = push_t0 + static_cast<unsigned long long>(r);
+                    const int64_t pos = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
+                    if (wait_turn(seq + pos, static_cast<unsigned>(tk), &c->error))
                     {
-                        out_popped[i] = v;
+                        data[pos] = values[i];
+                        store_turn(seq + pos, static_cast<unsigned>(tk + 1));
+                        ok = true;
                     }
-                    ok = true;
                 }
             }
+            else if (qm & bit)
+            {
+                const long long r = cpop[j * kWarps + warp] + __popc(qm & lanemask_lt());
+                if (r < pop_ok)
+                {
+                    const unsigned long long tk = pop_t0 + static_cast<unsigned long long>(r);
+                    const int64_t pos = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
+                    if (wait_turn(seq + pos, static_cast<unsigned>(tk + 1), &c->error))
+                    {
+                        const T v = *reinterpret_cast<volatile T*>(data + pos);
+                        store_turn(seq + pos, static_cast<unsigned>(tk + static_cast<unsigned long long>(cap)));
+                        if (out_popped != nullptr)
+                        {
+                            out_popped[i] = v;
+                        }
+                        ok = true;
+                    }
+                }
+            }
+            if (i < n && out_ok != nullptr)
+            {
+                out_ok[i] = static_cast<uint8_t>(ok);
+            }
         }
-        if (in && out_ok != nullptr)
-        {
-            out_ok[i] = static_cast<uint8_t>(ok);
-        }
+        __syncthreads(); // the counts and reservations are rewritten by the next tile
     }
 }
 
@@ -257,6 +358,7 @@ k_deque_reset(unsigned* seq, deque_counters* c, int64_t cap)
         c->begin = 0;
         c->end = 0;
         c->error = 0;
+        c->avail = 0;
     }
 }
 
@@ -556,14 +658,14 @@ sg_vector_push_back(sg_vector* v, const void* values, const uint8_t* pred, int64
     if (v->elem_bytes == 4)
     {
         static const int mg = persistent_grid(k_vector_push_back<uint32_t>, kCThreads);
-        k_vector_push_back<uint32_t><<<grid_for(n, kCThreads, mg), kCThreads, 0, s>>>(
+        k_vector_push_back<uint32_t><<<grid_for(n, static_cast<int>(kTileElems), mg), kCThreads, 0, s>>>(
                 static_cast<uint32_t*>(v->data), v->size, v->capacity, static_cast<const uint32_t*>(values), pred, n,
                 out_pushed);
     }
     else
     {
         static const int mg = persistent_grid(k_vector_push_back<unsigned long long>, kCThreads);
-        k_vector_push_back<unsigned long long><<<grid_for(n, kCThreads, mg), kCThreads, 0, s>>>(
+        k_vector_push_back<unsigned long long><<<grid_for(n, static_cast<int>(kTileElems), mg), kCThreads, 0, s>>>(
                 static_cast<unsigned long long*>(v->data), v->size, v->capacity,
                 static_cast<const unsigned long long*>(values), pred, n, out_pushed);
     }
@@ -705,14 +807,14 @@ sg_deque_ops(sg_deque* d, const uint8_t* is_push, const void* values, int64_t n,
     if (d->elem_bytes == 4)
     {
         static const int mg = persistent_grid(k_deque_ops<uint32_t>, kCThreads);
-        k_deque_ops<uint32_t><<<grid_for(n, kCThreads, mg), kCThreads, 0, s>>>(
+        k_deque_ops<uint32_t><<<grid_for(n, static_cast<int>(kTileElems), mg), kCThreads, 0, s>>>(
                 static_cast<uint32_t*>(d->data), d->seq, d->counters, d->capacity, is_push,
                 static_cast<const uint32_t*>(values), n, static_cast<uint32_t*>(out_popped), out_ok);
     }
     else
     {
         static const int mg = persistent_grid(k_deque_ops<unsigned long long>, kCThreads);
-        k_deque_ops<unsigned long long><<<grid_for(n, kCThreads, mg), kCThreads, 0, s>>>(
+        k_deque_ops<unsigned long long><<<grid_for(n, static_cast<int>(kTileElems), mg), kCThreads, 0, s>>>(
                 static_cast<unsigned long long*>(d->data), d->seq, d->counters, d->capacity, is_push,
                 static_cast<const unsigned long long*>(values), n, static_cast<unsigned long long*>(out_popped),
                 out_ok);
