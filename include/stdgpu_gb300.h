@@ -160,6 +160,35 @@ SG_API sg_status sg_unordered_view_of(const sg_unordered* table, sg_unordered_vi
 /* Geometry of createDeviceObject(capacity) without creating a table. */
 SG_API sg_status sg_unordered_geometry_for(int32_t kind, int64_t capacity, sg_geometry* out);
 
+/* ---------------- table calls on host buffers (no counterpart in the reference) ---------------- */
+
+/* The reference's bulk calls take device iterators; a caller whose keys are in host memory copies them
+ * in, calls, and copies the results out.  These entry points take HOST pointers (pinned for overlap)
+ * and pipeline the three: the input is cut into chunks of chunk_elems, each copied host->device into one
+ * of n_buffers device staging buffers while earlier chunks' kernels run, and each chunk's results are
+ * copied device->host while later chunks run.  Every copy of a call starts after the work already on
+ * `stream`, and `stream` waits for the call's last result copy, so a call behaves like one
+ * stream-ordered operation; host buffers must stay valid until the stream reaches that point.
+ * A stager belongs to the device current at its creation and to one host thread at a time; calls on
+ * several tables may share it.  Results per element are those of the device-pointer entry points
+ * (a duplicate key in one call is inserted once; which copy reports 1 may differ). */
+typedef struct sg_stager sg_stager;
+/* chunk_elems in [1, 2^30], n_buffers in [2, 8]; holds n_buffers x 33 x chunk_elems device bytes. */
+SG_API sg_status sg_stager_create(int64_t chunk_elems, int32_t n_buffers, sg_stager** out);
+SG_API sg_status sg_stager_destroy(sg_stager* stager);
+/* sg_unordered_insert / insert_kv / erase / find / contains with host buffers (outputs nullable); the
+ * find form writes 0 as the mapped value of an absent key. */
+SG_API sg_status sg_unordered_insert_host(sg_unordered* table, sg_stager* stager, const void* values, int64_t n,
+                                          uint8_t* out_inserted, void* stream);
+SG_API sg_status sg_unordered_insert_kv_host(sg_unordered* table, sg_stager* stager, const void* keys,
+                                             const void* mapped, int64_t n, uint8_t* out_inserted, void* stream);
+SG_API sg_status sg_unordered_erase_host(sg_unordered* table, sg_stager* stager, const void* keys, int64_t n,
+                                         uint8_t* out_erased, void* stream);
+SG_API sg_status sg_unordered_find_host(sg_unordered* table, sg_stager* stager, const void* keys, int64_t n,
+                                        void* out_mapped, uint8_t* out_found, void* stream);
+SG_API sg_status sg_unordered_contains_host(sg_unordered* table, sg_stager* stager, const void* keys, int64_t n,
+                                            uint8_t* out_flags, void* stream);
+
 /* ---------------- batched many-table objects (no counterpart in the reference) ---------------- */
 
 /* Thousands of independent unordered_set / unordered_map objects of one kind and uneven capacities,

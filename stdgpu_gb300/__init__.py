@@ -8,9 +8,11 @@ Python mirror of the reference's host API over that ABI.
 from .containers import (  # noqa: F401
     KINDS,
     bitset_count,
+    default_stager,
     deque,
     geometry_for,
     kernel_launch_count,
+    stager,
     table_batch,
     unordered_base,
     unordered_map,

@@ -90,6 +90,13 @@ SIGNATURES = {
     "sg_unordered_geometry": (c_int32, [c_void_p, POINTER(sg_geometry)]),
     "sg_unordered_view_of": (c_int32, [c_void_p, POINTER(sg_unordered_view)]),
     "sg_unordered_geometry_for": (c_int32, [c_int32, c_int64, POINTER(sg_geometry)]),
+    "sg_stager_create": (c_int32, [c_int64, c_int32, POINTER(c_void_p)]),
+    "sg_stager_destroy": (c_int32, [c_void_p]),
+    "sg_unordered_insert_host": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "sg_unordered_insert_kv_host": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "sg_unordered_erase_host": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "sg_unordered_find_host": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "sg_unordered_contains_host": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_batch_create": (c_int32, [c_int32, c_int32, c_void_p, c_void_p, POINTER(c_void_p)]),
     "sg_batch_destroy": (c_int32, [c_void_p]),
     "sg_batch_configure": (c_int32, [c_void_p, c_int32, c_int32, c_int32]),

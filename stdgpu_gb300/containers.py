@@ -48,6 +48,49 @@ def _as_bits(t: torch.Tensor, nbytes: int, what: str) -> torch.Tensor:
     return t.contiguous()
 
 
+def _hptr(t: torch.Tensor | None) -> c_void_p:
+    if t is None:
+        return c_void_p(0)
+    if t.is_cuda:
+        raise ValueError("host tensor expected")
+    if not t.is_contiguous():
+        raise ValueError("contiguous tensor expected")
+    return c_void_p(t.data_ptr())
+
+
+class stager:
+    """Pipeline for table calls on host tensors (sg_stager_*): chunks of `chunk_elems` elements are copied
+    in through `buffers` device staging buffers while earlier chunks' kernels run, and results are copied
+    back while later chunks run.  Host tensors should be pinned (``tensor.pin_memory()``) for overlap."""
+
+    def __init__(self, chunk_elems: int = 1 << 22, buffers: int = 4):
+        h = c_void_p()
+        N.check(N.load().sg_stager_create(int(chunk_elems), int(buffers), byref(h)), "stager::create")
+        self._h = h
+        self.chunk_elems = int(chunk_elems)
+        self.buffers = int(buffers)
+
+    def close(self) -> None:
+        if self._h:
+            N.check(N.load().sg_stager_destroy(self._h), "stager::destroy")
+            self._h = c_void_p(0)
+
+
+_default_stagers: dict[int, stager] = {}
+
+
+def default_stager() -> stager:
+    """One stager per device, created on first use by a call on host tensors."""
+    d = torch.cuda.current_device()
+    if d not in _default_stagers:
+        _default_stagers[d] = stager()
+    return _default_stagers[d]
+
+
+def _host_out(n: int, dtype) -> torch.Tensor:
+    return torch.empty(n, dtype=dtype).pin_memory()
+
+
 class unordered_base:
     """Shared implementation of unordered_set / unordered_map (src/stdgpu/impl/unordered_base.cuh:56-583)."""
 
@@ -100,8 +143,14 @@ class unordered_base:
         return out.value
 
     # ---- bulk operations
+    # Each accepts device tensors (stream-ordered, asynchronous) or host tensors; with host tensors the call
+    # streams through a stager (`stager=`, else the device's default one) and returns after the stream has
+    # finished it, so host inputs may be reused and host outputs read at once.
+    def _host_done(self, stream) -> None:
+        (stream if stream is not None else torch.cuda.current_stream()).synchronize()
+
     def insert(self, keys: torch.Tensor, mapped: torch.Tensor | None = None, *, flags: torch.Tensor | None = None,
-               stream=None) -> None:
+               stream=None, stager: "stager | None" = None) -> None:
         """insert(begin, end) over keys (+ mapped values for maps): unordered_base_detail.cuh:996-1017."""
         keys = _as_bits(keys, self.key_bytes, "keys")
         if self.mapped_bytes:
@@ -110,6 +159,12 @@ class unordered_base:
             mapped = _as_bits(mapped, self.mapped_bytes, "mapped")
         else:
             mapped = None
+        if not keys.is_cuda:
+            st = stager or default_stager()
+            N.check(N.load().sg_unordered_insert_kv_host(self._h, st._h, _hptr(keys), _hptr(mapped), keys.numel(),
+                                                         _hptr(flags), _stream(stream)), "insert")
+            self._host_done(stream)
+            return
         N.check(N.load().sg_unordered_insert_kv(self._h, _ptr(keys), _ptr(mapped), keys.numel(), _ptr(flags),
                                                 _stream(stream)), "insert")
 
@@ -119,14 +174,28 @@ class unordered_base:
             raise ValueError("values buffer too small")
         N.check(N.load().sg_unordered_insert(self._h, _ptr(values), int(n), _ptr(flags), _stream(stream)), "insert")
 
-    def erase(self, keys: torch.Tensor, *, flags: torch.Tensor | None = None, stream=None) -> None:
+    def erase(self, keys: torch.Tensor, *, flags: torch.Tensor | None = None, stream=None,
+              stager: "stager | None" = None) -> None:
         """erase(begin, end): unordered_base_detail.cuh:1045-1066."""
         keys = _as_bits(keys, self.key_bytes, "keys")
+        if not keys.is_cuda:
+            st = stager or default_stager()
+            N.check(N.load().sg_unordered_erase_host(self._h, st._h, _hptr(keys), keys.numel(), _hptr(flags),
+                                                     _stream(stream)), "erase")
+            self._host_done(stream)
+            return
         N.check(N.load().sg_unordered_erase(self._h, _ptr(keys), keys.numel(), _ptr(flags), _stream(stream)),
                 "erase")
 
-    def contains(self, keys: torch.Tensor, stream=None) -> torch.Tensor:
+    def contains(self, keys: torch.Tensor, stream=None, stager: "stager | None" = None) -> torch.Tensor:
         keys = _as_bits(keys, self.key_bytes, "keys")
+        if not keys.is_cuda:
+            st = stager or default_stager()
+            out = _host_out(keys.numel(), torch.uint8)
+            N.check(N.load().sg_unordered_contains_host(self._h, st._h, _hptr(keys), keys.numel(), _hptr(out),
+                                                        _stream(stream)), "contains")
+            self._host_done(stream)
+            return out
         out = torch.empty(keys.numel(), dtype=torch.uint8, device=keys.device)
         N.check(N.load().sg_unordered_contains(self._h, _ptr(keys), keys.numel(), _ptr(out), _stream(stream)),
                 "contains")
@@ -135,8 +204,17 @@ class unordered_base:
     def count(self, keys: torch.Tensor, stream=None) -> torch.Tensor:
         return self.contains(keys, stream)
 
-    def find(self, keys: torch.Tensor, stream=None) -> tuple[torch.Tensor | None, torch.Tensor]:
+    def find(self, keys: torch.Tensor, stream=None,
+             stager: "stager | None" = None) -> tuple[torch.Tensor | None, torch.Tensor]:
         keys = _as_bits(keys, self.key_bytes, "keys")
+        if not keys.is_cuda:
+            st = stager or default_stager()
+            found = _host_out(keys.numel(), torch.uint8)
+            vals = _host_out(keys.numel(), _INT_DTYPE[self.mapped_bytes]) if self.mapped_bytes else None
+            N.check(N.load().sg_unordered_find_host(self._h, st._h, _hptr(keys), keys.numel(), _hptr(vals),
+                                                    _hptr(found), _stream(stream)), "find")
+            self._host_done(stream)
+            return vals, found
         found = torch.empty(keys.numel(), dtype=torch.uint8, device=keys.device)
         vals = None
         if self.mapped_bytes:
