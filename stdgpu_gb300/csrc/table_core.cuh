@@ -122,6 +122,89 @@ store_value(const dview& t, uint32_t slot, typename kind_consts<KIND>::V v)
     }
 }
 
+// 16-byte compare-and-swap (sm_90 and later): old <- *p; if old == expected then *p <- desired.
+SG_D void
+cas128(void* p, unsigned long long e_lo, unsigned long long e_hi, unsigned long long d_lo, unsigned long long d_hi,
+       unsigned long long& o_lo, unsigned long long& o_hi)
+{
+    asm volatile("{\n\t.reg .b128 d, b, c;\n\t"
+                 "mov.b128 b, {%2, %3};\n\t"
+                 "mov.b128 c, {%4, %5};\n\t"
+                 "atom.global.cas.b128 d, [%6], b, c;\n\t"
+                 "mov.b128 {%0, %1}, d;\n\t}"
+                 : "=l"(o_lo), "=l"(o_hi)
+                 : "l"(e_lo), "l"(e_hi), "l"(d_lo), "l"(d_hi), "l"(p)
+                 : "memory");
+}
+
+SG_D unsigned long long
+pack2(uint32_t lo, uint32_t hi)
+{
+    return static_cast<unsigned long long>(hi) << 32 | lo;
+}
+
+// Claim of a free slot with one compare-and-swap over the whole slot -- key and mapped value written
+// together (4, 8 or 16 bytes), so no separate store of the value follows and no reader can see the key
+// without its value.  exp: the slot's words as read (the free marker in the key word; after an erase the
+// old value bytes stay and are part of the expected image).  Returns true when the claim took the slot;
+// old_key is the key word found there.
+template <int KIND>
+SG_D bool
+claim_slot(const dview& t, uint32_t slot, const uint32_t (&exp)[4], typename kind_consts<KIND>::K key,
+           typename kind_consts<KIND>::V val, typename kind_consts<KIND>::K& old_key)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    constexpr int sb = C::slot_bytes;
+    char* p = t.slots + static_cast<uint64_t>(slot) * sb;
+    uint32_t nw[4] = { exp[0], exp[1], exp[2], exp[3] };
+    if constexpr (sizeof(K) == 8)
+    {
+        nw[0] = static_cast<uint32_t>(key);
+        nw[1] = static_cast<uint32_t>(static_cast<uint64_t>(key) >> 32);
+    }
+    else
+    {
+        nw[0] = static_cast<uint32_t>(key);
+    }
+    if constexpr (kind_traits<KIND>::is_map)
+    {
+        constexpr int vo = kind_traits<KIND>::val_offset / 4;
+        if constexpr (sizeof(V) == 8)
+        {
+            nw[vo] = static_cast<uint32_t>(val);
+            nw[vo + 1] = static_cast<uint32_t>(static_cast<uint64_t>(val) >> 32);
+        }
+        else
+        {
+            nw[vo] = static_cast<uint32_t>(val);
+        }
+    }
+    if constexpr (sb == 4)
+    {
+        const uint32_t o = atomicCAS(reinterpret_cast<unsigned int*>(p), exp[0], nw[0]);
+        old_key = static_cast<K>(o);
+        return o == exp[0];
+    }
+    else if constexpr (sb == 8)
+    {
+        const unsigned long long e = pack2(exp[0], exp[1]);
+        const unsigned long long o = atomicCAS(reinterpret_cast<unsigned long long*>(p), e, pack2(nw[0], nw[1]));
+        old_key = sizeof(K) == 8 ? static_cast<K>(o) : static_cast<K>(static_cast<uint32_t>(o));
+        return o == e;
+    }
+    else
+    {
+        const unsigned long long e_lo = pack2(exp[0], exp[1]);
+        const unsigned long long e_hi = pack2(exp[2], exp[3]);
+        unsigned long long o_lo, o_hi;
+        cas128(p, e_lo, e_hi, pack2(nw[0], nw[1]), pack2(nw[2], nw[3]), o_lo, o_hi);
+        old_key = sizeof(K) == 8 ? static_cast<K>(o_lo) : static_cast<K>(static_cast<uint32_t>(o_lo));
+        return o_lo == e_lo && o_hi == e_hi;
+    }
+}
+
 // Input element i: value_type array (AoS) or separate key / mapped arrays.
 template <int KIND, bool AOS>
 SG_D void
@@ -525,8 +608,40 @@ struct step_counts
     unsigned long long retry = 0;   // retry limit reached
 };
 
-// One warp step over 32 consecutive elements (lane l owns element i; valid when i is in range), all
-// on table t.  Each tile loads the home groups of its 4 keys, then inserts them one after another.
+// ---------------------------------------------------------------- warp steps
+// One step covers 32 consecutive elements (lane l owns element i; valid when i is in range), all on
+// table t, and is called by all 32 lanes of the warp together.  Each tile of 4 lanes loads the home
+// groups of its 4 keys (4 x 128-byte requests per tile, 32 per warp).  Each group is then resolved
+// with full-warp ballots: nibble `tbase` of a ballot is the tile's view of its group (bit q = sector
+// q), so the common case -- the key's fate is decided in its home group -- runs without any branch
+// that differs between tiles.  Only keys whose home group is full of other keys (or whose claim lost
+// to another key) take the tile-cooperative slow path.
+
+SG_D unsigned
+tile_nibble(unsigned ballot, int tbase)
+{
+    return (ballot >> tbase) & 0xFu;
+}
+
+// Loads the home groups of the tile's 4 keys; a lane with nothing to probe reports home 0 (a valid
+// group, read and ignored).
+template <int KIND>
+SG_D void
+load_homes(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K key, bool probe,
+           uint32_t (&hr)[kTile], uint32_t (&pre)[kTile][8])
+{
+    const uint32_t home = probe ? home_of<KIND>(t, key) : 0u;
+#pragma unroll
+    for (int r = 0; r < kTile; ++r)
+    {
+        hr[r] = __shfl_sync(0xffffffffu, home, L.tbase + r);
+        load_sector(t, hr[r], L.q, pre[r]);
+    }
+}
+
+// Insert step.  Per key, from its home group: present (nothing to do), or a claim of the first erased
+// slot of the group (when the group also has a never-used slot) else of the first never-used slot, made
+// by the key's own lane with one compare-and-swap -- 32 claims in flight per warp.
 template <int KIND, bool AOS>
 SG_D void
 insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in1, int64_t i, bool valid,
@@ -535,6 +650,8 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
     using C = kind_consts<KIND>;
     using K = typename C::K;
     using V = typename C::V;
+    constexpr uint32_t G = C::slots_per_group;
+    constexpr uint32_t S = sector_consts<KIND>::slots;
     K key = C::empty_key;
     V val{};
     if (valid)
@@ -544,29 +661,95 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
     const bool special = valid && key >= C::tomb_key;
     int res = special ? special_insert<KIND>(t, key, val) : 0;
     const bool probe = valid && !special;
-    const unsigned pmask = __ballot_sync(L.tmask, probe) >> L.tbase;
-    uint32_t pre[kTile][8];
     uint32_t hr[kTile];
+    uint32_t pre[kTile][8];
+    load_homes<KIND>(t, L, key, probe, hr, pre);
+    constexpr int SW = sector_consts<KIND>::slot_words;
+    int my_state = 0; // 0 present, 1 claim my_target, 2 decided beyond the home group
+    uint32_t my_target = 0;
+    bool my_tomb = false;
+    uint32_t my_exp[4] = { ~0u, ~0u, ~0u, ~0u };
 #pragma unroll
     for (int r = 0; r < kTile; ++r)
     {
-        hr[r] = home_of<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r));
-        if (pmask & (1u << r))
+        const K kr = __shfl_sync(0xffffffffu, key, L.tbase + r);
+        unsigned mm, me, mt;
+        sector_masks<KIND, true>(pre[r], kr, hr[r] * G + L.q * S, t.total, mm, me, mt);
+        const unsigned tm = tile_nibble(__ballot_sync(0xffffffffu, mm != 0u), L.tbase);
+        const unsigned te = tile_nibble(__ballot_sync(0xffffffffu, me != 0u), L.tbase);
+        const unsigned tt = tile_nibble(__ballot_sync(0xffffffffu, mt != 0u), L.tbase);
+        const bool tomb = tt != 0u;
+        const int owner = (__ffs(tomb ? tt : te) - 1) & (kTile - 1);
+        // every lane picks its own sector's candidate slot; the owner's pick is the claim
+        const int mine = (__ffs(tomb ? mt : me) - 1) & (S - 1);
+        const int s_claim = __shfl_sync(0xffffffffu, mine, L.tbase + owner);
+        const uint32_t target = hr[r] * G + static_cast<uint32_t>(owner) * S + static_cast<uint32_t>(s_claim);
+        uint32_t ew[4] = { ~0u, ~0u, ~0u, ~0u };
+        if constexpr (SW > 1)
         {
-            load_sector(t, hr[r], L.q, pre[r]);
+            // the slot image as read, from the owner lane (an erased slot keeps its old value bytes)
+#pragma unroll
+            for (int j = 0; j < SW; ++j)
+            {
+                uint32_t v = pre[r][j];
+#pragma unroll
+                for (int cs = 1; cs < S; ++cs)
+                {
+                    v = mine == cs ? pre[r][cs * SW + j] : v;
+                }
+                ew[j] = __shfl_sync(0xffffffffu, v, L.tbase + owner);
+            }
+        }
+        else
+        {
+            ew[0] = static_cast<uint32_t>(tomb ? C::tomb_key : C::empty_key);
+        }
+        const int state = tm != 0u ? 0 : (te != 0u ? 1 : 2);
+        if (L.q == r)
+        {
+            my_state = state;
+            my_target = target;
+            my_tomb = tomb;
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+            {
+                my_exp[j] = ew[j];
+            }
         }
     }
-#pragma unroll
-    for (int r = 0; r < kTile; ++r)
+    bool again = false;
+    if (probe && my_state == 1)
     {
-        const K kr = __shfl_sync(L.tmask, key, L.tbase + r);
-        const V vr = __shfl_sync(L.tmask, val, L.tbase + r);
-        if (pmask & (1u << r))
+        K old;
+        if (claim_slot<KIND>(t, my_target, my_exp, key, val, old))
         {
-            const int x = tile_insert<KIND, true>(t, kr, vr, hr[r], pre[r], L.tmask, L.tbase, L.q, c.reused);
-            if (L.q == r)
+            c.reused += my_tomb ? 1ull : 0ull;
+            res = 1;
+        }
+        else
+        {
+            again = old != key; // lost the slot to another key; a copy of this key means present
+        }
+    }
+    again = again || (probe && my_state == 2);
+    const unsigned aball = __ballot_sync(0xffffffffu, again);
+    if (aball != 0u)
+    {
+        const unsigned amask = tile_nibble(aball, L.tbase);
+#pragma unroll 1
+        for (int r = 0; r < kTile; ++r)
+        {
+            if (amask & (1u << r))
             {
-                res = x;
+                const K kr = __shfl_sync(L.tmask, key, L.tbase + r);
+                const V vr = __shfl_sync(L.tmask, val, L.tbase + r);
+                uint32_t w[8];
+                load_sector(t, hr[r], L.q, w);
+                const int x = tile_insert<KIND, true>(t, kr, vr, hr[r], w, L.tmask, L.tbase, L.q, c.reused);
+                if (L.q == r)
+                {
+                    res = x;
+                }
             }
         }
     }
@@ -582,8 +765,75 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
     }
 }
 
-// Erase step: tiles locate the 4 keys of their lanes, then every lane swaps its own key's slot to the
-// erased marker.
+// Locates the slot of each lane's key (-1 when absent); with WANT_VALUE the mapped value comes back in
+// val.  Keys not decided in their home group (group full of other keys) continue with tile_find.
+template <int KIND, bool WANT_VALUE>
+SG_D int32_t
+locate_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K key, bool probe,
+            typename kind_consts<KIND>::V& val)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    constexpr uint32_t G = C::slots_per_group;
+    constexpr uint32_t S = sector_consts<KIND>::slots;
+    uint32_t hr[kTile];
+    uint32_t pre[kTile][8];
+    load_homes<KIND>(t, L, key, probe, hr, pre);
+    int32_t my_slot = -1;
+    bool my_more = false;
+#pragma unroll
+    for (int r = 0; r < kTile; ++r)
+    {
+        const K kr = __shfl_sync(0xffffffffu, key, L.tbase + r);
+        unsigned mm, me, mt;
+        sector_masks<KIND, false>(pre[r], kr, 0, 0, mm, me, mt);
+        const unsigned tm = tile_nibble(__ballot_sync(0xffffffffu, mm != 0u), L.tbase);
+        const unsigned te = tile_nibble(__ballot_sync(0xffffffffu, me != 0u), L.tbase);
+        const int owner = (__ffs(tm) - 1) & (kTile - 1);
+        const unsigned om = __shfl_sync(0xffffffffu, mm, L.tbase + owner);
+        V vr{};
+        if constexpr (WANT_VALUE && kind_traits<KIND>::is_map)
+        {
+            vr = __shfl_sync(0xffffffffu, select_sector_value<KIND>(pre[r], mm), L.tbase + owner);
+        }
+        const int32_t slot = tm != 0u ? static_cast<int32_t>(hr[r] * G + static_cast<uint32_t>(owner) * S +
+                                                             static_cast<uint32_t>(__ffs(om) - 1))
+                                      : -1;
+        if (L.q == r)
+        {
+            my_slot = slot;
+            my_more = tm == 0u && te == 0u;
+            val = vr;
+        }
+    }
+    const unsigned mball = __ballot_sync(0xffffffffu, probe && my_more);
+    if (mball != 0u)
+    {
+        const unsigned mmask = tile_nibble(mball, L.tbase);
+#pragma unroll 1
+        for (int r = 0; r < kTile; ++r)
+        {
+            if (mmask & (1u << r))
+            {
+                const K kr = __shfl_sync(L.tmask, key, L.tbase + r);
+                const uint32_t g = next_group32(hr[r], t.num_groups);
+                uint32_t w[8];
+                load_sector(t, g, L.q, w);
+                V vr{};
+                const int32_t slot = tile_find<KIND>(t, kr, g, w, L.tmask, L.tbase, L.q, vr);
+                if (L.q == r)
+                {
+                    my_slot = slot;
+                    val = vr;
+                }
+            }
+        }
+    }
+    return probe ? my_slot : -1;
+}
+
+// Erase step: every lane locates its key, then swaps its slot to the erased marker.
 template <int KIND>
 SG_D void
 erase_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool valid, uint8_t* out_flags,
@@ -601,34 +851,9 @@ erase_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, boo
         c.oob += static_cast<unsigned long long>(res);
     }
     const bool probe = valid && !special;
-    const unsigned pmask = __ballot_sync(L.tmask, probe) >> L.tbase;
-    uint32_t pre[kTile][8];
-    uint32_t hr[kTile];
-#pragma unroll
-    for (int r = 0; r < kTile; ++r)
-    {
-        hr[r] = home_of<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r));
-        if (pmask & (1u << r))
-        {
-            load_sector(t, hr[r], L.q, pre[r]);
-        }
-    }
-    int32_t my_slot = -1;
-#pragma unroll
-    for (int r = 0; r < kTile; ++r)
-    {
-        if (pmask & (1u << r))
-        {
-            V dummy{};
-            const int32_t slot = tile_find<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r), hr[r], pre[r], L.tmask,
-                                                 L.tbase, L.q, dummy);
-            if (L.q == r)
-            {
-                my_slot = slot;
-            }
-        }
-    }
-    if (probe && my_slot >= 0)
+    V dummy{};
+    const int32_t my_slot = locate_step<KIND, false>(t, L, key, probe, dummy);
+    if (my_slot >= 0)
     {
         res = cas_key<KIND>(t, static_cast<uint32_t>(my_slot), key, C::tomb_key) == key ? 1 : 0;
     }
@@ -656,32 +881,12 @@ find_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool
     V val{};
     bool found = special ? special_find<KIND>(t, key, val) : false;
     const bool probe = valid && !special;
-    const unsigned pmask = __ballot_sync(L.tmask, probe) >> L.tbase;
-    uint32_t pre[kTile][8];
-    uint32_t hr[kTile];
-#pragma unroll
-    for (int r = 0; r < kTile; ++r)
+    V pv{};
+    const int32_t slot = locate_step<KIND, WANT_VALUES>(t, L, key, probe, pv);
+    if (probe)
     {
-        hr[r] = home_of<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r));
-        if (pmask & (1u << r))
-        {
-            load_sector(t, hr[r], L.q, pre[r]);
-        }
-    }
-#pragma unroll
-    for (int r = 0; r < kTile; ++r)
-    {
-        if (pmask & (1u << r))
-        {
-            V vr{};
-            const int32_t slot = tile_find<KIND>(t, __shfl_sync(L.tmask, key, L.tbase + r), hr[r], pre[r], L.tmask,
-                                                 L.tbase, L.q, vr);
-            if (L.q == r)
-            {
-                found = slot >= 0;
-                val = vr;
-            }
-        }
+        found = slot >= 0;
+        val = pv;
     }
     if (valid)
     {
