@@ -109,6 +109,19 @@ SG_API sg_status sg_unordered_insert(sg_unordered* table, const void* values, in
 SG_API sg_status sg_unordered_insert_kv(sg_unordered* table, const void* keys, const void* mapped, int64_t n,
                                  uint8_t* out_inserted, void* stream);
 
+/* Bulk-insert strategy (no counterpart in the reference).  SG_INSERT_AUTO: when a call without per-element
+ * flags brings at least 2^22 keys and one key per two probe groups of a table of 256 MB or more, the keys
+ * are first partitioned by home-group range into a scratch array (n x sizeof(value_type), kept by the
+ * table until destroy) so that each group line is read from DRAM about once.  SG_INSERT_DIRECT never
+ * partitions; SG_INSERT_PARTITIONED partitions every call without flags.  Results are the same. */
+typedef enum sg_insert_mode
+{
+    SG_INSERT_AUTO = 0,
+    SG_INSERT_DIRECT = 1,
+    SG_INSERT_PARTITIONED = 2
+} sg_insert_mode;
+SG_API sg_status sg_unordered_set_insert_mode(sg_unordered* table, int32_t mode);
+
 /* erase(begin, end) over keys: src/stdgpu/impl/unordered_base_detail.cuh:1045-1066 (per key :1019-1043).
  * out_erased (nullable): per key 1 if this call erased it, else 0. */
 SG_API sg_status sg_unordered_erase(sg_unordered* table, const void* keys, int64_t n, uint8_t* out_erased, void* stream);

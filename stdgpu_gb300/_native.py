@@ -78,6 +78,7 @@ SIGNATURES = {
     "sg_unordered_insert": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_unordered_insert_kv": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_unordered_erase": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "sg_unordered_set_insert_mode": (c_int32, [c_void_p, c_int32]),
     "sg_unordered_find": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "sg_unordered_contains": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_unordered_size": (c_int32, [c_void_p, c_void_p, POINTER(c_int64)]),

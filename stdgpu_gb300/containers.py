@@ -244,6 +244,12 @@ class unordered_base:
     def clear(self, stream=None) -> None:
         N.check(N.load().sg_unordered_clear(self._h, _stream(stream)), "clear")
 
+    INSERT_MODES = {"auto": 0, "direct": 1, "partitioned": 2}
+
+    def set_insert_mode(self, mode: str) -> None:
+        """Bulk-insert strategy: "auto", "direct" or "partitioned" (sg_unordered_set_insert_mode)."""
+        N.check(N.load().sg_unordered_set_insert_mode(self._h, self.INSERT_MODES[mode]), "set_insert_mode")
+
     def valid(self, stream=None) -> bool:
         out = c_int32()
         N.check(N.load().sg_unordered_valid(self._h, _stream(stream), byref(out)), "valid")

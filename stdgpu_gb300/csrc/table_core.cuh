@@ -145,12 +145,12 @@ pack2(uint32_t lo, uint32_t hi)
 
 // Claim of a free slot with one compare-and-swap over the whole slot -- key and mapped value written
 // together (4, 8 or 16 bytes), so no separate store of the value follows and no reader can see the key
-// without its value.  exp: the slot's words as read (the free marker in the key word; after an erase the
-// old value bytes stay and are part of the expected image).  Returns true when the claim took the slot;
-// old_key is the key word found there.
+// without its value.  A never-used slot is all ones; an erased slot keeps its old value bytes, so for
+// it the expected image is read first (erased marker in the key word, the bytes found elsewhere).
+// Returns true when the claim took the slot; old_key is the key word found there.
 template <int KIND>
 SG_D bool
-claim_slot(const dview& t, uint32_t slot, const uint32_t (&exp)[4], typename kind_consts<KIND>::K key,
+claim_slot(const dview& t, uint32_t slot, bool erased, typename kind_consts<KIND>::K key,
            typename kind_consts<KIND>::V val, typename kind_consts<KIND>::K& old_key)
 {
     using C = kind_consts<KIND>;
@@ -158,6 +158,26 @@ claim_slot(const dview& t, uint32_t slot, const uint32_t (&exp)[4], typename kin
     using V = typename C::V;
     constexpr int sb = C::slot_bytes;
     char* p = t.slots + static_cast<uint64_t>(slot) * sb;
+    uint32_t exp[4] = { ~0u, ~0u, ~0u, ~0u };
+    if (erased)
+    {
+        if constexpr (sb == 16)
+        {
+            const uint4 w = __ldcg(reinterpret_cast<const uint4*>(p));
+            exp[1] = w.y;
+            exp[2] = w.z;
+            exp[3] = w.w;
+        }
+        else if constexpr (sb == 8)
+        {
+            exp[1] = __ldcg(reinterpret_cast<const unsigned int*>(p) + 1);
+        }
+        exp[0] = static_cast<uint32_t>(C::tomb_key);
+        if constexpr (sizeof(K) == 8)
+        {
+            exp[1] = static_cast<uint32_t>(static_cast<uint64_t>(C::tomb_key) >> 32);
+        }
+    }
     uint32_t nw[4] = { exp[0], exp[1], exp[2], exp[3] };
     if constexpr (sizeof(K) == 8)
     {
@@ -415,7 +435,7 @@ select_sector_value(const uint32_t (&w)[8], unsigned one_hot)
 template <int KIND, bool REUSE>
 SG_D int
 tile_insert(const dview& t, typename kind_consts<KIND>::K key, typename kind_consts<KIND>::V val, uint32_t home,
-            uint32_t (&w)[8], unsigned tmask, int tbase, int q, unsigned long long& tombs_reused)
+            uint32_t (&w)[8], unsigned tmask, int tbase, int q, unsigned int& tombs_reused)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
@@ -599,13 +619,15 @@ struct tile_lanes
 
 
 // Counts of one lane over the steps it ran.
+// 32-bit: a lane's count between two flushes stays far below 2^32, and registers are what bounds how
+// many warps the probe kernels keep in flight.
 struct step_counts
 {
-    unsigned long long done = 0;    // inserted / erased
-    unsigned long long refused = 0; // inserts refused: no free slot left
-    unsigned long long reused = 0;  // erased slots claimed by inserts
-    unsigned long long oob = 0;     // erased out-of-band keys
-    unsigned long long retry = 0;   // retry limit reached
+    unsigned int done = 0;    // inserted / erased
+    unsigned int refused = 0; // inserts refused: no free slot left
+    unsigned int reused = 0;  // erased slots claimed by inserts
+    unsigned int oob = 0;     // erased out-of-band keys
+    unsigned int retry = 0;   // retry limit reached
 };
 
 // ---------------------------------------------------------------- warp steps
@@ -664,11 +686,9 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
     uint32_t hr[kTile];
     uint32_t pre[kTile][8];
     load_homes<KIND>(t, L, key, probe, hr, pre);
-    constexpr int SW = sector_consts<KIND>::slot_words;
     int my_state = 0; // 0 present, 1 claim my_target, 2 decided beyond the home group
     uint32_t my_target = 0;
     bool my_tomb = false;
-    uint32_t my_exp[4] = { ~0u, ~0u, ~0u, ~0u };
 #pragma unroll
     for (int r = 0; r < kTile; ++r)
     {
@@ -684,46 +704,21 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
         const int mine = (__ffs(tomb ? mt : me) - 1) & (S - 1);
         const int s_claim = __shfl_sync(0xffffffffu, mine, L.tbase + owner);
         const uint32_t target = hr[r] * G + static_cast<uint32_t>(owner) * S + static_cast<uint32_t>(s_claim);
-        uint32_t ew[4] = { ~0u, ~0u, ~0u, ~0u };
-        if constexpr (SW > 1)
-        {
-            // the slot image as read, from the owner lane (an erased slot keeps its old value bytes)
-#pragma unroll
-            for (int j = 0; j < SW; ++j)
-            {
-                uint32_t v = pre[r][j];
-#pragma unroll
-                for (int cs = 1; cs < S; ++cs)
-                {
-                    v = mine == cs ? pre[r][cs * SW + j] : v;
-                }
-                ew[j] = __shfl_sync(0xffffffffu, v, L.tbase + owner);
-            }
-        }
-        else
-        {
-            ew[0] = static_cast<uint32_t>(tomb ? C::tomb_key : C::empty_key);
-        }
         const int state = tm != 0u ? 0 : (te != 0u ? 1 : 2);
         if (L.q == r)
         {
             my_state = state;
             my_target = target;
             my_tomb = tomb;
-#pragma unroll
-            for (int j = 0; j < 4; ++j)
-            {
-                my_exp[j] = ew[j];
-            }
         }
     }
     bool again = false;
     if (probe && my_state == 1)
     {
         K old;
-        if (claim_slot<KIND>(t, my_target, my_exp, key, val, old))
+        if (claim_slot<KIND>(t, my_target, my_tomb, key, val, old))
         {
-            c.reused += my_tomb ? 1ull : 0ull;
+            c.reused += my_tomb ? 1u : 0u;
             res = 1;
         }
         else
@@ -848,7 +843,7 @@ erase_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, boo
     if (special)
     {
         res = special_erase<KIND>(t, key);
-        c.oob += static_cast<unsigned long long>(res);
+        c.oob += static_cast<unsigned int>(res);
     }
     const bool probe = valid && !special;
     V dummy{};
@@ -859,7 +854,7 @@ erase_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, boo
     }
     if (valid)
     {
-        c.done += static_cast<unsigned long long>(res);
+        c.done += static_cast<unsigned int>(res);
         if (out_flags != nullptr)
         {
             out_flags[i] = static_cast<uint8_t>(res);

@@ -17,6 +17,7 @@
 #include <cstdint>
 #include <cstring>
 #include <new>
+#include <type_traits>
 
 #include "sg_internal.cuh"
 #include "stdgpu_gb300.h"
@@ -97,6 +98,278 @@ k_insert(dview t, const void* in0, const void* in1, int64_t n, uint8_t* out_flag
         atomicOr(&t.hdr->error, kErrRetry);
     }
     // size += inserted; refused += refused; tombstones -= reused
+    unsigned long long v[3] = { c.done, c.refused, 0ull - c.reused };
+    unsigned long long* const dst[3] = { &t.hdr->size, &t.hdr->refused, &t.hdr->tombstones };
+    block_add<3>(v, dst);
+}
+
+// ---------------------------------------------------------------- partitioned bulk insert
+// When a bulk insert brings many keys per probe group of a table far larger than L2, the keys are first
+// split into P partitions by home-group range (the top bits of the reference bucket) and written as
+// value_type elements into a scratch array, partition after partition; k_insert then walks that array
+// in order, so the warps in flight work inside one or two partitions' groups (tens of MB) at a time and
+// each group line is read from DRAM about once instead of once per key.  Element order inside a
+// partition is arbitrary, as is the order among duplicates of one key in a single bulk insert.
+
+constexpr int kPartMax = 256;
+constexpr int kPartPer = 8; // elements per thread per scatter round
+
+template <int KIND, bool AOS>
+SG_D typename kind_consts<KIND>::K
+load_key(const void* in0, int64_t i)
+{
+    using K = typename kind_consts<KIND>::K;
+    constexpr int sb = kind_consts<KIND>::slot_bytes;
+    if constexpr (AOS)
+    {
+        return *reinterpret_cast<const K*>(static_cast<const char*>(in0) + i * sb);
+    }
+    else
+    {
+        return reinterpret_cast<const K*>(in0)[i];
+    }
+}
+
+template <int KIND>
+SG_D uint32_t
+part_of(typename kind_consts<KIND>::K key, int bits, int shift)
+{
+    return static_cast<uint32_t>(fibonacci_bucket(static_cast<uint64_t>(key), bits)) >> shift;
+}
+
+template <int KIND>
+struct slot_image
+{
+    using type = typename std::conditional<kind_consts<KIND>::slot_bytes == 16, uint4,
+                                           typename std::conditional<kind_consts<KIND>::slot_bytes == 8, uint2,
+                                                                     unsigned int>::type>::type;
+};
+
+// value_type bytes of (key, mapped); padding bytes are zero.
+template <int KIND>
+SG_D typename slot_image<KIND>::type
+pack_element(typename kind_consts<KIND>::K key, typename kind_consts<KIND>::V val)
+{
+    using K = typename kind_consts<KIND>::K;
+    using V = typename kind_consts<KIND>::V;
+    uint32_t w[4] = { 0u, 0u, 0u, 0u };
+    w[0] = static_cast<uint32_t>(key);
+    if constexpr (sizeof(K) == 8)
+    {
+        w[1] = static_cast<uint32_t>(static_cast<uint64_t>(key) >> 32);
+    }
+    if constexpr (kind_traits<KIND>::is_map)
+    {
+        constexpr int vo = kind_traits<KIND>::val_offset / 4;
+        w[vo] = static_cast<uint32_t>(val);
+        if constexpr (sizeof(V) == 8)
+        {
+            w[vo + 1] = static_cast<uint32_t>(static_cast<uint64_t>(val) >> 32);
+        }
+    }
+    constexpr int sb = kind_consts<KIND>::slot_bytes;
+    if constexpr (sb == 16)
+    {
+        return make_uint4(w[0], w[1], w[2], w[3]);
+    }
+    else if constexpr (sb == 8)
+    {
+        return make_uint2(w[0], w[1]);
+    }
+    else
+    {
+        return w[0];
+    }
+}
+
+// Pass 1: how many keys fall in each partition.
+template <int KIND, bool AOS>
+__global__ void __launch_bounds__(kThreads)
+k_part_count(const void* in0, int64_t n, int bits, int shift, int parts, unsigned int* hist)
+{
+    __shared__ unsigned int h[kPartMax];
+    for (int p = threadIdx.x; p < parts; p += blockDim.x)
+    {
+        h[p] = 0u;
+    }
+    __syncthreads();
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        atomicAdd(&h[part_of<KIND>(load_key<KIND, AOS>(in0, i), bits, shift)], 1u);
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < parts; p += blockDim.x)
+    {
+        if (h[p] != 0u)
+        {
+            atomicAdd(&hist[p], h[p]);
+        }
+    }
+}
+
+// Exclusive scan of the partition sizes into the write cursors (one block, parts <= blockDim.x).
+__global__ void
+k_part_cursors(const unsigned int* hist, int parts, unsigned int* cursor)
+{
+    __shared__ unsigned int v[kPartMax];
+    const int p = threadIdx.x;
+    v[p] = p < parts ? hist[p] : 0u;
+    __syncthreads();
+    for (int d = 1; d < kPartMax; d <<= 1)
+    {
+        const unsigned int x = p >= d ? v[p - d] : 0u;
+        __syncthreads();
+        v[p] += x;
+        __syncthreads();
+    }
+    if (p < parts)
+    {
+        cursor[p] = v[p] - hist[p];
+    }
+}
+
+// Pass 2: each block takes kPartPer x kThreads elements, ranks them per partition in shared memory,
+// reserves one range per partition, sorts the elements by partition in shared memory and writes each
+// partition's run with consecutive threads, so stores reach L2 as whole lines rather than one request
+// per element (random small writes cost as many requests as random line reads).
+template <int KIND, bool AOS>
+__global__ void __launch_bounds__(kThreads)
+k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, int shift, int parts, unsigned int* cursor,
+               void* out)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    using E = typename slot_image<KIND>::type;
+    constexpr int kTileElems = kPartPer * kThreads;
+    __shared__ E stage[kTileElems];
+    __shared__ uint8_t spid[kTileElems];
+    __shared__ unsigned int cnt[kPartMax];
+    __shared__ unsigned int loff[kPartMax];
+    __shared__ unsigned int base[kPartMax];
+    E* dst = static_cast<E*>(out);
+    const int lane = threadIdx.x & 31;
+    for (int64_t tile = static_cast<int64_t>(blockIdx.x) * kTileElems; tile < n;
+         tile += static_cast<int64_t>(gridDim.x) * kTileElems)
+    {
+        for (int p = threadIdx.x; p < kPartMax; p += blockDim.x)
+        {
+            cnt[p] = 0u;
+        }
+        __syncthreads();
+        E elem[kPartPer];
+        uint32_t pid[kPartPer];
+        uint32_t rank[kPartPer];
+#pragma unroll
+        for (int j = 0; j < kPartPer; ++j)
+        {
+            const int64_t i = tile + j * kThreads + threadIdx.x;
+            pid[j] = 0u;
+            rank[j] = 0u;
+            if (i < n)
+            {
+                K key;
+                V val;
+                load_input<KIND, AOS>(in0, in1, i, key, val);
+                elem[j] = pack_element<KIND>(key, val);
+                pid[j] = part_of<KIND>(key, bits, shift);
+                rank[j] = atomicAdd(&cnt[pid[j]], 1u);
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < 32)
+        {
+            // exclusive scan of cnt[0, kPartMax): lane l sums entries [8l, 8l + 8)
+            constexpr int kPerLane = kPartMax / 32;
+            unsigned int local = 0u;
+#pragma unroll
+            for (int k = 0; k < kPerLane; ++k)
+            {
+                local += cnt[lane * kPerLane + k];
+            }
+            unsigned int incl = local;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1)
+            {
+                const unsigned int x = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d)
+                {
+                    incl += x;
+                }
+            }
+            unsigned int run = incl - local;
+#pragma unroll
+            for (int k = 0; k < kPerLane; ++k)
+            {
+                loff[lane * kPerLane + k] = run;
+                run += cnt[lane * kPerLane + k];
+            }
+        }
+        for (int p = threadIdx.x; p < parts; p += blockDim.x)
+        {
+            base[p] = cnt[p] != 0u ? atomicAdd(&cursor[p], cnt[p]) : 0u;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < kPartPer; ++j)
+        {
+            const int64_t i = tile + j * kThreads + threadIdx.x;
+            if (i < n)
+            {
+                const unsigned int pos = loff[pid[j]] + rank[j];
+                stage[pos] = elem[j];
+                spid[pos] = static_cast<uint8_t>(pid[j]);
+            }
+        }
+        __syncthreads();
+        const int count = n - tile < kTileElems ? static_cast<int>(n - tile) : kTileElems;
+        for (int e = threadIdx.x; e < count; e += kThreads)
+        {
+            const unsigned int p = spid[e];
+            dst[base[p] + (e - loff[p])] = stage[e];
+        }
+        __syncthreads(); // the counters and the stage are rewritten by the next tile
+    }
+}
+
+// Bulk insert over partitioned elements.  Blocks take chunks of kOrderedChunk elements in input order from
+// a shared counter instead of a fixed stride, so no block drifts ahead: the elements in flight stay
+// within about one partition, whose groups then stay in L2 while its keys arrive.
+constexpr int kOrderedChunk = 8 * kThreads;
+
+template <int KIND>
+__global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
+k_insert_ordered(dview t, const void* in0, int64_t n, unsigned long long* next_chunk)
+{
+    __shared__ long long s_first;
+    const tile_lanes L;
+    const int warp = threadIdx.x >> 5;
+    step_counts c;
+    while (true)
+    {
+        if (threadIdx.x == 0)
+        {
+            s_first = static_cast<long long>(atomicAdd(next_chunk, 1ull)) * kOrderedChunk;
+        }
+        __syncthreads();
+        const int64_t first = s_first;
+        __syncthreads();
+        if (first >= n)
+        {
+            break;
+        }
+        const int64_t last = first + kOrderedChunk < n ? first + kOrderedChunk : n;
+        for (int64_t base = first + warp * 32; base < last; base += kThreads)
+        {
+            const int64_t i = base + L.lane;
+            insert_step<KIND, true>(t, L, in0, nullptr, i, i < last, nullptr, c);
+        }
+    }
+    if (c.retry != 0)
+    {
+        atomicOr(&t.hdr->error, kErrRetry);
+    }
     unsigned long long v[3] = { c.done, c.refused, 0ull - c.reused };
     unsigned long long* const dst[3] = { &t.hdr->size, &t.hdr->refused, &t.hdr->tombstones };
     block_add<3>(v, dst);
@@ -395,6 +668,9 @@ struct sg_unordered
     int64_t nchunks;
     unsigned long long* host_hdr; // pinned mirror for synchronous reads
     int device;
+    int32_t insert_mode;        // 0 automatic, 1 always direct, 2 partitioned whenever allowed
+    char* part_scratch;         // partitioned bulk insert: value_type elements, then 2 x kPartMax counters
+    int64_t part_scratch_bytes;
 };
 
 namespace
@@ -483,12 +759,115 @@ struct do_init
     }
 };
 
+// Partition count for a table: home-group ranges of about 64 MB of slots.
+int
+partitions_for(const sg_unordered* t)
+{
+    const int64_t bytes = (t->num_groups + 1) * kGroupBytes;
+    int p = 2;
+    while (p < kPartMax && static_cast<int64_t>(p) * (int64_t{ 64 } << 20) < bytes)
+    {
+        p <<= 1;
+    }
+    return p <= (1 << t->bits) ? p : 0;
+}
+
+bool
+use_partitioned_insert(const sg_unordered* t, int64_t n, const uint8_t* flags)
+{
+    if (flags != nullptr || n >= (int64_t{ 1 } << 31) || t->insert_mode == 1 || partitions_for(t) == 0)
+    {
+        return false;
+    }
+    if (t->insert_mode == 2)
+    {
+        return true;
+    }
+    const int64_t bytes = (t->num_groups + 1) * kGroupBytes;
+    return n >= (int64_t{ 1 } << 22) && bytes >= (int64_t{ 256 } << 20) && n * 2 >= t->num_groups;
+}
+
+sg_status
+ensure_part_scratch(sg_unordered* t, int64_t bytes)
+{
+    if (t->part_scratch_bytes >= bytes)
+    {
+        return SG_OK;
+    }
+    if (t->part_scratch != nullptr)
+    {
+        // a launch queued earlier may still read the old array
+        SG_CUDA_TRY(cudaDeviceSynchronize());
+        cudaFree(t->part_scratch);
+        t->part_scratch = nullptr;
+        t->part_scratch_bytes = 0;
+    }
+    const cudaError_t e = cudaMalloc(&t->part_scratch, static_cast<size_t>(bytes));
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        t->part_scratch = nullptr;
+        return e == cudaErrorMemoryAllocation ? SG_ERR_OOM : SG_ERR_CUDA;
+    }
+    t->part_scratch_bytes = bytes;
+    return SG_OK;
+}
+
 template <int KIND>
 struct do_insert
 {
+    template <bool AOS>
+    static sg_status
+    partition(sg_unordered* t, const void* in0, const void* in1, int64_t n, cudaStream_t s)
+    {
+        const int parts = partitions_for(t);
+        int shift = t->bits;
+        for (int p = parts; p > 1; p >>= 1)
+        {
+            --shift;
+        }
+        const int64_t elems = ((n * t->slot_bytes + 255) / 256) * 256;
+        sg_status st = ensure_part_scratch(t, elems + 2 * kPartMax * static_cast<int64_t>(sizeof(unsigned int)) + 256);
+        if (st != SG_OK)
+        {
+            return st;
+        }
+        auto* hist = reinterpret_cast<unsigned int*>(t->part_scratch + elems);
+        unsigned int* cursor = hist + kPartMax;
+        // hist, cursor and the chunk counter of k_insert_ordered start at zero
+        SG_CUDA_TRY(cudaMemsetAsync(hist, 0, 2 * kPartMax * sizeof(unsigned int) + 256, s));
+        static const int g_count = persistent_grid(k_part_count<KIND, AOS>, kThreads);
+        k_part_count<KIND, AOS><<<grid_for(n, kThreads, g_count), kThreads, 0, s>>>(in0, n, t->bits, shift, parts, hist);
+        SG_LAUNCH_CHECK();
+        k_part_cursors<<<1, kPartMax, 0, s>>>(hist, parts, cursor);
+        SG_LAUNCH_CHECK();
+        static const int g_scatter = persistent_grid(k_part_scatter<KIND, AOS>, kThreads);
+        k_part_scatter<KIND, AOS><<<grid_for(n, kThreads * kPartPer, g_scatter), kThreads, 0, s>>>(
+                in0, in1, n, t->bits, shift, parts, cursor, t->part_scratch);
+        SG_LAUNCH_CHECK();
+        return SG_OK;
+    }
+
     static sg_status
     run(sg_unordered* t, const void* in0, const void* in1, bool aos, int64_t n, uint8_t* flags, cudaStream_t s)
     {
+        if (use_partitioned_insert(t, n, flags))
+        {
+            const sg_status st = aos ? partition<true>(t, in0, in1, n, s) : partition<false>(t, in0, in1, n, s);
+            if (st != SG_OK)
+            {
+                return st;
+            }
+            const int64_t elems = ((n * t->slot_bytes + 255) / 256) * 256;
+            auto* next_chunk = reinterpret_cast<unsigned long long*>(t->part_scratch + elems +
+                                                                     2 * kPartMax * sizeof(unsigned int));
+            static const int max_grid = persistent_grid(k_insert_ordered<KIND>, kThreads);
+            k_insert_ordered<KIND><<<grid_for(n, kOrderedChunk, max_grid), kThreads, 0, s>>>(view_of(t),
+                                                                                            t->part_scratch, n,
+                                                                                            next_chunk);
+            SG_LAUNCH_CHECK();
+            return SG_OK;
+        }
         if (aos)
         {
             static const int max_grid = persistent_grid(k_insert<KIND, true>, kThreads);
@@ -706,6 +1085,10 @@ sg_unordered_destroy(sg_unordered* t)
     {
         cudaFree(t->chunk_counts);
     }
+    if (t->part_scratch != nullptr)
+    {
+        cudaFree(t->part_scratch);
+    }
     if (t->host_hdr != nullptr)
     {
         cudaFreeHost(t->host_hdr);
@@ -741,6 +1124,17 @@ sg_unordered_insert_kv(sg_unordered* t, const void* keys, const void* mapped, in
         return SG_OK;
     }
     return dispatch<do_insert>(t->kind, t, keys, mapped, false, n, out_inserted, as_stream(stream));
+}
+
+sg_status
+sg_unordered_set_insert_mode(sg_unordered* t, int32_t mode)
+{
+    if (t == nullptr || mode < 0 || mode > 2)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    t->insert_mode = mode;
+    return SG_OK;
 }
 
 sg_status
