@@ -360,8 +360,11 @@ def native_arm(args):
             traffic = json.loads(tf.read_text()).get(dominant)
         except (ValueError, AttributeError):
             traffic = None
+    phase_kernels = {"insert": "k_part_count + k_part_cursors + k_part_scatter + k_insert_ordered (partitioned bulk "
+                               "insert, chosen automatically at this size)",
+                     "find": "k_find", "erase": "k_erase"}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": dominant, "peak_source": peak_src,
+                "traffic": traffic, "kernel": dominant, "kernels": phase_kernels[dominant], "peak_source": peak_src,
                 "bytes_per_op": BYTES_PER_OP[dominant],
                 "per_kernel": {k: {"ms": med[k], "mops": counts[k] / (med[k] * 1e-3) / 1e6,
                                    "gbs": BYTES_PER_OP[k] * counts[k] / (med[k] * 1e-3) / 1e9,

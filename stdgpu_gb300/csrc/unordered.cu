@@ -336,7 +336,10 @@ k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, int shift,
 // Bulk insert over partitioned elements.  Blocks take chunks of kOrderedChunk elements in input order from
 // a shared counter instead of a fixed stride, so no block drifts ahead: the elements in flight stay
 // within about one partition, whose groups then stay in L2 while its keys arrive.
-constexpr int kOrderedChunk = 8 * kThreads;
+#ifndef SG_ORDERED_ITERS
+#define SG_ORDERED_ITERS 16
+#endif
+constexpr int kOrderedChunk = SG_ORDERED_ITERS * kThreads;
 
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
@@ -759,13 +762,16 @@ struct do_init
     }
 };
 
-// Partition count for a table: home-group ranges of about 64 MB of slots.
+// Partition count for a table: home-group ranges of about SG_PART_REGION_MB of slots.
+#ifndef SG_PART_REGION_MB
+#define SG_PART_REGION_MB 64
+#endif
 int
 partitions_for(const sg_unordered* t)
 {
     const int64_t bytes = (t->num_groups + 1) * kGroupBytes;
     int p = 2;
-    while (p < kPartMax && static_cast<int64_t>(p) * (int64_t{ 64 } << 20) < bytes)
+    while (p < kPartMax && static_cast<int64_t>(p) * (int64_t{ SG_PART_REGION_MB } << 20) < bytes)
     {
         p <<= 1;
     }
