@@ -109,6 +109,27 @@ SG_API sg_status sg_unordered_insert(sg_unordered* table, const void* values, in
 SG_API sg_status sg_unordered_insert_kv(sg_unordered* table, const void* keys, const void* mapped, int64_t n,
                                  uint8_t* out_inserted, void* stream);
 
+/* ---- Custom key types and hash functions: unordered_set<Key, Hash> / unordered_map<Key, T, Hash>
+ * (src/stdgpu/unordered_map.cuh:70-80, unordered_set.cuh:61-69 with a user Hash; the reference's own tests use
+ * vec3int16 keys with vec_hash, tests/stdgpu/unordered_map.inc:178-206).  A key of at most 8 bytes whose
+ * equality is equality of its bytes (short3, vec3int16, packed coordinates) is stored as a zero-padded
+ * 4- or 8-byte key word, so the table is one of the six kinds; the bucket of a key is the fibonacci hashing
+ * of Hash(key) (unordered_base_detail.cuh:56-85), which the caller computes (the C++ API in
+ * stdgpu_gb300/stdgpu.cuh does it with the user's functor) and passes per key as a 64-bit hash.  A table
+ * created this way takes only the *_hashed bulk calls (the identity-hash calls return SG_ERR_BAD_ARG), and
+ * sg_unordered_valid checks it without re-deriving buckets (reachability needs the hash). */
+SG_API sg_status sg_unordered_create_hashed(int32_t kind, int64_t capacity, void* stream, sg_unordered** out);
+SG_API sg_status sg_unordered_insert_hashed(sg_unordered* table, const void* keys, const void* mapped,
+                                            const uint64_t* hashes, int64_t n, uint8_t* out_inserted, void* stream);
+SG_API sg_status sg_unordered_erase_hashed(sg_unordered* table, const void* keys, const uint64_t* hashes, int64_t n,
+                                           uint8_t* out_erased, void* stream);
+SG_API sg_status sg_unordered_find_hashed(sg_unordered* table, const void* keys, const uint64_t* hashes, int64_t n,
+                                          void* out_mapped, uint8_t* out_found, void* stream);
+SG_API sg_status sg_unordered_contains_hashed(sg_unordered* table, const void* keys, const uint64_t* hashes,
+                                              int64_t n, uint8_t* out_flags, void* stream);
+/* bucket() of a key whose hash is `hash`: fibonacci hashing onto bucket_count (unordered_base_detail.cuh:547-564). */
+SG_API sg_status sg_unordered_bucket_of_hash(const sg_unordered* table, uint64_t hash, int64_t* out_bucket);
+
 /* Bulk-insert strategy (no counterpart in the reference).  SG_INSERT_AUTO: when a call without per-element
  * flags brings at least 2^22 keys and one key per two probe groups of a table of 256 MB or more, the keys
  * are first partitioned by home-group range into a scratch array (n x sizeof(value_type), kept by the

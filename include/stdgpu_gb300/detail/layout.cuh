@@ -219,6 +219,92 @@ SG_HD typename kind_consts<KIND>::V value_in_lane(const uint4& d, int s)
     }
 }
 
+// The reference's hash<uint32_t> / hash<uint64_t> is the identity (src/stdgpu/impl/functional_detail.h:60-80):
+// the bucket of an integer key is the fibonacci hashing of the key itself.
+struct identity_word_hash
+{
+    template <typename K>
+    SG_HD uint64_t
+    operator()(K key_word) const
+    {
+        return static_cast<uint64_t>(key_word);
+    }
+};
+
+#if defined(__CUDACC__)
+// 16-byte compare-and-swap (sm_90 and later): old <- *p; if old == expected then *p <- desired.
+SG_D void
+cas128(void* p, unsigned long long e_lo, unsigned long long e_hi, unsigned long long d_lo, unsigned long long d_hi,
+       unsigned long long& o_lo, unsigned long long& o_hi)
+{
+    asm volatile("{\n\t.reg .b128 d, b, c;\n\t"
+                 "mov.b128 b, {%2, %3};\n\t"
+                 "mov.b128 c, {%4, %5};\n\t"
+                 "atom.global.cas.b128 d, [%6], b, c;\n\t"
+                 "mov.b128 {%0, %1}, d;\n\t}"
+                 : "=l"(o_lo), "=l"(o_hi)
+                 : "l"(e_lo), "l"(e_hi), "l"(d_lo), "l"(d_hi), "l"(p)
+                 : "memory");
+}
+
+SG_D unsigned long long
+pack2(uint32_t lo, uint32_t hi)
+{
+    return static_cast<unsigned long long>(hi) << 32 | lo;
+}
+
+// Claim of a slot whose image is exp (4 words; a never-used slot is all ones) with one compare-and-swap
+// over the whole slot: key and mapped value are written together (4, 8 or 16 bytes), so no reader sees
+// the key without its value.  Returns true when the claim took the slot; old_key is the key word found.
+template <int KIND>
+SG_D bool
+claim_slot_image(char* p, const uint32_t (&exp)[4], typename kind_consts<KIND>::K key,
+                 typename kind_consts<KIND>::V val, typename kind_consts<KIND>::K& old_key)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    constexpr int sb = C::slot_bytes;
+    uint32_t nw[4] = { exp[0], exp[1], exp[2], exp[3] };
+    nw[0] = static_cast<uint32_t>(key);
+    if constexpr (sizeof(K) == 8)
+    {
+        nw[1] = static_cast<uint32_t>(static_cast<uint64_t>(key) >> 32);
+    }
+    if constexpr (kind_traits<KIND>::is_map)
+    {
+        constexpr int vo = kind_traits<KIND>::val_offset / 4;
+        nw[vo] = static_cast<uint32_t>(val);
+        if constexpr (sizeof(V) == 8)
+        {
+            nw[vo + 1] = static_cast<uint32_t>(static_cast<uint64_t>(val) >> 32);
+        }
+    }
+    if constexpr (sb == 4)
+    {
+        const uint32_t o = atomicCAS(reinterpret_cast<unsigned int*>(p), exp[0], nw[0]);
+        old_key = static_cast<K>(o);
+        return o == exp[0];
+    }
+    else if constexpr (sb == 8)
+    {
+        const unsigned long long e = pack2(exp[0], exp[1]);
+        const unsigned long long o = atomicCAS(reinterpret_cast<unsigned long long*>(p), e, pack2(nw[0], nw[1]));
+        old_key = sizeof(K) == 8 ? static_cast<K>(o) : static_cast<K>(static_cast<uint32_t>(o));
+        return o == e;
+    }
+    else
+    {
+        const unsigned long long e_lo = pack2(exp[0], exp[1]);
+        const unsigned long long e_hi = pack2(exp[2], exp[3]);
+        unsigned long long o_lo, o_hi;
+        cas128(p, e_lo, e_hi, pack2(nw[0], nw[1]), pack2(nw[2], nw[3]), o_lo, o_hi);
+        old_key = sizeof(K) == 8 ? static_cast<K>(o_lo) : static_cast<K>(static_cast<uint32_t>(o_lo));
+        return o_lo == e_lo && o_hi == e_hi;
+    }
+}
+#endif
+
 } // namespace detail
 } // namespace sg
 

@@ -12,10 +12,14 @@
 //    insert entry point (sg_unordered_insert), which runs alone on a table.
 //  * erase marks the slot erased (compare-and-swap key -> erased marker);
 //    exactly one of several concurrent erases of a key reports success.
-//  * find run concurrently with an insert of the same key may see the key
-//    before its mapped value is stored; the reference orders the two with its
-//    per-slot lock.  Separate finds from inserts of the same keys by a launch
-//    boundary when the mapped value matters.
+//  * insert writes the key and its mapped value with one compare-and-swap over
+//    the whole slot (up to 16 bytes), so a concurrent find sees either no key
+//    or the key with its value (the reference orders the two with its per-slot
+//    lock).
+//
+// HashFn maps a key word to the 64-bit hash whose fibonacci hashing gives the
+// reference bucket (identity for integer keys; a custom key type packs into the
+// key word and supplies the reference's Hash, see stdgpu_gb300/stdgpu.cuh).
 #ifndef STDGPU_GB300_DEVICE_CUH
 #define STDGPU_GB300_DEVICE_CUH
 
@@ -27,7 +31,7 @@
 namespace sg
 {
 
-template <int KIND>
+template <int KIND, class HashFn = detail::identity_word_hash>
 struct unordered_ref
 {
     using C = detail::kind_consts<KIND>;
@@ -56,18 +60,17 @@ struct unordered_ref
         return reinterpret_cast<const uint4*>(static_cast<const char*>(v.slots) + g * detail::kGroupBytes);
     }
 
-    // bucket(key): the reference's fibonacci hashing of the identity hash
+    // bucket(key): the reference's fibonacci hashing of the key's hash
     __device__ __forceinline__ int64_t
     bucket(key_type key) const
     {
-        return static_cast<int64_t>(detail::fibonacci_bucket(static_cast<uint64_t>(key), v.bucket_bits));
+        return static_cast<int64_t>(detail::fibonacci_bucket(HashFn{}(key), v.bucket_bits));
     }
 
     __device__ __forceinline__ int64_t
     home_group(key_type key) const
     {
-        return detail::group_of_bucket(detail::fibonacci_bucket(static_cast<uint64_t>(key), v.bucket_bits),
-                                       v.bucket_bits,
+        return detail::group_of_bucket(detail::fibonacci_bucket(HashFn{}(key), v.bucket_bits), v.bucket_bits,
                                        v.num_groups);
     }
 
@@ -111,6 +114,52 @@ struct unordered_ref
                         return g * G + l * SPL + s;
                     }
                     any_empty |= (k == C::empty_key);
+                }
+            }
+            if (any_empty)
+            {
+                return -1;
+            }
+            g = detail::next_group(g, v.num_groups);
+        }
+        return -1;
+    }
+
+    // Slot of the stored key k for which eq(k) holds, searched along the probe sequence of the home group of
+    // `hash` (heterogeneous lookup: a key-like value with the same hash as the key it equals), or -1.
+    template <class Eq>
+    __device__ int64_t
+    find_slot_if(uint64_t hash, Eq eq) const
+    {
+        for (int s = 0; s < 2; ++s)
+        {
+            const key_type k = s == 0 ? C::empty_key : C::tomb_key;
+            if (*reinterpret_cast<volatile unsigned*>(&header()->special_state[s]) == 1u && eq(k))
+            {
+                return special_slot(k);
+            }
+        }
+        int64_t g = detail::group_of_bucket(detail::fibonacci_bucket(hash, v.bucket_bits), v.bucket_bits, v.num_groups);
+        for (int64_t probes = 0; probes < v.num_groups; ++probes)
+        {
+            const uint4* p = group_ptr(g);
+            bool any_empty = false;
+#pragma unroll
+            for (int l = 0; l < detail::kTileLanes; ++l)
+            {
+                const uint4 d = __ldcg(p + l);
+#pragma unroll
+                for (int s = 0; s < SPL; ++s)
+                {
+                    const key_type k = detail::key_in_lane<KIND>(d, s);
+                    if (k == C::empty_key)
+                    {
+                        any_empty = true;
+                    }
+                    else if (k != C::tomb_key && eq(k))
+                    {
+                        return g * G + l * SPL + s;
+                    }
                 }
             }
             if (any_empty)
@@ -205,14 +254,10 @@ struct unordered_ref
                 }
                 continue;
             }
-            const key_type old = cas_key(target, C::empty_key, key);
-            if (old == C::empty_key)
+            key_type old;
+            const uint32_t never_used[4] = { ~0u, ~0u, ~0u, ~0u };
+            if (detail::claim_slot_image<KIND>(slot_ptr(target), never_used, key, mapped, old))
             {
-                if constexpr (detail::kind_traits<KIND>::is_map)
-                {
-                    *reinterpret_cast<volatile mapped_type*>(slot_ptr(target) + detail::kind_traits<KIND>::val_offset) =
-                            mapped;
-                }
                 atomicAdd(&header()->size, 1ull);
                 return target;
             }

@@ -29,6 +29,41 @@ namespace stdgpu
 
 using index_t = std::int32_t; // the reference's default index type (src/stdgpu/cstddef.h:42-59)
 
+// stdgpu::hash: the identity for integer keys (src/stdgpu/impl/functional_detail.h:60-80).  Other key types
+// bring their own Hash.
+template <typename Key>
+struct hash
+{
+    template <typename K = Key, typename = std::enable_if_t<std::is_integral<K>::value>>
+    __host__ __device__ std::size_t
+    operator()(const Key& key) const
+    {
+        return static_cast<std::size_t>(key);
+    }
+};
+
+// stdgpu::equal_to (src/stdgpu/functional.h); equal_to<void> compares any two comparable values.
+template <typename T = void>
+struct equal_to
+{
+    __host__ __device__ bool
+    operator()(const T& a, const T& b) const
+    {
+        return a == b;
+    }
+};
+template <>
+struct equal_to<void>
+{
+    using is_transparent = void;
+    template <typename A, typename B>
+    __host__ __device__ bool
+    operator()(const A& a, const B& b) const
+    {
+        return a == b;
+    }
+};
+
 inline void (*gb300_error_handler)(sg_status, const char*) = [](sg_status st, const char* what) {
     std::fprintf(stderr, "stdgpu_gb300: %s failed: %s\n", what, sg_status_string(st));
     std::terminate();
@@ -357,12 +392,13 @@ protected:
 };
 } // namespace detail
 
-// stdgpu::unordered_map<Key, T> for 4/8-byte unsigned integer Key and T.
-template <typename Key, typename T>
-class unordered_map : public detail::gb300_unordered<Key, T, pair<const Key, T>, unordered_map<Key, T>>
+namespace detail
 {
-    using base = detail::gb300_unordered<Key, T, pair<const Key, T>, unordered_map<Key, T>>;
-    friend base;
+// unordered_map<Key, T> for 4/8-byte unsigned integer Key and T with the identity hash.
+template <typename Key, typename T, typename Derived>
+class native_map : public gb300_unordered<Key, T, pair<const Key, T>, Derived>
+{
+    using base = gb300_unordered<Key, T, pair<const Key, T>, Derived>;
 
 public:
     using mapped_type = T;
@@ -386,12 +422,11 @@ public:
     }
 };
 
-// stdgpu::unordered_set<Key> for 4/8-byte unsigned integer Key.
-template <typename Key>
-class unordered_set : public detail::gb300_unordered<Key, void, Key, unordered_set<Key>>
+// unordered_set<Key> for 4/8-byte unsigned integer Key with the identity hash.
+template <typename Key, typename Derived>
+class native_set : public gb300_unordered<Key, void, Key, Derived>
 {
-    using base = detail::gb300_unordered<Key, void, Key, unordered_set<Key>>;
-    friend base;
+    using base = gb300_unordered<Key, void, Key, Derived>;
 
 public:
     using typename base::iterator;
@@ -411,6 +446,33 @@ public:
     {
         return this->insert_impl(key, typename base::ref_type::mapped_type{});
     }
+};
+} // namespace detail
+} // namespace stdgpu
+
+#include "custom_key.cuh"
+
+namespace stdgpu
+{
+
+// stdgpu::unordered_map<Key, T, Hash>: integer keys with the default hash use the library's precompiled
+// kernels; any other key type of at most 8 bytes (short3, vec3int16, packed coordinates) with a user
+// Hash goes through the custom-key path of custom_key.cuh.
+template <typename Key, typename T, typename Hash = hash<Key>, typename KeyEqual = equal_to<Key>>
+class unordered_map
+  : public std::conditional_t<detail::is_native_key<Key, Hash>::value,
+                              detail::native_map<Key, T, unordered_map<Key, T, Hash, KeyEqual>>,
+                              detail::custom_map<Key, T, Hash, unordered_map<Key, T, Hash, KeyEqual>>>
+{
+};
+
+// stdgpu::unordered_set<Key, Hash>
+template <typename Key, typename Hash = hash<Key>, typename KeyEqual = equal_to<Key>>
+class unordered_set
+  : public std::conditional_t<detail::is_native_key<Key, Hash>::value,
+                              detail::native_set<Key, unordered_set<Key, Hash, KeyEqual>>,
+                              detail::custom_set<Key, Hash, unordered_set<Key, Hash, KeyEqual>>>
+{
 };
 
 // stdgpu::vector<T>: bulk push_back and size (src/stdgpu/vector.cuh); device push_back is

@@ -30,6 +30,44 @@ KEY_DTYPE = {SET_U32: np.uint32, SET_U64: np.uint64, MAP_U64_U32: np.uint64, MAP
 VAL_DTYPE = {SET_U32: None, SET_U64: None, MAP_U64_U32: np.uint32, MAP_U64_U64: np.uint64,
              MAP_U32_U32: np.uint32, MAP_U32_U64: np.uint64}
 
+# A custom key type with a user hash, as the reference's users write them: 3 x int16 coordinates hashed by
+# the spatial hash of Teschner et al. (2003) (oracle/ref_driver.cpp; the reference's tests use this pair,
+# tests/stdgpu/unordered_map.inc:178-206).  Only RefTable takes these kinds; the port and the GPU tables
+# store such a key as its zero-padded 8-byte word with the hash passed per key.
+SET_VEC3I16, MAP_VEC3I16_U32 = 6, 7
+VEC3I16 = np.dtype([("x", "<i2"), ("y", "<i2"), ("z", "<i2")])
+KEY_DTYPE[SET_VEC3I16] = VEC3I16
+KEY_DTYPE[MAP_VEC3I16_U32] = VEC3I16
+VAL_DTYPE[SET_VEC3I16] = None
+VAL_DTYPE[MAP_VEC3I16_U32] = np.uint32
+# the word-keyed kinds holding them (8-byte key words)
+WORD_KIND = {SET_VEC3I16: SET_U64, MAP_VEC3I16_U32: MAP_U64_U32}
+
+
+def vec3i16_words(keys: np.ndarray) -> np.ndarray:
+    """Object bytes of each 6-byte key, zero-padded to a little-endian 64-bit word."""
+    k = np.ascontiguousarray(keys, dtype=VEC3I16)
+    w = np.zeros(len(k), np.uint64)
+    w.view(np.uint8).reshape(-1, 8)[:, :6] = k.view(np.uint8).reshape(-1, 6)
+    return w
+
+
+def words_vec3i16(words: np.ndarray) -> np.ndarray:
+    w = np.ascontiguousarray(words, dtype=np.uint64)
+    k = np.zeros(len(w), VEC3I16)
+    k.view(np.uint8).reshape(-1, 6)[:] = w.view(np.uint8).reshape(-1, 8)[:, :6]
+    return k
+
+
+def spatial_hash(keys: np.ndarray) -> np.ndarray:
+    """(size_t(x) * 73856093) ^ (size_t(y) * 19349669) ^ (size_t(z) * 83492791), coordinates sign-extended."""
+    k = np.ascontiguousarray(keys, dtype=VEC3I16)
+    with np.errstate(over="ignore"):
+        hx = k["x"].astype(np.int64).astype(np.uint64) * np.uint64(73856093)
+        hy = k["y"].astype(np.int64).astype(np.uint64) * np.uint64(19349669)
+        hz = k["z"].astype(np.int64).astype(np.uint64) * np.uint64(83492791)
+    return hx ^ hy ^ hz
+
 _port = None
 _ref = None
 
@@ -68,6 +106,9 @@ def port_lib() -> ctypes.CDLL:
         L.port_deque_ops.argtypes = [c_int64, c_void_p, c_int64, c_void_p, c_void_p, c_int64, c_void_p, c_void_p,
                                      c_void_p]
         L.port_bitset_count.argtypes = [c_void_p, c_int64]
+        L.port_insert_bulk_h.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p]
+        L.port_erase_bulk_h.argtypes = [c_void_p, c_void_p, c_void_p, c_int64, c_void_p]
+        L.port_find_bulk_h.argtypes = [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]
     return _port
 
 
@@ -156,25 +197,38 @@ class PortTable(_TableBase):
 
     __del__ = close
 
-    def insert(self, keys, vals=None, flags: bool = False):
+    # hashes (optional, uint64 per key): Hash(key) of a custom key type; keys are then the key words
+    def insert(self, keys, vals=None, flags: bool = False, hashes=None):
         k = self._keys(keys).astype(np.uint64)
         v = self._vals(vals, len(k))
         v64 = None if v is None else v.astype(np.uint64)
         f = np.zeros(len(k), np.uint8) if flags else None
-        self.L.port_insert_bulk(self.h, _p(k), _p(v64), len(k), _p(f))
+        if hashes is None:
+            self.L.port_insert_bulk(self.h, _p(k), _p(v64), len(k), _p(f))
+        else:
+            h = np.ascontiguousarray(hashes, dtype=np.uint64)
+            self.L.port_insert_bulk_h(self.h, _p(k), _p(h), _p(v64), len(k), _p(f))
         return f
 
-    def erase(self, keys, flags: bool = False):
+    def erase(self, keys, flags: bool = False, hashes=None):
         k = self._keys(keys).astype(np.uint64)
         f = np.zeros(len(k), np.uint8) if flags else None
-        self.L.port_erase_bulk(self.h, _p(k), len(k), _p(f))
+        if hashes is None:
+            self.L.port_erase_bulk(self.h, _p(k), len(k), _p(f))
+        else:
+            h = np.ascontiguousarray(hashes, dtype=np.uint64)
+            self.L.port_erase_bulk_h(self.h, _p(k), _p(h), len(k), _p(f))
         return f
 
-    def find(self, keys):
+    def find(self, keys, hashes=None):
         k = self._keys(keys).astype(np.uint64)
         v = np.zeros(len(k), np.uint64)
         f = np.zeros(len(k), np.uint8)
-        self.L.port_find_bulk(self.h, _p(k), len(k), _p(v), _p(f))
+        if hashes is None:
+            self.L.port_find_bulk(self.h, _p(k), len(k), _p(v), _p(f))
+        else:
+            h = np.ascontiguousarray(hashes, dtype=np.uint64)
+            self.L.port_find_bulk_h(self.h, _p(k), _p(h), len(k), _p(v), _p(f))
         vd = VAL_DTYPE[self.kind]
         return (v.astype(vd) if vd is not None else None), f
 
@@ -268,6 +322,11 @@ class RefTable(_TableBase):
         self.L.sgref_clear(self.h)
 
     def bucket(self, key: int) -> int:
+        k = np.array([key], dtype=KEY_DTYPE[self.kind])
+        return int(self.L.sgref_bucket(self.h, _p(k)))
+
+    def bucket_of(self, key) -> int:
+        """bucket() of one key of any key type (a numpy scalar or record)."""
         k = np.array([key], dtype=KEY_DTYPE[self.kind])
         return int(self.L.sgref_bucket(self.h, _p(k)))
 

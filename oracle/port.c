@@ -21,6 +21,7 @@ struct port_table
     int64_t total_count;
     uint64_t* keys;    /* _values (key part)   unordered_base.cuh */
     uint64_t* vals;    /* _values (mapped part) */
+    uint64_t* hashes;  /* Hash(key) of each slot's key (the identity for integer keys) */
     int64_t* offsets;  /* _offsets: relative link to the next chain entry, 0 = end */
     uint8_t* occupied; /* _occupied bitset, one byte per slot here */
     int64_t occupied_count; /* _occupied_count */
@@ -98,6 +99,7 @@ port_table* port_create(int64_t capacity)
     t->keys = (uint64_t*)calloc(n, sizeof(uint64_t));
     t->vals = (uint64_t*)calloc(n, sizeof(uint64_t));
     t->offsets = (int64_t*)calloc(n, sizeof(int64_t));
+    t->hashes = (uint64_t*)calloc(n, sizeof(uint64_t));
     t->occupied = (uint8_t*)calloc(n, 1);
     t->excess = (int64_t*)calloc((size_t)t->excess_count, sizeof(int64_t));
     t->occupied_count = 0;
@@ -112,6 +114,7 @@ void port_destroy(port_table* t)
         return;
     free(t->keys);
     free(t->vals);
+    free(t->hashes);
     free(t->offsets);
     free(t->occupied);
     free(t->excess);
@@ -125,10 +128,11 @@ int64_t port_bucket(const port_table* t, uint64_t key)
     return port_fibonacci_hashing(key, t->bucket_count);
 }
 
-/* find_impl: src/stdgpu/impl/unordered_base_detail.cuh:653-682; returns the slot or -1 (end()) */
-static int64_t find_pos(const port_table* t, uint64_t key)
+/* find_impl: src/stdgpu/impl/unordered_base_detail.cuh:653-682; returns the slot or -1 (end()).
+ * hash: Hash(key), whose fibonacci hashing is the key's bucket (bucket_impl :547-564). */
+static int64_t find_pos_h(const port_table* t, uint64_t key, uint64_t hash)
 {
-    int64_t i = port_bucket(t, key);
+    int64_t i = port_fibonacci_hashing(hash, t->bucket_count);
     if (t->occupied[i] && t->keys[i] == key)
         return i;
     while (t->offsets[i] != 0)
@@ -138,6 +142,21 @@ static int64_t find_pos(const port_table* t, uint64_t key)
             return i;
     }
     return -1;
+}
+
+static int64_t find_pos(const port_table* t, uint64_t key)
+{
+    return find_pos_h(t, key, key);
+}
+
+int port_find_h(const port_table* t, uint64_t key, uint64_t hash, uint64_t* value)
+{
+    int64_t p = find_pos_h(t, key, hash);
+    if (p < 0)
+        return 0;
+    if (value)
+        *value = t->vals[p];
+    return 1;
 }
 
 int port_find(const port_table* t, uint64_t key, uint64_t* value)
@@ -181,20 +200,21 @@ static int is_full(const port_table* t)
 }
 
 /* insert(value) retry loop :967-994 around try_insert :708-809, run by one thread */
-int port_insert(port_table* t, uint64_t key, uint64_t value)
+int port_insert_h(port_table* t, uint64_t key, uint64_t hash, uint64_t value)
 {
     /* loop guard :980-981: refuse when full or when the excess free-list is empty */
     if (is_full(t) || t->excess_size == 0)
         return 0;
     /* :719 / :803-806 the key is present: no action */
-    if (find_pos(t, key) >= 0)
+    if (find_pos_h(t, key, hash) >= 0)
         return 0;
-    int64_t b = port_bucket(t, key);
+    int64_t b = port_fibonacci_hashing(hash, t->bucket_count);
     if (!t->occupied[b])
     {
         /* :723-753 free bucket: construct in place, the chain link is left untouched */
         t->keys[b] = key;
         t->vals[b] = value;
+        t->hashes[b] = hash;
         ++t->occupied_count;
         t->occupied[b] = 1;
         return 1;
@@ -206,6 +226,7 @@ int port_insert(port_table* t, uint64_t key, uint64_t value)
     int64_t p = t->excess[--t->excess_size]; /* vector::pop_back: vector_detail.cuh:240-299 */
     t->keys[p] = key;
     t->vals[p] = value;
+    t->hashes[p] = hash;
     t->offsets[p] = 0;
     ++t->occupied_count;
     t->occupied[p] = 1;
@@ -213,13 +234,18 @@ int port_insert(port_table* t, uint64_t key, uint64_t value)
     return 1;
 }
 
-/* erase(key) retry loop :1019-1043 around try_erase :811-913, run by one thread */
-int port_erase(port_table* t, uint64_t key)
+int port_insert(port_table* t, uint64_t key, uint64_t value)
 {
-    int64_t p = find_pos(t, key);
+    return port_insert_h(t, key, key, value);
+}
+
+/* erase(key) retry loop :1019-1043 around try_erase :811-913, run by one thread */
+int port_erase_h(port_table* t, uint64_t key, uint64_t hash)
+{
+    int64_t p = find_pos_h(t, key, hash);
     if (p < 0)
         return 0;
-    int64_t b = port_bucket(t, key);
+    int64_t b = port_fibonacci_hashing(hash, t->bucket_count);
     if (p == b)
     {
         /* :826-857 bucket head: reset occupancy, leave the chain link */
@@ -237,6 +263,47 @@ int port_erase(port_table* t, uint64_t key)
     --t->occupied_count;
     t->excess[t->excess_size++] = p; /* vector::push_back: vector_detail.cuh:181-238 */
     return 1;
+}
+
+int port_erase(port_table* t, uint64_t key)
+{
+    return port_erase_h(t, key, key);
+}
+
+/* bulk forms with caller-supplied hashes (a user Hash functor); flags / values / found may be NULL */
+void port_insert_bulk_h(port_table* t, const uint64_t* keys, const uint64_t* hashes, const uint64_t* values, int64_t n,
+                        uint8_t* flags)
+{
+    for (int64_t i = 0; i < n; ++i)
+    {
+        int r = port_insert_h(t, keys[i], hashes[i], values ? values[i] : 0);
+        if (flags)
+            flags[i] = (uint8_t)r;
+    }
+}
+
+void port_erase_bulk_h(port_table* t, const uint64_t* keys, const uint64_t* hashes, int64_t n, uint8_t* flags)
+{
+    for (int64_t i = 0; i < n; ++i)
+    {
+        int r = port_erase_h(t, keys[i], hashes[i]);
+        if (flags)
+            flags[i] = (uint8_t)r;
+    }
+}
+
+void port_find_bulk_h(const port_table* t, const uint64_t* keys, const uint64_t* hashes, int64_t n, uint64_t* values,
+                      uint8_t* found)
+{
+    for (int64_t i = 0; i < n; ++i)
+    {
+        uint64_t v = 0;
+        int r = port_find_h(t, keys[i], hashes[i], &v);
+        if (found)
+            found[i] = (uint8_t)r;
+        if (values)
+            values[i] = r ? v : 0;
+    }
 }
 
 /* bulk insert(begin,end): :996-1017 -- one insert(value) per element */
@@ -349,7 +416,7 @@ int port_valid(const port_table* t)
         if (!t->occupied[i])
             continue;
         ++pop;
-        if (find_pos(t, t->keys[i]) != i)
+        if (find_pos_h(t, t->keys[i], t->hashes[i]) != i)
             return 0;
     }
     /* occupied_count_valid :453-468 */

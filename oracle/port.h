@@ -41,6 +41,15 @@ int port_find(const port_table* t, uint64_t key, uint64_t* value);
 void port_insert_bulk(port_table* t, const uint64_t* keys, const uint64_t* values, int64_t n, uint8_t* flags);
 void port_erase_bulk(port_table* t, const uint64_t* keys, int64_t n, uint8_t* flags);
 void port_find_bulk(const port_table* t, const uint64_t* keys, int64_t n, uint64_t* values, uint8_t* found);
+/* the same with a caller-supplied Hash(key) per key (custom key types; bucket = fibonacci_hashing(hash)) */
+int port_insert_h(port_table* t, uint64_t key, uint64_t hash, uint64_t value);
+int port_erase_h(port_table* t, uint64_t key, uint64_t hash);
+int port_find_h(const port_table* t, uint64_t key, uint64_t hash, uint64_t* value);
+void port_insert_bulk_h(port_table* t, const uint64_t* keys, const uint64_t* hashes, const uint64_t* values, int64_t n,
+                        uint8_t* flags);
+void port_erase_bulk_h(port_table* t, const uint64_t* keys, const uint64_t* hashes, int64_t n, uint8_t* flags);
+void port_find_bulk_h(const port_table* t, const uint64_t* keys, const uint64_t* hashes, int64_t n, uint64_t* values,
+                      uint8_t* found);
 int64_t port_size(const port_table* t);
 int64_t port_bucket_count(const port_table* t);
 int64_t port_max_size(const port_table* t);

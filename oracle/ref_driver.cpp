@@ -42,6 +42,36 @@ enum kind_t
     MAP_U64_U64 = 3,
     MAP_U32_U32 = 4,
     MAP_U32_U64 = 5,
+    SET_VEC3I16 = 6,     // unordered_set<vec3i16, spatial_hash>
+    MAP_VEC3I16_U32 = 7, // unordered_map<vec3i16, uint32_t, spatial_hash>
+};
+
+// A custom key type and hash as the reference's users write them (the reference's own tests use a
+// 3 x int16 key with this hash: tests/stdgpu/unordered_map.inc:178-206).  The hash is the spatial hash
+// of Teschner et al., "Optimized Spatial Hashing for Collision Detection of Deformable Objects" (2003):
+// each coordinate, sign-extended to 64 bits, times one of three large primes, combined by xor.
+struct vec3i16
+{
+    std::int16_t x = 0;
+    std::int16_t y = 0;
+    std::int16_t z = 0;
+};
+
+inline bool
+operator==(const vec3i16& a, const vec3i16& b)
+{
+    return a.x == b.x && a.y == b.y && a.z == b.z;
+}
+
+struct spatial_hash
+{
+    std::size_t
+    operator()(const vec3i16& k) const
+    {
+        return (static_cast<std::size_t>(k.x) * static_cast<std::size_t>(73856093U)) ^
+               (static_cast<std::size_t>(k.y) * static_cast<std::size_t>(19349669U)) ^
+               (static_cast<std::size_t>(k.z) * static_cast<std::size_t>(83492791U));
+    }
 };
 
 struct table_base
@@ -63,10 +93,10 @@ struct table_base
 
 // ---- key/value plumbing: sets carry Key, maps carry pair<const Key, T> ----
 
-template <typename Key>
+template <typename Key, typename Hash = stdgpu::hash<Key>>
 struct set_traits
 {
-    using container = stdgpu::unordered_set<Key>;
+    using container = stdgpu::unordered_set<Key, Hash>;
     using key_type = Key;
     using mapped_type = std::uint8_t; // unused
     using value_type = Key;
@@ -84,10 +114,10 @@ struct set_traits
     }
 };
 
-template <typename Key, typename T>
+template <typename Key, typename T, typename Hash = stdgpu::hash<Key>>
 struct map_traits
 {
-    using container = stdgpu::unordered_map<Key, T>;
+    using container = stdgpu::unordered_map<Key, T, Hash>;
     using key_type = Key;
     using mapped_type = T;
     using value_type = stdgpu::pair<const Key, T>;
@@ -417,6 +447,10 @@ sgref_create(int kind, std::int64_t capacity)
             return new table_impl<map_traits<std::uint32_t, std::uint32_t>>(capacity);
         case MAP_U32_U64:
             return new table_impl<map_traits<std::uint32_t, std::uint64_t>>(capacity);
+        case SET_VEC3I16:
+            return new table_impl<set_traits<vec3i16, spatial_hash>>(capacity);
+        case MAP_VEC3I16_U32:
+            return new table_impl<map_traits<vec3i16, std::uint32_t, spatial_hash>>(capacity);
         default:
             return nullptr;
     }

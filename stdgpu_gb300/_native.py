@@ -7,7 +7,7 @@ fallback: if the library cannot be loaded, every entry point raises.
 from __future__ import annotations
 
 import ctypes
-from ctypes import POINTER, c_char_p, c_int32, c_int64, c_uint8, c_uint32, c_void_p
+from ctypes import c_uint64, POINTER, c_char_p, c_int32, c_int64, c_uint8, c_uint32, c_void_p
 from pathlib import Path
 
 from . import build as _build
@@ -79,6 +79,12 @@ SIGNATURES = {
     "sg_unordered_insert_kv": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_unordered_erase": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_unordered_set_insert_mode": (c_int32, [c_void_p, c_int32]),
+    "sg_unordered_create_hashed": (c_int32, [c_int32, c_int64, c_void_p, POINTER(c_void_p)]),
+    "sg_unordered_insert_hashed": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "sg_unordered_erase_hashed": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "sg_unordered_find_hashed": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "sg_unordered_contains_hashed": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "sg_unordered_bucket_of_hash": (c_int32, [c_void_p, c_uint64, POINTER(c_int64)]),
     "sg_unordered_find": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "sg_unordered_contains": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_unordered_size": (c_int32, [c_void_p, c_void_p, POINTER(c_int64)]),

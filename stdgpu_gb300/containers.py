@@ -94,9 +94,11 @@ def _host_out(n: int, dtype) -> torch.Tensor:
 class unordered_base:
     """Shared implementation of unordered_set / unordered_map (src/stdgpu/impl/unordered_base.cuh:56-583)."""
 
-    def __init__(self, handle: int, kind: int):
+    def __init__(self, handle: int, kind: int, custom_hash: bool = False):
         self._h = c_void_p(handle)
         self.kind = kind
+        # custom key types: keys are key words, and every bulk call takes hashes=Hash(key) per key
+        self.custom_hash = custom_hash
         self.key_bytes = _KEY_BYTES[kind]
         self.mapped_bytes = _MAPPED_BYTES[kind]
         g = N.sg_geometry()
@@ -105,11 +107,21 @@ class unordered_base:
 
     # ---- create / destroy: unordered_base_detail.cuh:1254-1348
     @classmethod
-    def _create(cls, kind: int, capacity: int, stream=None):
+    def _create(cls, kind: int, capacity: int, stream=None, custom_hash: bool = False):
         lib = N.load()
         h = c_void_p()
-        N.check(lib.sg_unordered_create(kind, int(capacity), _stream(stream), byref(h)), "createDeviceObject")
-        return cls(h.value, kind)
+        create = lib.sg_unordered_create_hashed if custom_hash else lib.sg_unordered_create
+        N.check(create(kind, int(capacity), _stream(stream), byref(h)), "createDeviceObject")
+        return cls(h.value, kind, custom_hash)
+
+    def _hashes(self, hashes, n: int) -> c_void_p:
+        if not self.custom_hash:
+            if hashes is not None:
+                raise ValueError("hashes are for tables created with custom_hash=True")
+            return c_void_p(0)
+        if hashes is None or hashes.numel() != n or hashes.element_size() != 8:
+            raise ValueError("a custom-hash table needs one 64-bit hash per key")
+        return _ptr(hashes.contiguous())
 
     @staticmethod
     def destroyDeviceObject(obj: "unordered_base") -> None:
@@ -135,6 +147,12 @@ class unordered_base:
         import numpy as np
         return float(np.float32(self.size(stream)) / np.float32(self.bucket_count()))
 
+    def bucket_of_hash(self, hash_value: int) -> int:
+        """bucket() of a key whose Hash is hash_value (custom key types)."""
+        out = c_int64()
+        N.check(N.load().sg_unordered_bucket_of_hash(self._h, int(hash_value) & (2**64 - 1), byref(out)), "bucket")
+        return out.value
+
     def bucket(self, key: int) -> int:
         kb = self.key_bytes
         buf = (ctypes.c_uint32 if kb == 4 else ctypes.c_uint64)(int(key) & ((1 << (8 * kb)) - 1))
@@ -150,7 +168,7 @@ class unordered_base:
         (stream if stream is not None else torch.cuda.current_stream()).synchronize()
 
     def insert(self, keys: torch.Tensor, mapped: torch.Tensor | None = None, *, flags: torch.Tensor | None = None,
-               stream=None, stager: "stager | None" = None) -> None:
+               stream=None, stager: "stager | None" = None, hashes: torch.Tensor | None = None) -> None:
         """insert(begin, end) over keys (+ mapped values for maps): unordered_base_detail.cuh:996-1017."""
         keys = _as_bits(keys, self.key_bytes, "keys")
         if self.mapped_bytes:
@@ -159,6 +177,11 @@ class unordered_base:
             mapped = _as_bits(mapped, self.mapped_bytes, "mapped")
         else:
             mapped = None
+        if self.custom_hash:
+            N.check(N.load().sg_unordered_insert_hashed(self._h, _ptr(keys), _ptr(mapped),
+                                                        self._hashes(hashes, keys.numel()), keys.numel(), _ptr(flags),
+                                                        _stream(stream)), "insert")
+            return
         if not keys.is_cuda:
             st = stager or default_stager()
             N.check(N.load().sg_unordered_insert_kv_host(self._h, st._h, _hptr(keys), _hptr(mapped), keys.numel(),
@@ -175,9 +198,13 @@ class unordered_base:
         N.check(N.load().sg_unordered_insert(self._h, _ptr(values), int(n), _ptr(flags), _stream(stream)), "insert")
 
     def erase(self, keys: torch.Tensor, *, flags: torch.Tensor | None = None, stream=None,
-              stager: "stager | None" = None) -> None:
+              stager: "stager | None" = None, hashes: torch.Tensor | None = None) -> None:
         """erase(begin, end): unordered_base_detail.cuh:1045-1066."""
         keys = _as_bits(keys, self.key_bytes, "keys")
+        if self.custom_hash:
+            N.check(N.load().sg_unordered_erase_hashed(self._h, _ptr(keys), self._hashes(hashes, keys.numel()),
+                                                       keys.numel(), _ptr(flags), _stream(stream)), "erase")
+            return
         if not keys.is_cuda:
             st = stager or default_stager()
             N.check(N.load().sg_unordered_erase_host(self._h, st._h, _hptr(keys), keys.numel(), _hptr(flags),
@@ -187,8 +214,14 @@ class unordered_base:
         N.check(N.load().sg_unordered_erase(self._h, _ptr(keys), keys.numel(), _ptr(flags), _stream(stream)),
                 "erase")
 
-    def contains(self, keys: torch.Tensor, stream=None, stager: "stager | None" = None) -> torch.Tensor:
+    def contains(self, keys: torch.Tensor, stream=None, stager: "stager | None" = None,
+                 hashes: torch.Tensor | None = None) -> torch.Tensor:
         keys = _as_bits(keys, self.key_bytes, "keys")
+        if self.custom_hash:
+            out = torch.empty(keys.numel(), dtype=torch.uint8, device=keys.device)
+            N.check(N.load().sg_unordered_contains_hashed(self._h, _ptr(keys), self._hashes(hashes, keys.numel()),
+                                                          keys.numel(), _ptr(out), _stream(stream)), "contains")
+            return out
         if not keys.is_cuda:
             st = stager or default_stager()
             out = _host_out(keys.numel(), torch.uint8)
@@ -201,12 +234,20 @@ class unordered_base:
                 "contains")
         return out
 
-    def count(self, keys: torch.Tensor, stream=None) -> torch.Tensor:
-        return self.contains(keys, stream)
+    def count(self, keys: torch.Tensor, stream=None, hashes: torch.Tensor | None = None) -> torch.Tensor:
+        return self.contains(keys, stream, hashes=hashes)
 
-    def find(self, keys: torch.Tensor, stream=None,
-             stager: "stager | None" = None) -> tuple[torch.Tensor | None, torch.Tensor]:
+    def find(self, keys: torch.Tensor, stream=None, stager: "stager | None" = None,
+             hashes: torch.Tensor | None = None) -> tuple[torch.Tensor | None, torch.Tensor]:
         keys = _as_bits(keys, self.key_bytes, "keys")
+        if self.custom_hash:
+            found = torch.empty(keys.numel(), dtype=torch.uint8, device=keys.device)
+            vals = None
+            if self.mapped_bytes:
+                vals = torch.zeros(keys.numel(), dtype=_INT_DTYPE[self.mapped_bytes], device=keys.device)
+            N.check(N.load().sg_unordered_find_hashed(self._h, _ptr(keys), self._hashes(hashes, keys.numel()),
+                                                      keys.numel(), _ptr(vals), _ptr(found), _stream(stream)), "find")
+            return vals, found
         if not keys.is_cuda:
             st = stager or default_stager()
             found = _host_out(keys.numel(), torch.uint8)
@@ -282,8 +323,9 @@ class unordered_set(unordered_base):
     """stdgpu::unordered_set<Key> for Key = uint32_t / uint64_t (src/stdgpu/unordered_set.cuh:61-65)."""
 
     @classmethod
-    def createDeviceObject(cls, capacity: int, key: str = "u64", stream=None) -> "unordered_set":
-        return cls._create(KINDS[(key, None)], capacity, stream)
+    def createDeviceObject(cls, capacity: int, key: str = "u64", stream=None,
+                           custom_hash: bool = False) -> "unordered_set":
+        return cls._create(KINDS[(key, None)], capacity, stream, custom_hash)
 
 
 class unordered_map(unordered_base):
@@ -291,8 +333,8 @@ class unordered_map(unordered_base):
 
     @classmethod
     def createDeviceObject(cls, capacity: int, key: str = "u64", mapped: str = "u32",
-                           stream=None) -> "unordered_map":
-        return cls._create(KINDS[(key, mapped)], capacity, stream)
+                           stream=None, custom_hash: bool = False) -> "unordered_map":
+        return cls._create(KINDS[(key, mapped)], capacity, stream, custom_hash)
 
 
 def geometry_for(kind: int, capacity: int) -> N.sg_geometry:

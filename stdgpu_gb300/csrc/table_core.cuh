@@ -78,9 +78,9 @@ log2_exact(int64_t x)
 // Home group: the reference's bucket(key) scaled from 2^bits buckets onto num_groups groups.
 template <int KIND>
 SG_D uint32_t
-home_of(const dview& t, typename kind_consts<KIND>::K key)
+home_of(const dview& t, uint64_t hash)
 {
-    const uint32_t b = static_cast<uint32_t>(fibonacci_bucket(static_cast<uint64_t>(key), t.bits));
+    const uint32_t b = static_cast<uint32_t>(fibonacci_bucket(hash, t.bits));
     return static_cast<uint32_t>((static_cast<uint64_t>(b) * t.num_groups) >> t.bits);
 }
 
@@ -122,27 +122,6 @@ store_value(const dview& t, uint32_t slot, typename kind_consts<KIND>::V v)
     }
 }
 
-// 16-byte compare-and-swap (sm_90 and later): old <- *p; if old == expected then *p <- desired.
-SG_D void
-cas128(void* p, unsigned long long e_lo, unsigned long long e_hi, unsigned long long d_lo, unsigned long long d_hi,
-       unsigned long long& o_lo, unsigned long long& o_hi)
-{
-    asm volatile("{\n\t.reg .b128 d, b, c;\n\t"
-                 "mov.b128 b, {%2, %3};\n\t"
-                 "mov.b128 c, {%4, %5};\n\t"
-                 "atom.global.cas.b128 d, [%6], b, c;\n\t"
-                 "mov.b128 {%0, %1}, d;\n\t}"
-                 : "=l"(o_lo), "=l"(o_hi)
-                 : "l"(e_lo), "l"(e_hi), "l"(d_lo), "l"(d_hi), "l"(p)
-                 : "memory");
-}
-
-SG_D unsigned long long
-pack2(uint32_t lo, uint32_t hi)
-{
-    return static_cast<unsigned long long>(hi) << 32 | lo;
-}
-
 // Claim of a free slot with one compare-and-swap over the whole slot -- key and mapped value written
 // together (4, 8 or 16 bytes), so no separate store of the value follows and no reader can see the key
 // without its value.  A never-used slot is all ones; an erased slot keeps its old value bytes, so for
@@ -178,51 +157,7 @@ claim_slot(const dview& t, uint32_t slot, bool erased, typename kind_consts<KIND
             exp[1] = static_cast<uint32_t>(static_cast<uint64_t>(C::tomb_key) >> 32);
         }
     }
-    uint32_t nw[4] = { exp[0], exp[1], exp[2], exp[3] };
-    if constexpr (sizeof(K) == 8)
-    {
-        nw[0] = static_cast<uint32_t>(key);
-        nw[1] = static_cast<uint32_t>(static_cast<uint64_t>(key) >> 32);
-    }
-    else
-    {
-        nw[0] = static_cast<uint32_t>(key);
-    }
-    if constexpr (kind_traits<KIND>::is_map)
-    {
-        constexpr int vo = kind_traits<KIND>::val_offset / 4;
-        if constexpr (sizeof(V) == 8)
-        {
-            nw[vo] = static_cast<uint32_t>(val);
-            nw[vo + 1] = static_cast<uint32_t>(static_cast<uint64_t>(val) >> 32);
-        }
-        else
-        {
-            nw[vo] = static_cast<uint32_t>(val);
-        }
-    }
-    if constexpr (sb == 4)
-    {
-        const uint32_t o = atomicCAS(reinterpret_cast<unsigned int*>(p), exp[0], nw[0]);
-        old_key = static_cast<K>(o);
-        return o == exp[0];
-    }
-    else if constexpr (sb == 8)
-    {
-        const unsigned long long e = pack2(exp[0], exp[1]);
-        const unsigned long long o = atomicCAS(reinterpret_cast<unsigned long long*>(p), e, pack2(nw[0], nw[1]));
-        old_key = sizeof(K) == 8 ? static_cast<K>(o) : static_cast<K>(static_cast<uint32_t>(o));
-        return o == e;
-    }
-    else
-    {
-        const unsigned long long e_lo = pack2(exp[0], exp[1]);
-        const unsigned long long e_hi = pack2(exp[2], exp[3]);
-        unsigned long long o_lo, o_hi;
-        cas128(p, e_lo, e_hi, pack2(nw[0], nw[1]), pack2(nw[2], nw[3]), o_lo, o_hi);
-        old_key = sizeof(K) == 8 ? static_cast<K>(o_lo) : static_cast<K>(static_cast<uint32_t>(o_lo));
-        return o_lo == e_lo && o_hi == e_hi;
-    }
+    return claim_slot_image<KIND>(p, exp, key, val, old_key);
 }
 
 // Input element i: value_type array (AoS) or separate key / mapped arrays.
@@ -649,10 +584,10 @@ tile_nibble(unsigned ballot, int tbase)
 // group, read and ignored).
 template <int KIND>
 SG_D void
-load_homes(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K key, bool probe,
-           uint32_t (&hr)[kTile], uint32_t (&pre)[kTile][8])
+load_homes(const dview& t, const tile_lanes& L, uint64_t hash, bool probe, uint32_t (&hr)[kTile],
+           uint32_t (&pre)[kTile][8])
 {
-    const uint32_t home = probe ? home_of<KIND>(t, key) : 0u;
+    const uint32_t home = probe ? home_of<KIND>(t, hash) : 0u;
 #pragma unroll
     for (int r = 0; r < kTile; ++r)
     {
@@ -667,7 +602,7 @@ load_homes(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K ke
 template <int KIND, bool AOS>
 SG_D void
 insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in1, int64_t i, bool valid,
-            uint8_t* out_flags, step_counts& c)
+            uint8_t* out_flags, step_counts& c, const uint64_t* hashes = nullptr)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
@@ -685,7 +620,8 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
     const bool probe = valid && !special;
     uint32_t hr[kTile];
     uint32_t pre[kTile][8];
-    load_homes<KIND>(t, L, key, probe, hr, pre);
+    const uint64_t hash = hashes != nullptr && probe ? __ldcs(hashes + i) : static_cast<uint64_t>(key);
+    load_homes<KIND>(t, L, hash, probe, hr, pre);
     int my_state = 0; // 0 present, 1 claim my_target, 2 decided beyond the home group
     uint32_t my_target = 0;
     bool my_tomb = false;
@@ -764,7 +700,7 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
 // val.  Keys not decided in their home group (group full of other keys) continue with tile_find.
 template <int KIND, bool WANT_VALUE>
 SG_D int32_t
-locate_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K key, bool probe,
+locate_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K key, uint64_t hash, bool probe,
             typename kind_consts<KIND>::V& val)
 {
     using C = kind_consts<KIND>;
@@ -774,7 +710,7 @@ locate_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K k
     constexpr uint32_t S = sector_consts<KIND>::slots;
     uint32_t hr[kTile];
     uint32_t pre[kTile][8];
-    load_homes<KIND>(t, L, key, probe, hr, pre);
+    load_homes<KIND>(t, L, hash, probe, hr, pre);
     int32_t my_slot = -1;
     bool my_more = false;
 #pragma unroll
@@ -832,7 +768,7 @@ locate_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K k
 template <int KIND>
 SG_D void
 erase_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool valid, uint8_t* out_flags,
-           step_counts& c)
+           step_counts& c, const uint64_t* hashes = nullptr)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
@@ -847,7 +783,8 @@ erase_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, boo
     }
     const bool probe = valid && !special;
     V dummy{};
-    const int32_t my_slot = locate_step<KIND, false>(t, L, key, probe, dummy);
+    const uint64_t hash = hashes != nullptr && probe ? __ldcs(hashes + i) : static_cast<uint64_t>(key);
+    const int32_t my_slot = locate_step<KIND, false>(t, L, key, hash, probe, dummy);
     if (my_slot >= 0)
     {
         res = cas_key<KIND>(t, static_cast<uint32_t>(my_slot), key, C::tomb_key) == key ? 1 : 0;
@@ -866,7 +803,7 @@ erase_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, boo
 template <int KIND, bool WANT_VALUES>
 SG_D void
 find_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool valid, void* out_vals,
-          uint8_t* out_found)
+          uint8_t* out_found, const uint64_t* hashes = nullptr)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
@@ -877,7 +814,8 @@ find_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool
     bool found = special ? special_find<KIND>(t, key, val) : false;
     const bool probe = valid && !special;
     V pv{};
-    const int32_t slot = locate_step<KIND, WANT_VALUES>(t, L, key, probe, pv);
+    const uint64_t hash = hashes != nullptr && probe ? __ldcs(hashes + i) : static_cast<uint64_t>(key);
+    const int32_t slot = locate_step<KIND, WANT_VALUES>(t, L, key, hash, probe, pv);
     if (probe)
     {
         found = slot >= 0;

@@ -82,7 +82,7 @@ k_init(dview t)
 // Bulk insert: src/stdgpu/impl/unordered_base_detail.cuh:996-1017 (insert_value :470-495).
 template <int KIND, bool AOS>
 __global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
-k_insert(dview t, const void* in0, const void* in1, int64_t n, uint8_t* out_flags)
+k_insert(dview t, const void* in0, const void* in1, int64_t n, uint8_t* out_flags, const uint64_t* hashes)
 {
     const tile_lanes L;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -91,7 +91,7 @@ k_insert(dview t, const void* in0, const void* in1, int64_t n, uint8_t* out_flag
     for (int64_t base = warp * 32; base < n; base += nwarps * 32)
     {
         const int64_t i = base + L.lane;
-        insert_step<KIND, AOS>(t, L, in0, in1, i, i < n, out_flags, c);
+        insert_step<KIND, AOS>(t, L, in0, in1, i, i < n, out_flags, c, hashes);
     }
     if (c.retry != 0)
     {
@@ -381,7 +381,7 @@ k_insert_ordered(dview t, const void* in0, int64_t n, unsigned long long* next_c
 // Bulk erase: src/stdgpu/impl/unordered_base_detail.cuh:1045-1066 (erase_from_key :497-522).
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
-k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags)
+k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags, const uint64_t* hashes)
 {
     const tile_lanes L;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -390,7 +390,7 @@ k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags)
     for (int64_t base = warp * 32; base < n; base += nwarps * 32)
     {
         const int64_t i = base + L.lane;
-        erase_step<KIND>(t, L, keys, i, i < n, out_flags, c);
+        erase_step<KIND>(t, L, keys, i, i < n, out_flags, c, hashes);
     }
     // size -= erased; tombstones += erased probed keys
     unsigned long long v[2] = { 0ull - c.done, c.done - c.oob };
@@ -401,7 +401,7 @@ k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags)
 // Bulk find / contains (device-only find/contains in the reference, :619-706).
 template <int KIND, bool WANT_VALUES>
 __global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
-k_find(dview t, const void* keys, int64_t n, void* out_vals, uint8_t* out_found)
+k_find(dview t, const void* keys, int64_t n, void* out_vals, uint8_t* out_found, const uint64_t* hashes)
 {
     const tile_lanes L;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
@@ -409,7 +409,7 @@ k_find(dview t, const void* keys, int64_t n, void* out_vals, uint8_t* out_found)
     for (int64_t base = warp * 32; base < n; base += nwarps * 32)
     {
         const int64_t i = base + L.lane;
-        find_step<KIND, WANT_VALUES>(t, L, keys, i, i < n, out_vals, out_found);
+        find_step<KIND, WANT_VALUES>(t, L, keys, i, i < n, out_vals, out_found, hashes);
     }
 }
 
@@ -417,7 +417,7 @@ k_find(dview t, const void* keys, int64_t n, void* out_vals, uint8_t* out_found)
 // the erased marker, and the stored-key count plus out-of-band keys equals size().
 template <int KIND>
 __global__ void __launch_bounds__(kThreads)
-k_valid(dview t, sg_unordered_view v, unsigned long long* bad)
+k_valid(dview t, sg_unordered_view v, unsigned long long* bad, bool check_reach)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
@@ -439,7 +439,7 @@ k_valid(dview t, sg_unordered_view v, unsigned long long* bad)
             continue;
         }
         ++live;
-        wrong += (ref.find_slot(k) != s);
+        wrong += check_reach && (ref.find_slot(k) != s);
     }
     unsigned long long vv[2] = { live, wrong };
     unsigned long long* const dst[2] = { &t.hdr->count, bad };
@@ -672,6 +672,7 @@ struct sg_unordered
     unsigned long long* host_hdr; // pinned mirror for synchronous reads
     int device;
     int32_t insert_mode;        // 0 automatic, 1 always direct, 2 partitioned whenever allowed
+    bool custom_hash;           // buckets come from caller-supplied hashes (the *_hashed entry points)
     char* part_scratch;         // partitioned bulk insert: value_type elements, then 2 x kPartMax counters
     int64_t part_scratch_bytes;
 };
@@ -855,9 +856,10 @@ struct do_insert
     }
 
     static sg_status
-    run(sg_unordered* t, const void* in0, const void* in1, bool aos, int64_t n, uint8_t* flags, cudaStream_t s)
+    run(sg_unordered* t, const void* in0, const void* in1, bool aos, int64_t n, uint8_t* flags, cudaStream_t s,
+        const uint64_t* hashes = nullptr)
     {
-        if (use_partitioned_insert(t, n, flags))
+        if (hashes == nullptr && use_partitioned_insert(t, n, flags))
         {
             const sg_status st = aos ? partition<true>(t, in0, in1, n, s) : partition<false>(t, in0, in1, n, s);
             if (st != SG_OK)
@@ -877,12 +879,14 @@ struct do_insert
         if (aos)
         {
             static const int max_grid = persistent_grid(k_insert<KIND, true>, kThreads);
-            k_insert<KIND, true><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), in0, in1, n, flags);
+            k_insert<KIND, true><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), in0, in1, n, flags,
+                                                                                     hashes);
         }
         else
         {
             static const int max_grid = persistent_grid(k_insert<KIND, false>, kThreads);
-            k_insert<KIND, false><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), in0, in1, n, flags);
+            k_insert<KIND, false><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), in0, in1, n,
+                                                                                      flags, hashes);
         }
         SG_LAUNCH_CHECK();
         return SG_OK;
@@ -893,10 +897,10 @@ template <int KIND>
 struct do_erase
 {
     static sg_status
-    run(sg_unordered* t, const void* keys, int64_t n, uint8_t* flags, cudaStream_t s)
+    run(sg_unordered* t, const void* keys, int64_t n, uint8_t* flags, cudaStream_t s, const uint64_t* hashes = nullptr)
     {
         static const int max_grid = persistent_grid(k_erase<KIND>, kThreads);
-        k_erase<KIND><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n, flags);
+        k_erase<KIND><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n, flags, hashes);
         SG_LAUNCH_CHECK();
         return SG_OK;
     }
@@ -906,17 +910,20 @@ template <int KIND>
 struct do_find
 {
     static sg_status
-    run(sg_unordered* t, const void* keys, int64_t n, void* vals, uint8_t* found, cudaStream_t s)
+    run(sg_unordered* t, const void* keys, int64_t n, void* vals, uint8_t* found, cudaStream_t s,
+        const uint64_t* hashes = nullptr)
     {
         if (vals != nullptr)
         {
             static const int max_grid = persistent_grid(k_find<KIND, true>, kThreads);
-            k_find<KIND, true><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n, vals, found);
+            k_find<KIND, true><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n, vals, found,
+                                                                                   hashes);
         }
         else
         {
             static const int max_grid = persistent_grid(k_find<KIND, false>, kThreads);
-            k_find<KIND, false><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n, vals, found);
+            k_find<KIND, false><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n, vals,
+                                                                                    found, hashes);
         }
         SG_LAUNCH_CHECK();
         return SG_OK;
@@ -931,7 +938,8 @@ struct do_valid
     {
         static const int max_grid = persistent_grid(k_valid<KIND>, kThreads);
         const int64_t nslots = t->num_groups * (kGroupBytes / t->slot_bytes);
-        k_valid<KIND><<<grid_for(nslots, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), public_view(t), bad);
+        k_valid<KIND><<<grid_for(nslots, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), public_view(t), bad,
+                                                                                !t->custom_hash);
         SG_LAUNCH_CHECK();
         return SG_OK;
     }
@@ -1106,7 +1114,7 @@ sg_unordered_destroy(sg_unordered* t)
 sg_status
 sg_unordered_insert(sg_unordered* t, const void* values, int64_t n, uint8_t* out_inserted, void* stream)
 {
-    if (t == nullptr || n < 0 || (n > 0 && values == nullptr))
+    if (t == nullptr || t->custom_hash || n < 0 || (n > 0 && values == nullptr))
     {
         return SG_ERR_BAD_ARG;
     }
@@ -1121,7 +1129,7 @@ sg_status
 sg_unordered_insert_kv(sg_unordered* t, const void* keys, const void* mapped, int64_t n, uint8_t* out_inserted,
                        void* stream)
 {
-    if (t == nullptr || n < 0 || (n > 0 && keys == nullptr))
+    if (t == nullptr || t->custom_hash || n < 0 || (n > 0 && keys == nullptr))
     {
         return SG_ERR_BAD_ARG;
     }
@@ -1130,6 +1138,78 @@ sg_unordered_insert_kv(sg_unordered* t, const void* keys, const void* mapped, in
         return SG_OK;
     }
     return dispatch<do_insert>(t->kind, t, keys, mapped, false, n, out_inserted, as_stream(stream));
+}
+
+sg_status
+sg_unordered_create_hashed(int32_t kind, int64_t capacity, void* stream, sg_unordered** out)
+{
+    const sg_status st = sg_unordered_create(kind, capacity, stream, out);
+    if (st == SG_OK)
+    {
+        (*out)->custom_hash = true;
+    }
+    return st;
+}
+
+sg_status
+sg_unordered_insert_hashed(sg_unordered* t, const void* keys, const void* mapped, const uint64_t* hashes, int64_t n,
+                           uint8_t* out_inserted, void* stream)
+{
+    if (t == nullptr || !t->custom_hash || n < 0 || (n > 0 && (keys == nullptr || hashes == nullptr)))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    return dispatch<do_insert>(t->kind, t, keys, mapped, false, n, out_inserted, as_stream(stream), hashes);
+}
+
+sg_status
+sg_unordered_erase_hashed(sg_unordered* t, const void* keys, const uint64_t* hashes, int64_t n, uint8_t* out_erased,
+                          void* stream)
+{
+    if (t == nullptr || !t->custom_hash || n < 0 || (n > 0 && (keys == nullptr || hashes == nullptr)))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    return dispatch<do_erase>(t->kind, t, keys, n, out_erased, as_stream(stream), hashes);
+}
+
+sg_status
+sg_unordered_find_hashed(sg_unordered* t, const void* keys, const uint64_t* hashes, int64_t n, void* out_mapped,
+                         uint8_t* out_found, void* stream)
+{
+    if (t == nullptr || !t->custom_hash || n < 0 || (n > 0 && (keys == nullptr || hashes == nullptr)))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    const bool is_map = t->kind >= SG_MAP_U64_U32;
+    return dispatch<do_find>(t->kind, t, keys, n, is_map ? out_mapped : nullptr, out_found, as_stream(stream), hashes);
+}
+
+sg_status
+sg_unordered_contains_hashed(sg_unordered* t, const void* keys, const uint64_t* hashes, int64_t n,
+                             uint8_t* out_flags, void* stream)
+{
+    if (t == nullptr || !t->custom_hash || n < 0 || (n > 0 && (keys == nullptr || hashes == nullptr)))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    return dispatch<do_find>(t->kind, t, keys, n, nullptr, out_flags, as_stream(stream), hashes);
 }
 
 sg_status
@@ -1146,7 +1226,7 @@ sg_unordered_set_insert_mode(sg_unordered* t, int32_t mode)
 sg_status
 sg_unordered_erase(sg_unordered* t, const void* keys, int64_t n, uint8_t* out_erased, void* stream)
 {
-    if (t == nullptr || n < 0 || (n > 0 && keys == nullptr))
+    if (t == nullptr || t->custom_hash || n < 0 || (n > 0 && keys == nullptr))
     {
         return SG_ERR_BAD_ARG;
     }
@@ -1160,7 +1240,7 @@ sg_unordered_erase(sg_unordered* t, const void* keys, int64_t n, uint8_t* out_er
 sg_status
 sg_unordered_find(sg_unordered* t, const void* keys, int64_t n, void* out_mapped, uint8_t* out_found, void* stream)
 {
-    if (t == nullptr || n < 0 || (n > 0 && keys == nullptr))
+    if (t == nullptr || t->custom_hash || n < 0 || (n > 0 && keys == nullptr))
     {
         return SG_ERR_BAD_ARG;
     }
@@ -1175,7 +1255,7 @@ sg_unordered_find(sg_unordered* t, const void* keys, int64_t n, void* out_mapped
 sg_status
 sg_unordered_contains(sg_unordered* t, const void* keys, int64_t n, uint8_t* out_flags, void* stream)
 {
-    if (t == nullptr || n < 0 || (n > 0 && (keys == nullptr || out_flags == nullptr)))
+    if (t == nullptr || t->custom_hash || n < 0 || (n > 0 && (keys == nullptr || out_flags == nullptr)))
     {
         return SG_ERR_BAD_ARG;
     }
@@ -1322,7 +1402,7 @@ sg_unordered_range_copy(sg_unordered* t, void* out_keys, void* out_mapped, void*
 sg_status
 sg_unordered_bucket(const sg_unordered* t, const void* key, int64_t* out_bucket)
 {
-    if (t == nullptr || key == nullptr || out_bucket == nullptr)
+    if (t == nullptr || t->custom_hash || key == nullptr || out_bucket == nullptr)
     {
         return SG_ERR_BAD_ARG;
     }
@@ -1336,6 +1416,17 @@ sg_unordered_bucket(const sg_unordered* t, const void* key, int64_t* out_bucket)
         k = *static_cast<const uint64_t*>(key);
     }
     *out_bucket = static_cast<int64_t>(fibonacci_bucket(k, t->bits));
+    return SG_OK;
+}
+
+sg_status
+sg_unordered_bucket_of_hash(const sg_unordered* t, uint64_t hash, int64_t* out_bucket)
+{
+    if (t == nullptr || out_bucket == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    *out_bucket = static_cast<int64_t>(fibonacci_bucket(hash, t->bits));
     return SG_OK;
 }
 

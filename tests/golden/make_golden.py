@@ -8,6 +8,7 @@ thread so that every per-element outcome is deterministic:
 * geometry.npz       createDeviceObject(capacity) -> bucket_count, max_size
 * buckets.npz        bucket(key) for several table sizes and key patterns
 * table_<kind>.npz   insert (with duplicates) / find / erase / final contents per container kind
+* table_vec3i16_<kind>.npz  the same for a 3 x int16 key type with a user hash (spatial hash), plus bucket()
 * refusal.npz        inserts into tiny tables until refusal (capacity 1..8)
 * vector.npz, deque.npz, bitset.npz
 
@@ -102,6 +103,44 @@ def table_scenario(kind: int, seed: int):
     np.savez_compressed(OUT / f"table_{kind}.npz", **out)
 
 
+def table_vec3i16(kind: int, seed: int):
+    """unordered_set / unordered_map keyed by 3 x int16 with the spatial hash: coordinates in a small cube so that
+    keys repeat and buckets collide."""
+    rng = np.random.default_rng(700 + seed)
+    cap = 6000
+    n = 5000
+    coords = rng.integers(-24, 24, size=(n, 3)).astype(np.int16)
+    keys = np.zeros(n, O.VEC3I16)
+    keys["x"], keys["y"], keys["z"] = coords[:, 0], coords[:, 1], coords[:, 2]
+    vals = None
+    if O.VAL_DTYPE[kind] is not None:
+        vals = (O_mix(O.vec3i16_words(keys)) & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    t = O.RefTable(kind, cap)
+    ins_flags = t.insert(keys, vals, flags=True)
+    size_after_insert = t.size()
+    qc = rng.integers(-30, 30, size=(n, 3)).astype(np.int16)
+    queries = np.zeros(n, O.VEC3I16)
+    queries["x"], queries["y"], queries["z"] = qc[:, 0], qc[:, 1], qc[:, 2]
+    fvals, found = t.find(queries)
+    erase = np.concatenate([keys[rng.integers(0, n, size=n // 2)], queries[: n // 4]])
+    erase_flags = t.erase(erase, flags=True)
+    size_after_erase = t.size()
+    buckets = np.array([t.bucket_of(k) for k in keys[:512]], np.int64)
+    rk, rv = t.range()
+    words = O.vec3i16_words(rk)
+    order = np.argsort(words)
+    out = dict(capacity=np.array(cap), keys=keys, insert_flags=ins_flags, size_after_insert=np.array(size_after_insert),
+               queries=queries, found=found, erase=erase, erase_flags=erase_flags,
+               size_after_erase=np.array(size_after_erase), valid=np.array(t.valid()), final_keys=rk[order],
+               buckets=buckets, bucket_count=np.array(t.geometry()[0]))
+    if vals is not None:
+        out["values"] = vals
+        out["found_values"] = np.where(found == 1, fvals, 0).astype(np.uint32)
+        out["final_values"] = rv[order]
+    t.close()
+    np.savez_compressed(OUT / f"table_vec3i16_{kind}.npz", **out)
+
+
 def O_mix(x: np.ndarray) -> np.ndarray:
     z = x.copy()
     with np.errstate(over="ignore"):
@@ -169,6 +208,8 @@ def main():
     buckets()
     for kind in range(6):
         table_scenario(kind, kind)
+    for kind in (O.SET_VEC3I16, O.MAP_VEC3I16_U32):
+        table_vec3i16(kind, kind)
     refusal()
     vector()
     deque()

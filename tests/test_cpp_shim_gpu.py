@@ -11,14 +11,15 @@ from stdgpu_gb300 import build as B
 
 ROOT = Path(__file__).resolve().parents[1]
 SRC = ROOT / "tests" / "cpp" / "shim_test.cu"
+CUSTOM = ROOT / "tests" / "cpp" / "custom_key_test.cu"
 OUT = ROOT / "tests" / "cpp" / "_build"
 
 
-def _compile(flags=()):
+def _compile(flags=(), src=SRC):
     OUT.mkdir(exist_ok=True)
     lib = stdgpu_gb300.library_path()
-    exe = OUT / "shim_test"
-    cmd = [B.nvcc(), *B.ARCH_FLAGS, "-std=c++17", "-O2", *flags, "-I", str(ROOT / "include"), str(SRC),
+    exe = OUT / src.stem
+    cmd = [B.nvcc(), *B.ARCH_FLAGS, "-std=c++17", "-O2", *flags, "-I", str(ROOT / "include"), str(src),
            "-L", str(lib.parent), "-lstdgpu_gb300", f"-Xlinker=-rpath={lib.parent}", "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
@@ -35,6 +36,23 @@ def test_shim_compiles_for_sm103a():
 def test_shim_reference_scenarios_on_gpu():
     stdgpu_gb300.load()
     exe = _compile()
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "ALL PASS" in r.stdout
+
+
+def test_custom_key_program_compiles_for_sm103a():
+    stdgpu_gb300.load()
+    _compile(src=CUSTOM)
+
+
+@pytest.mark.gpu
+def test_custom_key_types_with_user_hash_on_gpu():
+    """3 x int16 keys with the spatial hash: bulk and device calls, heterogeneous lookup, the README's
+    neighbour-update kernel, all against std::unordered_set / std::unordered_map."""
+    stdgpu_gb300.load()
+    exe = _compile(src=CUSTOM)
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr

@@ -60,6 +60,46 @@ def test_table_scenario_matches_reference(golden, kind):
         assert np.array_equal(rv[o], g["final_values"])
 
 
+@pytest.mark.parametrize("kind", [O.SET_VEC3I16, O.MAP_VEC3I16_U32])
+def test_custom_key_hash_scenario_matches_reference(golden, kind):
+    """3 x int16 keys with a user hash: the port, fed key words and per-key hashes, answers what the reference's
+    unordered_set / unordered_map<Key, T, Hash> answered, element by element, and gives the same bucket()."""
+    g = golden(f"table_vec3i16_{kind}.npz")
+    wk = O.WORD_KIND[kind]
+    t = O.PortTable(wk, int(g["capacity"]))
+    keys = g["keys"]
+    vals = g["values"] if "values" in g else None
+    flags = t.insert(O.vec3i16_words(keys), vals, flags=True, hashes=O.spatial_hash(keys))
+    assert np.array_equal(flags, g["insert_flags"])
+    assert t.size() == int(g["size_after_insert"])
+    q = g["queries"]
+    fv, found = t.find(O.vec3i16_words(q), hashes=O.spatial_hash(q))
+    assert np.array_equal(found, g["found"])
+    if vals is not None:
+        assert np.array_equal(np.where(found == 1, fv, 0).astype(np.uint32), g["found_values"])
+    e = g["erase"]
+    ef = t.erase(O.vec3i16_words(e), flags=True, hashes=O.spatial_hash(e))
+    assert np.array_equal(ef, g["erase_flags"])
+    assert t.size() == int(g["size_after_erase"])
+    assert t.valid() == bool(g["valid"])
+    rk, rv = t.range()
+    o = np.argsort(rk)
+    assert np.array_equal(rk[o], O.vec3i16_words(g["final_keys"]))
+    if vals is not None:
+        assert np.array_equal(rv[o], g["final_values"])
+    bc = int(g["bucket_count"])
+    got = np.array([O.port_fibonacci_hashing(int(h), bc) for h in O.spatial_hash(keys[:512])])
+    assert np.array_equal(got, g["buckets"])
+
+
+def test_vec3i16_words_round_trip():
+    k = np.zeros(4, O.VEC3I16)
+    k["x"], k["y"], k["z"] = [-1, 0, 32767, -32768], [2, -3, 0, 1], [0, 0, -1, 5]
+    w = O.vec3i16_words(k)
+    assert w[0] == 0x0000_0000_0002_FFFF
+    assert np.array_equal(O.words_vec3i16(w), k)
+
+
 def test_refusal_matches_reference(golden):
     g = golden("refusal.npz")
     for cap in [1, 2, 3, 4, 5, 8]:
