@@ -130,6 +130,21 @@ SG_API sg_status sg_unordered_contains_hashed(sg_unordered* table, const void* k
 /* bucket() of a key whose hash is `hash`: fibonacci hashing onto bucket_count (unordered_base_detail.cuh:547-564). */
 SG_API sg_status sg_unordered_bucket_of_hash(const sg_unordered* table, uint64_t hash, int64_t* out_bucket);
 
+/* 1 when the table was created by sg_unordered_create_hashed. */
+SG_API sg_status sg_unordered_is_hashed(const sg_unordered* table, int32_t* out);
+
+/* ---- Rehash and snapshots (no counterpart in the reference: its capacity is fixed at creation,
+ * src/stdgpu/unordered_map.cuh:61, and it has no on-disk form).
+ * rehash: moves every element into storage built for new_capacity (the geometry of
+ * createDeviceObject(new_capacity)); the handle stays valid, views taken before it do not.  Synchronises.
+ * SG_ERR_FULL (table unchanged) when the elements do not fit; SG_ERR_BAD_ARG on a custom-hash table.
+ * save / load: a binary file holding the creation capacity, the geometry and the raw image of the table
+ * (device header, every probe group), so a loaded table is bit for bit the saved one; load checks the
+ * header and the geometry before it allocates anything.  Both synchronise. */
+SG_API sg_status sg_unordered_rehash(sg_unordered* table, int64_t new_capacity, void* stream);
+SG_API sg_status sg_unordered_save(sg_unordered* table, const char* path, void* stream);
+SG_API sg_status sg_unordered_load(const char* path, void* stream, sg_unordered** out);
+
 /* Bulk-insert strategy (no counterpart in the reference).  SG_INSERT_AUTO: when a call without per-element
  * flags brings at least 2^22 keys and one key per two probe groups of a table of 256 MB or more, the keys
  * are first partitioned by home-group range into a scratch array (n x sizeof(value_type), kept by the

@@ -85,6 +85,10 @@ SIGNATURES = {
     "sg_unordered_find_hashed": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "sg_unordered_contains_hashed": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_unordered_bucket_of_hash": (c_int32, [c_void_p, c_uint64, POINTER(c_int64)]),
+    "sg_unordered_is_hashed": (c_int32, [c_void_p, POINTER(c_int32)]),
+    "sg_unordered_rehash": (c_int32, [c_void_p, c_int64, c_void_p]),
+    "sg_unordered_save": (c_int32, [c_void_p, c_char_p, c_void_p]),
+    "sg_unordered_load": (c_int32, [c_char_p, c_void_p, POINTER(c_void_p)]),
     "sg_unordered_find": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "sg_unordered_contains": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_unordered_size": (c_int32, [c_void_p, c_void_p, POINTER(c_int64)]),

@@ -285,6 +285,29 @@ class unordered_base:
     def clear(self, stream=None) -> None:
         N.check(N.load().sg_unordered_clear(self._h, _stream(stream)), "clear")
 
+    def rehash(self, new_capacity: int, stream=None) -> None:
+        """Move every element into storage for new_capacity (sg_unordered_rehash); synchronises."""
+        N.check(N.load().sg_unordered_rehash(self._h, int(new_capacity), _stream(stream)), "rehash")
+        g = N.sg_geometry()
+        N.check(N.load().sg_unordered_geometry(self._h, byref(g)), "geometry")
+        self._geom = g
+
+    def save(self, path, stream=None) -> None:
+        """Write a snapshot file (sg_unordered_save)."""
+        N.check(N.load().sg_unordered_save(self._h, str(path).encode(), _stream(stream)), "save")
+
+    @classmethod
+    def load(cls, path, stream=None) -> "unordered_base":
+        """Recreate a table from a snapshot file (sg_unordered_load)."""
+        lib = N.load()
+        h = c_void_p()
+        N.check(lib.sg_unordered_load(str(path).encode(), _stream(stream), byref(h)), "load")
+        v = N.sg_unordered_view()
+        N.check(lib.sg_unordered_view_of(h, byref(v)), "load")
+        hashed = c_int32()
+        N.check(lib.sg_unordered_is_hashed(h, byref(hashed)), "load")
+        return cls(h.value, v.kind, bool(hashed.value))
+
     INSERT_MODES = {"auto": 0, "direct": 1, "partitioned": 2}
 
     def set_insert_mode(self, mode: str) -> None:

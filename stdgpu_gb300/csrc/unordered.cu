@@ -1213,6 +1213,83 @@ sg_unordered_contains_hashed(sg_unordered* t, const void* keys, const uint64_t* 
 }
 
 sg_status
+sg_unordered_is_hashed(const sg_unordered* t, int32_t* out)
+{
+    if (t == nullptr || out == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    *out = t->custom_hash ? 1 : 0;
+    return SG_OK;
+}
+
+sg_status
+sg_unordered_rehash(sg_unordered* t, int64_t new_capacity, void* stream)
+{
+    if (t == nullptr || t->custom_hash)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    sg_geometry g{};
+    sg_status st = sg_unordered_geometry_for(t->kind, new_capacity, &g);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    cudaStream_t s = as_stream(stream);
+    st = read_header(t, s);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    const int64_t n = static_cast<int64_t>(host_header(t).size);
+    const int kb = (t->kind == SG_SET_U32 || t->kind == SG_MAP_U32_U32 || t->kind == SG_MAP_U32_U64) ? 4 : 8;
+    const int mb = t->kind == SG_MAP_U64_U32 || t->kind == SG_MAP_U32_U32 ? 4
+                   : (t->kind == SG_MAP_U64_U64 || t->kind == SG_MAP_U32_U64) ? 8
+                                                                             : 0;
+    char* buf = nullptr;
+    const int64_t cap = n + 2;
+    const int64_t kbytes = ((cap * kb + 255) / 256) * 256;
+    if (cudaMalloc(&buf, static_cast<size_t>(kbytes + cap * (mb > 0 ? mb : 1))) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return SG_ERR_OOM;
+    }
+    sg_unordered* fresh = nullptr;
+    int64_t copied = 0;
+    st = sg_unordered_range_copy(t, buf, mb > 0 ? buf + kbytes : nullptr, stream, &copied);
+    if (st == SG_OK)
+    {
+        st = sg_unordered_create(t->kind, new_capacity, stream, &fresh);
+    }
+    if (st == SG_OK && copied > 0)
+    {
+        st = dispatch<do_insert>(fresh->kind, fresh, buf, mb > 0 ? buf + kbytes : nullptr, false, copied, nullptr, s);
+    }
+    int64_t refused = 0;
+    if (st == SG_OK)
+    {
+        st = sg_unordered_status(fresh, stream, &refused, nullptr);
+    }
+    cudaFree(buf);
+    if (st != SG_OK)
+    {
+        if (fresh != nullptr)
+        {
+            sg_unordered_destroy(fresh);
+        }
+        return st == SG_ERR_FULL ? SG_ERR_FULL : st;
+    }
+    // the table keeps its handle and its settings; the old storage leaves with `fresh`
+    const int32_t mode = t->insert_mode;
+    sg_unordered tmp = *t;
+    *t = *fresh;
+    *fresh = tmp;
+    t->insert_mode = mode;
+    return sg_unordered_destroy(fresh);
+}
+
+sg_status
 sg_unordered_set_insert_mode(sg_unordered* t, int32_t mode)
 {
     if (t == nullptr || mode < 0 || mode > 2)
