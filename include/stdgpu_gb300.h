@@ -369,6 +369,15 @@ SG_API sg_status sg_vector_push_back(sg_vector* vec, const void* values, const u
 SG_API sg_status sg_vector_size(sg_vector* vec, void* stream, int64_t* out_size);
 /* clear() */
 SG_API sg_status sg_vector_clear(sg_vector* vec, void* stream);
+/* pop_back() n times (src/stdgpu/impl/vector_detail.cuh:240-299): element i takes the i-th element from the
+ * back; out_ok[i] = 0 once the vector is empty.  Outputs nullable. */
+SG_API sg_status sg_vector_pop_back(sg_vector* vec, int64_t n, void* out_values, uint8_t* out_ok, void* stream);
+/* insert(device_end(), begin, end) (vector_detail.cuh:372-410): appends n device values; SG_ERR_FULL and
+ * nothing inserted when they do not fit.  Synchronises. */
+SG_API sg_status sg_vector_insert(sg_vector* vec, const void* values, int64_t n, void* stream);
+/* erase(device_end() - n, device_end()) (vector_detail.cuh:418-450): drops the last n elements;
+ * SG_ERR_BAD_ARG and nothing erased when n > size().  Synchronises. */
+SG_API sg_status sg_vector_erase(sg_vector* vec, int64_t n, void* stream);
 SG_API sg_status sg_vector_view_of(const sg_vector* vec, sg_vector_view* out);
 
 /* ---------------- deque<T> (T = 4 or 8 bytes), push_back / pop_front ---------------- */
@@ -379,7 +388,8 @@ typedef struct sg_deque_view
 {
     void* data;
     void* seq;      /* per-slot turn counter of the ring (uint32) */
-    void* counters; /* device {int64 size, uint64 begin, uint64 end, uint32 error, uint32 pad, int64 avail} */
+    void* counters; /* device {int64 size, uint64 begin, uint64 end, uint32 error, uint32 pad, int64 avail,
+                     * uint64 op_t0, int64 op_k}; begin / end are tickets, ticket mod capacity is the slot */
     int64_t capacity;
     int32_t elem_bytes;
     int32_t pad;
@@ -398,6 +408,12 @@ SG_API sg_status sg_deque_size(sg_deque* dq, void* stream, int64_t* out_size);
 /* Copy the stored elements front to back to out (device) and return their count (synchronises). */
 SG_API sg_status sg_deque_copy_out(sg_deque* dq, void* out, void* stream, int64_t* out_n);
 SG_API sg_status sg_deque_clear(sg_deque* dq, void* stream);
+/* push_front() / pop_back() n times (deque_detail.cuh:314-386, :260-312), one kind per launch: element i acts
+ * as the i-th of a sequence of calls (push_front of values[0..n) leaves values[n-1] at the front; pop_back
+ * pops the back element first).  Launches of either kind may follow sg_deque_ops launches on the same stream
+ * in any order.  out_ok / out_popped nullable. */
+SG_API sg_status sg_deque_push_front(sg_deque* dq, const void* values, int64_t n, uint8_t* out_ok, void* stream);
+SG_API sg_status sg_deque_pop_back(sg_deque* dq, int64_t n, void* out_popped, uint8_t* out_ok, void* stream);
 SG_API sg_status sg_deque_view_of(const sg_deque* dq, sg_deque_view* out);
 
 /* ---------------- bitset<unsigned int>::count ---------------- */

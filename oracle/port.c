@@ -478,11 +478,40 @@ int64_t port_deque_ops(int64_t capacity, const uint64_t* init, int64_t n_init, c
     int64_t size = 0, begin = 0, end = 0;
     for (int64_t j = 0; j < n_init + n; ++j)
     {
-        int push = j < n_init ? 1 : is_push[j - n_init];
+        /* op: 0 pop_front, 1 push_back, 2 push_front (:314-386), 3 pop_back (:260-312) */
+        int op = j < n_init ? 1 : is_push[j - n_init];
+        int push = op == 1 || op == 2;
         uint64_t v = j < n_init ? init[j] : values[j - n_init];
         uint8_t r = 0;
         uint64_t pv = 0;
-        if (push)
+        if (op == 2)
+        {
+            if (size != capacity)
+            {
+                int64_t cur = size++;
+                if (cur < capacity)
+                {
+                    /* begin.fetch_dec_mod(capacity), then the position before the old begin */
+                    begin = (begin == 0) ? capacity - 1 : begin - 1;
+                    data[begin] = v;
+                    r = 1;
+                }
+            }
+        }
+        else if (op == 3)
+        {
+            if (size != 0)
+            {
+                int64_t cur = size--;
+                if (cur > 0)
+                {
+                    end = (end == 0) ? capacity - 1 : end - 1;
+                    pv = data[end];
+                    r = 1;
+                }
+            }
+        }
+        else if (push)
         {
             if (size != capacity)
             {

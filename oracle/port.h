@@ -64,7 +64,8 @@ int64_t port_range(const port_table* t, uint64_t* keys, uint64_t* values);
  * returns size() afterwards, contents to out (storage order). */
 int64_t port_vector_push_back(int64_t capacity, const uint64_t* values, const uint8_t* pred, int64_t n,
                               uint8_t* pushed, uint64_t* out);
-/* deque<T>: n_init push_backs then ops in index order (deque_detail.cuh:202-258, 388-446) */
+/* deque<T>: n_init push_backs then ops in index order; op[i]: 0 pop_front (deque_detail.cuh:388-446),
+ * 1 push_back (:202-258), 2 push_front (:314-386), 3 pop_back (:260-312) */
 int64_t port_deque_ops(int64_t capacity, const uint64_t* init, int64_t n_init, const uint8_t* is_push,
                        const uint64_t* values, int64_t n, uint64_t* popped, uint8_t* ok, uint64_t* remaining);
 /* bitset<unsigned int>::count over nbits bits (bitset_detail.cuh:130-160, 388-404) */

@@ -377,16 +377,17 @@ struct deque_op_functor
     std::uint64_t* popped;
     std::uint8_t* ok;
 
+    // is_push[i]: 0 pop_front, 1 push_back, 2 push_front, 3 pop_back
     void
     operator()(const stdgpu::index_t i)
     {
-        if (is_push[i] != 0)
+        if (is_push[i] == 1 || is_push[i] == 2)
         {
-            ok[i] = d.push_back(values[i]) ? 1 : 0;
+            ok[i] = (is_push[i] == 1 ? d.push_back(values[i]) : d.push_front(values[i])) ? 1 : 0;
         }
         else
         {
-            stdgpu::pair<std::uint64_t, bool> r = d.pop_front();
+            stdgpu::pair<std::uint64_t, bool> r = is_push[i] == 0 ? d.pop_front() : d.pop_back();
             ok[i] = r.second ? 1 : 0;
             popped[i] = r.second ? r.first : 0;
         }

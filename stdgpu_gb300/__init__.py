@@ -12,6 +12,8 @@ from .containers import (  # noqa: F401
     deque,
     geometry_for,
     kernel_launch_count,
+    queue,
+    stack,
     stager,
     table_batch,
     unordered_base,

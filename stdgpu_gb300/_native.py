@@ -133,6 +133,11 @@ SIGNATURES = {
     "sg_server_table_size": (c_int32, [c_void_p, c_int32, POINTER(c_int64)]),
     "sg_server_table_view": (c_int32, [c_void_p, c_int32, POINTER(sg_unordered_view)]),
     "sg_vector_create": (c_int32, [c_int32, c_int64, POINTER(c_void_p)]),
+    "sg_vector_pop_back": (c_int32, [c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
+    "sg_vector_insert": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),
+    "sg_vector_erase": (c_int32, [c_void_p, c_int64, c_void_p]),
+    "sg_deque_push_front": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
+    "sg_deque_pop_back": (c_int32, [c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "sg_vector_destroy": (c_int32, [c_void_p]),
     "sg_vector_push_back": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_vector_size": (c_int32, [c_void_p, c_void_p, POINTER(c_int64)]),

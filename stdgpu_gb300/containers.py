@@ -515,6 +515,22 @@ class vector:
     def clear(self, stream=None) -> None:
         N.check(N.load().sg_vector_clear(self._h, _stream(stream)), "vector::clear")
 
+    def pop_back(self, n: int, stream=None) -> tuple[torch.Tensor, torch.Tensor]:
+        """pop_back() n times; returns (values, ok): element i is the i-th from the back."""
+        vals = torch.zeros(n, dtype=_INT_DTYPE[self.elem_bytes], device="cuda")
+        ok = torch.zeros(n, dtype=torch.uint8, device="cuda")
+        N.check(N.load().sg_vector_pop_back(self._h, int(n), _ptr(vals), _ptr(ok), _stream(stream)), "pop_back")
+        return vals, ok
+
+    def insert(self, values: torch.Tensor, stream=None) -> None:
+        """insert(device_end(), begin, end): append a range (refused whole when it does not fit)."""
+        values = _as_bits(values, self.elem_bytes, "values")
+        N.check(N.load().sg_vector_insert(self._h, _ptr(values), values.numel(), _stream(stream)), "vector::insert")
+
+    def erase(self, n: int, stream=None) -> None:
+        """erase(device_end() - n, device_end())."""
+        N.check(N.load().sg_vector_erase(self._h, int(n), _stream(stream)), "vector::erase")
+
     def data(self) -> torch.Tensor:
         v = N.sg_vector_view()
         N.check(N.load().sg_vector_view_of(self._h, byref(v)), "vector::data")
@@ -565,6 +581,83 @@ class deque:
 
     def clear(self, stream=None) -> None:
         N.check(N.load().sg_deque_clear(self._h, _stream(stream)), "deque::clear")
+
+    def push_back(self, values: torch.Tensor, stream=None) -> torch.Tensor:
+        values = _as_bits(values, self.elem_bytes, "values")
+        return self.ops(None, values, stream=stream)[1]
+
+    def pop_front(self, n: int, stream=None) -> tuple[torch.Tensor, torch.Tensor]:
+        return self.ops(torch.zeros(n, dtype=torch.uint8, device="cuda"),
+                        torch.zeros(n, dtype=_INT_DTYPE[self.elem_bytes], device="cuda"), stream=stream)
+
+    def push_front(self, values: torch.Tensor, stream=None) -> torch.Tensor:
+        """push_front() of each value in order (the last one ends at the front); returns ok flags."""
+        values = _as_bits(values, self.elem_bytes, "values")
+        ok = torch.zeros(values.numel(), dtype=torch.uint8, device=values.device)
+        N.check(N.load().sg_deque_push_front(self._h, _ptr(values), values.numel(), _ptr(ok), _stream(stream)),
+                "deque::push_front")
+        return ok
+
+    def pop_back(self, n: int, stream=None) -> tuple[torch.Tensor, torch.Tensor]:
+        """pop_back() n times (the back element first); returns (values, ok)."""
+        vals = torch.zeros(n, dtype=_INT_DTYPE[self.elem_bytes], device="cuda")
+        ok = torch.zeros(n, dtype=torch.uint8, device="cuda")
+        N.check(N.load().sg_deque_pop_back(self._h, int(n), _ptr(vals), _ptr(ok), _stream(stream)), "deque::pop_back")
+        return vals, ok
+
+
+class queue:
+    """stdgpu::queue<T> (src/stdgpu/queue.cuh): push = deque::push_back, pop = deque::pop_front."""
+
+    def __init__(self, d: deque):
+        self.c = d
+
+    @classmethod
+    def createDeviceObject(cls, capacity: int, elem_bytes: int = 8) -> "queue":
+        return cls(deque.createDeviceObject(capacity, elem_bytes))
+
+    @staticmethod
+    def destroyDeviceObject(q: "queue") -> None:
+        deque.destroyDeviceObject(q.c)
+
+    def push(self, values: torch.Tensor, stream=None) -> torch.Tensor:
+        return self.c.push_back(values, stream)
+
+    def pop(self, n: int, stream=None) -> tuple[torch.Tensor, torch.Tensor]:
+        return self.c.pop_front(n, stream)
+
+    def size(self, stream=None) -> int:
+        return self.c.size(stream)
+
+    def empty(self, stream=None) -> bool:
+        return self.size(stream) == 0
+
+
+class stack:
+    """stdgpu::stack<T> (src/stdgpu/stack.cuh): push = deque::push_back, pop = deque::pop_back."""
+
+    def __init__(self, d: deque):
+        self.c = d
+
+    @classmethod
+    def createDeviceObject(cls, capacity: int, elem_bytes: int = 8) -> "stack":
+        return cls(deque.createDeviceObject(capacity, elem_bytes))
+
+    @staticmethod
+    def destroyDeviceObject(s: "stack") -> None:
+        deque.destroyDeviceObject(s.c)
+
+    def push(self, values: torch.Tensor, stream=None) -> torch.Tensor:
+        return self.c.push_back(values, stream)
+
+    def pop(self, n: int, stream=None) -> tuple[torch.Tensor, torch.Tensor]:
+        return self.c.pop_back(n, stream)
+
+    def size(self, stream=None) -> int:
+        return self.c.size(stream)
+
+    def empty(self, stream=None) -> bool:
+        return self.size(stream) == 0
 
 
 def bitset_count(blocks: torch.Tensor, nbits: int, stream=None) -> int:

@@ -51,6 +51,8 @@ struct deque_counters
     unsigned int error;
     unsigned int pad;
     long long avail;
+    unsigned long long op_t0; // push_front / pop_back launches: the end before the launch
+    long long op_k;           // and how many elements it moves
 };
 
 SG_D unsigned
@@ -344,6 +346,99 @@ k_deque_ops(T* data, unsigned* seq, deque_counters* c, int64_t cap, const uint8_
     }
 }
 
+// push_front / pop_back: a launch holds one of them only (the reference runs them concurrently with the
+// other end under per-slot locks, src/stdgpu/impl/deque_detail.cuh:260-386).  Element i of the launch acts
+// as the i-th of a sequence of calls: push_front of values[0..n) leaves values[n-1] at the front, pop_back
+// pops the back element first.  One thread first reserves min(n, room) elements and moves the end
+// (k_deque_reserve_end); then element i < k takes ticket t0 - 1 - i.  Nothing else runs on the deque
+// during the launch, so there are no slot waits; the slot's turn word is left as the FIFO launches that
+// follow expect (a front push leaves the word a push_back of its ticket would leave; a back pop leaves the
+// word that lets push_back reuse its ticket).
+template <bool FRONT_PUSH>
+__global__ void
+k_deque_reserve_end(deque_counters* c, int64_t cap, int64_t n)
+{
+    // push_front needs free capacity (size), pop_back needs elements (avail); both move their end down
+    const long long room = FRONT_PUSH ? cap - c->size : c->avail;
+    const long long k = room <= 0 ? 0 : (room < n ? room : n);
+    unsigned long long* end = FRONT_PUSH ? &c->begin : &c->end;
+    c->op_t0 = *end;
+    c->op_k = k;
+    *end -= static_cast<unsigned long long>(k);
+    c->size += FRONT_PUSH ? k : -k;
+    c->avail += FRONT_PUSH ? k : -k;
+}
+
+template <typename T, bool FRONT_PUSH>
+__global__ void
+k_deque_end_ops(T* data, unsigned* seq, const deque_counters* c, int64_t cap, const T* values, int64_t n,
+                T* out_popped, uint8_t* out_ok)
+{
+    const unsigned long long t0 = c->op_t0;
+    const long long k = c->op_k;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    {
+        const bool ok = i < k;
+        if (ok)
+        {
+            const unsigned long long tk = t0 - 1ull - static_cast<unsigned long long>(i);
+            const int64_t pos = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
+            if constexpr (FRONT_PUSH)
+            {
+                data[pos] = values[i];
+                store_turn(seq + pos, static_cast<unsigned>(tk + 1));
+            }
+            else
+            {
+                const T v = data[pos];
+                store_turn(seq + pos, static_cast<unsigned>(tk));
+                if (out_popped != nullptr)
+                {
+                    out_popped[i] = v;
+                }
+            }
+        }
+        if (out_ok != nullptr)
+        {
+            out_ok[i] = static_cast<uint8_t>(ok);
+        }
+    }
+}
+
+// vector::pop_back for n elements (src/stdgpu/impl/vector_detail.cuh:240-299): element i takes the i-th
+// element from the back.  The size is clamped into [0, capacity] first (a push launch may leave it above),
+// read by every thread, and lowered by one thread afterwards.
+__global__ void
+k_vector_clamp(long long* size, int64_t cap, int64_t minus)
+{
+    long long s = *size;
+    s = s < 0 ? 0 : (s > cap ? cap : s);
+    s -= minus;
+    *size = s < 0 ? 0 : s;
+}
+
+template <typename T>
+__global__ void
+k_vector_pop_back(const T* data, const long long* size, int64_t n, T* out_values, uint8_t* out_ok)
+{
+    const long long sz = *size;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    {
+        const long long pos = sz - 1 - i;
+        const bool ok = pos >= 0;
+        if (ok && out_values != nullptr)
+        {
+            out_values[i] = data[pos];
+        }
+        if (out_ok != nullptr)
+        {
+            out_ok[i] = static_cast<uint8_t>(ok);
+        }
+    }
+}
+
 __global__ void
 k_deque_reset(unsigned* seq, deque_counters* c, int64_t cap)
 {
@@ -354,9 +449,12 @@ k_deque_reset(unsigned* seq, deque_counters* c, int64_t cap)
     }
     if (blockIdx.x == 0 && threadIdx.x == 0)
     {
+        // tickets start at capacity x 2^32: a multiple of the capacity (so ticket mod capacity is the slot)
+        // and of 2^32 (so the 32-bit turn words start at the slot index), far enough from zero for
+        // push_front to move begin down
         c->size = 0;
-        c->begin = 0;
-        c->end = 0;
+        c->begin = static_cast<unsigned long long>(cap) << 32;
+        c->end = static_cast<unsigned long long>(cap) << 32;
         c->error = 0;
         c->avail = 0;
     }
@@ -584,6 +682,43 @@ count_scratch g_count_scratch[64];
 
 } // namespace
 
+namespace
+{
+
+template <bool FRONT_PUSH>
+sg_status
+deque_end_ops(sg_deque* d, const void* values, int64_t n, void* out_popped, uint8_t* out_ok, void* stream)
+{
+    if (d == nullptr || n < 0 || (FRONT_PUSH && n > 0 && values == nullptr))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    cudaStream_t s = as_stream(stream);
+    k_deque_reserve_end<FRONT_PUSH><<<1, 1, 0, s>>>(d->counters, d->capacity, n);
+    SG_LAUNCH_CHECK();
+    const int g = grid_for(n, kCThreads, 4096);
+    if (d->elem_bytes == 4)
+    {
+        k_deque_end_ops<uint32_t, FRONT_PUSH><<<g, kCThreads, 0, s>>>(
+                static_cast<uint32_t*>(d->data), d->seq, d->counters, d->capacity, static_cast<const uint32_t*>(values), n,
+                static_cast<uint32_t*>(out_popped), out_ok);
+    }
+    else
+    {
+        k_deque_end_ops<unsigned long long, FRONT_PUSH><<<g, kCThreads, 0, s>>>(
+                static_cast<unsigned long long*>(d->data), d->seq, d->counters, d->capacity,
+                static_cast<const unsigned long long*>(values), n, static_cast<unsigned long long*>(out_popped), out_ok);
+    }
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+}
+
+} // namespace
+
 extern "C" {
 
 sg_status
@@ -700,6 +835,88 @@ sg_vector_clear(sg_vector* v, void* stream)
 }
 
 sg_status
+sg_vector_pop_back(sg_vector* v, int64_t n, void* out_values, uint8_t* out_ok, void* stream)
+{
+    if (v == nullptr || n < 0)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (n == 0)
+    {
+        return SG_OK;
+    }
+    cudaStream_t s = as_stream(stream);
+    k_vector_clamp<<<1, 1, 0, s>>>(v->size, v->capacity, 0);
+    SG_LAUNCH_CHECK();
+    const int g = grid_for(n, kCThreads, 4096);
+    if (v->elem_bytes == 4)
+    {
+        k_vector_pop_back<uint32_t><<<g, kCThreads, 0, s>>>(static_cast<const uint32_t*>(v->data), v->size, n,
+                                                            static_cast<uint32_t*>(out_values), out_ok);
+    }
+    else
+    {
+        k_vector_pop_back<unsigned long long><<<g, kCThreads, 0, s>>>(
+                static_cast<const unsigned long long*>(v->data), v->size, n, static_cast<unsigned long long*>(out_values),
+                out_ok);
+    }
+    SG_LAUNCH_CHECK();
+    k_vector_clamp<<<1, 1, 0, s>>>(v->size, v->capacity, n);
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+}
+
+sg_status
+sg_vector_insert(sg_vector* v, const void* values, int64_t n, void* stream)
+{
+    if (v == nullptr || n < 0 || (n > 0 && values == nullptr))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    int64_t size = 0;
+    const sg_status st = sg_vector_size(v, stream, &size);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    if (size + n > v->capacity)
+    {
+        return SG_ERR_FULL; // nothing inserted (vector_detail.cuh:372-410 refuses the whole range)
+    }
+    cudaStream_t s = as_stream(stream);
+    SG_CUDA_TRY(cudaMemcpyAsync(static_cast<char*>(v->data) + size * v->elem_bytes, values,
+                                static_cast<size_t>(n) * v->elem_bytes, cudaMemcpyDeviceToDevice, s));
+    *v->host = size + n;
+    SG_CUDA_TRY(cudaMemcpyAsync(v->size, v->host, sizeof(long long), cudaMemcpyHostToDevice, s));
+    SG_CUDA_TRY(cudaStreamSynchronize(s));
+    return SG_OK;
+}
+
+sg_status
+sg_vector_erase(sg_vector* v, int64_t n, void* stream)
+{
+    if (v == nullptr || n < 0)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    int64_t size = 0;
+    const sg_status st = sg_vector_size(v, stream, &size);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    if (n > size)
+    {
+        return SG_ERR_BAD_ARG; // nothing erased (vector_detail.cuh:418-450 refuses a range past the start)
+    }
+    cudaStream_t s = as_stream(stream);
+    *v->host = size - n;
+    SG_CUDA_TRY(cudaMemcpyAsync(v->size, v->host, sizeof(long long), cudaMemcpyHostToDevice, s));
+    SG_CUDA_TRY(cudaStreamSynchronize(s));
+    return SG_OK;
+}
+
+sg_status
 sg_vector_view_of(const sg_vector* v, sg_vector_view* out)
 {
     if (v == nullptr || out == nullptr)
@@ -789,6 +1006,18 @@ sg_deque_clear(sg_deque* d, void* stream)
     k_deque_reset<<<grid_for(d->capacity, kCThreads, mg), kCThreads, 0, s>>>(d->seq, d->counters, d->capacity);
     SG_LAUNCH_CHECK();
     return SG_OK;
+}
+
+sg_status
+sg_deque_push_front(sg_deque* d, const void* values, int64_t n, uint8_t* out_ok, void* stream)
+{
+    return deque_end_ops<true>(d, values, n, nullptr, out_ok, stream);
+}
+
+sg_status
+sg_deque_pop_back(sg_deque* d, int64_t n, void* out_popped, uint8_t* out_ok, void* stream)
+{
+    return deque_end_ops<false>(d, nullptr, n, out_popped, out_ok, stream);
 }
 
 sg_status

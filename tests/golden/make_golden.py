@@ -11,6 +11,7 @@ thread so that every per-element outcome is deterministic:
 * table_vec3i16_<kind>.npz  the same for a 3 x int16 key type with a user hash (spatial hash), plus bucket()
 * refusal.npz        inserts into tiny tables until refusal (capacity 1..8)
 * vector.npz, deque.npz, bitset.npz
+* deque_ends.npz     batches of push_back / pop_front / push_front / pop_back in sequence
 
 Usage (needs the reference tree; see oracle/build_oracle.py):
     python tests/golden/make_golden.py
@@ -192,6 +193,25 @@ def deque():
                         size=np.array(size), popped=popped, ok=ok, remaining=rem)
 
 
+def deque_ends():
+    """Sequences of batches, each of one operation (push_back / pop_front / push_front / pop_back), run in
+    order through the reference deque with one thread."""
+    rng = np.random.default_rng(31)
+    cap = 3000
+    init = rng.integers(0, 2**62, size=1200, dtype=np.uint64)
+    ops, values = [], []
+    for b in range(24):
+        op = int(rng.integers(0, 4))
+        n = int(rng.integers(1, 900))
+        ops.append(np.full(n, op, np.uint8))
+        values.append(rng.integers(0, 2**62, size=n, dtype=np.uint64))
+    ops = np.concatenate(ops)
+    values = np.concatenate(values)
+    size, popped, ok, remaining = O.ref_deque_ops(cap, init, ops, values)
+    np.savez_compressed(OUT / "deque_ends.npz", capacity=np.array(cap), init=init, ops=ops, values=values,
+                        size=np.array(size), popped=popped, ok=ok, remaining=remaining)
+
+
 def bitset():
     rng = np.random.default_rng(8)
     out = {}
@@ -213,6 +233,7 @@ def main():
     refusal()
     vector()
     deque()
+    deque_ends()
     bitset()
     print("fixtures written to", OUT)
 

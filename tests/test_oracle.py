@@ -139,6 +139,14 @@ def test_deque_matches_reference(golden):
     assert np.array_equal(rem, g["remaining"])
 
 
+def test_deque_both_ends_matches_reference(golden):
+    g = golden("deque_ends.npz")
+    n, popped, ok, rem = O.port_deque_ops(int(g["capacity"]), g["init"], g["ops"], g["values"])
+    assert n == int(g["size"])
+    assert np.array_equal(ok, g["ok"]) and np.array_equal(popped, g["popped"])
+    assert np.array_equal(rem, g["remaining"])
+
+
 def test_bitset_matches_reference(golden):
     g = golden("bitset.npz")
     for nbits in [1, 31, 32, 33, 1000, 4096, 100003]:
