@@ -378,6 +378,40 @@ k_insert_ordered(dview t, const void* in0, int64_t n, unsigned long long* next_c
     block_add<3>(v, dst);
 }
 
+// Bulk erase over partitioned keys, chunks taken in order as in k_insert_ordered.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
+k_erase_ordered(dview t, const void* keys, int64_t n, unsigned long long* next_chunk)
+{
+    __shared__ long long s_first;
+    const tile_lanes L;
+    const int warp = threadIdx.x >> 5;
+    step_counts c;
+    while (true)
+    {
+        if (threadIdx.x == 0)
+        {
+            s_first = static_cast<long long>(atomicAdd(next_chunk, 1ull)) * kOrderedChunk;
+        }
+        __syncthreads();
+        const int64_t first = s_first;
+        __syncthreads();
+        if (first >= n)
+        {
+            break;
+        }
+        const int64_t last = first + kOrderedChunk < n ? first + kOrderedChunk : n;
+        for (int64_t base = first + warp * 32; base < last; base += kThreads)
+        {
+            const int64_t i = base + L.lane;
+            erase_step<KIND>(t, L, keys, i, i < last, nullptr, c);
+        }
+    }
+    unsigned long long v[2] = { 0ull - c.done, c.done - c.oob };
+    unsigned long long* const dst[2] = { &t.hdr->size, &t.hdr->tombstones };
+    block_add<2>(v, dst);
+}
+
 // Bulk erase: src/stdgpu/impl/unordered_base_detail.cuh:1045-1066 (erase_from_key :497-522).
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
@@ -820,55 +854,77 @@ ensure_part_scratch(sg_unordered* t, int64_t bytes)
     return SG_OK;
 }
 
+// Partitions n input elements into the table's scratch array as PKIND's value_type elements (a set kind
+// gives bare keys); returns the chunk counter of the ordered kernel that follows, zeroed.
+template <int PKIND, bool AOS>
+sg_status
+partition_into_scratch(sg_unordered* t, const void* in0, const void* in1, int64_t n, cudaStream_t s,
+                       unsigned long long** next_chunk)
+{
+    const int parts = partitions_for(t);
+    int shift = t->bits;
+    for (int p = parts; p > 1; p >>= 1)
+    {
+        --shift;
+    }
+    const int64_t elems = ((n * kind_consts<PKIND>::slot_bytes + 255) / 256) * 256;
+    sg_status st = ensure_part_scratch(t, elems + 2 * kPartMax * static_cast<int64_t>(sizeof(unsigned int)) + 256);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    auto* hist = reinterpret_cast<unsigned int*>(t->part_scratch + elems);
+    unsigned int* cursor = hist + kPartMax;
+    // hist, cursor and the chunk counter of the ordered kernel start at zero
+    SG_CUDA_TRY(cudaMemsetAsync(hist, 0, 2 * kPartMax * sizeof(unsigned int) + 256, s));
+    static const int g_count = persistent_grid(k_part_count<PKIND, AOS>, kThreads);
+    k_part_count<PKIND, AOS><<<grid_for(n, kThreads, g_count), kThreads, 0, s>>>(in0, n, t->bits, shift, parts, hist);
+    SG_LAUNCH_CHECK();
+    k_part_cursors<<<1, kPartMax, 0, s>>>(hist, parts, cursor);
+    SG_LAUNCH_CHECK();
+    static const int g_scatter = persistent_grid(k_part_scatter<PKIND, AOS>, kThreads);
+    k_part_scatter<PKIND, AOS><<<grid_for(n, kThreads * kPartPer, g_scatter), kThreads, 0, s>>>(
+            in0, in1, n, t->bits, shift, parts, cursor, t->part_scratch);
+    SG_LAUNCH_CHECK();
+    *next_chunk = reinterpret_cast<unsigned long long*>(cursor + kPartMax);
+    return SG_OK;
+}
+
+// The set kind holding the key type of KIND (erase partitions bare keys).
+template <int KIND>
+constexpr int keys_kind = sizeof(typename kind_consts<KIND>::K) == 8 ? SG_SET_U64 : SG_SET_U32;
+
+bool
+use_partitioned_erase(const sg_unordered* t, int64_t n, const uint8_t* flags)
+{
+    if (flags != nullptr || n >= (int64_t{ 1 } << 31) || t->insert_mode == 1 || partitions_for(t) == 0)
+    {
+        return false;
+    }
+    if (t->insert_mode == 2)
+    {
+        return true;
+    }
+    const int64_t bytes = (t->num_groups + 1) * kGroupBytes;
+    return n >= (int64_t{ 1 } << 22) && bytes >= (int64_t{ 256 } << 20);
+}
+
 template <int KIND>
 struct do_insert
 {
-    template <bool AOS>
-    static sg_status
-    partition(sg_unordered* t, const void* in0, const void* in1, int64_t n, cudaStream_t s)
-    {
-        const int parts = partitions_for(t);
-        int shift = t->bits;
-        for (int p = parts; p > 1; p >>= 1)
-        {
-            --shift;
-        }
-        const int64_t elems = ((n * t->slot_bytes + 255) / 256) * 256;
-        sg_status st = ensure_part_scratch(t, elems + 2 * kPartMax * static_cast<int64_t>(sizeof(unsigned int)) + 256);
-        if (st != SG_OK)
-        {
-            return st;
-        }
-        auto* hist = reinterpret_cast<unsigned int*>(t->part_scratch + elems);
-        unsigned int* cursor = hist + kPartMax;
-        // hist, cursor and the chunk counter of k_insert_ordered start at zero
-        SG_CUDA_TRY(cudaMemsetAsync(hist, 0, 2 * kPartMax * sizeof(unsigned int) + 256, s));
-        static const int g_count = persistent_grid(k_part_count<KIND, AOS>, kThreads);
-        k_part_count<KIND, AOS><<<grid_for(n, kThreads, g_count), kThreads, 0, s>>>(in0, n, t->bits, shift, parts, hist);
-        SG_LAUNCH_CHECK();
-        k_part_cursors<<<1, kPartMax, 0, s>>>(hist, parts, cursor);
-        SG_LAUNCH_CHECK();
-        static const int g_scatter = persistent_grid(k_part_scatter<KIND, AOS>, kThreads);
-        k_part_scatter<KIND, AOS><<<grid_for(n, kThreads * kPartPer, g_scatter), kThreads, 0, s>>>(
-                in0, in1, n, t->bits, shift, parts, cursor, t->part_scratch);
-        SG_LAUNCH_CHECK();
-        return SG_OK;
-    }
-
     static sg_status
     run(sg_unordered* t, const void* in0, const void* in1, bool aos, int64_t n, uint8_t* flags, cudaStream_t s,
         const uint64_t* hashes = nullptr)
     {
         if (hashes == nullptr && use_partitioned_insert(t, n, flags))
         {
-            const sg_status st = aos ? partition<true>(t, in0, in1, n, s) : partition<false>(t, in0, in1, n, s);
+            unsigned long long* next_chunk = nullptr;
+            const sg_status st = aos ? partition_into_scratch<KIND, true>(t, in0, in1, n, s, &next_chunk)
+                                     : partition_into_scratch<KIND, false>(t, in0, in1, n, s, &next_chunk);
             if (st != SG_OK)
             {
                 return st;
             }
-            const int64_t elems = ((n * t->slot_bytes + 255) / 256) * 256;
-            auto* next_chunk = reinterpret_cast<unsigned long long*>(t->part_scratch + elems +
-                                                                     2 * kPartMax * sizeof(unsigned int));
             static const int max_grid = persistent_grid(k_insert_ordered<KIND>, kThreads);
             k_insert_ordered<KIND><<<grid_for(n, kOrderedChunk, max_grid), kThreads, 0, s>>>(view_of(t),
                                                                                             t->part_scratch, n,
@@ -899,6 +955,20 @@ struct do_erase
     static sg_status
     run(sg_unordered* t, const void* keys, int64_t n, uint8_t* flags, cudaStream_t s, const uint64_t* hashes = nullptr)
     {
+        if (hashes == nullptr && use_partitioned_erase(t, n, flags))
+        {
+            unsigned long long* next_chunk = nullptr;
+            const sg_status st = partition_into_scratch<keys_kind<KIND>, false>(t, keys, nullptr, n, s, &next_chunk);
+            if (st != SG_OK)
+            {
+                return st;
+            }
+            static const int g_ordered = persistent_grid(k_erase_ordered<KIND>, kThreads);
+            k_erase_ordered<KIND><<<grid_for(n, kOrderedChunk, g_ordered), kThreads, 0, s>>>(view_of(t), t->part_scratch,
+                                                                                           n, next_chunk);
+            SG_LAUNCH_CHECK();
+            return SG_OK;
+        }
         static const int max_grid = persistent_grid(k_erase<KIND>, kThreads);
         k_erase<KIND><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n, flags, hashes);
         SG_LAUNCH_CHECK();
