@@ -112,7 +112,10 @@ k_insert(dview t, const void* in0, const void* in1, int64_t n, uint8_t* out_flag
 // partition is arbitrary, as is the order among duplicates of one key in a single bulk insert.
 
 constexpr int kPartMax = 256;
-constexpr int kPartPer = 8; // elements per thread per scatter round
+#ifndef SG_PART_PER
+#define SG_PART_PER 4
+#endif
+constexpr int kPartPer = SG_PART_PER; // elements per thread per scatter round
 
 template <int KIND, bool AOS>
 SG_D typename kind_consts<KIND>::K
@@ -340,6 +343,11 @@ k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, int shift,
 #define SG_ORDERED_ITERS 16
 #endif
 constexpr int kOrderedChunk = SG_ORDERED_ITERS * kThreads;
+// erase prefers short chunks (measured: 512 keys 1.26 ms, 4096 keys 1.48 ms for 2^25 keys)
+#ifndef SG_ERASE_ORDERED_ITERS
+#define SG_ERASE_ORDERED_ITERS 2
+#endif
+constexpr int kEraseChunk = SG_ERASE_ORDERED_ITERS * kThreads;
 
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
@@ -349,11 +357,18 @@ k_insert_ordered(dview t, const void* in0, int64_t n, unsigned long long* next_c
     const tile_lanes L;
     const int warp = threadIdx.x >> 5;
     step_counts c;
+    // thread 0 claims the block's next chunk while the current one is processed, so the claim's round
+    // trip is hidden
+    unsigned long long claimed = 0;
+    if (threadIdx.x == 0)
+    {
+        claimed = atomicAdd(next_chunk, 1ull);
+    }
     while (true)
     {
         if (threadIdx.x == 0)
         {
-            s_first = static_cast<long long>(atomicAdd(next_chunk, 1ull)) * kOrderedChunk;
+            s_first = static_cast<long long>(claimed) * kOrderedChunk;
         }
         __syncthreads();
         const int64_t first = s_first;
@@ -361,6 +376,10 @@ k_insert_ordered(dview t, const void* in0, int64_t n, unsigned long long* next_c
         if (first >= n)
         {
             break;
+        }
+        if (threadIdx.x == 0)
+        {
+            claimed = atomicAdd(next_chunk, 1ull);
         }
         const int64_t last = first + kOrderedChunk < n ? first + kOrderedChunk : n;
         for (int64_t base = first + warp * 32; base < last; base += kThreads)
@@ -387,11 +406,18 @@ k_erase_ordered(dview t, const void* keys, int64_t n, unsigned long long* next_c
     const tile_lanes L;
     const int warp = threadIdx.x >> 5;
     step_counts c;
+    // thread 0 claims the block's next chunk while the current one is processed, so the claim's round
+    // trip is hidden
+    unsigned long long claimed = 0;
+    if (threadIdx.x == 0)
+    {
+        claimed = atomicAdd(next_chunk, 1ull);
+    }
     while (true)
     {
         if (threadIdx.x == 0)
         {
-            s_first = static_cast<long long>(atomicAdd(next_chunk, 1ull)) * kOrderedChunk;
+            s_first = static_cast<long long>(claimed) * kEraseChunk;
         }
         __syncthreads();
         const int64_t first = s_first;
@@ -400,7 +426,11 @@ k_erase_ordered(dview t, const void* keys, int64_t n, unsigned long long* next_c
         {
             break;
         }
-        const int64_t last = first + kOrderedChunk < n ? first + kOrderedChunk : n;
+        if (threadIdx.x == 0)
+        {
+            claimed = atomicAdd(next_chunk, 1ull);
+        }
+        const int64_t last = first + kEraseChunk < n ? first + kEraseChunk : n;
         for (int64_t base = first + warp * 32; base < last; base += kThreads)
         {
             const int64_t i = base + L.lane;
@@ -964,7 +994,7 @@ struct do_erase
                 return st;
             }
             static const int g_ordered = persistent_grid(k_erase_ordered<KIND>, kThreads);
-            k_erase_ordered<KIND><<<grid_for(n, kOrderedChunk, g_ordered), kThreads, 0, s>>>(view_of(t), t->part_scratch,
+            k_erase_ordered<KIND><<<grid_for(n, kEraseChunk, g_ordered), kThreads, 0, s>>>(view_of(t), t->part_scratch,
                                                                                            n, next_chunk);
             SG_LAUNCH_CHECK();
             return SG_OK;
