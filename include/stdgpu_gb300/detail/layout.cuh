@@ -231,7 +231,63 @@ struct identity_word_hash
     }
 };
 
+// ---- deque ring state, shared by the library's bulk kernels and the device-side calls of
+// stdgpu_gb300/stdgpu.cuh.  A deque of capacity c is a ring of c slots plus one 32-bit turn word per slot:
+// push k and pop k use slot (ticket k) mod c; the k-th push waits for turn k, writes, and sets k + 1; the
+// k-th pop waits for k + 1, reads, and sets k + c.  Tickets start at c x 2^32 (a multiple of c and of 2^32).
+constexpr unsigned int kDequeErrWait = 1u;
+constexpr long long kWaitLimit = 1ll << 22; // polls of a ring slot before giving up (about 1-2 s with backoff)
+
+// size guards the capacity: a push reservation adds to it first, a pop reservation subtracts from it
+// only after its tickets are claimed.  avail guards pop_front: a push reservation adds to it only after
+// its tickets are claimed, a pop reservation subtracts from it first.  So a pop is only reserved for a
+// ticket that a push has claimed, and a push only for a slot whose previous pop has been claimed; an
+// over-reservation is undone and can make a concurrent reservation fail near the bounds, never succeed
+// wrongly.  Both equal the element count when no launch is running.
+struct deque_counters
+{
+    long long size;
+    unsigned long long begin;
+    unsigned long long end;
+    unsigned int error;
+    unsigned int pad;
+    long long avail;
+    unsigned long long op_t0; // push_front / pop_back launches: the end before the launch
+    long long op_k;           // and how many elements it moves
+};
+
+
 #if defined(__CUDACC__)
+SG_D bool
+wait_turn(const unsigned* seq, unsigned want, unsigned* error)
+{
+    long long polls = 0;
+    unsigned backoff = 32;
+    while (true)
+    {
+        unsigned cur;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(seq) : "memory");
+        if (cur == want)
+        {
+            return true;
+        }
+        if (++polls > kWaitLimit)
+        {
+            atomicOr(error, kDequeErrWait);
+            return false;
+        }
+        __nanosleep(backoff);
+        backoff = backoff < 256 ? backoff * 2 : 256;
+    }
+}
+
+SG_D void
+store_turn(unsigned* seq, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(seq), "r"(v) : "memory");
+}
+
+
 // 16-byte compare-and-swap (sm_90 and later): old <- *p; if old == expected then *p <- desired.
 SG_D void
 cas128(void* p, unsigned long long e_lo, unsigned long long e_hi, unsigned long long d_lo, unsigned long long d_hi,

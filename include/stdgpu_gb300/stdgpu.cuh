@@ -557,6 +557,223 @@ private:
     sg_vector_view _view{};
 };
 
+// stdgpu::deque<T> (src/stdgpu/deque.cuh) for 4/8-byte T.  Device push_back / pop_front may run
+// concurrently in one kernel (the ring's turn words order a pop after the push of its ticket, with
+// bounded waits: a wait that runs out sets the deque's error bit, which size() reports, and the call fails);
+// host bulk calls cover push_back / pop_front mixes, push_front and pop_back.
+template <typename T>
+class deque
+{
+    static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
+
+public:
+    static deque
+    createDeviceObject(const index_t& capacity)
+    {
+        deque d;
+        detail::gb300_check(sg_deque_create(sizeof(T), capacity, &d._handle), "deque::createDeviceObject");
+        detail::gb300_check(sg_deque_view_of(d._handle, &d._view), "deque::createDeviceObject");
+        return d;
+    }
+
+    static void
+    destroyDeviceObject(deque& d)
+    {
+        if (d._handle != nullptr)
+        {
+            detail::gb300_check(sg_deque_destroy(d._handle), "deque::destroyDeviceObject");
+        }
+        d._handle = nullptr;
+        d._view = sg_deque_view{};
+    }
+
+    index_t
+    size(execution::device_policy policy = execution::device) const
+    {
+        int64_t n = 0;
+        detail::gb300_check(sg_deque_size(_handle, policy.stream, &n), "deque::size");
+        return static_cast<index_t>(n);
+    }
+
+    bool
+    empty(execution::device_policy policy = execution::device) const
+    {
+        return size(policy) == 0;
+    }
+
+    bool
+    full(execution::device_policy policy = execution::device) const
+    {
+        return size(policy) == capacity();
+    }
+
+    __host__ __device__ index_t
+    capacity() const
+    {
+        return static_cast<index_t>(_view.capacity);
+    }
+
+    void
+    clear(execution::device_policy policy = execution::device)
+    {
+        detail::gb300_check(sg_deque_clear(_handle, policy.stream), "deque::clear");
+    }
+
+    // host bulk forms (device pointers): push_front / pop_back of n elements, as sequences of calls
+    void
+    push_front(const T* values, index_t n, std::uint8_t* ok = nullptr,
+               execution::device_policy policy = execution::device)
+    {
+        detail::gb300_check(sg_deque_push_front(_handle, values, n, ok, policy.stream), "deque::push_front");
+    }
+
+    void
+    pop_back(index_t n, T* popped, std::uint8_t* ok = nullptr, execution::device_policy policy = execution::device)
+    {
+        detail::gb300_check(sg_deque_pop_back(_handle, n, popped, ok, policy.stream), "deque::pop_back");
+    }
+
+    // device push_back (src/stdgpu/impl/deque_detail.cuh:202-258)
+    __device__ bool
+    push_back(const T& element) const
+    {
+        auto* c = counters();
+        const long long cap = _view.capacity;
+        if (*reinterpret_cast<volatile long long*>(&c->size) >= cap) // preemptive full() check
+        {
+            return false;
+        }
+        if (static_cast<long long>(atomicAdd(reinterpret_cast<unsigned long long*>(&c->size), 1ull)) >= cap)
+        {
+            atomicAdd(reinterpret_cast<unsigned long long*>(&c->size), ~0ull);
+            return false;
+        }
+        const unsigned long long tk = atomicAdd(&c->end, 1ull);
+        const long long pos = static_cast<long long>(tk % static_cast<unsigned long long>(cap));
+        unsigned* seq = static_cast<unsigned*>(_view.seq);
+        if (!sg::detail::wait_turn(seq + pos, static_cast<unsigned>(tk), &c->error))
+        {
+            return false;
+        }
+        static_cast<T*>(_view.data)[pos] = element;
+        sg::detail::store_turn(seq + pos, static_cast<unsigned>(tk + 1));
+        atomicAdd(reinterpret_cast<unsigned long long*>(&c->avail), 1ull);
+        return true;
+    }
+
+    // device pop_front (src/stdgpu/impl/deque_detail.cuh:388-446)
+    __device__ pair<T, bool>
+    pop_front() const
+    {
+        auto* c = counters();
+        if (*reinterpret_cast<volatile long long*>(&c->avail) <= 0) // preemptive empty() check
+        {
+            return pair<T, bool>(T{}, false);
+        }
+        if (static_cast<long long>(atomicAdd(reinterpret_cast<unsigned long long*>(&c->avail), ~0ull)) <= 0)
+        {
+            atomicAdd(reinterpret_cast<unsigned long long*>(&c->avail), 1ull);
+            return pair<T, bool>(T{}, false);
+        }
+        const unsigned long long tk = atomicAdd(&c->begin, 1ull);
+        const long long cap = _view.capacity;
+        const long long pos = static_cast<long long>(tk % static_cast<unsigned long long>(cap));
+        unsigned* seq = static_cast<unsigned*>(_view.seq);
+        if (!sg::detail::wait_turn(seq + pos, static_cast<unsigned>(tk + 1), &c->error))
+        {
+            return pair<T, bool>(T{}, false);
+        }
+        const T v = *reinterpret_cast<volatile T*>(static_cast<T*>(_view.data) + pos);
+        sg::detail::store_turn(seq + pos, static_cast<unsigned>(tk + static_cast<unsigned long long>(cap)));
+        atomicAdd(reinterpret_cast<unsigned long long*>(&c->size), ~0ull);
+        return pair<T, bool>(v, true);
+    }
+
+private:
+    __device__ sg::detail::deque_counters*
+    counters() const
+    {
+        return static_cast<sg::detail::deque_counters*>(_view.counters);
+    }
+
+    sg_deque* _handle = nullptr;
+    sg_deque_view _view{};
+};
+
+// stdgpu::queue<T> / stack<T> (src/stdgpu/queue.cuh, stack.cuh): adapters over deque.  queue::push / pop
+// are push_back / pop_front (device calls, concurrent); stack::push is push_back and stack::pop the host
+// bulk pop_back.
+template <typename T>
+class queue
+{
+public:
+    static queue
+    createDeviceObject(const index_t& capacity)
+    {
+        return queue{ deque<T>::createDeviceObject(capacity) };
+    }
+    static void
+    destroyDeviceObject(queue& q)
+    {
+        deque<T>::destroyDeviceObject(q._c);
+    }
+    __device__ bool
+    push(const T& element) const
+    {
+        return _c.push_back(element);
+    }
+    __device__ pair<T, bool>
+    pop() const
+    {
+        return _c.pop_front();
+    }
+    index_t
+    size(execution::device_policy policy = execution::device) const
+    {
+        return _c.size(policy);
+    }
+    bool
+    empty(execution::device_policy policy = execution::device) const
+    {
+        return _c.empty(policy);
+    }
+
+    deque<T> _c;
+};
+
+template <typename T>
+class stack
+{
+public:
+    static stack
+    createDeviceObject(const index_t& capacity)
+    {
+        return stack{ deque<T>::createDeviceObject(capacity) };
+    }
+    static void
+    destroyDeviceObject(stack& s)
+    {
+        deque<T>::destroyDeviceObject(s._c);
+    }
+    __device__ bool
+    push(const T& element) const
+    {
+        return _c.push_back(element);
+    }
+    void
+    pop(index_t n, T* popped, std::uint8_t* ok = nullptr, execution::device_policy policy = execution::device)
+    {
+        _c.pop_back(n, popped, ok, policy);
+    }
+    index_t
+    size(execution::device_policy policy = execution::device) const
+    {
+        return _c.size(policy);
+    }
+
+    deque<T> _c;
+};
+
 // bitset::count() over raw blocks (src/stdgpu/impl/bitset_detail.cuh:388-404).
 inline std::int64_t
 bitset_count(const std::uint32_t* blocks, std::int64_t nbits, execution::device_policy policy = execution::device)

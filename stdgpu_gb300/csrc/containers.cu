@@ -34,27 +34,6 @@ namespace detail
 {
 
 constexpr int kCThreads = 256;
-constexpr unsigned int kDequeErrWait = 1u;
-constexpr long long kWaitLimit = 1ll << 22; // polls of a ring slot before giving up (about 1-2 s with backoff)
-
-// size guards the capacity: a push reservation adds to it first, a pop reservation subtracts from it
-// only after its tickets are claimed.  avail guards pop_front: a push reservation adds to it only after
-// its tickets are claimed, a pop reservation subtracts from it first.  So a pop is only reserved for a
-// ticket that a push has claimed, and a push only for a slot whose previous pop has been claimed; an
-// over-reservation is undone and can make a concurrent reservation fail near the bounds, never succeed
-// wrongly.  Both equal the element count when no launch is running.
-struct deque_counters
-{
-    long long size;
-    unsigned long long begin;
-    unsigned long long end;
-    unsigned int error;
-    unsigned int pad;
-    long long avail;
-    unsigned long long op_t0; // push_front / pop_back launches: the end before the launch
-    long long op_k;           // and how many elements it moves
-};
-
 SG_D unsigned
 lanemask_lt()
 {
@@ -172,35 +151,6 @@ k_vector_push_back(T* data, long long* size, int64_t cap, const T* values, const
 }
 
 // ---------------------------------------------------------------- deque
-
-SG_D bool
-wait_turn(const unsigned* seq, unsigned want, unsigned* error)
-{
-    long long polls = 0;
-    unsigned backoff = 32;
-    while (true)
-    {
-        unsigned cur;
-        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(seq) : "memory");
-        if (cur == want)
-        {
-            return true;
-        }
-        if (++polls > kWaitLimit)
-        {
-            atomicOr(error, kDequeErrWait);
-            return false;
-        }
-        __nanosleep(backoff);
-        backoff = backoff < 256 ? backoff * 2 : 256;
-    }
-}
-
-SG_D void
-store_turn(unsigned* seq, unsigned v)
-{
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(seq), "r"(v) : "memory");
-}
 
 SG_D long long
 atomic_add_ll(long long* p, long long v)

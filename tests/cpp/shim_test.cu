@@ -5,6 +5,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <random>
+#include <set>
 #include <unordered_set>
 #include <vector>
 
@@ -163,6 +164,72 @@ k_push_if(stdgpu::vector<std::uint32_t> v, int n, int* pushed)
     }
 }
 
+static long long
+count_ok(const std::uint8_t* d, int n)
+{
+    long long c = 0;
+    for (auto x : to_host(d, n))
+    {
+        c += x;
+    }
+    return c;
+}
+
+// deque: thread i pushes values[i] when i is even, else pops the front (deque.inc:406-560 pushes and pops
+// from many threads of one launch)
+__global__ void
+deque_mixed(stdgpu::deque<std::uint64_t> d, const std::uint64_t* values, int n, std::uint64_t* popped,
+            std::uint8_t* ok)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n)
+    {
+        return;
+    }
+    if ((i & 1) == 0)
+    {
+        ok[i] = d.push_back(values[i]) ? 1 : 0;
+    }
+    else
+    {
+        auto r = d.pop_front();
+        ok[i] = r.second ? 1 : 0;
+        popped[i] = r.second ? r.first : 0;
+    }
+}
+
+__global__ void
+deque_fill(stdgpu::deque<std::uint64_t> d, const std::uint64_t* values, int n, std::uint8_t* ok)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        ok[i] = d.push_back(values[i]) ? 1 : 0;
+    }
+}
+
+__global__ void
+deque_drain(stdgpu::deque<std::uint64_t> d, int n, std::uint64_t* popped, std::uint8_t* ok)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        auto r = d.pop_front();
+        ok[i] = r.second ? 1 : 0;
+        popped[i] = r.second ? r.first : 0;
+    }
+}
+
+__global__ void
+queue_push(stdgpu::queue<std::uint32_t> q, int n, int* pushed)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && q.push(static_cast<std::uint32_t>(i)))
+    {
+        atomicAdd(pushed, 1);
+    }
+}
+
 static int
 sum_of(const int* d, int n)
 {
@@ -302,6 +369,84 @@ main()
         std::uint32_t* d_words = to_device(words);
         check(stdgpu::bitset_count(d_words, 32000) == want, "bitset count");
         cudaFree(d_words);
+    }
+
+    // deque: device push_back / pop_front from one launch, then FIFO order across launches
+    {
+        const int n = 1 << 16;
+        auto d = stdgpu::deque<std::uint64_t>::createDeviceObject(n);
+        std::vector<std::uint64_t> v(n);
+        for (int i = 0; i < n; ++i)
+        {
+            v[i] = 1000000ull + static_cast<std::uint64_t>(i);
+        }
+        std::uint64_t* d_v = to_device(v);
+        std::uint64_t* d_p = nullptr;
+        std::uint8_t* d_ok = nullptr;
+        cudaMalloc(&d_p, sizeof(std::uint64_t) * n);
+        cudaMalloc(&d_ok, n);
+        deque_fill<<<(n / 2 + 255) / 256, 256>>>(d, d_v, n / 2, d_ok); // first half of the values, in one launch
+        check(d.size() == n / 2 && count_ok(d_ok, n / 2) == n / 2, "deque push_back from a kernel");
+        deque_mixed<<<(n + 255) / 256, 256>>>(d, d_v + n / 2 - 1, n, d_p, d_ok);
+        auto ok = to_host(d_ok, n);
+        auto popped = to_host(d_p, n);
+        std::multiset<std::uint64_t> out, in;
+        long long pushes = 0, pops = 0;
+        for (int i = 0; i < n; ++i)
+        {
+            if (i & 1)
+            {
+                pops += ok[i];
+                if (ok[i])
+                {
+                    out.insert(popped[i]);
+                }
+            }
+            else
+            {
+                pushes += ok[i];
+            }
+        }
+        // everything popped was in the deque before the launch or pushed during it
+        for (int i = 0; i < n / 2; ++i)
+        {
+            in.insert(v[i]);
+        }
+        for (int i = 0; i < n; i += 2)
+        {
+            if (ok[i])
+            {
+                in.insert(v[n / 2 - 1 + i]);
+            }
+        }
+        bool sub = true;
+        for (auto x : out)
+        {
+            auto it = in.find(x);
+            sub = sub && it != in.end();
+            if (it != in.end())
+            {
+                in.erase(it);
+            }
+        }
+        check(sub && d.size() == n / 2 + pushes - pops, "deque mixed push_back / pop_front: conservation");
+        // drain: what is left comes out, and a second drain finds it empty
+        const stdgpu::index_t left = d.size();
+        deque_drain<<<(n + 255) / 256, 256>>>(d, n, d_p, d_ok);
+        check(count_ok(d_ok, n) == left && d.empty(), "deque drain");
+        stdgpu::deque<std::uint64_t>::destroyDeviceObject(d);
+        cudaFree(d_v);
+        cudaFree(d_p);
+        cudaFree(d_ok);
+
+        auto q = stdgpu::queue<std::uint32_t>::createDeviceObject(1000);
+        int* d_pushed = nullptr;
+        cudaMalloc(&d_pushed, sizeof(int));
+        cudaMemset(d_pushed, 0, sizeof(int));
+        queue_push<<<8, 256>>>(q, 2048, d_pushed);
+        check(to_host(d_pushed, 1)[0] == 1000 && q.size() == 1000, "queue push stops at capacity");
+        stdgpu::queue<std::uint32_t>::destroyDeviceObject(q);
+        cudaFree(d_pushed);
     }
 
     cudaError_t e = cudaDeviceSynchronize();
