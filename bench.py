@@ -362,7 +362,8 @@ def native_arm(args):
             traffic = None
     phase_kernels = {"insert": "k_part_count + k_part_cursors + k_part_scatter + k_insert_ordered (partitioned bulk "
                                "insert, chosen automatically at this size)",
-                     "find": "k_find", "erase": "k_erase"}
+                     "find": "k_find", "erase": "k_part_count + k_part_cursors + k_part_scatter + k_erase_ordered "
+                                                 "(partitioned bulk erase, chosen automatically at this size)"}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": dominant, "kernels": phase_kernels[dominant], "peak_source": peak_src,
                 "bytes_per_op": BYTES_PER_OP[dominant],
