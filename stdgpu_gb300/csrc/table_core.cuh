@@ -625,6 +625,7 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
     int my_state = 0; // 0 present, 1 claim my_target, 2 decided beyond the home group
     uint32_t my_target = 0;
     bool my_tomb = false;
+    unsigned my_free = 0u; // never-used slots of the home group as read (bit = slot within the group)
 #pragma unroll
     for (int r = 0; r < kTile; ++r)
     {
@@ -640,12 +641,17 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
         const int mine = (__ffs(tomb ? mt : me) - 1) & (S - 1);
         const int s_claim = __shfl_sync(0xffffffffu, mine, L.tbase + owner);
         const uint32_t target = hr[r] * G + static_cast<uint32_t>(owner) * S + static_cast<uint32_t>(s_claim);
+        // the group's never-used slots, gathered from the tile's 4 sectors
+        unsigned gfree = me << (L.q * S);
+        gfree |= __shfl_xor_sync(0xffffffffu, gfree, 1);
+        gfree |= __shfl_xor_sync(0xffffffffu, gfree, 2);
         const int state = tm != 0u ? 0 : (te != 0u ? 1 : 2);
         if (L.q == r)
         {
             my_state = state;
             my_target = target;
             my_tomb = tomb;
+            my_free = gfree;
         }
     }
     bool again = false;
@@ -657,9 +663,34 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
             c.reused += my_tomb ? 1u : 0u;
             res = 1;
         }
-        else
+        else if (old != key)
         {
-            again = old != key; // lost the slot to another key; a copy of this key means present
+            // Lost the slot to another key.  Without erased slots in the group, try its next never-used
+            // slots as read: every slot before each of them holds another key (read so, or returned by a
+            // failed claim), so a claim there keeps the first-free-slot rule; a returned copy of this key
+            // means present.  Whatever is left goes to the tile's slow path.
+            again = true;
+            if (!my_tomb)
+            {
+                const uint32_t gbase = my_target - my_target % G;
+                unsigned rest = my_free & ~(1u << (my_target - gbase));
+                while (rest != 0u)
+                {
+                    const uint32_t slot = gbase + static_cast<uint32_t>(__ffs(rest) - 1);
+                    rest &= rest - 1u;
+                    if (claim_slot<KIND>(t, slot, false, key, val, old))
+                    {
+                        res = 1;
+                        again = false;
+                        break;
+                    }
+                    if (old == key)
+                    {
+                        again = false;
+                        break;
+                    }
+                }
+            }
         }
     }
     again = again || (probe && my_state == 2);
