@@ -345,7 +345,7 @@ struct table_impl final : table_base
     }
 };
 
-// ---- containers used by the C5 workload ----
+// ---- vector, deque and bitset entry points ----
 
 struct vec_push_functor
 {
