@@ -66,7 +66,7 @@ def parse():
     p.add_argument("--keys-log2", type=int, default=KEYS_LOG2, help="2^k keys (default: the full workload)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--workload", choices=["voxel", "batched", "serve", "large"], default="voxel",
+    p.add_argument("--workload", choices=["voxel", "batched", "serve", "large", "small"], default="voxel",
                    help="voxel: the headline map workload; batched: 4096 small sets, batched vs plain calls; "
                         "serve: request stream over 256 resident maps, continuous batching vs serial calls")
     p.add_argument("--requests", type=int, default=600, help="serve workload: number of requests")
@@ -441,12 +441,27 @@ def large_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def small_arm(args):
+    """unordered_set<uint32_t> capacity 2^21, 2^20 keys: an L2-resident table, eager and CUDA-graph steps."""
+    from stdgpu_gb300 import small_bench
+    r = small_bench.run(steps=max(args.steps, 20), warmup=max(args.warmup, 5))
+    line = {"metric": "small-table clear+insert+contains+erase Mops/s", "value": r["graph_mops"], "unit": UNIT,
+            "n_gpus": 1, "steps": max(args.steps, 20), "warmup": max(args.warmup, 5), "ms_per_step": r["graph_ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": "unordered_set<uint32_t>, capacity 2^21, 2^20 uniform keys; contains 50% hits; "
+                                   "erase half; step replayed as one CUDA graph (table resident in L2)"},
+            "small": r}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
     elif args.workload == "large":
         large_arm(args)
+    elif args.workload == "small":
+        small_arm(args)
     elif args.workload == "serve":
         serve_arm(args)
     elif args.workload == "batched":

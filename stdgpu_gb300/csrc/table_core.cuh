@@ -361,6 +361,50 @@ select_sector_value(const uint32_t (&w)[8], unsigned one_hot)
     return v;
 }
 
+// Per-key rotation of the slot order inside a group.  Every insert of a key takes, within a group, the
+// first free slot at or after slot rot_of(hash) (cyclically), where the reference-compatible rule would take
+// the first free slot.  Copies of one key follow the same order, so the duplicate argument below holds
+// unchanged, and concurrent inserts of different keys into one group start at different slots instead of
+// all racing for its first free slot.  Lookups scan whole groups, so they do not depend on the order.
+SG_D uint32_t
+rot_of(uint64_t hash)
+{
+    return static_cast<uint32_t>((hash * 0xD6E8FEB86659FD93ull) >> 59);
+}
+
+// Index of the first set bit of the G-bit mask m at or after bit o, cyclically; -1 when m is empty.
+template <uint32_t G>
+SG_D int
+first_from(unsigned m, uint32_t o)
+{
+    if (m == 0u)
+    {
+        return -1;
+    }
+    o &= G - 1;
+    unsigned r;
+    if constexpr (G == 32)
+    {
+        r = __funnelshift_r(m, m, o);
+    }
+    else
+    {
+        r = ((m >> o) | (m << (G - o))) & ((1u << G) - 1u);
+    }
+    return static_cast<int>((static_cast<uint32_t>(__ffs(r) - 1) + o) & (G - 1));
+}
+
+// G-bit mask of a group from the tile's four S-bit sector masks (lane q holds sector q).
+template <uint32_t S>
+SG_D unsigned
+group_mask(unsigned sector_mask, int q, unsigned mask)
+{
+    unsigned g = sector_mask << (q * S);
+    g |= __shfl_xor_sync(mask, g, 1);
+    g |= __shfl_xor_sync(mask, g, 2);
+    return g;
+}
+
 // Insert of one key by one tile (all 4 lanes call it with the same key; w is this lane's sector of the
 // key's home group).  Returns 1 inserted, 0 already present, 2 refused (no free slot in the table),
 // 3 retry limit.  With REUSE, erased slots are claimed too: the tile scans to the first group holding a
@@ -370,7 +414,7 @@ select_sector_value(const uint32_t (&w)[8], unsigned one_hot)
 template <int KIND, bool REUSE>
 SG_D int
 tile_insert(const dview& t, typename kind_consts<KIND>::K key, typename kind_consts<KIND>::V val, uint32_t home,
-            uint32_t (&w)[8], unsigned tmask, int tbase, int q, unsigned int& tombs_reused)
+            uint32_t (&w)[8], unsigned tmask, int tbase, int q, unsigned int& tombs_reused, uint32_t rot)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
@@ -392,17 +436,15 @@ tile_insert(const dview& t, typename kind_consts<KIND>::K key, typename kind_con
         {
             if (free_slot < 0)
             {
-                const unsigned bt = __ballot_sync(tmask, mt != 0u);
-                if (bt != 0u)
+                const int s = first_from<G>(group_mask<S>(mt, q, tmask), rot);
+                if (s >= 0)
                 {
-                    const int owner = __ffs(bt) - 1;
-                    free_slot = static_cast<int32_t>(g * G + (owner - tbase) * S +
-                                                     (__ffs(__shfl_sync(tmask, mt, owner)) - 1));
+                    free_slot = static_cast<int32_t>(g * G + static_cast<uint32_t>(s));
                 }
             }
         }
-        const unsigned be = __ballot_sync(tmask, me != 0u);
-        bool claim = be != 0u;
+        const unsigned ge = group_mask<S>(me, q, tmask);
+        bool claim = ge != 0u;
         if (!claim && ++probes >= t.num_groups)
         {
             if (!(REUSE && free_slot >= 0))
@@ -426,8 +468,7 @@ tile_insert(const dview& t, typename kind_consts<KIND>::K key, typename kind_con
         }
         else
         {
-            const int owner = __ffs(be) - 1;
-            target = g * G + (owner - tbase) * S + (__ffs(__shfl_sync(tmask, me, owner)) - 1);
+            target = g * G + static_cast<uint32_t>(first_from<G>(ge, rot));
             expected = C::empty_key;
         }
         K old = expected;
@@ -626,26 +667,22 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
     uint32_t my_target = 0;
     bool my_tomb = false;
     unsigned my_free = 0u; // never-used slots of the home group as read (bit = slot within the group)
+    const uint32_t my_rot = rot_of(hash);
 #pragma unroll
     for (int r = 0; r < kTile; ++r)
     {
         const K kr = __shfl_sync(0xffffffffu, key, L.tbase + r);
+        const uint32_t rot = __shfl_sync(0xffffffffu, my_rot, L.tbase + r);
         unsigned mm, me, mt;
         sector_masks<KIND, true>(pre[r], kr, hr[r] * G + L.q * S, t.total, mm, me, mt);
         const unsigned tm = tile_nibble(__ballot_sync(0xffffffffu, mm != 0u), L.tbase);
-        const unsigned te = tile_nibble(__ballot_sync(0xffffffffu, me != 0u), L.tbase);
-        const unsigned tt = tile_nibble(__ballot_sync(0xffffffffu, mt != 0u), L.tbase);
-        const bool tomb = tt != 0u;
-        const int owner = (__ffs(tomb ? tt : te) - 1) & (kTile - 1);
-        // every lane picks its own sector's candidate slot; the owner's pick is the claim
-        const int mine = (__ffs(tomb ? mt : me) - 1) & (S - 1);
-        const int s_claim = __shfl_sync(0xffffffffu, mine, L.tbase + owner);
-        const uint32_t target = hr[r] * G + static_cast<uint32_t>(owner) * S + static_cast<uint32_t>(s_claim);
-        // the group's never-used slots, gathered from the tile's 4 sectors
-        unsigned gfree = me << (L.q * S);
-        gfree |= __shfl_xor_sync(0xffffffffu, gfree, 1);
-        gfree |= __shfl_xor_sync(0xffffffffu, gfree, 2);
-        const int state = tm != 0u ? 0 : (te != 0u ? 1 : 2);
+        // the group's never-used and erased slots, gathered from the tile's 4 sectors
+        const unsigned gfree = group_mask<S>(me, L.q, 0xffffffffu);
+        const unsigned gtomb = group_mask<S>(mt, L.q, 0xffffffffu);
+        const bool tomb = gtomb != 0u;
+        const int s_claim = first_from<G>(tomb ? gtomb : gfree, rot);
+        const uint32_t target = hr[r] * G + static_cast<uint32_t>(s_claim < 0 ? 0 : s_claim);
+        const int state = tm != 0u ? 0 : (gfree != 0u ? 1 : 2);
         if (L.q == r)
         {
             my_state = state;
@@ -676,8 +713,9 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
                 unsigned rest = my_free & ~(1u << (my_target - gbase));
                 while (rest != 0u)
                 {
-                    const uint32_t slot = gbase + static_cast<uint32_t>(__ffs(rest) - 1);
-                    rest &= rest - 1u;
+                    const uint32_t s = static_cast<uint32_t>(first_from<G>(rest, my_rot));
+                    const uint32_t slot = gbase + s;
+                    rest &= ~(1u << s);
                     if (claim_slot<KIND>(t, slot, false, key, val, old))
                     {
                         res = 1;
@@ -707,7 +745,8 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
                 const V vr = __shfl_sync(L.tmask, val, L.tbase + r);
                 uint32_t w[8];
                 load_sector(t, hr[r], L.q, w);
-                const int x = tile_insert<KIND, true>(t, kr, vr, hr[r], w, L.tmask, L.tbase, L.q, c.reused);
+                const uint32_t rot = __shfl_sync(L.tmask, my_rot, L.tbase + r);
+                const int x = tile_insert<KIND, true>(t, kr, vr, hr[r], w, L.tmask, L.tbase, L.q, c.reused, rot);
                 if (L.q == r)
                 {
                     res = x;
