@@ -57,7 +57,7 @@ ERASE_FRAC = 0.25
 BYTES_PER_OP = {"insert": 16 + 128 + 32, "find": 8 + 5 + 128, "erase": 8 + 128 + 32}
 
 
-def parse():
+def parse_args(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=5)
@@ -68,9 +68,15 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--workload", choices=["voxel", "batched", "serve", "large", "small"], default="voxel",
                    help="voxel: the headline map workload; batched: 4096 small sets, batched vs plain calls; "
-                        "serve: request stream over 256 resident maps, continuous batching vs serial calls")
+                        "serve: request stream over 256 resident maps, continuous batching vs serial calls; "
+                        "large: capacity-2^30 map at 0.5/0.75/0.9 load plus vector / deque / bitset; "
+                        "small: an L2-resident 2^20-key set, eager and as one CUDA graph")
     p.add_argument("--requests", type=int, default=600, help="serve workload: number of requests")
-    return p.parse_args()
+    return p.parse_args(argv)
+
+
+def parse():
+    return parse_args()
 
 
 def dist_info():
@@ -78,6 +84,23 @@ def dist_info():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def slowest_rank_ms(ms: float, ws: int, device) -> float:
+    """The largest per-step time over all ranks (every rank runs its own replica of the workload)."""
+    if ws <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replicas_value(ops_per_step: int, ms: float, ws: int, device) -> tuple[float, float]:
+    """(whole-job Mops/s, slowest rank's ms per step): all ranks' operations over the slowest rank's time."""
+    worst = slowest_rank_ms(ms, ws, device)
+    return ops_per_step * ws / (worst * 1e-3) / 1e6, worst
 
 
 # ------------------------------------------------------------------ clocks
@@ -282,13 +305,8 @@ def native_arm(args):
     total_ms = t_start.elapsed_time(t_end)
     phase_ms = {name: [evs[k][i].elapsed_time(evs[k][i + 1]) for k in range(args.steps)]
                 for i, name in enumerate(["clear", "insert", "find", "erase"])}
-    ms_per_step = total_ms / args.steps
-    if ws > 1:
-        t = torch.tensor([ms_per_step], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_per_step = float(t.item())
     ops_per_step = n + n_q + n_e
-    value = ops_per_step * ws / (ms_per_step * 1e-3) / 1e6
+    value, ms_per_step = replicas_value(ops_per_step, total_ms / args.steps, ws, dev)
 
     # ---------------- e2e: host buffers through the C ABI, copies inside the timed region
     e2e = None
@@ -335,8 +353,8 @@ def native_arm(args):
             found_h.zero_()
             return a.elapsed_time(b) / args.steps
 
-        e2e_ms = time_steps(e2e_step)
-        serial_ms = time_steps(e2e_serial_step)
+        e2e_ms = slowest_rank_ms(time_steps(e2e_step), ws, dev)
+        serial_ms = slowest_rank_ms(time_steps(e2e_serial_step), ws, dev)
         stager.close()
         h2d = pairs_h.numel() * 8 + queries_h.numel() * 8 + erase_h.numel() * 8
         d2h = vals_h.numel() * 4 + found_h.numel()
