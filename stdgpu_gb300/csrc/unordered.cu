@@ -946,15 +946,20 @@ struct do_insert
     run(sg_unordered* t, const void* in0, const void* in1, bool aos, int64_t n, uint8_t* flags, cudaStream_t s,
         const uint64_t* hashes = nullptr)
     {
+        unsigned long long* next_chunk = nullptr;
+        sg_status st = SG_ERR_OOM;
         if (hashes == nullptr && use_partitioned_insert(t, n, flags))
         {
-            unsigned long long* next_chunk = nullptr;
-            const sg_status st = aos ? partition_into_scratch<KIND, true>(t, in0, in1, n, s, &next_chunk)
-                                     : partition_into_scratch<KIND, false>(t, in0, in1, n, s, &next_chunk);
-            if (st != SG_OK)
+            st = aos ? partition_into_scratch<KIND, true>(t, in0, in1, n, s, &next_chunk)
+                     : partition_into_scratch<KIND, false>(t, in0, in1, n, s, &next_chunk);
+            if (st != SG_OK && st != SG_ERR_OOM)
             {
                 return st;
             }
+        }
+        // without room for the scratch array the direct kernel does the same insert
+        if (st == SG_OK)
+        {
             static const int max_grid = persistent_grid(k_insert_ordered<KIND>, kThreads);
             k_insert_ordered<KIND><<<grid_for(n, kOrderedChunk, max_grid), kThreads, 0, s>>>(view_of(t),
                                                                                             t->part_scratch, n,
@@ -985,14 +990,18 @@ struct do_erase
     static sg_status
     run(sg_unordered* t, const void* keys, int64_t n, uint8_t* flags, cudaStream_t s, const uint64_t* hashes = nullptr)
     {
+        unsigned long long* next_chunk = nullptr;
+        sg_status st = SG_ERR_OOM;
         if (hashes == nullptr && use_partitioned_erase(t, n, flags))
         {
-            unsigned long long* next_chunk = nullptr;
-            const sg_status st = partition_into_scratch<keys_kind<KIND>, false>(t, keys, nullptr, n, s, &next_chunk);
-            if (st != SG_OK)
+            st = partition_into_scratch<keys_kind<KIND>, false>(t, keys, nullptr, n, s, &next_chunk);
+            if (st != SG_OK && st != SG_ERR_OOM)
             {
                 return st;
             }
+        }
+        if (st == SG_OK)
+        {
             static const int g_ordered = persistent_grid(k_erase_ordered<KIND>, kThreads);
             k_erase_ordered<KIND><<<grid_for(n, kEraseChunk, g_ordered), kThreads, 0, s>>>(view_of(t), t->part_scratch,
                                                                                            n, next_chunk);
