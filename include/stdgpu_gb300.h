@@ -21,6 +21,7 @@
 #ifndef STDGPU_GB300_H
 #define STDGPU_GB300_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #if defined(__GNUC__)
@@ -88,6 +89,20 @@ typedef struct sg_unordered_view
     int32_t bucket_bits;     /* log2(bucket_count) */
     int32_t kind;
 } sg_unordered_view;
+
+/* ---------------- device memory ---------------- */
+
+/* The allocator of every container's device storage (the reference's Allocator template parameter,
+ * src/stdgpu/memory.h; safe_device_allocator by default).  alloc returns device memory of at least `bytes`
+ * (NULL when it cannot), release gives it back; both get ctx.  Passing NULL for both restores
+ * cudaMalloc / cudaFree.  SG_ERR_BAD_ARG (nothing changed) while storage made through the current pair is
+ * still allocated, or when only one of the two functions is given.  Pinned host buffers are not
+ * affected. */
+typedef void* (*sg_device_alloc_fn)(size_t bytes, void* ctx);
+typedef void (*sg_device_free_fn)(void* ptr, void* ctx);
+SG_API sg_status sg_set_device_allocator(sg_device_alloc_fn alloc, sg_device_free_fn release, void* ctx);
+/* Number of device allocations the library holds (all containers, staging and scratch buffers). */
+SG_API int64_t sg_live_device_allocations(void);
 
 /* ---------------- unordered_set / unordered_map ---------------- */
 

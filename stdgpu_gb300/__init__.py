@@ -12,6 +12,7 @@ from .containers import (  # noqa: F401
     deque,
     geometry_for,
     kernel_launch_count,
+    live_device_allocations,
     queue,
     stack,
     stager,
@@ -19,6 +20,7 @@ from .containers import (  # noqa: F401
     unordered_base,
     unordered_map,
     unordered_set,
+    use_torch_allocator,
     vector,
 )
 from ._native import StdgpuError, library_path, load  # noqa: F401

@@ -73,6 +73,8 @@ class sg_server_stats(ctypes.Structure):
 
 # name -> (restype, argtypes); every symbol the header declares
 SIGNATURES = {
+    "sg_set_device_allocator": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "sg_live_device_allocations": (c_int64, []),
     "sg_unordered_create": (c_int32, [c_int32, c_int64, c_void_p, POINTER(c_void_p)]),
     "sg_unordered_destroy": (c_int32, [c_void_p]),
     "sg_unordered_insert": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),

@@ -360,6 +360,40 @@ class unordered_map(unordered_base):
         return cls._create(KINDS[(key, mapped)], capacity, stream, custom_hash)
 
 
+_allocator_callbacks = None
+
+
+def use_torch_allocator(enable: bool = True) -> None:
+    """Route the device storage of every container through PyTorch's caching allocator
+    (sg_set_device_allocator), or back to cudaMalloc / cudaFree.  Only while no container is alive."""
+    global _allocator_callbacks
+    lib = N.load()
+    if not enable:
+        N.check(lib.sg_set_device_allocator(None, None, None), "set_device_allocator")
+        _allocator_callbacks = None
+        return
+    alloc_t = ctypes.CFUNCTYPE(c_void_p, ctypes.c_size_t, c_void_p)
+    free_t = ctypes.CFUNCTYPE(None, c_void_p, c_void_p)
+
+    def alloc(nbytes, _ctx):
+        try:
+            return torch.cuda.caching_allocator_alloc(int(nbytes))
+        except RuntimeError:
+            return None
+
+    def release(ptr, _ctx):
+        torch.cuda.caching_allocator_delete(ptr)
+
+    callbacks = (alloc_t(alloc), free_t(release))
+    N.check(lib.sg_set_device_allocator(ctypes.cast(callbacks[0], c_void_p), ctypes.cast(callbacks[1], c_void_p),
+                                        None), "set_device_allocator")
+    _allocator_callbacks = callbacks  # the C function pointers must outlive their use
+
+
+def live_device_allocations() -> int:
+    return int(N.load().sg_live_device_allocations())
+
+
 def geometry_for(kind: int, capacity: int) -> N.sg_geometry:
     g = N.sg_geometry()
     N.check(N.load().sg_unordered_geometry_for(kind, int(capacity), byref(g)), "geometry_for")

@@ -453,26 +453,26 @@ sg_batch_create(int32_t kind, int32_t n_tables, const int64_t* capacities, void*
         }
     }
     b->nchunks = static_cast<int64_t>(chunks.size());
-    cudaError_t e = cudaMalloc(&b->arena, static_cast<size_t>(b->arena_bytes));
+    cudaError_t e = sg::detail::dev_malloc(&b->arena, static_cast<size_t>(b->arena_bytes));
     if (e == cudaSuccess)
     {
-        e = cudaMalloc(&b->headers, sizeof(table_header) * n_tables);
+        e = sg::detail::dev_malloc(&b->headers, sizeof(table_header) * n_tables);
     }
     if (e == cudaSuccess)
     {
-        e = cudaMalloc(&b->views, sizeof(dview) * n_tables);
+        e = sg::detail::dev_malloc(&b->views, sizeof(dview) * n_tables);
     }
     if (e == cudaSuccess)
     {
-        e = cudaMalloc(&b->chunks, sizeof(init_chunk) * chunks.size());
+        e = sg::detail::dev_malloc(&b->chunks, sizeof(init_chunk) * chunks.size());
     }
     if (e == cudaSuccess)
     {
-        e = cudaMalloc(&b->prefix, sizeof(int64_t) * (n_tables + 1));
+        e = sg::detail::dev_malloc(&b->prefix, sizeof(int64_t) * (n_tables + 1));
     }
     if (e == cudaSuccess)
     {
-        e = cudaMalloc(&b->sizes_dev, sizeof(long long) * n_tables);
+        e = sg::detail::dev_malloc(&b->sizes_dev, sizeof(long long) * n_tables);
     }
     if (e == cudaSuccess)
     {
@@ -523,12 +523,12 @@ sg_batch_destroy(sg_table_batch* b)
         return SG_ERR_BAD_ARG;
     }
     cudaDeviceSynchronize();
-    cudaFree(b->arena);
-    cudaFree(b->headers);
-    cudaFree(b->views);
-    cudaFree(b->chunks);
-    cudaFree(b->prefix);
-    cudaFree(b->sizes_dev);
+    sg::detail::dev_free(b->arena);
+    sg::detail::dev_free(b->headers);
+    sg::detail::dev_free(b->views);
+    sg::detail::dev_free(b->chunks);
+    sg::detail::dev_free(b->prefix);
+    sg::detail::dev_free(b->sizes_dev);
     if (b->sizes_host != nullptr)
     {
         cudaFreeHost(b->sizes_host);

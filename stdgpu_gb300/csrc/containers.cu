@@ -686,10 +686,10 @@ sg_vector_create(int32_t elem_bytes, int64_t capacity, sg_vector** out)
     }
     v->elem_bytes = elem_bytes;
     v->capacity = capacity;
-    cudaError_t e = cudaMalloc(&v->data, static_cast<size_t>(capacity) * elem_bytes);
+    cudaError_t e = sg::detail::dev_malloc(&v->data, static_cast<size_t>(capacity) * elem_bytes);
     if (e == cudaSuccess)
     {
-        e = cudaMalloc(&v->size, sizeof(long long));
+        e = sg::detail::dev_malloc(&v->size, sizeof(long long));
     }
     if (e == cudaSuccess)
     {
@@ -717,8 +717,8 @@ sg_vector_destroy(sg_vector* v)
         return SG_ERR_BAD_ARG;
     }
     cudaDeviceSynchronize();
-    cudaFree(v->data);
-    cudaFree(v->size);
+    sg::detail::dev_free(v->data);
+    sg::detail::dev_free(v->size);
     if (v->host != nullptr)
     {
         cudaFreeHost(v->host);
@@ -896,14 +896,14 @@ sg_deque_create(int32_t elem_bytes, int64_t capacity, sg_deque** out)
     }
     d->elem_bytes = elem_bytes;
     d->capacity = capacity;
-    cudaError_t e = cudaMalloc(&d->data, static_cast<size_t>(capacity) * elem_bytes);
+    cudaError_t e = sg::detail::dev_malloc(&d->data, static_cast<size_t>(capacity) * elem_bytes);
     if (e == cudaSuccess)
     {
-        e = cudaMalloc(&d->seq, static_cast<size_t>(capacity) * sizeof(unsigned));
+        e = sg::detail::dev_malloc(&d->seq, static_cast<size_t>(capacity) * sizeof(unsigned));
     }
     if (e == cudaSuccess)
     {
-        e = cudaMalloc(&d->counters, sizeof(deque_counters));
+        e = sg::detail::dev_malloc(&d->counters, sizeof(deque_counters));
     }
     if (e == cudaSuccess)
     {
@@ -933,9 +933,9 @@ sg_deque_destroy(sg_deque* d)
         return SG_ERR_BAD_ARG;
     }
     cudaDeviceSynchronize();
-    cudaFree(d->data);
-    cudaFree(d->seq);
-    cudaFree(d->counters);
+    sg::detail::dev_free(d->data);
+    sg::detail::dev_free(d->seq);
+    sg::detail::dev_free(d->counters);
     if (d->host != nullptr)
     {
         cudaFreeHost(d->host);

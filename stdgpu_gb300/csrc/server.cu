@@ -403,10 +403,10 @@ sg_server::grow(table_rec& t, int64_t need)
     }
     void* keys = nullptr;
     void* vals = nullptr;
-    if (cudaMalloc(&keys, static_cast<size_t>((cur + 2) * 8)) != cudaSuccess ||
-        cudaMalloc(&vals, static_cast<size_t>((cur + 2) * 8)) != cudaSuccess)
+    if (sg::detail::dev_malloc(&keys, static_cast<size_t>((cur + 2) * 8)) != cudaSuccess ||
+        sg::detail::dev_malloc(&vals, static_cast<size_t>((cur + 2) * 8)) != cudaSuccess)
     {
-        cudaFree(keys);
+        sg::detail::dev_free(keys);
         sg_unordered_destroy(nh);
         cudaGetLastError();
         return SG_ERR_OOM;
@@ -422,8 +422,8 @@ sg_server::grow(table_rec& t, int64_t need)
     {
         st = cudaDeviceSynchronize() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
     }
-    cudaFree(keys);
-    cudaFree(vals);
+    sg::detail::dev_free(keys);
+    sg::detail::dev_free(vals);
     (void)elem;
     if (st != SG_OK)
     {
@@ -743,8 +743,8 @@ sg_server_create(int32_t kind, int64_t hbm_budget_bytes, int32_t n_streams, int3
     srv->slots.resize(n_slots);
     for (auto& sl : srv->slots)
     {
-        if (cudaMalloc(&sl.d_segs, sizeof(seg_desc) * kSlotSegments) != cudaSuccess ||
-            cudaMalloc(&sl.d_prefix, sizeof(int64_t) * (kSlotSegments + 3)) != cudaSuccess ||
+        if (sg::detail::dev_malloc(&sl.d_segs, sizeof(seg_desc) * kSlotSegments) != cudaSuccess ||
+            sg::detail::dev_malloc(&sl.d_prefix, sizeof(int64_t) * (kSlotSegments + 3)) != cudaSuccess ||
             cudaMallocHost(&sl.h_segs, sizeof(seg_desc) * kSlotSegments) != cudaSuccess ||
             cudaMallocHost(&sl.h_prefix, sizeof(int64_t) * (kSlotSegments + 3)) != cudaSuccess ||
             cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess)
@@ -782,8 +782,8 @@ sg_server_destroy(sg_server* srv)
     }
     for (auto& sl : srv->slots)
     {
-        cudaFree(sl.d_segs);
-        cudaFree(sl.d_prefix);
+        sg::detail::dev_free(sl.d_segs);
+        sg::detail::dev_free(sl.d_prefix);
         if (sl.h_segs != nullptr)
         {
             cudaFreeHost(sl.h_segs);

@@ -28,6 +28,78 @@ as_stream(void* s)
     return static_cast<cudaStream_t>(s);
 }
 
+// Device storage of every container goes through one allocator: cudaMalloc / cudaFree, or the pair a
+// caller installs with sg_set_device_allocator (the reference's Allocator parameter,
+// src/stdgpu/memory.h).  `live` counts allocations not yet freed, so the pair is only swapped while none
+// made through the current one remain.
+struct device_allocator
+{
+    std::atomic<sg_device_alloc_fn> alloc{ nullptr };
+    std::atomic<sg_device_free_fn> release{ nullptr };
+    std::atomic<void*> ctx{ nullptr };
+    std::atomic<long long> live{ 0 };
+};
+
+inline device_allocator&
+allocator()
+{
+    static device_allocator a;
+    return a;
+}
+
+template <typename T>
+inline cudaError_t
+dev_malloc(T** p, size_t bytes)
+{
+    device_allocator& a = allocator();
+    const sg_device_alloc_fn f = a.alloc.load();
+    void* q = nullptr;
+    if (f != nullptr)
+    {
+        q = f(bytes > 0 ? bytes : 1, a.ctx.load());
+        if (q == nullptr)
+        {
+            *p = nullptr;
+            return cudaErrorMemoryAllocation;
+        }
+    }
+    else
+    {
+        const cudaError_t e = cudaMalloc(&q, bytes);
+        if (e != cudaSuccess)
+        {
+            *p = nullptr;
+            return e;
+        }
+    }
+    a.live.fetch_add(1);
+    *p = static_cast<T*>(q);
+    return cudaSuccess;
+}
+
+inline void
+dev_free(void* p)
+{
+    if (p == nullptr)
+    {
+        return;
+    }
+    device_allocator& a = allocator();
+    const sg_device_free_fn f = a.release.load();
+    if (f != nullptr)
+    {
+        // cudaFree waits for the device before it returns memory; a caller's release may hand the memory
+        // to other users at once, so wait the same way
+        cudaDeviceSynchronize();
+        f(p, a.ctx.load());
+    }
+    else
+    {
+        cudaFree(p);
+    }
+    a.live.fetch_sub(1);
+}
+
 // Blocks per SM at which `kernel` is resident with `threads` threads, times the SM count.
 template <typename Kernel>
 int

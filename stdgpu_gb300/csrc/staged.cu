@@ -194,7 +194,7 @@ sg_stager_create(int64_t chunk_elems, int32_t n_buffers, sg_stager** out)
     cudaError_t e = cudaGetDevice(&sg->device);
     if (e == cudaSuccess)
     {
-        e = cudaMalloc(reinterpret_cast<void**>(&sg->mem), static_cast<size_t>(sg->buffer_bytes) * n_buffers);
+        e = sg::detail::dev_malloc(reinterpret_cast<void**>(&sg->mem), static_cast<size_t>(sg->buffer_bytes) * n_buffers);
     }
     if (e == cudaSuccess)
     {
@@ -288,7 +288,7 @@ sg_stager_destroy(sg_stager* sg)
     {
         cudaStreamDestroy(sg->down);
     }
-    cudaFree(sg->mem);
+    sg::detail::dev_free(sg->mem);
     delete sg;
     return SG_OK;
 }

@@ -869,11 +869,11 @@ ensure_part_scratch(sg_unordered* t, int64_t bytes)
     {
         // a launch queued earlier may still read the old array
         SG_CUDA_TRY(cudaDeviceSynchronize());
-        cudaFree(t->part_scratch);
+        sg::detail::dev_free(t->part_scratch);
         t->part_scratch = nullptr;
         t->part_scratch_bytes = 0;
     }
-    const cudaError_t e = cudaMalloc(&t->part_scratch, static_cast<size_t>(bytes));
+    const cudaError_t e = sg::detail::dev_malloc(&t->part_scratch, static_cast<size_t>(bytes));
     if (e != cudaSuccess)
     {
         cudaGetLastError();
@@ -1107,6 +1107,30 @@ host_header(const sg_unordered* t)
 extern "C" {
 
 sg_status
+sg_set_device_allocator(sg_device_alloc_fn alloc, sg_device_free_fn release, void* ctx)
+{
+    if ((alloc == nullptr) != (release == nullptr))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    device_allocator& a = allocator();
+    if (a.live.load() != 0)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    a.alloc.store(alloc);
+    a.release.store(release);
+    a.ctx.store(ctx);
+    return SG_OK;
+}
+
+int64_t
+sg_live_device_allocations(void)
+{
+    return allocator().live.load();
+}
+
+sg_status
 sg_unordered_geometry_for(int32_t kind, int64_t capacity, sg_geometry* out)
 {
     if (!kind_ok(kind) || capacity <= 0 || out == nullptr)
@@ -1155,14 +1179,14 @@ sg_unordered_create(int32_t kind, int64_t capacity, void* stream, sg_unordered**
     t->bits = log2_exact(g.bucket_count);
     t->nchunks = (t->total + kRangeChunk - 1) / kRangeChunk;
     t->device = dev;
-    cudaError_t e = cudaMalloc(&t->slots, static_cast<size_t>((t->num_groups + 1) * kGroupBytes));
+    cudaError_t e = sg::detail::dev_malloc(&t->slots, static_cast<size_t>((t->num_groups + 1) * kGroupBytes));
     if (e == cudaSuccess)
     {
-        e = cudaMalloc(&t->hdr, sizeof(table_header));
+        e = sg::detail::dev_malloc(&t->hdr, sizeof(table_header));
     }
     if (e == cudaSuccess)
     {
-        e = cudaMalloc(&t->chunk_counts, static_cast<size_t>(t->nchunks + 1) * sizeof(unsigned int));
+        e = sg::detail::dev_malloc(&t->chunk_counts, static_cast<size_t>(t->nchunks + 1) * sizeof(unsigned int));
     }
     if (e == cudaSuccess)
     {
@@ -1198,19 +1222,19 @@ sg_unordered_destroy(sg_unordered* t)
     }
     if (t->slots != nullptr)
     {
-        cudaFree(t->slots);
+        sg::detail::dev_free(t->slots);
     }
     if (t->hdr != nullptr)
     {
-        cudaFree(t->hdr);
+        sg::detail::dev_free(t->hdr);
     }
     if (t->chunk_counts != nullptr)
     {
-        cudaFree(t->chunk_counts);
+        sg::detail::dev_free(t->chunk_counts);
     }
     if (t->part_scratch != nullptr)
     {
-        cudaFree(t->part_scratch);
+        sg::detail::dev_free(t->part_scratch);
     }
     if (t->host_hdr != nullptr)
     {
@@ -1359,7 +1383,7 @@ sg_unordered_rehash(sg_unordered* t, int64_t new_capacity, void* stream)
     char* buf = nullptr;
     const int64_t cap = n + 2;
     const int64_t kbytes = ((cap * kb + 255) / 256) * 256;
-    if (cudaMalloc(&buf, static_cast<size_t>(kbytes + cap * (mb > 0 ? mb : 1))) != cudaSuccess)
+    if (sg::detail::dev_malloc(&buf, static_cast<size_t>(kbytes + cap * (mb > 0 ? mb : 1))) != cudaSuccess)
     {
         cudaGetLastError();
         return SG_ERR_OOM;
@@ -1380,7 +1404,7 @@ sg_unordered_rehash(sg_unordered* t, int64_t new_capacity, void* stream)
     {
         st = sg_unordered_status(fresh, stream, &refused, nullptr);
     }
-    cudaFree(buf);
+    sg::detail::dev_free(buf);
     if (st != SG_OK)
     {
         if (fresh != nullptr)
