@@ -233,15 +233,31 @@ def test_device_range_slots_point_at_stored_elements():
     t.close()
 
 
-def test_clear_and_empty():
-    t = Table(O.SET_U32, 1000)
-    t.insert(np.arange(500, dtype=np.uint32))
-    t.erase(np.arange(100, dtype=np.uint32))
-    assert t.size() == 400
+@pytest.mark.parametrize("kind", range(6))
+def test_clear_and_valid_every_kind(kind):
+    """clear() / valid() / empty() after inserts, erases and out-of-band keys, for every kind, with the oracle
+    repeating the same calls (the reference's clear tests, tests/stdgpu/unordered_datastructure.inc:2450-2559)."""
+    kd = O.KEY_DTYPE[kind]
+    top = np.iinfo(kd).max
+    keys = np.concatenate([np.arange(1, 600, dtype=np.uint64), np.array([top, top - 1], np.uint64)]).astype(kd)
+    vd = O.VAL_DTYPE[kind]
+    vals = None if vd is None else (keys.astype(np.uint64) * np.uint64(5)).astype(vd)
+    t = Table(kind, 2000)
+    P = O.PortTable(kind, 2000)
+    for _ in range(2):
+        t.insert(keys, vals)
+        P.insert(keys, vals)
+        t.erase(keys[::3])
+        P.erase(keys[::3])
+        assert t.size() == P.size() and t.valid() and P.valid()
+        t.t.clear()
+        P.clear()
+        assert t.size() == 0 == P.size() and t.t.empty() and t.valid()
+        assert t.contains(keys).sum() == 0
+    assert t.insert(keys[:10], None if vals is None else vals[:10]).sum() == 10
     t.t.clear()
-    assert t.size() == 0 and t.t.empty() and t.valid()
-    assert t.contains(np.arange(500, dtype=np.uint32)).sum() == 0
-    assert t.insert(np.arange(10, dtype=np.uint32)).sum() == 10
+    t.t.clear()  # clearing an empty table
+    assert t.size() == 0 and t.valid()
     t.close()
 
 
@@ -255,7 +271,7 @@ def test_bucket_matches_reference(golden):
         sg.unordered_base.destroyDeviceObject(t)
 
 
-def test_c1_full_size_against_oracle():
+def test_set_u32_2e20_keys_against_oracle():
     """unordered_set<uint32_t>, capacity 2^21: 2^20 keys, 2^20 contains, erase of half -- against the oracle."""
     w = W.uniform_set_u32(1 << 20, seed=0)
     P = O.PortTable(O.SET_U32, 1 << 21)
