@@ -259,8 +259,9 @@ SG_API sg_status sg_unordered_contains_host(sg_unordered* table, sg_stager* stag
  * each with the geometry and behaviour of a single table, stored in one device arena.  Every batched
  * operation takes the keys of all tables concatenated, table t owning elements [offsets[t],
  * offsets[t+1]) of the input (offsets: DEVICE array of n_tables + 1 int64), and runs as one
- * persistent launch over (table, 32-key range) tiles.  No host work depends on the sizes, so a
- * sequence of batched calls can be captured in a CUDA graph. */
+ * persistent launch over (table, 32-key range) tiles.  A NULL key array (all ranges empty, as an empty
+ * tensor gives) walks no tile.  No host work depends on the sizes, so a sequence of batched calls can be
+ * captured in a CUDA graph. */
 typedef struct sg_table_batch sg_table_batch;
 
 /* capacities: HOST array of n_tables capacities (createDeviceObject(capacity) of each table). */

@@ -37,7 +37,7 @@ struct init_chunk
 
 // Prefix of tile counts: prefix[t] = sum over u < t of ceil(n_u / 32); prefix[n] = all tiles.
 __global__ void __launch_bounds__(1024)
-k_batch_tiles(const int64_t* offsets, int32_t n, int64_t* prefix)
+k_batch_tiles(const int64_t* offsets, int32_t n, int64_t* prefix, bool has_keys)
 {
     __shared__ long long part[1024];
     const int64_t per = (static_cast<int64_t>(n) + blockDim.x - 1) / blockDim.x;
@@ -46,7 +46,7 @@ k_batch_tiles(const int64_t* offsets, int32_t n, int64_t* prefix)
     long long s = 0;
     for (int64_t t = lo; t < hi; ++t)
     {
-        const int64_t cnt = offsets[t + 1] - offsets[t];
+        const int64_t cnt = has_keys ? offsets[t + 1] - offsets[t] : 0;
         s += cnt > 0 ? (cnt + 31) / 32 : 0;
     }
     part[threadIdx.x] = s;
@@ -67,7 +67,7 @@ k_batch_tiles(const int64_t* offsets, int32_t n, int64_t* prefix)
     for (int64_t t = lo; t < hi; ++t)
     {
         prefix[t] = run;
-        const int64_t cnt = offsets[t + 1] - offsets[t];
+        const int64_t cnt = has_keys ? offsets[t + 1] - offsets[t] : 0;
         run += cnt > 0 ? (cnt + 31) / 32 : 0;
     }
 }
@@ -347,7 +347,8 @@ sg_status
 dispatch_op(sg_table_batch* b, int op, const int64_t* offsets, const void* in0, const void* in1, void* out_vals,
             uint8_t* out_flags, cudaStream_t s)
 {
-    k_batch_tiles<<<1, 1024, 0, s>>>(offsets, b->n, b->prefix);
+    // a NULL key array (all ranges empty, as an empty tensor gives) walks no tile
+    k_batch_tiles<<<1, 1024, 0, s>>>(offsets, b->n, b->prefix, in0 != nullptr);
     SG_LAUNCH_CHECK();
     switch (b->kind)
     {
@@ -393,7 +394,8 @@ dispatch_init(sg_table_batch* b, cudaStream_t s)
 bool
 args_ok(const sg_table_batch* b, const void* in0, const int64_t* offsets)
 {
-    return b != nullptr && in0 != nullptr && offsets != nullptr;
+    (void)in0; // NULL keys are allowed: the call then walks no tile
+    return b != nullptr && offsets != nullptr;
 }
 
 } // namespace
@@ -608,7 +610,7 @@ sg_batch_find(sg_table_batch* b, const void* keys, const int64_t* offsets, void*
 sg_status
 sg_batch_contains(sg_table_batch* b, const void* keys, const int64_t* offsets, uint8_t* out_flags, void* stream)
 {
-    if (!args_ok(b, keys, offsets) || out_flags == nullptr)
+    if (!args_ok(b, keys, offsets) || (keys != nullptr && out_flags == nullptr))
     {
         return SG_ERR_BAD_ARG;
     }
