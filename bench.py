@@ -55,6 +55,7 @@ ERASE_FRAC = 0.25
 #   find:   8 B key in + 4 B value + 1 B flag out + 128 B home group (the value sits in the same line)
 #   erase:  8 B key in + 128 B home group + one 32 B sector written back (the erased marker)
 BYTES_PER_OP = {"insert": 16 + 128 + 32, "find": 8 + 5 + 128, "erase": 8 + 128 + 32}
+NOMINAL_HBM_GBS = 7900.0  # HBM3e nominal, reported beside the measured copy peak
 
 
 def parse_args(argv=None):
@@ -101,6 +102,28 @@ def replicas_value(ops_per_step: int, ms: float, ws: int, device) -> tuple[float
     """(whole-job Mops/s, slowest rank's ms per step): all ranks' operations over the slowest rank's time."""
     worst = slowest_rank_ms(ms, ws, device)
     return ops_per_step * ws / (worst * 1e-3) / 1e6, worst
+
+
+def link_bandwidth(host, device_buf, stream, device, reps: int = 3) -> dict:
+    """Pinned host<->device copy bandwidth of this GPU's host link (GB/s), measured on the same box as the e2e
+    step: the best of `reps` whole-buffer copies each way, CUDA events on the copying stream."""
+    import torch
+    nbytes = host.numel() * host.element_size()
+    out = {}
+    for name, dst, src in (("h2d_gbs", device_buf, host), ("d2h_gbs", host, device_buf)):
+        best = None
+        for _ in range(reps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize(device)
+            a.record(stream)
+            dst.copy_(src, non_blocking=True)
+            b.record(stream)
+            torch.cuda.synchronize(device)
+            ms = a.elapsed_time(b)
+            best = ms if best is None else min(best, ms)
+        out[name] = nbytes / (best * 1e-3) / 1e9
+    return out
 
 
 # ------------------------------------------------------------------ clocks
@@ -358,8 +381,12 @@ def native_arm(args):
         stager.close()
         h2d = pairs_h.numel() * 8 + queries_h.numel() * 8 + erase_h.numel() * 8
         d2h = vals_h.numel() * 4 + found_h.numel()
+        link = link_bandwidth(pairs_h, pairs, stream, dev)
+        # the link bound of one step: every input byte up, every result byte down, both directions at once
+        link_ms = max(h2d / link["h2d_gbs"], d2h / link["d2h_gbs"]) / 1e6
+        link.update({"bound_ms": link_ms, "frac": link_ms / e2e_ms})
         e2e = {"value": ops_per_step * ws / (e2e_ms * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "api": "sg_unordered_*_host (pipelined, 2^22-element chunks)",
+               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "api": "sg_unordered_*_host (pipelined, 2^22-element chunks)", "link": link,
                "serial_copies": {"value": ops_per_step * ws / (serial_ms * 1e-3) / 1e6, "ms_per_step": serial_ms}}
 
     # ---------------- roofline of the dominant kernel
@@ -383,7 +410,7 @@ def native_arm(args):
                      "find": "k_find", "erase": "k_part_count + k_part_cursors + k_part_scatter + k_erase_ordered "
                                                  "(partitioned bulk erase, chosen automatically at this size)"}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": dominant, "kernels": phase_kernels[dominant], "peak_source": peak_src,
+                "frac_of_nominal": achieved / NOMINAL_HBM_GBS, "traffic": traffic, "kernel": dominant, "kernels": phase_kernels[dominant], "peak_source": peak_src,
                 "bytes_per_op": BYTES_PER_OP[dominant],
                 "per_kernel": {k: {"ms": med[k], "mops": counts[k] / (med[k] * 1e-3) / 1e6,
                                    "gbs": BYTES_PER_OP[k] * counts[k] / (med[k] * 1e-3) / 1e9,

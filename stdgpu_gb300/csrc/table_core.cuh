@@ -21,6 +21,12 @@ constexpr int kThreads = 256;
 #ifndef SG_BULK_MIN_BLOCKS
 #define SG_BULK_MIN_BLOCKS 4
 #endif
+#ifndef SG_FIND_MIN_BLOCKS
+#define SG_FIND_MIN_BLOCKS SG_BULK_MIN_BLOCKS
+#endif
+#ifndef SG_ORDERED_MIN_BLOCKS
+#define SG_ORDERED_MIN_BLOCKS SG_BULK_MIN_BLOCKS
+#endif
 constexpr int kRangeChunk = 2048; // slots per block in the compaction kernels (256 threads x 8 slots)
 
 // Kernel view of a table.  Group and slot indices fit 32 bits (max_size() < 2^31), so the hot paths

@@ -350,7 +350,7 @@ constexpr int kOrderedChunk = SG_ORDERED_ITERS * kThreads;
 constexpr int kEraseChunk = SG_ERASE_ORDERED_ITERS * kThreads;
 
 template <int KIND>
-__global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
+__global__ void __launch_bounds__(kThreads, SG_ORDERED_MIN_BLOCKS)
 k_insert_ordered(dview t, const void* in0, int64_t n, unsigned long long* next_chunk)
 {
     __shared__ long long s_first;
@@ -399,7 +399,7 @@ k_insert_ordered(dview t, const void* in0, int64_t n, unsigned long long* next_c
 
 // Bulk erase over partitioned keys, chunks taken in order as in k_insert_ordered.
 template <int KIND>
-__global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
+__global__ void __launch_bounds__(kThreads, SG_ORDERED_MIN_BLOCKS)
 k_erase_ordered(dview t, const void* keys, int64_t n, unsigned long long* next_chunk)
 {
     __shared__ long long s_first;
@@ -464,7 +464,7 @@ k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags, const uint64_t
 
 // Bulk find / contains (device-only find/contains in the reference, :619-706).
 template <int KIND, bool WANT_VALUES>
-__global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
+__global__ void __launch_bounds__(kThreads, SG_FIND_MIN_BLOCKS)
 k_find(dview t, const void* keys, int64_t n, void* out_vals, uint8_t* out_found, const uint64_t* hashes)
 {
     const tile_lanes L;
