@@ -451,27 +451,69 @@ public:
 } // namespace stdgpu
 
 #include "custom_key.cuh"
+#include "wide_key.cuh"
+
+namespace stdgpu
+{
+namespace detail
+{
+// Which storage an element type takes: the library's precompiled kinds (integer keys with the identity hash
+// and 4/8-byte unsigned mapped integers), the word-keyed custom path (any trivially copyable key of at most 8
+// bytes with a trivially copyable 4/8-byte mapped type), or the wide path of wide_key.cuh (everything else:
+// keys of 9-16 bytes, other mapped types, types with destructors).
+template <typename T>
+struct mapped_fits_word
+  : std::integral_constant<bool, (sizeof(T) == 4 || sizeof(T) == 8) && std::is_trivially_copyable<T>::value>
+{
+};
+template <>
+struct mapped_fits_word<void> : std::true_type
+{
+};
+
+template <typename Key, typename T, typename Hash>
+struct is_native_table
+  : std::integral_constant<bool, is_native_key<Key, Hash>::value &&
+                                         (std::is_void<T>::value || std::is_same<T, std::uint32_t>::value ||
+                                          std::is_same<T, std::uint64_t>::value)>
+{
+};
+
+template <typename Key, typename T>
+struct fits_word_table
+  : std::integral_constant<bool, sizeof(Key) <= 8 && std::is_trivially_copyable<Key>::value &&
+                                         mapped_fits_word<T>::value>
+{
+};
+} // namespace detail
+} // namespace stdgpu
 
 namespace stdgpu
 {
 
-// stdgpu::unordered_map<Key, T, Hash>: integer keys with the default hash use the library's precompiled
-// kernels; any other key type of at most 8 bytes (short3, vec3int16, packed coordinates) with a user
-// Hash goes through the custom-key path of custom_key.cuh.
+// stdgpu::unordered_map<Key, T, Hash>: integer keys with the default hash and integer mapped values use the
+// library's precompiled kernels; other keys of at most 8 bytes (short3, vec3int16, packed coordinates) with a
+// user Hash and a 4/8-byte mapped type go through the word-keyed path of custom_key.cuh; every other element
+// type (a 3 x int32 key, an empty or 16-byte mapped type, a type with a destructor) through wide_key.cuh.
 template <typename Key, typename T, typename Hash = hash<Key>, typename KeyEqual = equal_to<Key>>
 class unordered_map
-  : public std::conditional_t<detail::is_native_key<Key, Hash>::value,
-                              detail::native_map<Key, T, unordered_map<Key, T, Hash, KeyEqual>>,
-                              detail::custom_map<Key, T, Hash, unordered_map<Key, T, Hash, KeyEqual>>>
+  : public std::conditional_t<
+            detail::is_native_table<Key, T, Hash>::value,
+            detail::native_map<Key, T, unordered_map<Key, T, Hash, KeyEqual>>,
+            std::conditional_t<detail::fits_word_table<Key, T>::value,
+                               detail::custom_map<Key, T, Hash, unordered_map<Key, T, Hash, KeyEqual>>,
+                               detail::wide_map<Key, T, Hash, unordered_map<Key, T, Hash, KeyEqual>>>>
 {
 };
 
 // stdgpu::unordered_set<Key, Hash>
 template <typename Key, typename Hash = hash<Key>, typename KeyEqual = equal_to<Key>>
 class unordered_set
-  : public std::conditional_t<detail::is_native_key<Key, Hash>::value,
+  : public std::conditional_t<detail::is_native_table<Key, void, Hash>::value,
                               detail::native_set<Key, unordered_set<Key, Hash, KeyEqual>>,
-                              detail::custom_set<Key, Hash, unordered_set<Key, Hash, KeyEqual>>>
+                              std::conditional_t<detail::fits_word_table<Key, void>::value,
+                                                 detail::custom_set<Key, Hash, unordered_set<Key, Hash, KeyEqual>>,
+                                                 detail::wide_set<Key, Hash, unordered_set<Key, Hash, KeyEqual>>>>
 {
 };
 

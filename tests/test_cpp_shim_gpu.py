@@ -12,6 +12,7 @@ from stdgpu_gb300 import build as B
 ROOT = Path(__file__).resolve().parents[1]
 SRC = ROOT / "tests" / "cpp" / "shim_test.cu"
 CUSTOM = ROOT / "tests" / "cpp" / "custom_key_test.cu"
+WIDE = ROOT / "tests" / "cpp" / "wide_key_test.cu"
 OUT = ROOT / "tests" / "cpp" / "_build"
 
 
@@ -53,6 +54,24 @@ def test_custom_key_types_with_user_hash_on_gpu():
     neighbour-update kernel, all against std::unordered_set / std::unordered_map."""
     stdgpu_gb300.load()
     exe = _compile(src=CUSTOM)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "ALL PASS" in r.stdout
+
+
+def test_wide_key_program_compiles_for_sm103a():
+    stdgpu_gb300.load()
+    _compile(src=WIDE)
+
+
+@pytest.mark.gpu
+def test_wide_keys_and_nontrivial_types_on_gpu():
+    """The reference's nontrivial-type table (3 x int32 key with a destructor, empty mapped type) and its
+    clear_nontrivial scenario, 16-byte keys on every bit pattern, 16-byte mapped values, mapped destructors
+    counted through erase / clear / destroy, refusal at max_size(), against the host containers."""
+    stdgpu_gb300.load()
+    exe = _compile(src=WIDE)
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
