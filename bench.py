@@ -405,10 +405,11 @@ def native_arm(args):
             traffic = json.loads(tf.read_text()).get(dominant)
         except (ValueError, AttributeError):
             traffic = None
-    phase_kernels = {"insert": "k_part_count + k_part_cursors + k_part_scatter + k_insert_ordered (partitioned bulk "
-                               "insert, chosen automatically at this size)",
-                     "find": "k_find", "erase": "k_part_count + k_part_cursors + k_part_scatter + k_erase_ordered "
-                                                 "(partitioned bulk erase, chosen automatically at this size)"}
+    phase_kernels = {"insert": "k_part_scatter + k_insert_ordered (+ the gated direct k_insert, which exits at once "
+                               "unless the scatter left elements out); partitioned bulk insert, chosen automatically "
+                               "at this size",
+                     "find": "k_find", "erase": "k_part_scatter + k_erase_ordered (+ the gated direct k_erase); "
+                                                 "partitioned bulk erase, chosen automatically at this size"}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "frac_of_nominal": achieved / NOMINAL_HBM_GBS, "traffic": traffic, "kernel": dominant, "kernels": phase_kernels[dominant], "peak_source": peak_src,
                 "bytes_per_op": BYTES_PER_OP[dominant],

@@ -82,8 +82,14 @@ k_init(dview t)
 // Bulk insert: src/stdgpu/impl/unordered_base_detail.cuh:996-1017 (insert_value :470-495).
 template <int KIND, bool AOS>
 __global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
-k_insert(dview t, const void* in0, const void* in1, int64_t n, uint8_t* out_flags, const uint64_t* hashes)
+k_insert(dview t, const void* in0, const void* in1, int64_t n, uint8_t* out_flags, const uint64_t* hashes,
+         const unsigned int* gate)
 {
+    // a gated launch (the fallback of a partitioned insert) runs only when its gate word is set
+    if (gate != nullptr && *gate == 0u)
+    {
+        return;
+    }
     const tile_lanes L;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
@@ -185,61 +191,30 @@ pack_element(typename kind_consts<KIND>::K key, typename kind_consts<KIND>::V va
     }
 }
 
-// Pass 1: how many keys fall in each partition.
-template <int KIND, bool AOS>
-__global__ void __launch_bounds__(kThreads)
-k_part_count(const void* in0, int64_t n, int bits, int shift, int parts, unsigned int* hist)
+// Scratch layout of a partitioned call: partition p owns elements [p * cap, (p + 1) * cap); elements past
+// a partition's capacity go to the overflow region [parts * cap, parts * cap + ocap); an element that finds
+// no room there either is not stored and sets *lost, and the direct kernel then runs over the whole input
+// (inserting or erasing what is already in or out again changes nothing).  cap and ocap are multiples of
+// the ordered kernel's chunk, so a chunk never straddles two regions.
+struct part_layout
 {
-    __shared__ unsigned int h[kPartMax];
-    for (int p = threadIdx.x; p < parts; p += blockDim.x)
-    {
-        h[p] = 0u;
-    }
-    __syncthreads();
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
-    {
-        atomicAdd(&h[part_of<KIND>(load_key<KIND, AOS>(in0, i), bits, shift)], 1u);
-    }
-    __syncthreads();
-    for (int p = threadIdx.x; p < parts; p += blockDim.x)
-    {
-        if (h[p] != 0u)
-        {
-            atomicAdd(&hist[p], h[p]);
-        }
-    }
-}
+    int parts;
+    int shift;          // part = bucket >> shift
+    unsigned int cap;   // elements per partition
+    unsigned int ocap;  // elements of the overflow region
+    unsigned int* fill; // [kPartMax] elements offered to each partition (may exceed cap)
+    unsigned int* ofill; // elements offered to the overflow region (may exceed ocap)
+    unsigned int* lost;  // set when an element found no room
+};
 
-// Exclusive scan of the partition sizes into the write cursors (one block, parts <= blockDim.x).
-__global__ void
-k_part_cursors(const unsigned int* hist, int parts, unsigned int* cursor)
-{
-    __shared__ unsigned int v[kPartMax];
-    const int p = threadIdx.x;
-    v[p] = p < parts ? hist[p] : 0u;
-    __syncthreads();
-    for (int d = 1; d < kPartMax; d <<= 1)
-    {
-        const unsigned int x = p >= d ? v[p - d] : 0u;
-        __syncthreads();
-        v[p] += x;
-        __syncthreads();
-    }
-    if (p < parts)
-    {
-        cursor[p] = v[p] - hist[p];
-    }
-}
-
-// Pass 2: each block takes kPartPer x kThreads elements, ranks them per partition in shared memory,
-// reserves one range per partition, sorts the elements by partition in shared memory and writes each
-// partition's run with consecutive threads, so stores reach L2 as whole lines rather than one request
-// per element (random small writes cost as many requests as random line reads).
+// One pass over the input: each block takes kPartPer x kThreads elements, ranks them per partition in
+// shared memory, reserves one range per partition (and one in the overflow region for what a partition
+// has no room for), sorts the elements by partition in shared memory and writes each partition's run with
+// consecutive threads, so stores reach L2 as whole lines rather than one request per element (random small
+// writes cost as many requests as random line reads).
 template <int KIND, bool AOS>
-__global__ void __launch_bounds__(kThreads)
-k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, int shift, int parts, unsigned int* cursor,
-               void* out)
+__global__ void __launch_bounds__(kThreads, 6)
+k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, part_layout pl, void* out)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
@@ -251,6 +226,7 @@ k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, int shift,
     __shared__ unsigned int cnt[kPartMax];
     __shared__ unsigned int loff[kPartMax];
     __shared__ unsigned int base[kPartMax];
+    __shared__ unsigned int obase[kPartMax];
     E* dst = static_cast<E*>(out);
     const int lane = threadIdx.x & 31;
     for (int64_t tile = static_cast<int64_t>(blockIdx.x) * kTileElems; tile < n;
@@ -276,7 +252,7 @@ k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, int shift,
                 V val;
                 load_input<KIND, AOS>(in0, in1, i, key, val);
                 elem[j] = pack_element<KIND>(key, val);
-                pid[j] = part_of<KIND>(key, bits, shift);
+                pid[j] = part_of<KIND>(key, bits, pl.shift);
                 rank[j] = atomicAdd(&cnt[pid[j]], 1u);
             }
         }
@@ -309,9 +285,22 @@ k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, int shift,
                 run += cnt[lane * kPerLane + k];
             }
         }
-        for (int p = threadIdx.x; p < parts; p += blockDim.x)
+        for (int p = threadIdx.x; p < pl.parts; p += blockDim.x)
         {
-            base[p] = cnt[p] != 0u ? atomicAdd(&cursor[p], cnt[p]) : 0u;
+            const unsigned int c = cnt[p];
+            unsigned int b = 0u;
+            unsigned int ob = 0u;
+            if (c != 0u)
+            {
+                b = atomicAdd(&pl.fill[p], c);
+                const unsigned int room = b < pl.cap ? pl.cap - b : 0u;
+                if (c > room)
+                {
+                    ob = atomicAdd(pl.ofill, c - room);
+                }
+            }
+            base[p] = b;
+            obase[p] = ob;
         }
         __syncthreads();
 #pragma unroll
@@ -330,7 +319,25 @@ k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, int shift,
         for (int e = threadIdx.x; e < count; e += kThreads)
         {
             const unsigned int p = spid[e];
-            dst[base[p] + (e - loff[p])] = stage[e];
+            const unsigned int r = static_cast<unsigned int>(e) - loff[p];
+            const unsigned int b = base[p];
+            const unsigned int room = b < pl.cap ? pl.cap - b : 0u;
+            if (r < room)
+            {
+                dst[static_cast<int64_t>(p) * pl.cap + b + r] = stage[e];
+            }
+            else
+            {
+                const unsigned int o = obase[p] + (r - room);
+                if (o < pl.ocap)
+                {
+                    dst[static_cast<int64_t>(pl.parts) * pl.cap + o] = stage[e];
+                }
+                else
+                {
+                    *pl.lost = 1u;
+                }
+            }
         }
         __syncthreads(); // the counters and the stage are rewritten by the next tile
     }
@@ -349,11 +356,46 @@ constexpr int kOrderedChunk = SG_ORDERED_ITERS * kThreads;
 #endif
 constexpr int kEraseChunk = SG_ERASE_ORDERED_ITERS * kThreads;
 
+// Elements [first, last) of ordered chunk c of a partitioned scratch array: the chunks of partition 0, then
+// of partition 1, ..., then of the overflow region; a chunk past its partition's fill is empty.  False once
+// c is past the last element.
+template <int CHUNK>
+SG_D bool
+ordered_chunk(const part_layout& pl, unsigned long long c, int64_t& first, int64_t& last)
+{
+    const unsigned long long per = pl.cap / CHUNK;
+    const unsigned long long in_parts = per * static_cast<unsigned long long>(pl.parts);
+    int64_t origin;
+    unsigned long long off;
+    unsigned int fill;
+    if (c < in_parts)
+    {
+        const unsigned long long p = c / per;
+        off = (c - p * per) * CHUNK;
+        origin = static_cast<int64_t>(p) * pl.cap;
+        fill = min(pl.fill[p], pl.cap);
+    }
+    else
+    {
+        // the overflow region is the last: its first empty chunk ends the walk
+        off = (c - in_parts) * CHUNK;
+        origin = static_cast<int64_t>(pl.parts) * pl.cap;
+        fill = min(*pl.ofill, pl.ocap);
+        if (off >= fill)
+        {
+            return false;
+        }
+    }
+    first = origin + static_cast<int64_t>(off);
+    last = off >= fill ? first : origin + static_cast<int64_t>(min(off + CHUNK, static_cast<unsigned long long>(fill)));
+    return true;
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, SG_ORDERED_MIN_BLOCKS)
-k_insert_ordered(dview t, const void* in0, int64_t n, unsigned long long* next_chunk)
+k_insert_ordered(dview t, const void* in0, part_layout pl, unsigned long long* next_chunk)
 {
-    __shared__ long long s_first;
+    __shared__ unsigned long long s_claim;
     const tile_lanes L;
     const int warp = threadIdx.x >> 5;
     step_counts c;
@@ -368,12 +410,13 @@ k_insert_ordered(dview t, const void* in0, int64_t n, unsigned long long* next_c
     {
         if (threadIdx.x == 0)
         {
-            s_first = static_cast<long long>(claimed) * kOrderedChunk;
+            s_claim = claimed;
         }
         __syncthreads();
-        const int64_t first = s_first;
+        int64_t first, last;
+        const bool more = ordered_chunk<kOrderedChunk>(pl, s_claim, first, last);
         __syncthreads();
-        if (first >= n)
+        if (!more)
         {
             break;
         }
@@ -381,7 +424,6 @@ k_insert_ordered(dview t, const void* in0, int64_t n, unsigned long long* next_c
         {
             claimed = atomicAdd(next_chunk, 1ull);
         }
-        const int64_t last = first + kOrderedChunk < n ? first + kOrderedChunk : n;
         for (int64_t base = first + warp * 32; base < last; base += kThreads)
         {
             const int64_t i = base + L.lane;
@@ -400,9 +442,9 @@ k_insert_ordered(dview t, const void* in0, int64_t n, unsigned long long* next_c
 // Bulk erase over partitioned keys, chunks taken in order as in k_insert_ordered.
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, SG_ORDERED_MIN_BLOCKS)
-k_erase_ordered(dview t, const void* keys, int64_t n, unsigned long long* next_chunk)
+k_erase_ordered(dview t, const void* keys, part_layout pl, unsigned long long* next_chunk)
 {
-    __shared__ long long s_first;
+    __shared__ unsigned long long s_claim;
     const tile_lanes L;
     const int warp = threadIdx.x >> 5;
     step_counts c;
@@ -417,12 +459,13 @@ k_erase_ordered(dview t, const void* keys, int64_t n, unsigned long long* next_c
     {
         if (threadIdx.x == 0)
         {
-            s_first = static_cast<long long>(claimed) * kEraseChunk;
+            s_claim = claimed;
         }
         __syncthreads();
-        const int64_t first = s_first;
+        int64_t first, last;
+        const bool more = ordered_chunk<kEraseChunk>(pl, s_claim, first, last);
         __syncthreads();
-        if (first >= n)
+        if (!more)
         {
             break;
         }
@@ -430,7 +473,6 @@ k_erase_ordered(dview t, const void* keys, int64_t n, unsigned long long* next_c
         {
             claimed = atomicAdd(next_chunk, 1ull);
         }
-        const int64_t last = first + kEraseChunk < n ? first + kEraseChunk : n;
         for (int64_t base = first + warp * 32; base < last; base += kThreads)
         {
             const int64_t i = base + L.lane;
@@ -445,8 +487,12 @@ k_erase_ordered(dview t, const void* keys, int64_t n, unsigned long long* next_c
 // Bulk erase: src/stdgpu/impl/unordered_base_detail.cuh:1045-1066 (erase_from_key :497-522).
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
-k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags, const uint64_t* hashes)
+k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags, const uint64_t* hashes, const unsigned int* gate)
 {
+    if (gate != nullptr && *gate == 0u)
+    {
+        return;
+    }
     const tile_lanes L;
     const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
@@ -885,10 +931,12 @@ ensure_part_scratch(sg_unordered* t, int64_t bytes)
 }
 
 // Partitions n input elements into the table's scratch array as PKIND's value_type elements (a set kind
-// gives bare keys); returns the chunk counter of the ordered kernel that follows, zeroed.
-template <int PKIND, bool AOS>
+// gives bare keys), in one pass: each partition gets room for its mean share plus 1/16 and two chunks, the
+// overflow region n/16 plus one scatter tile.  Returns the layout and the ordered kernel's chunk counter,
+// both zeroed.
+template <int PKIND, bool AOS, int CHUNK>
 sg_status
-partition_into_scratch(sg_unordered* t, const void* in0, const void* in1, int64_t n, cudaStream_t s,
+partition_into_scratch(sg_unordered* t, const void* in0, const void* in1, int64_t n, cudaStream_t s, part_layout* pl,
                        unsigned long long** next_chunk)
 {
     const int parts = partitions_for(t);
@@ -897,26 +945,26 @@ partition_into_scratch(sg_unordered* t, const void* in0, const void* in1, int64_
     {
         --shift;
     }
-    const int64_t elems = ((n * kind_consts<PKIND>::slot_bytes + 255) / 256) * 256;
-    sg_status st = ensure_part_scratch(t, elems + 2 * kPartMax * static_cast<int64_t>(sizeof(unsigned int)) + 256);
+    const auto round_up = [](int64_t x, int64_t m) { return (x + m - 1) / m * m; };
+    const int64_t mean = (n + parts - 1) / parts;
+    const int64_t cap = round_up(mean + mean / 16 + 2 * CHUNK, CHUNK);
+    const int64_t ocap = round_up(n / 16 + kPartPer * kThreads, CHUNK);
+    const int64_t ebytes = round_up((parts * cap + ocap) * kind_consts<PKIND>::slot_bytes, 256);
+    constexpr int64_t kControlBytes = 2048; // fill[kPartMax], ofill, lost, then the 8-byte chunk counter
+    sg_status st = ensure_part_scratch(t, ebytes + kControlBytes);
     if (st != SG_OK)
     {
         return st;
     }
-    auto* hist = reinterpret_cast<unsigned int*>(t->part_scratch + elems);
-    unsigned int* cursor = hist + kPartMax;
-    // hist, cursor and the chunk counter of the ordered kernel start at zero
-    SG_CUDA_TRY(cudaMemsetAsync(hist, 0, 2 * kPartMax * sizeof(unsigned int) + 256, s));
-    static const int g_count = persistent_grid(k_part_count<PKIND, AOS>, kThreads);
-    k_part_count<PKIND, AOS><<<grid_for(n, kThreads, g_count), kThreads, 0, s>>>(in0, n, t->bits, shift, parts, hist);
-    SG_LAUNCH_CHECK();
-    k_part_cursors<<<1, kPartMax, 0, s>>>(hist, parts, cursor);
-    SG_LAUNCH_CHECK();
+    auto* control = reinterpret_cast<unsigned int*>(t->part_scratch + ebytes);
+    SG_CUDA_TRY(cudaMemsetAsync(control, 0, kControlBytes, s));
+    *pl = part_layout{ parts,   shift,          static_cast<unsigned int>(cap), static_cast<unsigned int>(ocap),
+                       control, control + kPartMax, control + kPartMax + 1 };
+    *next_chunk = reinterpret_cast<unsigned long long*>(control + kPartMax + 2);
     static const int g_scatter = persistent_grid(k_part_scatter<PKIND, AOS>, kThreads);
     k_part_scatter<PKIND, AOS><<<grid_for(n, kThreads * kPartPer, g_scatter), kThreads, 0, s>>>(
-            in0, in1, n, t->bits, shift, parts, cursor, t->part_scratch);
+            in0, in1, n, t->bits, *pl, t->part_scratch);
     SG_LAUNCH_CHECK();
-    *next_chunk = reinterpret_cast<unsigned long long*>(cursor + kPartMax);
     return SG_OK;
 }
 
@@ -946,38 +994,41 @@ struct do_insert
     run(sg_unordered* t, const void* in0, const void* in1, bool aos, int64_t n, uint8_t* flags, cudaStream_t s,
         const uint64_t* hashes = nullptr)
     {
+        part_layout pl{};
         unsigned long long* next_chunk = nullptr;
         sg_status st = SG_ERR_OOM;
         if (hashes == nullptr && use_partitioned_insert(t, n, flags))
         {
-            st = aos ? partition_into_scratch<KIND, true>(t, in0, in1, n, s, &next_chunk)
-                     : partition_into_scratch<KIND, false>(t, in0, in1, n, s, &next_chunk);
+            st = aos ? partition_into_scratch<KIND, true, kOrderedChunk>(t, in0, in1, n, s, &pl, &next_chunk)
+                     : partition_into_scratch<KIND, false, kOrderedChunk>(t, in0, in1, n, s, &pl, &next_chunk);
             if (st != SG_OK && st != SG_ERR_OOM)
             {
                 return st;
             }
         }
-        // without room for the scratch array the direct kernel does the same insert
+        // the direct kernel: without room for the scratch array it does the whole insert; after a partitioned
+        // insert it is gated on the scatter having left elements out
+        const unsigned int* gate = nullptr;
         if (st == SG_OK)
         {
             static const int max_grid = persistent_grid(k_insert_ordered<KIND>, kThreads);
             k_insert_ordered<KIND><<<grid_for(n, kOrderedChunk, max_grid), kThreads, 0, s>>>(view_of(t),
-                                                                                            t->part_scratch, n,
+                                                                                            t->part_scratch, pl,
                                                                                             next_chunk);
             SG_LAUNCH_CHECK();
-            return SG_OK;
+            gate = pl.lost;
         }
         if (aos)
         {
             static const int max_grid = persistent_grid(k_insert<KIND, true>, kThreads);
             k_insert<KIND, true><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), in0, in1, n, flags,
-                                                                                     hashes);
+                                                                                     hashes, gate);
         }
         else
         {
             static const int max_grid = persistent_grid(k_insert<KIND, false>, kThreads);
             k_insert<KIND, false><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), in0, in1, n,
-                                                                                      flags, hashes);
+                                                                                      flags, hashes, gate);
         }
         SG_LAUNCH_CHECK();
         return SG_OK;
@@ -990,26 +1041,28 @@ struct do_erase
     static sg_status
     run(sg_unordered* t, const void* keys, int64_t n, uint8_t* flags, cudaStream_t s, const uint64_t* hashes = nullptr)
     {
+        part_layout pl{};
         unsigned long long* next_chunk = nullptr;
         sg_status st = SG_ERR_OOM;
         if (hashes == nullptr && use_partitioned_erase(t, n, flags))
         {
-            st = partition_into_scratch<keys_kind<KIND>, false>(t, keys, nullptr, n, s, &next_chunk);
+            st = partition_into_scratch<keys_kind<KIND>, false, kEraseChunk>(t, keys, nullptr, n, s, &pl, &next_chunk);
             if (st != SG_OK && st != SG_ERR_OOM)
             {
                 return st;
             }
         }
+        const unsigned int* gate = nullptr;
         if (st == SG_OK)
         {
             static const int g_ordered = persistent_grid(k_erase_ordered<KIND>, kThreads);
             k_erase_ordered<KIND><<<grid_for(n, kEraseChunk, g_ordered), kThreads, 0, s>>>(view_of(t), t->part_scratch,
-                                                                                           n, next_chunk);
+                                                                                           pl, next_chunk);
             SG_LAUNCH_CHECK();
-            return SG_OK;
+            gate = pl.lost;
         }
         static const int max_grid = persistent_grid(k_erase<KIND>, kThreads);
-        k_erase<KIND><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n, flags, hashes);
+        k_erase<KIND><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n, flags, hashes, gate);
         SG_LAUNCH_CHECK();
         return SG_OK;
     }
