@@ -295,6 +295,17 @@ def native_arm(args):
         if ev is not None:
             ev[4].record(stream)
 
+    # the random-read ceiling of this GPU's memory, on a buffer the size of the table (untimed, before the run)
+    from ctypes import byref, c_double
+    table_bytes = int(table.geometry().storage_bytes)
+    rate = c_double(0.0)
+    ceiling = None
+    if lib.sg_measure_random_reads(table_bytes, n, 128, sp, byref(rate)) == 0 and rate.value > 0:
+        ceiling = {"reads_per_s": rate.value, "unit_bytes": 128, "buffer_bytes": table_bytes,
+                   "note": "random 128-byte reads per second of this GPU's memory (sg_measure_random_reads); "
+                           "32- and 64-byte reads complete at the same rate, so a probe kernel that reads one "
+                           "group line per key is bound by this count, not by bytes"}
+
     # correctness guard on the timed configuration (one untimed pass)
     step()
     torch.cuda.synchronize(dev)
@@ -417,6 +428,10 @@ def native_arm(args):
                                    "gbs": BYTES_PER_OP[k] * counts[k] / (med[k] * 1e-3) / 1e9,
                                    "frac": BYTES_PER_OP[k] * counts[k] / (med[k] * 1e-3) / 1e9 / peak}
                                for k in counts}}
+    if ceiling is not None:
+        # keys (queries) per second of each phase against the random-read ceiling: one group line per key
+        ceiling["per_kernel_frac"] = {k: counts[k] / (med[k] * 1e-3) / ceiling["reads_per_s"] for k in counts}
+        roofline["access_ceiling"] = ceiling
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:

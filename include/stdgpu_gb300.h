@@ -455,6 +455,14 @@ SG_API sg_status sg_bitset_count_noalloc(const uint32_t* blocks, int64_t nbits, 
 
 /* ---------------- library ---------------- */
 
+/* Random-read ceiling of the device memory (a diagnostic with no counterpart in the reference): `reads`
+ * reads of unit_bytes (32, 64 or 128) each at random positions of a freshly allocated device buffer of
+ * buffer_bytes (>= 1 MiB; make it far larger than L2), timed with events on `stream` (best of three after
+ * a warm-up); the rate in reads per second goes to out_reads_per_s.  The table kernels read one random
+ * 128-byte group line per key, so this rate bounds them alongside the copy bandwidth.  Synchronises. */
+SG_API sg_status sg_measure_random_reads(int64_t buffer_bytes, int64_t reads, int32_t unit_bytes, void* stream,
+                                         double* out_reads_per_s);
+
 /* Number of kernels this library has launched since load (all entry points). */
 SG_API int64_t sg_kernel_launch_count(void);
 /* Human-readable text for a status. */

@@ -154,6 +154,7 @@ SIGNATURES = {
     "sg_deque_view_of": (c_int32, [c_void_p, POINTER(sg_deque_view)]),
     "sg_bitset_count": (c_int32, [c_void_p, c_int64, c_void_p, POINTER(c_int64)]),
     "sg_bitset_count_noalloc": (c_int32, [c_void_p, c_int64, c_void_p, c_void_p]),
+    "sg_measure_random_reads": (c_int32, [c_int64, c_int64, c_int32, c_void_p, c_void_p]),
     "sg_kernel_launch_count": (c_int64, []),
     "sg_status_string": (c_char_p, [c_int32]),
 }

@@ -22,7 +22,7 @@ INCLUDE = ROOT / "include"
 LIB_NAME = "libstdgpu_gb300.so"
 
 # translation units of the product library
-SOURCES = ["unordered.cu", "containers.cu", "batch.cu", "server.cu", "staged.cu", "snapshot.cu"]
+SOURCES = ["unordered.cu", "containers.cu", "batch.cu", "server.cu", "staged.cu", "snapshot.cu", "diag.cu"]
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
