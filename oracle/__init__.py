@@ -43,6 +43,16 @@ VAL_DTYPE[MAP_VEC3I16_U32] = np.uint32
 # the word-keyed kinds holding them (8-byte key words)
 WORD_KIND = {SET_VEC3I16: SET_U64, MAP_VEC3I16_U32: MAP_U64_U32}
 
+# A 12-byte key (3 x int32, with a user-declared destructor in oracle/ref_driver.cpp, the shape of the
+# reference's nontrivial-type tests) under the same spatial hash; the GPU side holds it in the wide tables
+# of the C++ API (16-byte key words).  Only RefTable takes these kinds.
+SET_VEC3I32, MAP_VEC3I32_U64 = 8, 9
+VEC3I32 = np.dtype([("x", "<i4"), ("y", "<i4"), ("z", "<i4")])
+KEY_DTYPE[SET_VEC3I32] = VEC3I32
+KEY_DTYPE[MAP_VEC3I32_U64] = VEC3I32
+VAL_DTYPE[SET_VEC3I32] = None
+VAL_DTYPE[MAP_VEC3I32_U64] = np.uint64
+
 
 def vec3i16_words(keys: np.ndarray) -> np.ndarray:
     """Object bytes of each 6-byte key, zero-padded to a little-endian 64-bit word."""
@@ -59,14 +69,73 @@ def words_vec3i16(words: np.ndarray) -> np.ndarray:
     return k
 
 
+def fibonacci_buckets(hashes: np.ndarray, bucket_count: int) -> np.ndarray:
+    """The reference's fibonacci_hashing of each hash (src/stdgpu/impl/unordered_base_detail.cuh:56-85)."""
+    h = np.ascontiguousarray(hashes, dtype=np.uint64)
+    bits = int(bucket_count).bit_length() - 1
+    if bits <= 0:
+        return np.zeros(len(h), np.uint64)
+    drop = np.uint64(64 - bits)
+    with np.errstate(over="ignore"):
+        return ((h ^ (h >> drop)) * np.uint64(11400714819323198485)) >> drop
+
+
 def spatial_hash(keys: np.ndarray) -> np.ndarray:
-    """(size_t(x) * 73856093) ^ (size_t(y) * 19349669) ^ (size_t(z) * 83492791), coordinates sign-extended."""
-    k = np.ascontiguousarray(keys, dtype=VEC3I16)
+    """(size_t(x) * 73856093) ^ (size_t(y) * 19349669) ^ (size_t(z) * 83492791), coordinates sign-extended;
+    keys of VEC3I16 or VEC3I32."""
+    k = np.ascontiguousarray(keys, dtype=keys.dtype if keys.dtype == VEC3I32 else VEC3I16)
     with np.errstate(over="ignore"):
         hx = k["x"].astype(np.int64).astype(np.uint64) * np.uint64(73856093)
         hy = k["y"].astype(np.int64).astype(np.uint64) * np.uint64(19349669)
         hz = k["z"].astype(np.int64).astype(np.uint64) * np.uint64(83492791)
     return hx ^ hy ^ hz
+
+class SeqKeyTable:
+    """Element-by-element restatement of the reference's bulk insert / erase / find for keys of any numpy
+    record type (here the 12-byte VEC3I32): with one thread the reference processes a bulk call in input
+    order, so an insert succeeds for the first copy of a key that is not stored yet
+    (src/stdgpu/impl/unordered_base_detail.cuh:708-809, insert_value :996-1017) and an erase for the first
+    copy of a stored key (:811-913, erase_from_key :1045-1066); a map keeps the value of the copy that was
+    inserted.  Pure Python: small cases only."""
+
+    def __init__(self, capacity: int, max_size: int):
+        self.capacity = capacity
+        self.max_size = max_size
+        self.items: dict[bytes, object] = {}
+
+    def insert(self, keys: np.ndarray, vals=None) -> np.ndarray:
+        flags = np.zeros(len(keys), np.uint8)
+        raw = np.ascontiguousarray(keys).view(np.uint8).reshape(len(keys), -1)
+        for i in range(len(keys)):
+            b = raw[i].tobytes()
+            if b not in self.items and len(self.items) < self.max_size:
+                self.items[b] = None if vals is None else vals[i]
+                flags[i] = 1
+        return flags
+
+    def erase(self, keys: np.ndarray) -> np.ndarray:
+        flags = np.zeros(len(keys), np.uint8)
+        raw = np.ascontiguousarray(keys).view(np.uint8).reshape(len(keys), -1)
+        for i in range(len(keys)):
+            b = raw[i].tobytes()
+            if b in self.items:
+                del self.items[b]
+                flags[i] = 1
+        return flags
+
+    def find(self, keys: np.ndarray):
+        raw = np.ascontiguousarray(keys).view(np.uint8).reshape(len(keys), -1)
+        found = np.array([raw[i].tobytes() in self.items for i in range(len(keys))], np.uint8)
+        vals = [self.items.get(raw[i].tobytes()) for i in range(len(keys))]
+        return vals, found
+
+    def size(self) -> int:
+        return len(self.items)
+
+    def keys(self, dtype) -> np.ndarray:
+        buf = b"".join(self.items.keys())
+        return np.frombuffer(buf, dtype=dtype).copy() if buf else np.zeros(0, dtype)
+
 
 _port = None
 _ref = None

@@ -44,6 +44,8 @@ enum kind_t
     MAP_U32_U64 = 5,
     SET_VEC3I16 = 6,     // unordered_set<vec3i16, spatial_hash>
     MAP_VEC3I16_U32 = 7, // unordered_map<vec3i16, uint32_t, spatial_hash>
+    SET_VEC3I32 = 8,     // unordered_set<vec3i32, spatial_hash>
+    MAP_VEC3I32_U64 = 9, // unordered_map<vec3i32, uint64_t, spatial_hash>
 };
 
 // A custom key type and hash as the reference's users write them (the reference's own tests use a
@@ -63,10 +65,37 @@ operator==(const vec3i16& a, const vec3i16& b)
     return a.x == b.x && a.y == b.y && a.z == b.z;
 }
 
+// A 12-byte key with a user-declared destructor, the shape of the reference's nontrivial-type tests
+// (tests/stdgpu/unordered_map.inc:132-161).
+struct vec3i32
+{
+    vec3i32() = default;
+    vec3i32(const vec3i32&) = default;
+    vec3i32& operator=(const vec3i32&) = default;
+    ~vec3i32() {}
+
+    std::int32_t x = 0;
+    std::int32_t y = 0;
+    std::int32_t z = 0;
+};
+
+inline bool
+operator==(const vec3i32& a, const vec3i32& b)
+{
+    return a.x == b.x && a.y == b.y && a.z == b.z;
+}
+
 struct spatial_hash
 {
     std::size_t
     operator()(const vec3i16& k) const
+    {
+        return (static_cast<std::size_t>(k.x) * static_cast<std::size_t>(73856093U)) ^
+               (static_cast<std::size_t>(k.y) * static_cast<std::size_t>(19349669U)) ^
+               (static_cast<std::size_t>(k.z) * static_cast<std::size_t>(83492791U));
+    }
+    std::size_t
+    operator()(const vec3i32& k) const
     {
         return (static_cast<std::size_t>(k.x) * static_cast<std::size_t>(73856093U)) ^
                (static_cast<std::size_t>(k.y) * static_cast<std::size_t>(19349669U)) ^
@@ -452,6 +481,10 @@ sgref_create(int kind, std::int64_t capacity)
             return new table_impl<set_traits<vec3i16, spatial_hash>>(capacity);
         case MAP_VEC3I16_U32:
             return new table_impl<map_traits<vec3i16, std::uint32_t, spatial_hash>>(capacity);
+        case SET_VEC3I32:
+            return new table_impl<set_traits<vec3i32, spatial_hash>>(capacity);
+        case MAP_VEC3I32_U64:
+            return new table_impl<map_traits<vec3i32, std::uint64_t, spatial_hash>>(capacity);
         default:
             return nullptr;
     }

@@ -9,6 +9,7 @@ thread so that every per-element outcome is deterministic:
 * buckets.npz        bucket(key) for several table sizes and key patterns
 * table_<kind>.npz   insert (with duplicates) / find / erase / final contents per container kind
 * table_vec3i16_<kind>.npz  the same for a 3 x int16 key type with a user hash (spatial hash), plus bucket()
+* table_vec3i32_<kind>.npz  the same for a 12-byte 3 x int32 key with a user-declared destructor
 * refusal.npz        inserts into tiny tables until refusal (capacity 1..8)
 * vector.npz, deque.npz, bitset.npz
 * deque_ends.npz     batches of push_back / pop_front / push_front / pop_back in sequence
@@ -142,6 +143,46 @@ def table_vec3i16(kind: int, seed: int):
     np.savez_compressed(OUT / f"table_vec3i16_{kind}.npz", **out)
 
 
+def table_vec3i32(kind: int, seed: int):
+    """unordered_set / unordered_map<., uint64_t> keyed by 3 x int32 (a 12-byte key with a user-declared
+    destructor) with the spatial hash: coordinates in a small cube so that keys repeat and buckets collide;
+    a few coordinates far outside the int16 range so that all 12 bytes matter."""
+    rng = np.random.default_rng(900 + seed)
+    cap = 6000
+    n = 5000
+    coords = rng.integers(-24, 24, size=(n, 3)).astype(np.int32)
+    coords[::97] += np.int32(1 << 20)
+    keys = np.zeros(n, O.VEC3I32)
+    keys["x"], keys["y"], keys["z"] = coords[:, 0], coords[:, 1], coords[:, 2]
+    vals = None
+    if O.VAL_DTYPE[kind] is not None:
+        vals = O_mix(O.spatial_hash(keys))  # a function of the key: duplicates carry equal values
+    t = O.RefTable(kind, cap)
+    ins_flags = t.insert(keys, vals, flags=True)
+    size_after_insert = t.size()
+    qc = rng.integers(-30, 30, size=(n, 3)).astype(np.int32)
+    queries = np.zeros(n, O.VEC3I32)
+    queries["x"], queries["y"], queries["z"] = qc[:, 0], qc[:, 1], qc[:, 2]
+    queries[::5] = keys[rng.integers(0, n, size=len(queries[::5]))]
+    fvals, found = t.find(queries)
+    erase = np.concatenate([keys[rng.integers(0, n, size=n // 2)], queries[: n // 4]])
+    erase_flags = t.erase(erase, flags=True)
+    size_after_erase = t.size()
+    buckets = np.array([t.bucket_of(k) for k in keys[:512]], np.int64)
+    rk, rv = t.range()
+    order = np.lexsort((rk["z"], rk["y"], rk["x"]))
+    out = dict(capacity=np.array(cap), keys=keys, insert_flags=ins_flags, size_after_insert=np.array(size_after_insert),
+               queries=queries, found=found, erase=erase, erase_flags=erase_flags,
+               size_after_erase=np.array(size_after_erase), valid=np.array(t.valid()), final_keys=rk[order],
+               buckets=buckets, bucket_count=np.array(t.geometry()[0]), max_size=np.array(t.geometry()[1]))
+    if vals is not None:
+        out["values"] = vals
+        out["found_values"] = np.where(found == 1, fvals, 0).astype(np.uint64)
+        out["final_values"] = rv[order]
+    t.close()
+    np.savez_compressed(OUT / f"table_vec3i32_{kind}.npz", **out)
+
+
 def O_mix(x: np.ndarray) -> np.ndarray:
     z = x.copy()
     with np.errstate(over="ignore"):
@@ -224,12 +265,18 @@ def bitset():
 
 def main():
     O.ref_set_threads(1)
+    if sys.argv[1:] == ["vec3i32"]:  # only the 3 x int32 fixtures
+        for kind in (O.SET_VEC3I32, O.MAP_VEC3I32_U64):
+            table_vec3i32(kind, kind)
+        return
     geometry()
     buckets()
     for kind in range(6):
         table_scenario(kind, kind)
     for kind in (O.SET_VEC3I16, O.MAP_VEC3I16_U32):
         table_vec3i16(kind, kind)
+    for kind in (O.SET_VEC3I32, O.MAP_VEC3I32_U64):
+        table_vec3i32(kind, kind)
     refusal()
     vector()
     deque()

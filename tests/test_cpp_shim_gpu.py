@@ -13,6 +13,8 @@ ROOT = Path(__file__).resolve().parents[1]
 SRC = ROOT / "tests" / "cpp" / "shim_test.cu"
 CUSTOM = ROOT / "tests" / "cpp" / "custom_key_test.cu"
 WIDE = ROOT / "tests" / "cpp" / "wide_key_test.cu"
+WIDE_GOLDEN = ROOT / "tests" / "cpp" / "wide_golden_test.cu"
+GOLDEN = ROOT / "tests" / "golden"
 OUT = ROOT / "tests" / "cpp" / "_build"
 
 
@@ -73,6 +75,39 @@ def test_wide_keys_and_nontrivial_types_on_gpu():
     stdgpu_gb300.load()
     exe = _compile(src=WIDE)
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "ALL PASS" in r.stdout
+
+
+def test_wide_golden_program_compiles_for_sm103a():
+    stdgpu_gb300.load()
+    _compile(src=WIDE_GOLDEN)
+
+
+def write_fixture(npz, out_dir):
+    """The arrays of a table_vec3i32 fixture as raw little-endian files for the C++ replay."""
+    import numpy as np
+    g = np.load(npz)
+    meta = np.array([g["capacity"], g["max_size"], g["bucket_count"], g["size_after_insert"],
+                     g["size_after_erase"]], np.int64)
+    meta.tofile(out_dir / "meta.bin")
+    for name in ("keys", "queries", "found", "erase", "final_keys", "buckets", "insert_flags", "erase_flags",
+                 "values", "found_values", "final_values"):
+        if name in g.files:
+            np.ascontiguousarray(g[name]).tofile(out_dir / f"{name}.bin")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,mode", [(8, "set"), (9, "map")])
+def test_wide_keys_replay_reference_fixtures(tmp_path, kind, mode):
+    """unordered_set<vec3i32> / unordered_map<vec3i32, uint64_t> with the spatial hash on the wide tables:
+    geometry, bucket(), sizes, find answers and values, final contents and per-key device outcomes equal
+    what the reference itself recorded (tests/golden/table_vec3i32_<kind>.npz)."""
+    stdgpu_gb300.load()
+    exe = _compile(src=WIDE_GOLDEN)
+    write_fixture(GOLDEN / f"table_vec3i32_{kind}.npz", tmp_path)
+    r = subprocess.run([str(exe), str(tmp_path), mode], capture_output=True, text=True, timeout=300)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "ALL PASS" in r.stdout

@@ -92,6 +92,35 @@ def test_custom_key_hash_scenario_matches_reference(golden, kind):
     assert np.array_equal(got, g["buckets"])
 
 
+@pytest.mark.parametrize("kind", [O.SET_VEC3I32, O.MAP_VEC3I32_U64])
+def test_wide_key_scenario_matches_reference(golden, kind):
+    """12-byte keys (3 x int32 with a user-declared destructor) under the spatial hash: the element-by-element
+    restatement answers what the reference's unordered_set / unordered_map<vec3i32, uint64_t, Hash> answered,
+    and bucket() is the fibonacci hashing of the spatial hash."""
+    g = golden(f"table_vec3i32_{kind}.npz")
+    t = O.SeqKeyTable(int(g["capacity"]), int(g["max_size"]))
+    keys = g["keys"]
+    vals = g["values"] if "values" in g else None
+    assert np.array_equal(t.insert(keys, vals), g["insert_flags"])
+    assert t.size() == int(g["size_after_insert"])
+    fv, found = t.find(g["queries"])
+    assert np.array_equal(found, g["found"])
+    if vals is not None:
+        got = np.array([v if f else 0 for v, f in zip(fv, found)], np.uint64)
+        assert np.array_equal(got, g["found_values"])
+    assert np.array_equal(t.erase(g["erase"]), g["erase_flags"])
+    assert t.size() == int(g["size_after_erase"])
+    rk = t.keys(O.VEC3I32)
+    o = np.lexsort((rk["z"], rk["y"], rk["x"]))
+    assert np.array_equal(rk[o], g["final_keys"])
+    if vals is not None:
+        final_vals = np.array([t.items[k.tobytes()] for k in rk[o]], np.uint64)
+        assert np.array_equal(final_vals, g["final_values"])
+    buckets = O.fibonacci_buckets(O.spatial_hash(keys[:512]), int(g["bucket_count"]))
+    assert np.array_equal(buckets.astype(np.int64), g["buckets"])
+    assert bool(g["valid"])
+
+
 def test_vec3i16_words_round_trip():
     k = np.zeros(4, O.VEC3I16)
     k["x"], k["y"], k["z"] = [-1, 0, 32767, -32768], [2, -3, 0, 1], [0, 0, -1, 5]
