@@ -282,6 +282,10 @@ struct unordered_ref
     __device__ int64_t
     bucket_size(int64_t n) const
     {
+        if (n < 0 || n >= (int64_t{ 1 } << v.bucket_bits))
+        {
+            return 0; // no such bucket (the reference requires n < bucket_count())
+        }
         int64_t g = detail::group_of_bucket(static_cast<uint64_t>(n), v.bucket_bits, v.num_groups);
         int64_t c = 0;
         for (int64_t probes = 0; probes < v.num_groups; ++probes)

@@ -527,6 +527,10 @@ struct wide_ref
             return static_cast<std::int64_t>(
                     sg::detail::fibonacci_bucket(static_cast<std::uint64_t>(Hash{}(from_wide<Key>(x))), bucket_bits));
         };
+        if (b < 0 || b >= bucket_count)
+        {
+            return 0; // no such bucket (the reference requires b < bucket_count())
+        }
         std::int64_t count = 0;
         std::int64_t g = sg::detail::group_of_bucket(static_cast<std::uint64_t>(b), bucket_bits, num_groups);
         for (std::int64_t n = 0; n < num_groups; ++n)
