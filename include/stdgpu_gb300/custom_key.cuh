@@ -387,6 +387,10 @@ public:
     index_t
     size(execution::device_policy policy = execution::device) const
     {
+        if (_handle == nullptr)
+        {
+            return 0; // a default-constructed object holds nothing, as in the reference
+        }
         int64_t n = 0;
         gb300_check(sg_unordered_size(_handle, policy.stream, &n), "size");
         return static_cast<index_t>(n);

@@ -247,6 +247,10 @@ public:
     index_t
     size(execution::device_policy policy = execution::device) const
     {
+        if (_handle == nullptr)
+        {
+            return 0; // a default-constructed object holds nothing, as in the reference
+        }
         int64_t n = 0;
         gb300_check(sg_unordered_size(_handle, policy.stream, &n), "size");
         return static_cast<index_t>(n);
@@ -504,6 +508,22 @@ class unordered_map
                                detail::custom_map<Key, T, Hash, unordered_map<Key, T, Hash, KeyEqual>>,
                                detail::wide_map<Key, T, Hash, unordered_map<Key, T, Hash, KeyEqual>>>>
 {
+public:
+    using key_equal = KeyEqual;
+    using hasher = Hash;
+
+    // hash_function() / key_eq() (src/stdgpu/impl/unordered_base_detail.cuh:1178-1190)
+    __host__ __device__ hasher
+    hash_function() const
+    {
+        return hasher{};
+    }
+
+    __host__ __device__ key_equal
+    key_eq() const
+    {
+        return key_equal{};
+    }
 };
 
 // stdgpu::unordered_set<Key, Hash>
@@ -515,6 +535,21 @@ class unordered_set
                                                  detail::custom_set<Key, Hash, unordered_set<Key, Hash, KeyEqual>>,
                                                  detail::wide_set<Key, Hash, unordered_set<Key, Hash, KeyEqual>>>>
 {
+public:
+    using key_equal = KeyEqual;
+    using hasher = Hash;
+
+    __host__ __device__ hasher
+    hash_function() const
+    {
+        return hasher{};
+    }
+
+    __host__ __device__ key_equal
+    key_eq() const
+    {
+        return key_equal{};
+    }
 };
 
 // stdgpu::vector<T>: bulk push_back and size (src/stdgpu/vector.cuh); device push_back is
@@ -548,6 +583,10 @@ public:
     index_t
     size(execution::device_policy policy = execution::device) const
     {
+        if (_handle == nullptr)
+        {
+            return 0;
+        }
         int64_t n = 0;
         detail::gb300_check(sg_vector_size(_handle, policy.stream, &n), "vector::size");
         return static_cast<index_t>(n);
@@ -632,6 +671,10 @@ public:
     index_t
     size(execution::device_policy policy = execution::device) const
     {
+        if (_handle == nullptr)
+        {
+            return 0;
+        }
         int64_t n = 0;
         detail::gb300_check(sg_deque_size(_handle, policy.stream, &n), "deque::size");
         return static_cast<index_t>(n);

@@ -935,7 +935,7 @@ public:
     index_t
     size(execution::device_policy policy = execution::device) const
     {
-        return static_cast<index_t>(header(policy).size);
+        return _t.keys == nullptr ? 0 : static_cast<index_t>(header(policy).size); // default-constructed: empty
     }
 
     bool

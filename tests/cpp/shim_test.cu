@@ -449,6 +449,65 @@ main()
         cudaFree(d_pushed);
     }
 
+    // empty_container (unordered_datastructure.inc:72-80): a default-constructed object
+    {
+        map_t empty_container;
+        check(empty_container.empty() && empty_container.full() && empty_container.size() == 0 &&
+                      empty_container.valid(),
+              "empty_container");
+        stdgpu::vector<std::uint32_t> v;
+        stdgpu::deque<std::uint64_t> d;
+        check(v.size() == 0 && d.size() == 0, "default-constructed vector / deque hold nothing");
+    }
+
+    // empty_size_limits and the custom-execution-policy variant (unordered_datastructure.inc:249-265),
+    // hash_objects (:267-279), hash_inside_range (:84-108)
+    {
+        cudaStream_t st = nullptr;
+        cudaStreamCreate(&st);
+        const auto policy = stdgpu::execution::on(st);
+        map_t m = map_t::createDeviceObject(policy, N);
+        check(m.empty() && !m.full() && m.size() <= m.max_size() && m.load_factor() <= m.max_load_factor(),
+              "empty_size_limits");
+        check(m.empty(policy) && !m.full(policy) && m.size(policy) <= m.max_size() &&
+                      m.load_factor(policy) <= m.max_load_factor(),
+              "empty_size_limits_custom_execution_policy");
+        const std::uint64_t key = 0x1234567890ull;
+        check(m.key_eq()(key, key) && m.hash_function()(key) == m.hash_function()(key), "hash_objects");
+        bool inside = true;
+        std::uint64_t x = 88172645463325252ull;
+        for (int i = 0; i < (1 << 16); ++i)
+        {
+            x ^= x << 13;
+            x ^= x >> 7;
+            x ^= x << 17;
+            const stdgpu::index_t b = m.bucket(x);
+            inside = inside && b >= 0 && b < m.bucket_count();
+        }
+        check(inside, "hash_inside_range");
+        // insert_range / erase_range / clear with a custom execution policy (unordered_datastructure.inc:1933,
+        // :2015, :2494)
+        std::vector<map_t::value_type> values;
+        values.reserve(N);
+        for (int i = 0; i < N; ++i)
+        {
+            values.emplace_back(keys[i], static_cast<std::uint32_t>(i));
+        }
+        map_t::value_type* d_values = nullptr;
+        cudaMalloc(&d_values, sizeof(map_t::value_type) * N);
+        cudaMemcpy(d_values, values.data(), sizeof(map_t::value_type) * N, cudaMemcpyHostToDevice);
+        m.insert(policy, d_values, d_values + N);
+        check(m.size(policy) == N && m.valid(policy), "insert_range_unique_parallel_custom_execution_policy");
+        m.erase(policy, d_keys, d_keys + N);
+        check(m.size(policy) == 0 && m.valid(policy), "erase_range_unique_parallel_custom_execution_policy");
+        m.insert(policy, d_values, d_values + N);
+        m.clear(policy);
+        check(m.size(policy) == 0 && m.valid(policy), "clear_custom_execution_policy");
+        map_t::destroyDeviceObject(policy, m);
+        cudaFree(d_values);
+        cudaStreamDestroy(st);
+    }
+
     cudaError_t e = cudaDeviceSynchronize();
     check(e == cudaSuccess, "no CUDA error");
     cudaFree(d_keys);
