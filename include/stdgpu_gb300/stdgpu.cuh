@@ -552,16 +552,54 @@ public:
     }
 };
 
-// stdgpu::vector<T>: bulk push_back and size (src/stdgpu/vector.cuh); device push_back is
-// warp-aggregated like the bulk kernel.
+// A contiguous device range [begin, begin + count): device_range() of vector and deque.
+template <typename T>
+struct device_range_of
+{
+    T* first = nullptr;
+    index_t count = 0;
+
+    __host__ __device__ index_t
+    size() const
+    {
+        return count;
+    }
+    __host__ __device__ T*
+    begin() const
+    {
+        return first;
+    }
+    __host__ __device__ T*
+    end() const
+    {
+        return first + count;
+    }
+    __device__ T&
+    operator[](index_t i) const
+    {
+        return first[i];
+    }
+};
+
+// stdgpu::vector<T> (src/stdgpu/vector.cuh) for 4/8-byte T: the reference's host calls over the C ABI and
+// its device calls on the vector's view.  Device push_back is warp-aggregated like the bulk kernel;
+// push_back and pop_back do not share a launch (a pop may read a slot whose push has not written it yet).
 template <typename T>
 class vector
 {
     static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
 
 public:
+    using value_type = T;
+
     static vector
     createDeviceObject(const index_t& capacity)
+    {
+        return createDeviceObject(execution::device, capacity);
+    }
+
+    static vector
+    createDeviceObject(execution::device_policy, const index_t& capacity)
     {
         vector v;
         detail::gb300_check(sg_vector_create(sizeof(T), capacity, &v._handle), "vector::createDeviceObject");
@@ -571,6 +609,12 @@ public:
 
     static void
     destroyDeviceObject(vector& v)
+    {
+        destroyDeviceObject(execution::device, v);
+    }
+
+    static void
+    destroyDeviceObject(execution::device_policy, vector& v)
     {
         if (v._handle != nullptr)
         {
@@ -592,16 +636,112 @@ public:
         return static_cast<index_t>(n);
     }
 
+    bool
+    empty(execution::device_policy policy = execution::device) const
+    {
+        return size(policy) == 0;
+    }
+
+    bool
+    full(execution::device_policy policy = execution::device) const
+    {
+        return size(policy) == max_size();
+    }
+
     __host__ __device__ index_t
     capacity() const
     {
         return static_cast<index_t>(_view.capacity);
     }
 
+    __host__ __device__ index_t
+    max_size() const noexcept
+    {
+        return capacity();
+    }
+
     __host__ __device__ T*
     data() const
     {
         return static_cast<T*>(_view.data);
+    }
+
+    void
+    clear(execution::device_policy policy = execution::device)
+    {
+        detail::gb300_check(sg_vector_clear(_handle, policy.stream), "vector::clear");
+    }
+
+    // valid() (src/stdgpu/impl/vector_detail.cuh:614-640): the element count lies in [0, capacity()]
+    bool
+    valid(execution::device_policy policy = execution::device) const
+    {
+        if (_handle == nullptr)
+        {
+            return true;
+        }
+        long long n = -1;
+        const bool ok = cudaMemcpyAsync(&n, _view.size, sizeof(n), cudaMemcpyDeviceToHost, policy.stream) == cudaSuccess &&
+                        cudaStreamSynchronize(policy.stream) == cudaSuccess;
+        detail::gb300_check(ok ? SG_OK : SG_ERR_CUDA, "vector::valid");
+        return n >= 0 && n <= _view.capacity;
+    }
+
+    // device_begin() / device_end() / device_range(): the stored elements [data(), data() + size())
+    T*
+    device_begin() const
+    {
+        return data();
+    }
+
+    T*
+    device_end(execution::device_policy policy = execution::device) const
+    {
+        return data() + size(policy);
+    }
+
+    device_range_of<T>
+    device_range(execution::device_policy policy = execution::device) const
+    {
+        return device_range_of<T>{ data(), size(policy) };
+    }
+
+    // insert(position, begin, end) (src/stdgpu/impl/vector_detail.cuh:372-410): position must be device_end();
+    // values that would not fit are not inserted at all, as in the reference.
+    void
+    insert(const T* position, const T* begin, const T* end)
+    {
+        insert(execution::device, position, begin, end);
+    }
+
+    void
+    insert(execution::device_policy policy, const T* position, const T* begin, const T* end)
+    {
+        if (position != device_end(policy))
+        {
+            detail::gb300_check(SG_ERR_BAD_ARG, "vector::insert (only at device_end())");
+            return;
+        }
+        const sg_status st = sg_vector_insert(_handle, begin, end - begin, policy.stream);
+        detail::gb300_check(st == SG_ERR_FULL ? SG_OK : st, "vector::insert");
+    }
+
+    // erase(begin, end) (src/stdgpu/impl/vector_detail.cuh:418-450): a suffix ending at device_end()
+    void
+    erase(const T* begin, const T* end)
+    {
+        erase(execution::device, begin, end);
+    }
+
+    void
+    erase(execution::device_policy policy, const T* begin, const T* end)
+    {
+        if (end != device_end(policy) || begin > end || begin < device_begin())
+        {
+            detail::gb300_check(SG_ERR_BAD_ARG, "vector::erase (only a suffix ending at device_end())");
+            return;
+        }
+        detail::gb300_check(sg_vector_erase(_handle, end - begin, policy.stream), "vector::erase");
     }
 
     // Device push_back (src/stdgpu/impl/vector_detail.cuh:181-238): the calling lanes that are active
@@ -633,6 +773,64 @@ public:
         return true;
     }
 
+    template <typename... Args>
+    __device__ bool
+    emplace_back(Args&&... args) const
+    {
+        return push_back(T(static_cast<Args&&>(args)...));
+    }
+
+    // Device pop_back (src/stdgpu/impl/vector_detail.cuh:240-299): takes the last element, or fails on an
+    // empty vector.  The count is taken down with a bounded compare-and-swap loop.
+    __device__ pair<T, bool>
+    pop_back() const
+    {
+        unsigned long long* size = static_cast<unsigned long long*>(_view.size);
+        long long cur = *reinterpret_cast<volatile long long*>(size);
+        for (int tries = 0; tries < (1 << 20); ++tries)
+        {
+            if (cur <= 0)
+            {
+                return pair<T, bool>(T{}, false);
+            }
+            const long long n = cur > _view.capacity ? _view.capacity : cur;
+            const long long seen = static_cast<long long>(atomicCAS(size, static_cast<unsigned long long>(cur),
+                                                                    static_cast<unsigned long long>(n - 1)));
+            if (seen == cur)
+            {
+                return pair<T, bool>(data()[n - 1], true);
+            }
+            cur = seen;
+        }
+        return pair<T, bool>(T{}, false);
+    }
+
+    // element access (src/stdgpu/impl/vector_detail.cuh:113-175: at, operator[], front, back)
+    __device__ T&
+    at(index_t n) const
+    {
+        return data()[n];
+    }
+
+    __device__ T&
+    operator[](index_t n) const
+    {
+        return data()[n];
+    }
+
+    __device__ T&
+    front() const
+    {
+        return data()[0];
+    }
+
+    __device__ T&
+    back() const
+    {
+        const long long n = *reinterpret_cast<volatile long long*>(_view.size);
+        return data()[(n > _view.capacity ? _view.capacity : n) - 1];
+    }
+
 private:
     sg_vector* _handle = nullptr;
     sg_vector_view _view{};
@@ -648,8 +846,16 @@ class deque
     static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
 
 public:
+    using value_type = T;
+
     static deque
     createDeviceObject(const index_t& capacity)
+    {
+        return createDeviceObject(execution::device, capacity);
+    }
+
+    static deque
+    createDeviceObject(execution::device_policy, const index_t& capacity)
     {
         deque d;
         detail::gb300_check(sg_deque_create(sizeof(T), capacity, &d._handle), "deque::createDeviceObject");
@@ -660,12 +866,20 @@ public:
     static void
     destroyDeviceObject(deque& d)
     {
+        destroyDeviceObject(execution::device, d);
+    }
+
+    static void
+    destroyDeviceObject(execution::device_policy, deque& d)
+    {
         if (d._handle != nullptr)
         {
             detail::gb300_check(sg_deque_destroy(d._handle), "deque::destroyDeviceObject");
         }
+        cudaFree(d._range);
         d._handle = nullptr;
         d._view = sg_deque_view{};
+        d._range = nullptr;
     }
 
     index_t
@@ -696,6 +910,41 @@ public:
     capacity() const
     {
         return static_cast<index_t>(_view.capacity);
+    }
+
+    __host__ __device__ index_t
+    max_size() const noexcept
+    {
+        return capacity();
+    }
+
+    // valid() (src/stdgpu/impl/deque_detail.cuh:635-660): the count lies in [0, capacity()] and no bounded wait
+    // of a device call has given up
+    bool
+    valid(execution::device_policy policy = execution::device) const
+    {
+        if (_handle == nullptr)
+        {
+            return true;
+        }
+        int64_t n = 0;
+        const sg_status st = sg_deque_size(_handle, policy.stream, &n);
+        return st == SG_OK && n >= 0 && n <= _view.capacity;
+    }
+
+    // device_range(): the stored elements front to back.  Unlike the reference's range, which indexes the
+    // deque's own storage, this is a copy in an array the object keeps (allocated by the first call).
+    device_range_of<T>
+    device_range(execution::device_policy policy = execution::device)
+    {
+        if (_range == nullptr && _view.capacity > 0)
+        {
+            detail::gb300_check(cudaMalloc(&_range, sizeof(T) * _view.capacity) == cudaSuccess ? SG_OK : SG_ERR_OOM,
+                                "deque::device_range");
+        }
+        int64_t n = 0;
+        detail::gb300_check(sg_deque_copy_out(_handle, _range, policy.stream, &n), "deque::device_range");
+        return device_range_of<T>{ _range, static_cast<index_t>(n) };
     }
 
     void
@@ -746,6 +995,43 @@ public:
         return true;
     }
 
+    template <typename... Args>
+    __device__ bool
+    emplace_back(Args&&... args) const
+    {
+        return push_back(T(static_cast<Args&&>(args)...));
+    }
+
+    // element access relative to the front (src/stdgpu/impl/deque_detail.cuh:133-192: at, operator[], front,
+    // back); valid while no push or pop runs
+    __device__ T&
+    operator[](index_t n) const
+    {
+        const auto* c = counters();
+        const unsigned long long cap = static_cast<unsigned long long>(_view.capacity);
+        return static_cast<T*>(_view.data)[(c->begin + static_cast<unsigned long long>(n)) % cap];
+    }
+
+    __device__ T&
+    at(index_t n) const
+    {
+        return (*this)[n];
+    }
+
+    __device__ T&
+    front() const
+    {
+        return (*this)[0];
+    }
+
+    __device__ T&
+    back() const
+    {
+        const auto* c = counters();
+        const unsigned long long cap = static_cast<unsigned long long>(_view.capacity);
+        return static_cast<T*>(_view.data)[(c->end + cap - 1) % cap];
+    }
+
     // device pop_front (src/stdgpu/impl/deque_detail.cuh:388-446)
     __device__ pair<T, bool>
     pop_front() const
@@ -783,6 +1069,7 @@ private:
 
     sg_deque* _handle = nullptr;
     sg_deque_view _view{};
+    T* _range = nullptr;
 };
 
 // stdgpu::queue<T> / stack<T> (src/stdgpu/queue.cuh, stack.cuh): adapters over deque.  queue::push / pop

@@ -2,6 +2,7 @@
 // tests/stdgpu/vector.inc), written against the C++ API of include/stdgpu_gb300/stdgpu.cuh: native
 // device calls inside user kernels plus the host bulk calls.  Prints one line per check and ends with
 // "ALL PASS" when every check holds.
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <random>
@@ -240,6 +241,43 @@ sum_of(const int* d, int n)
         s += x;
     }
     return s;
+}
+
+// vector / deque device element access and the other device calls of the reference's containers
+__global__ void
+vector_pop(stdgpu::vector<std::uint32_t> v, int n, std::uint32_t* popped, int* ok)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        const auto r = v.pop_back();
+        popped[i] = r.first;
+        ok[i] = r.second ? 1 : 0;
+    }
+}
+
+__global__ void
+vector_peek(stdgpu::vector<std::uint32_t> v, std::uint32_t* out)
+{
+    out[0] = v.front();
+    out[1] = v.back();
+    out[2] = v.at(3);
+    out[3] = v[4];
+    out[4] = v.emplace_back(777u) ? 1u : 0u;
+}
+
+__global__ void
+deque_sequence(stdgpu::deque<std::uint64_t> d, int n, std::uint64_t* out)
+{
+    // one thread: pushes in program order, then reads the ends and one element by index
+    for (int i = 0; i < n; ++i)
+    {
+        d.emplace_back(static_cast<std::uint64_t>(1000 + i));
+    }
+    out[0] = d.front();
+    out[1] = d.back();
+    out[2] = d.at(7);
+    out[3] = d[n - 2];
 }
 
 int
@@ -506,6 +544,83 @@ main()
         map_t::destroyDeviceObject(policy, m);
         cudaFree(d_values);
         cudaStreamDestroy(st);
+    }
+
+    // vector: range insert / erase at the end, device pop_back / element access / emplace_back, valid, clear
+    // (vector.inc scenarios on insert, erase, pop_back, front / back / at)
+    {
+        using vec_t = stdgpu::vector<std::uint32_t>;
+        vec_t v = vec_t::createDeviceObject(100);
+        std::vector<std::uint32_t> h(60);
+        for (int i = 0; i < 60; ++i)
+        {
+            h[i] = static_cast<std::uint32_t>(10 * i);
+        }
+        std::uint32_t* d_h = to_device(h);
+        v.insert(v.device_end(), d_h, d_h + 50);
+        check(v.size() == 50 && v.valid(), "vector insert(device_end(), begin, end)");
+        v.insert(v.device_end(), d_h, d_h + 60);
+        check(v.size() == 50, "vector insert that would overflow inserts nothing");
+        auto r = v.device_range();
+        check(r.size() == 50 && to_host(r.begin(), 50) == std::vector<std::uint32_t>(h.begin(), h.begin() + 50),
+              "vector device_range()");
+        v.erase(v.device_end() - 20, v.device_end());
+        check(v.size() == 30 && v.valid(), "vector erase(device_end() - 20, device_end())");
+        std::uint32_t* d_out = nullptr;
+        int* d_ok = nullptr;
+        cudaMalloc(&d_out, sizeof(std::uint32_t) * 64);
+        cudaMalloc(&d_ok, sizeof(int) * 64);
+        vector_peek<<<1, 1>>>(v, d_out);
+        const auto peek = to_host(d_out, 5);
+        check(peek[0] == 0 && peek[1] == 290 && peek[2] == 30 && peek[3] == 40 && peek[4] == 1 && v.size() == 31,
+              "vector front / back / at / operator[] / emplace_back");
+        vector_pop<<<1, 64>>>(v, 40, d_out, d_ok);
+        const auto popped = to_host(d_out, 40);
+        const auto okv = to_host(d_ok, 40);
+        std::vector<std::uint32_t> got;
+        for (int i = 0; i < 40; ++i)
+        {
+            if (okv[i])
+            {
+                got.push_back(popped[i]);
+            }
+        }
+        std::sort(got.begin(), got.end());
+        std::vector<std::uint32_t> want(h.begin(), h.begin() + 30);
+        want.push_back(777u);
+        std::sort(want.begin(), want.end());
+        check(got == want && v.size() == 0 && v.empty() && v.valid(),
+              "vector pop_back: each element once, then fails on empty");
+        v.insert(v.device_end(), d_h, d_h + 10);
+        v.clear();
+        check(v.size() == 0 && v.valid(), "vector clear");
+        vec_t::destroyDeviceObject(v);
+        cudaFree(d_h);
+        cudaFree(d_out);
+        cudaFree(d_ok);
+    }
+
+    // deque: device emplace_back, front / back / at / operator[], device_range, valid, max_size
+    {
+        using dq_t = stdgpu::deque<std::uint64_t>;
+        dq_t d = dq_t::createDeviceObject(64);
+        std::uint64_t* d_out = nullptr;
+        cudaMalloc(&d_out, sizeof(std::uint64_t) * 4);
+        deque_sequence<<<1, 1>>>(d, 40, d_out);
+        const auto out = to_host(d_out, 4);
+        check(out[0] == 1000 && out[1] == 1039 && out[2] == 1007 && out[3] == 1038 && d.size() == 40 && d.valid() &&
+                      d.max_size() == 64,
+              "deque emplace_back / front / back / at / operator[]");
+        auto r = d.device_range();
+        const auto all = to_host(r.begin(), r.size());
+        bool in_order = r.size() == 40;
+        for (int i = 0; in_order && i < 40; ++i)
+        {
+            in_order = all[i] == static_cast<std::uint64_t>(1000 + i);
+        }
+        check(in_order, "deque device_range(): front to back");
+        dq_t::destroyDeviceObject(d);
+        cudaFree(d_out);
     }
 
     cudaError_t e = cudaDeviceSynchronize();
