@@ -96,6 +96,38 @@ struct pair
     }
 };
 
+// stdgpu::safe_device_allocator<T> (src/stdgpu/memory.h:340-420): device memory through cudaMalloc / cudaFree.
+// The containers accept an allocator type parameter, as the reference's do, for source compatibility; their
+// storage itself goes through the library's allocator pair (sg_set_device_allocator, one per process), and
+// get_allocator() returns a default-constructed allocator of the given type.
+template <typename T>
+struct safe_device_allocator
+{
+    using value_type = T;
+
+    safe_device_allocator() noexcept = default;
+
+    template <typename U>
+    safe_device_allocator(const safe_device_allocator<U>&) noexcept
+    {
+    }
+
+    T*
+    allocate(std::int64_t n)
+    {
+        T* p = nullptr;
+        detail::gb300_check(cudaMalloc(&p, sizeof(T) * static_cast<std::size_t>(n)) == cudaSuccess ? SG_OK : SG_ERR_OOM,
+                            "safe_device_allocator::allocate");
+        return p;
+    }
+
+    void
+    deallocate(T* p, std::int64_t)
+    {
+        cudaFree(p);
+    }
+};
+
 // Execution policies: the reference's execution::device plus a stream-carrying policy.
 namespace execution
 {
@@ -499,18 +531,49 @@ namespace stdgpu
 // library's precompiled kernels; other keys of at most 8 bytes (short3, vec3int16, packed coordinates) with a
 // user Hash and a 4/8-byte mapped type go through the word-keyed path of custom_key.cuh; every other element
 // type (a 3 x int32 key, an empty or 16-byte mapped type, a type with a destructor) through wide_key.cuh.
-template <typename Key, typename T, typename Hash = hash<Key>, typename KeyEqual = equal_to<Key>>
+template <typename Key, typename T, typename Hash = hash<Key>, typename KeyEqual = equal_to<Key>,
+          typename Allocator = safe_device_allocator<pair<const Key, T>>>
 class unordered_map
   : public std::conditional_t<
             detail::is_native_table<Key, T, Hash>::value,
-            detail::native_map<Key, T, unordered_map<Key, T, Hash, KeyEqual>>,
+            detail::native_map<Key, T, unordered_map<Key, T, Hash, KeyEqual, Allocator>>,
             std::conditional_t<detail::fits_word_table<Key, T>::value,
-                               detail::custom_map<Key, T, Hash, unordered_map<Key, T, Hash, KeyEqual>>,
-                               detail::wide_map<Key, T, Hash, unordered_map<Key, T, Hash, KeyEqual>>>>
+                               detail::custom_map<Key, T, Hash, unordered_map<Key, T, Hash, KeyEqual, Allocator>>,
+                               detail::wide_map<Key, T, Hash, unordered_map<Key, T, Hash, KeyEqual, Allocator>>>>
 {
+    using base = std::conditional_t<
+            detail::is_native_table<Key, T, Hash>::value,
+            detail::native_map<Key, T, unordered_map>,
+            std::conditional_t<detail::fits_word_table<Key, T>::value, detail::custom_map<Key, T, Hash, unordered_map>,
+                               detail::wide_map<Key, T, Hash, unordered_map>>>;
+
 public:
     using key_equal = KeyEqual;
     using hasher = Hash;
+    using allocator_type = Allocator;
+    using base::createDeviceObject;
+
+    // createDeviceObject(capacity, allocator) (src/stdgpu/impl/unordered_map_detail.cuh): the allocator is kept
+    // and returned by get_allocator()
+    static unordered_map
+    createDeviceObject(const index_t& capacity, const Allocator& allocator)
+    {
+        return createDeviceObject(execution::device, capacity, allocator);
+    }
+
+    static unordered_map
+    createDeviceObject(execution::device_policy policy, const index_t& capacity, const Allocator& allocator)
+    {
+        unordered_map m = base::createDeviceObject(policy, capacity);
+        m._allocator = allocator;
+        return m;
+    }
+
+    allocator_type
+    get_allocator() const noexcept
+    {
+        return _allocator;
+    }
 
     // hash_function() / key_eq() (src/stdgpu/impl/unordered_base_detail.cuh:1178-1190)
     __host__ __device__ hasher
@@ -524,20 +587,53 @@ public:
     {
         return key_equal{};
     }
+
+private:
+    Allocator _allocator{};
 };
 
 // stdgpu::unordered_set<Key, Hash>
-template <typename Key, typename Hash = hash<Key>, typename KeyEqual = equal_to<Key>>
+template <typename Key, typename Hash = hash<Key>, typename KeyEqual = equal_to<Key>,
+          typename Allocator = safe_device_allocator<Key>>
 class unordered_set
-  : public std::conditional_t<detail::is_native_table<Key, void, Hash>::value,
-                              detail::native_set<Key, unordered_set<Key, Hash, KeyEqual>>,
-                              std::conditional_t<detail::fits_word_table<Key, void>::value,
-                                                 detail::custom_set<Key, Hash, unordered_set<Key, Hash, KeyEqual>>,
-                                                 detail::wide_set<Key, Hash, unordered_set<Key, Hash, KeyEqual>>>>
+  : public std::conditional_t<
+            detail::is_native_table<Key, void, Hash>::value,
+            detail::native_set<Key, unordered_set<Key, Hash, KeyEqual, Allocator>>,
+            std::conditional_t<detail::fits_word_table<Key, void>::value,
+                               detail::custom_set<Key, Hash, unordered_set<Key, Hash, KeyEqual, Allocator>>,
+                               detail::wide_set<Key, Hash, unordered_set<Key, Hash, KeyEqual, Allocator>>>>
 {
+    using base = std::conditional_t<detail::is_native_table<Key, void, Hash>::value,
+                                    detail::native_set<Key, unordered_set>,
+                                    std::conditional_t<detail::fits_word_table<Key, void>::value,
+                                                       detail::custom_set<Key, Hash, unordered_set>,
+                                                       detail::wide_set<Key, Hash, unordered_set>>>;
+
 public:
     using key_equal = KeyEqual;
     using hasher = Hash;
+    using allocator_type = Allocator;
+    using base::createDeviceObject;
+
+    static unordered_set
+    createDeviceObject(const index_t& capacity, const Allocator& allocator)
+    {
+        return createDeviceObject(execution::device, capacity, allocator);
+    }
+
+    static unordered_set
+    createDeviceObject(execution::device_policy policy, const index_t& capacity, const Allocator& allocator)
+    {
+        unordered_set m = base::createDeviceObject(policy, capacity);
+        m._allocator = allocator;
+        return m;
+    }
+
+    allocator_type
+    get_allocator() const noexcept
+    {
+        return _allocator;
+    }
 
     __host__ __device__ hasher
     hash_function() const
@@ -550,6 +646,9 @@ public:
     {
         return key_equal{};
     }
+
+private:
+    Allocator _allocator{};
 };
 
 // A contiguous device range [begin, begin + count): device_range() of vector and deque.
@@ -584,13 +683,29 @@ struct device_range_of
 // stdgpu::vector<T> (src/stdgpu/vector.cuh) for 4/8-byte T: the reference's host calls over the C ABI and
 // its device calls on the vector's view.  Device push_back is warp-aggregated like the bulk kernel;
 // push_back and pop_back do not share a launch (a pop may read a slot whose push has not written it yet).
-template <typename T>
+template <typename T, typename Allocator = safe_device_allocator<T>>
 class vector
 {
     static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
 
 public:
     using value_type = T;
+    using allocator_type = Allocator;
+
+    allocator_type
+    get_allocator() const noexcept
+    {
+        return _allocator;
+    }
+
+    // createDeviceObject(capacity, allocator): the allocator is kept and returned by get_allocator()
+    static vector
+    createDeviceObject(const index_t& capacity, const Allocator& allocator)
+    {
+        vector x = createDeviceObject(execution::device, capacity);
+        x._allocator = allocator;
+        return x;
+    }
 
     static vector
     createDeviceObject(const index_t& capacity)
@@ -834,19 +949,36 @@ public:
 private:
     sg_vector* _handle = nullptr;
     sg_vector_view _view{};
+    Allocator _allocator{};
 };
 
 // stdgpu::deque<T> (src/stdgpu/deque.cuh) for 4/8-byte T.  Device push_back / pop_front may run
 // concurrently in one kernel (the ring's turn words order a pop after the push of its ticket, with
 // bounded waits: a wait that runs out sets the deque's error bit, which size() reports, and the call fails);
 // host bulk calls cover push_back / pop_front mixes, push_front and pop_back.
-template <typename T>
+template <typename T, typename Allocator = safe_device_allocator<T>>
 class deque
 {
     static_assert(sizeof(T) == 4 || sizeof(T) == 8, "4- or 8-byte elements");
 
 public:
     using value_type = T;
+    using allocator_type = Allocator;
+
+    allocator_type
+    get_allocator() const noexcept
+    {
+        return _allocator;
+    }
+
+    // createDeviceObject(capacity, allocator): the allocator is kept and returned by get_allocator()
+    static deque
+    createDeviceObject(const index_t& capacity, const Allocator& allocator)
+    {
+        deque x = createDeviceObject(execution::device, capacity);
+        x._allocator = allocator;
+        return x;
+    }
 
     static deque
     createDeviceObject(const index_t& capacity)
@@ -1069,25 +1201,29 @@ private:
 
     sg_deque* _handle = nullptr;
     sg_deque_view _view{};
+    Allocator _allocator{};
     T* _range = nullptr;
 };
 
 // stdgpu::queue<T> / stack<T> (src/stdgpu/queue.cuh, stack.cuh): adapters over deque.  queue::push / pop
 // are push_back / pop_front (device calls, concurrent); stack::push is push_back and stack::pop the host
 // bulk pop_back.
-template <typename T>
+template <typename T, typename ContainerT = deque<T>>
 class queue
 {
 public:
+    using container_type = ContainerT;
+    using value_type = typename ContainerT::value_type;
+
     static queue
     createDeviceObject(const index_t& capacity)
     {
-        return queue{ deque<T>::createDeviceObject(capacity) };
+        return queue{ ContainerT::createDeviceObject(capacity) };
     }
     static void
     destroyDeviceObject(queue& q)
     {
-        deque<T>::destroyDeviceObject(q._c);
+        ContainerT::destroyDeviceObject(q._c);
     }
     __device__ bool
     push(const T& element) const
@@ -1110,22 +1246,25 @@ public:
         return _c.empty(policy);
     }
 
-    deque<T> _c;
+    ContainerT _c;
 };
 
-template <typename T>
+template <typename T, typename ContainerT = deque<T>>
 class stack
 {
 public:
+    using container_type = ContainerT;
+    using value_type = typename ContainerT::value_type;
+
     static stack
     createDeviceObject(const index_t& capacity)
     {
-        return stack{ deque<T>::createDeviceObject(capacity) };
+        return stack{ ContainerT::createDeviceObject(capacity) };
     }
     static void
     destroyDeviceObject(stack& s)
     {
-        deque<T>::destroyDeviceObject(s._c);
+        ContainerT::destroyDeviceObject(s._c);
     }
     __device__ bool
     push(const T& element) const
@@ -1143,7 +1282,7 @@ public:
         return _c.size(policy);
     }
 
-    deque<T> _c;
+    ContainerT _c;
 };
 
 // bitset::count() over raw blocks (src/stdgpu/impl/bitset_detail.cuh:388-404).

@@ -243,6 +243,25 @@ sum_of(const int* d, int n)
     return s;
 }
 
+// An allocator type of the caller's, as the reference's custom_allocator tests use
+// (tests/stdgpu/unordered_datastructure.inc:2510-2548): the containers accept and return it.
+template <typename T>
+struct tagged_allocator : stdgpu::safe_device_allocator<T>
+{
+    using value_type = T;
+    int tag = 0;
+    tagged_allocator() = default;
+    explicit tagged_allocator(int t)
+      : tag(t)
+    {
+    }
+    template <typename U>
+    tagged_allocator(const tagged_allocator<U>& o)
+      : tag(o.tag)
+    {
+    }
+};
+
 // vector / deque device element access and the other device calls of the reference's containers
 __global__ void
 vector_pop(stdgpu::vector<std::uint32_t> v, int n, std::uint32_t* popped, int* ok)
@@ -621,6 +640,30 @@ main()
         check(in_order, "deque device_range(): front to back");
         dq_t::destroyDeviceObject(d);
         cudaFree(d_out);
+    }
+
+    // get_allocator and custom_allocator (unordered_datastructure.inc:2510-2548)
+    {
+        using alloc_t = tagged_allocator<map_t::value_type>;
+        using custom_map_t = stdgpu::unordered_map<std::uint64_t, std::uint32_t, stdgpu::hash<std::uint64_t>,
+                                                   stdgpu::equal_to<std::uint64_t>, alloc_t>;
+        custom_map_t m = custom_map_t::createDeviceObject(10000, alloc_t(7));
+        alloc_t a = m.get_allocator();
+        custom_map_t::value_type* array = a.allocate(10000);
+        const bool allocated = array != nullptr && cudaMemset(array, 0, sizeof(*array) * 10000) == cudaSuccess;
+        a.deallocate(array, 10000);
+        map_t plain = map_t::createDeviceObject(100);
+        auto pa = plain.get_allocator();
+        map_t::value_type* parray = pa.allocate(100);
+        pa.deallocate(parray, 100);
+        check(a.tag == 7 && allocated && parray != nullptr && m.size() == 0 && m.valid(),
+              "get_allocator / custom_allocator");
+        custom_map_t::destroyDeviceObject(m);
+        map_t::destroyDeviceObject(plain);
+        stdgpu::vector<std::uint32_t, tagged_allocator<std::uint32_t>> v =
+                stdgpu::vector<std::uint32_t, tagged_allocator<std::uint32_t>>::createDeviceObject(16);
+        check(v.capacity() == 16 && v.get_allocator().tag == 0, "vector with an allocator type");
+        stdgpu::vector<std::uint32_t, tagged_allocator<std::uint32_t>>::destroyDeviceObject(v);
     }
 
     cudaError_t e = cudaDeviceSynchronize();
