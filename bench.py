@@ -73,6 +73,8 @@ def parse_args(argv=None):
                         "large: capacity-2^30 map at 0.5/0.75/0.9 load plus vector / deque / bitset; "
                         "small: an L2-resident 2^20-key set, eager and as one CUDA graph")
     p.add_argument("--requests", type=int, default=600, help="serve workload: number of requests")
+    p.add_argument("--e2e-chunk-log2", type=int, default=22, help="e2e: elements per staged chunk, log2")
+    p.add_argument("--e2e-buffers", type=int, default=4, help="e2e: staging buffers in the ring")
     return p.parse_args(argv)
 
 
@@ -351,7 +353,7 @@ def native_arm(args):
         vals_h = torch.empty(n_q, dtype=torch.int32).pin_memory()
         found_h = torch.empty(n_q, dtype=torch.uint8).pin_memory()
 
-        stager = sg.stager(1 << 22, 4)
+        stager = sg.stager(1 << args.e2e_chunk_log2, args.e2e_buffers)
         hp = lambda t: c_void_p(t.data_ptr())
 
         def e2e_step():
@@ -397,7 +399,7 @@ def native_arm(args):
         link_ms = max(h2d / link["h2d_gbs"], d2h / link["d2h_gbs"]) / 1e6
         link.update({"bound_ms": link_ms, "frac": link_ms / e2e_ms})
         e2e = {"value": ops_per_step * ws / (e2e_ms * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "api": "sg_unordered_*_host (pipelined, 2^22-element chunks)", "link": link,
+               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "api": f"sg_unordered_*_host (pipelined, 2^{args.e2e_chunk_log2}-element chunks, {args.e2e_buffers} buffers)", "link": link,
                "serial_copies": {"value": ops_per_step * ws / (serial_ms * 1e-3) / 1e6, "ms_per_step": serial_ms}}
 
     # ---------------- roofline of the dominant kernel
