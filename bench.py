@@ -356,13 +356,25 @@ def native_arm(args):
         stager = sg.stager(1 << args.e2e_chunk_log2, args.e2e_buffers)
         hp = lambda t: c_void_p(t.data_ptr())
 
-        def e2e_step():
+        e2e_phase_ms = {"clear": [], "insert_host": [], "find_host": [], "erase_host": []}
+
+        def e2e_step(ev=None):
             # the host-buffer entry points: chunked copies in, kernels, results out, overlapped
+            if ev is not None:
+                ev[0].record(stream)
             call(lib.sg_unordered_clear(h, sp), "clear")
+            if ev is not None:
+                ev[1].record(stream)
             call(lib.sg_unordered_insert_host(h, stager._h, hp(pairs_h), n, None, sp), "insert_host")
+            if ev is not None:
+                ev[2].record(stream)
             call(lib.sg_unordered_find_host(h, stager._h, hp(queries_h), n_q, hp(vals_h), hp(found_h), sp),
                  "find_host")
+            if ev is not None:
+                ev[3].record(stream)
             call(lib.sg_unordered_erase_host(h, stager._h, hp(erase_h), n_e, None, sp), "erase_host")
+            if ev is not None:
+                ev[4].record(stream)
 
         def e2e_serial_step():
             # the same step as separate whole-array copies around the device-pointer calls
@@ -391,6 +403,13 @@ def native_arm(args):
 
         e2e_ms = slowest_rank_ms(time_steps(e2e_step), ws, dev)
         serial_ms = slowest_rank_ms(time_steps(e2e_serial_step), ws, dev)
+        # one more, untimed step with events between the calls: where the e2e time goes
+        pev = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
+        e2e_step(pev)
+        torch.cuda.synchronize(dev)
+        for i, name in enumerate(e2e_phase_ms):
+            e2e_phase_ms[name] = pev[i].elapsed_time(pev[i + 1])
+        found_h.zero_()
         stager.close()
         h2d = pairs_h.numel() * 8 + queries_h.numel() * 8 + erase_h.numel() * 8
         d2h = vals_h.numel() * 4 + found_h.numel()
@@ -400,6 +419,7 @@ def native_arm(args):
         link.update({"bound_ms": link_ms, "frac": link_ms / e2e_ms})
         e2e = {"value": ops_per_step * ws / (e2e_ms * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "api": f"sg_unordered_*_host (pipelined, 2^{args.e2e_chunk_log2}-element chunks, {args.e2e_buffers} buffers)", "link": link,
+               "phases_ms": e2e_phase_ms,
                "serial_copies": {"value": ops_per_step * ws / (serial_ms * 1e-3) / 1e6, "ms_per_step": serial_ms}}
 
     # ---------------- roofline of the dominant kernel
