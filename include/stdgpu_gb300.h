@@ -162,9 +162,12 @@ SG_API sg_status sg_unordered_load(const char* path, void* stream, sg_unordered*
 
 /* Bulk-insert strategy (no counterpart in the reference).  SG_INSERT_AUTO: when a call without per-element
  * flags brings at least 2^22 keys and one key per two probe groups of a table of 256 MB or more, the keys
- * are first partitioned by home-group range into a scratch array (n x sizeof(value_type), kept by the
- * table until destroy) so that each group line is read from DRAM about once.  SG_INSERT_DIRECT never
- * partitions; SG_INSERT_PARTITIONED partitions every call without flags.  Results are the same. */
+ * are first partitioned by home-group range, in one pass, into a scratch array (about 1.13 x n x
+ * sizeof(value_type): each range's share plus slack and an overflow region; kept by the table until
+ * destroy) so that each group line is read from DRAM about once; elements that find no room there (keys
+ * crowded into few ranges) are inserted by a direct pass over the whole input.  Bulk erase partitions its
+ * keys the same way from 2^22 keys on.  SG_INSERT_DIRECT never partitions; SG_INSERT_PARTITIONED
+ * partitions every call without flags.  Results are the same. */
 typedef enum sg_insert_mode
 {
     SG_INSERT_AUTO = 0,
