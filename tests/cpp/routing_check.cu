@@ -1,0 +1,95 @@
+// Compile-time check of which storage each element type takes in the C++ API (include/stdgpu_gb300/stdgpu.cuh):
+// integer keys with the default hash and integer mapped values -> the library's precompiled kinds; other
+// trivially copyable keys of at most 8 bytes with a 4/8-byte trivially copyable mapped type -> the word-keyed
+// custom path; everything else -> the wide tables.  Builds to a program that does nothing.
+#include <cstdint>
+#include <type_traits>
+
+#include <stdgpu_gb300/stdgpu.cuh>
+
+struct short3_key
+{
+    std::int16_t x, y, z;
+};
+struct vec3i32_key
+{
+    std::int32_t x, y, z;
+};
+struct key16
+{
+    std::uint64_t a, b;
+};
+struct with_destructor
+{
+    std::uint32_t v = 0;
+    __host__ __device__ ~with_destructor() {}
+};
+struct empty_tag
+{
+};
+struct any_hash
+{
+    template <typename K>
+    __host__ __device__ std::size_t
+    operator()(const K&) const
+    {
+        return 0;
+    }
+};
+
+template <typename Container, typename Base>
+constexpr bool routes_to = std::is_base_of<Base, Container>::value;
+
+using namespace stdgpu;
+using detail::custom_map;
+using detail::custom_set;
+using detail::native_map;
+using detail::native_set;
+using detail::wide_map;
+using detail::wide_set;
+
+// precompiled kinds
+using m1 = unordered_map<std::uint64_t, std::uint32_t>;
+using m2 = unordered_map<std::uint32_t, std::uint64_t>;
+using s1 = unordered_set<std::uint32_t>;
+static_assert(routes_to<m1, native_map<std::uint64_t, std::uint32_t, m1>>, "u64 -> u32 map");
+static_assert(routes_to<m2, native_map<std::uint32_t, std::uint64_t, m2>>, "u32 -> u64 map");
+static_assert(routes_to<s1, native_set<std::uint32_t, s1>>, "u32 set");
+
+// word-keyed custom path
+using c1 = unordered_set<short3_key, any_hash>;
+using c2 = unordered_map<short3_key, float, any_hash>;
+using c3 = unordered_map<std::uint64_t, float>; // integer key, non-integer mapped type
+using c4 = unordered_map<std::uint64_t, std::uint32_t, any_hash>; // integer key, user hash
+static_assert(routes_to<c1, custom_set<short3_key, any_hash, c1>>, "6-byte key set");
+static_assert(routes_to<c2, custom_map<short3_key, float, any_hash, c2>>, "6-byte key, float");
+static_assert(routes_to<c3, custom_map<std::uint64_t, float, hash<std::uint64_t>, c3>>, "u64 -> float");
+static_assert(routes_to<c4, custom_map<std::uint64_t, std::uint32_t, any_hash, c4>>, "u64 with a user hash");
+
+// wide tables
+using w1 = unordered_set<vec3i32_key, any_hash>;
+using w2 = unordered_map<key16, std::uint64_t, any_hash>;
+using w3 = unordered_map<std::uint64_t, key16>;
+using w4 = unordered_map<std::uint32_t, with_destructor>;
+using w5 = unordered_map<vec3i32_key, empty_tag, any_hash>;
+using w6 = unordered_set<with_destructor, any_hash>;
+static_assert(routes_to<w1, wide_set<vec3i32_key, any_hash, w1>>, "12-byte key set");
+static_assert(routes_to<w2, wide_map<key16, std::uint64_t, any_hash, w2>>, "16-byte key");
+static_assert(routes_to<w3, wide_map<std::uint64_t, key16, hash<std::uint64_t>, w3>>, "16-byte mapped type");
+static_assert(routes_to<w4, wide_map<std::uint32_t, with_destructor, hash<std::uint32_t>, w4>>,
+              "mapped type with a destructor");
+static_assert(routes_to<w5, wide_map<vec3i32_key, empty_tag, any_hash, w5>>, "empty mapped type");
+static_assert(routes_to<w6, wide_set<with_destructor, any_hash, w6>>, "key with a destructor");
+
+// the allocator parameter and get_allocator()
+using a1 = unordered_map<std::uint64_t, std::uint32_t, hash<std::uint64_t>, equal_to<std::uint64_t>,
+                         safe_device_allocator<pair<const std::uint64_t, std::uint32_t>>>;
+static_assert(std::is_same<a1, m1>::value, "the default allocator is the reference's");
+static_assert(std::is_same<decltype(a1{}.get_allocator()), safe_device_allocator<pair<const std::uint64_t, std::uint32_t>>>::value,
+              "get_allocator() returns the allocator type");
+
+int
+main()
+{
+    return 0;
+}

@@ -14,6 +14,7 @@ SRC = ROOT / "tests" / "cpp" / "shim_test.cu"
 CUSTOM = ROOT / "tests" / "cpp" / "custom_key_test.cu"
 WIDE = ROOT / "tests" / "cpp" / "wide_key_test.cu"
 WIDE_GOLDEN = ROOT / "tests" / "cpp" / "wide_golden_test.cu"
+ROUTING = ROOT / "tests" / "cpp" / "routing_check.cu"
 GOLDEN = ROOT / "tests" / "golden"
 OUT = ROOT / "tests" / "cpp" / "_build"
 
@@ -111,3 +112,10 @@ def test_wide_keys_replay_reference_fixtures(tmp_path, kind, mode):
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "ALL PASS" in r.stdout
+
+
+def test_element_types_route_to_the_intended_storage():
+    """Compile-time: precompiled kinds for integer keys with the default hash, the word-keyed path for other
+    keys of up to 8 bytes, the wide tables for the rest (static_asserts in tests/cpp/routing_check.cu)."""
+    stdgpu_gb300.load()
+    _compile(src=ROUTING)
