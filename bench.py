@@ -226,12 +226,20 @@ def reference_arm(args):
         if i >= args.warmup:
             vals.append(mops)
     value = statistics.median(vals)
+    n = 1 << args.keys_log2
+    full_ops = n + n + n // 4
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "steps": args.steps, "warmup": args.warmup,
+        # the full-size step at the sampled rate (each timed step is a 2^18-key sample of it)
+        "ms_per_step": full_ops / (value * 1e6) * 1e3,
+        "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": "voxel-block unordered_map<uint64_t,uint32_t>, capacity 2^28, 2^27 keys; "
-                               "insert, find (70% hits), erase 25%", "sampled": True},
+        "config": {"workload": f"voxel-block unordered_map<uint64_t,uint32_t>, capacity 2^{args.keys_log2 + 1}, "
+                               f"2^{args.keys_log2} keys; clear+insert+find(70% hits)+erase(25%) per step",
+                   "capacity": 2 * n, "keys": n, "finds": n, "erases": n // 4,
+                   "parallelism": f"host threads ({threads})", "l2": "not applicable (host)",
+                   "sampled": sample},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": kind, "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "phases_s": detail,
