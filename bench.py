@@ -213,6 +213,28 @@ def cpu_sample_run(threads: int, keys_log2: int = 20, reps: int = 1):
     return best[0], kind, threads, sample, best[1]
 
 
+def std_map_sample(keys_log2: int = 21) -> dict:
+    """Sanity line beside the reference: std::unordered_map<uint64_t, uint32_t> in one host thread on the same
+    sample of the workload (insert, find 70 % hits, erase 25 %)."""
+    import oracle as O
+    from stdgpu_gb300 import workloads as W
+
+    n = 1 << keys_log2
+    w = W.voxel_map(n, hit_frac=HIT_FRAC, erase_frac=ERASE_FRAC, seed=0)
+    secs, hits, _, size = O.ref_std_unordered_map(w.keys, w.values, w.queries, w.erase)
+    ops = len(w.keys) + len(w.queries) + len(w.erase)
+    return {"value": ops / secs / 1e6, "unit": UNIT, "cores": 1, "kind": "std::unordered_map",
+            "sample": f"2^{keys_log2} voxel keys, 2^{keys_log2} finds ({hits} hits), {len(w.erase)} erases; "
+                      f"final size {size}"}
+
+
+def std_map_line(keys_log2: int) -> dict:
+    try:
+        return std_map_sample(keys_log2)
+    except Exception as ex:  # the sanity line never costs the benchmark its result
+        return {"unavailable": str(ex)[:200]}
+
+
 def reference_arm(args):
     ws, rank, _ = dist_info()
     if rank != 0:
@@ -240,7 +262,8 @@ def reference_arm(args):
                    "capacity": 2 * n, "keys": n, "finds": n, "erases": n // 4,
                    "parallelism": f"host threads ({threads})", "l2": "not applicable (host)",
                    "sampled": sample},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": kind, "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": kind, "sample": sample,
+                         "std_unordered_map": std_map_line(18)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "phases_s": detail,
     }
@@ -466,7 +489,8 @@ def native_arm(args):
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         mops, kind, used, sample, _ = cpu_sample_run(1, keys_log2=21, reps=1)
-        cpu = {"value": mops, "unit": UNIT, "cores": used, "kind": kind, "sample": sample}
+        cpu = {"value": mops, "unit": UNIT, "cores": used, "kind": kind, "sample": sample,
+               "std_unordered_map": std_map_line(21)}
 
     if rank == 0:
         line = {

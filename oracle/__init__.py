@@ -222,8 +222,24 @@ def ref_lib() -> ctypes.CDLL:
                                       c_void_p]
         L.sgref_bitset_count.restype = c_int64
         L.sgref_bitset_count.argtypes = [c_void_p, c_int64]
+        L.sgref_std_unordered_map_run.restype = ctypes.c_double
+        L.sgref_std_unordered_map_run.argtypes = [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_int64,
+                                                  POINTER(c_int64), POINTER(ctypes.c_uint64), POINTER(c_int64)]
         _ref = L
     return _ref
+
+
+def ref_std_unordered_map(keys, vals, queries, erase) -> tuple[float, int, int, int]:
+    """std::unordered_map<uint64_t, uint32_t> in one thread over the same insert / find / erase sequence:
+    (wall seconds, hits, sum of the values found, final size)."""
+    k = np.ascontiguousarray(keys, dtype=np.uint64)
+    v = np.ascontiguousarray(vals, dtype=np.uint32)
+    q = np.ascontiguousarray(queries, dtype=np.uint64)
+    e = np.ascontiguousarray(erase, dtype=np.uint64)
+    hits, vsum, size = c_int64(), ctypes.c_uint64(), c_int64()
+    secs = ref_lib().sgref_std_unordered_map_run(_p(k), _p(v), len(k), _p(q), len(q), _p(e), len(e), byref(hits),
+                                                  byref(vsum), byref(size))
+    return float(secs), hits.value, vsum.value, size.value
 
 
 def ref_set_threads(n: int) -> None:

@@ -16,8 +16,10 @@
 
 #include <cstdint>
 #include <cstdlib>
+#include <chrono>
 #include <cstring>
 #include <new>
+#include <unordered_map>
 #include <vector>
 
 #include <stdgpu/algorithm.h>
@@ -644,6 +646,43 @@ sgref_bitset_count(const std::uint32_t* words, std::int64_t nbits)
     std::int64_t c = static_cast<std::int64_t>(b.count());
     stdgpu::bitset<>::destroyDeviceObject(b);
     return c;
+}
+
+// Sanity line beside the reference: the same insert / find / erase sequence on std::unordered_map<uint64_t,
+// uint32_t> in one thread (reserved for n elements).  Returns the wall seconds of the three phases; hits,
+// value_sum (of the values found) and final_size report what it did, so no part of the work can be dropped.
+double
+sgref_std_unordered_map_run(const std::uint64_t* keys, const std::uint32_t* vals, std::int64_t n,
+                            const std::uint64_t* queries, std::int64_t nq, const std::uint64_t* erase,
+                            std::int64_t ne, std::int64_t* hits, std::uint64_t* value_sum, std::int64_t* final_size)
+{
+    std::unordered_map<std::uint64_t, std::uint32_t> m;
+    m.reserve(static_cast<std::size_t>(n));
+    const auto t0 = std::chrono::steady_clock::now();
+    for (std::int64_t i = 0; i < n; ++i)
+    {
+        m.emplace(keys[i], vals[i]);
+    }
+    std::int64_t h = 0;
+    std::uint64_t sum = 0;
+    for (std::int64_t i = 0; i < nq; ++i)
+    {
+        const auto it = m.find(queries[i]);
+        if (it != m.end())
+        {
+            ++h;
+            sum += it->second;
+        }
+    }
+    for (std::int64_t i = 0; i < ne; ++i)
+    {
+        m.erase(erase[i]);
+    }
+    const auto t1 = std::chrono::steady_clock::now();
+    *hits = h;
+    *value_sum = sum;
+    *final_size = static_cast<std::int64_t>(m.size());
+    return std::chrono::duration<double>(t1 - t0).count();
 }
 
 } // extern "C"

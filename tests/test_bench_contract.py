@@ -23,6 +23,9 @@ def test_reference_arm_line_has_the_contract_keys():
     assert {"workload", "capacity", "keys", "finds", "erases"} <= set(d["config"])
     cb = d["cpu_baseline"]
     assert {"value", "unit", "cores", "kind", "sample"} <= set(cb) and cb["kind"] in ("reference", "port")
+    # the std::unordered_map sanity line (one host thread, same sample)
+    sm = cb["std_unordered_map"]
+    assert "unavailable" in sm or (sm["kind"] == "std::unordered_map" and sm["value"] > 0 and sm["cores"] == 1)
     e = d["e2e"]
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0

@@ -199,3 +199,18 @@ def test_port_against_reference_fresh_inputs(kind):
         assert np.array_equal(P.erase(e, flags=True), R.erase(e, flags=True))
         assert P.size() == R.size()
         assert P.valid() and R.valid()
+
+
+def test_std_unordered_map_sanity_run():
+    """The std::unordered_map run beside the reference does the same work: 70 % of the queries hit, the
+    values found are the inserted ones, and the erases leave the expected size."""
+    if not O.ref_available():
+        pytest.skip("reference library not built")
+    from stdgpu_gb300 import workloads as W
+    w = W.voxel_map(1 << 14, hit_frac=0.7, erase_frac=0.25, seed=3)
+    secs, hits, vsum, size = O.ref_std_unordered_map(w.keys, w.values, w.queries, w.erase)
+    present = np.isin(w.queries, w.keys)
+    assert secs > 0 and hits == int(present.sum())
+    lookup = dict(zip(w.keys.tolist(), w.values.tolist()))
+    assert vsum == sum(lookup[q] for q in w.queries[present].tolist())
+    assert size == len(np.unique(w.keys)) - len(np.unique(w.erase[np.isin(w.erase, w.keys)]))
