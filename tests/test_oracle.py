@@ -214,3 +214,28 @@ def test_std_unordered_map_sanity_run():
     lookup = dict(zip(w.keys.tolist(), w.values.tolist()))
     assert vsum == sum(lookup[q] for q in w.queries[present].tolist())
     assert size == len(np.unique(w.keys)) - len(np.unique(w.erase[np.isin(w.erase, w.keys)]))
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_seq_key_table_agrees_with_port(seed):
+    """The element-by-element restatement (used for 12-byte keys) and the C port (pinned to the reference's
+    fixtures) give the same per-element insert / erase outcomes, lookups and contents on word keys, with
+    repeated keys in every call."""
+    rng = np.random.default_rng(seed)
+    cap = 4096
+    keys = rng.integers(0, 3000, size=3000, dtype=np.uint64)
+    vals = (keys * np.uint64(2654435761) & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    port = O.PortTable(O.MAP_U64_U32, cap)
+    bc, ms = port.geometry()
+    seq = O.SeqKeyTable(cap, ms)
+    assert np.array_equal(seq.insert(keys, vals), port.insert(keys, vals, flags=True))
+    q = rng.integers(0, 4000, size=2000, dtype=np.uint64)
+    sv, sf = seq.find(q)
+    pv, pf = port.find(q)
+    assert np.array_equal(sf, pf)
+    assert all(int(a) == int(b) for a, b, f in zip(sv, pv, sf) if f)
+    e = rng.integers(0, 4000, size=1500, dtype=np.uint64)
+    assert np.array_equal(seq.erase(e), port.erase(e, flags=True))
+    assert seq.size() == port.size()
+    rk, _ = port.range()
+    assert np.array_equal(np.sort(seq.keys(np.uint64)), np.sort(rk))
