@@ -56,6 +56,9 @@ ERASE_FRAC = 0.25
 #   erase:  8 B key in + 128 B home group + one 32 B sector written back (the erased marker)
 BYTES_PER_OP = {"insert": 16 + 128 + 32, "find": 8 + 5 + 128, "erase": 8 + 128 + 32}
 NOMINAL_HBM_GBS = 7900.0  # HBM3e nominal, reported beside the measured copy peak
+# the native arm's cpu_baseline: one host thread on 2^23 keys of the workload (capacity 2^24; the
+# reference's arrays, about 0.3 GB, are larger than the host's caches)
+CPU_BASELINE_KEYS_LOG2 = 23
 
 
 def parse_args(argv=None):
@@ -75,6 +78,11 @@ def parse_args(argv=None):
     p.add_argument("--requests", type=int, default=600, help="serve workload: number of requests")
     p.add_argument("--e2e-chunk-log2", type=int, default=22, help="e2e: elements per staged chunk, log2")
     p.add_argument("--e2e-buffers", type=int, default=4, help="e2e: staging buffers in the ring")
+    p.add_argument("--ref-keys-log2", type=int, default=20,
+                   help="reference arm, voxel workload: keys per timed sample step, log2")
+    p.add_argument("--ref-full", action="store_true",
+                   help="reference arm: time the voxel workload at --keys-log2 itself instead of a sample")
+    p.add_argument("--ref-threads", type=int, default=0, help="reference arm: host threads (default: all)")
     return p.parse_args(argv)
 
 
@@ -180,7 +188,8 @@ class ClockSampler:
 # ------------------------------------------------------------------ CPU side
 
 def cpu_sample_run(threads: int, keys_log2: int = 20, reps: int = 1):
-    """Reference (or oracle restatement) on a bounded sample of the workload: returns (Mops/s, kind, sample)."""
+    """Reference (or oracle restatement) on 2^keys_log2 keys of the voxel workload at the benchmark's load
+    (capacity 2^(keys_log2+1)): returns (Mops/s, kind, threads used, sample text, phase seconds, step seconds)."""
     import oracle as O
     from stdgpu_gb300 import workloads as W
 
@@ -203,14 +212,17 @@ def cpu_sample_run(threads: int, keys_log2: int = 20, reps: int = 1):
         t2 = time.perf_counter()
         t.erase(w.erase)
         t3 = time.perf_counter()
+        size = t.size()
         t.close()
+        if size != n - len(w.erase):
+            raise RuntimeError(f"{kind} size {size} after the sample step, want {n - len(w.erase)}")
         ops = len(w.keys) + len(w.queries) + len(w.erase)
         mops = ops / (t3 - t0) / 1e6
         if best is None or mops > best[0]:
-            best = (mops, {"insert_s": t1 - t0, "find_s": t2 - t1, "erase_s": t3 - t2})
+            best = (mops, {"insert_s": t1 - t0, "find_s": t2 - t1, "erase_s": t3 - t2}, t3 - t0)
     sample = (f"2^{keys_log2} voxel keys into capacity 2^{keys_log2 + 1} (same 0.5 load), 2^{keys_log2} finds "
               f"(70% hits), {len(w.erase)} erases; insert+find+erase wall time, best of {reps}")
-    return best[0], kind, threads, sample, best[1]
+    return best[0], kind, threads, sample, best[1], best[2]
 
 
 def std_map_sample(keys_log2: int = 21) -> dict:
@@ -235,35 +247,87 @@ def std_map_line(keys_log2: int) -> dict:
         return {"unavailable": str(ex)[:200]}
 
 
+def small_cpu_run(threads: int, reps: int = 1):
+    """The small configuration at its full size on the host: unordered_set<uint32_t> capacity 2^21, 2^20
+    uniform keys, 2^20 contains (50 % hits), erase of half the keys; (Mops/s, kind, threads, phase s, step s)."""
+    import oracle as O
+    from stdgpu_gb300 import small_bench
+
+    keys, queries, erase = small_bench.make_inputs()
+    kind = "reference" if O.ref_available() else "port"
+    if kind == "reference":
+        O.ref_set_threads(threads)
+        make = lambda: O.RefTable(O.SET_U32, 1 << 21)
+    else:
+        threads = 1
+        make = lambda: O.PortTable(O.SET_U32, 1 << 21)
+    best = None
+    for _ in range(reps):
+        t = make()
+        t0 = time.perf_counter()
+        t.insert(keys)
+        t1 = time.perf_counter()
+        t.contains(queries)
+        t2 = time.perf_counter()
+        t.erase(erase)
+        t3 = time.perf_counter()
+        t.close()
+        ops = len(keys) + len(queries) + len(erase)
+        mops = ops / (t3 - t0) / 1e6
+        if best is None or mops > best[0]:
+            best = (mops, {"insert_s": t1 - t0, "contains_s": t2 - t1, "erase_s": t3 - t2}, t3 - t0)
+    return best[0], kind, threads, best[1], best[2]
+
+
 def reference_arm(args):
+    """The reference's own CPU implementation (oracle/_ref, OpenMP backend) on the host cores.  Each step
+    is the sample that the config names -- for the voxel workload 2^ref_keys_log2 keys at the benchmark's
+    0.5 load (the 2^27-key workload itself takes minutes per step on the host), for the small workload the
+    full configuration -- and ms_per_step is that step's measured wall time."""
     ws, rank, _ = dist_info()
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
-    vals = []
+    threads = args.ref_threads or os.cpu_count() or 1
+    vals, step_s = [], []
     detail = None
     kind = sample = None
-    for i in range(args.warmup + args.steps):
-        mops, kind, used, sample, detail = cpu_sample_run(threads, keys_log2=18, reps=1)
-        if i >= args.warmup:
-            vals.append(mops)
+    if args.workload == "small":
+        for i in range(args.warmup + args.steps):
+            mops, kind, used, detail, secs = small_cpu_run(threads)
+            if i >= args.warmup:
+                vals.append(mops)
+                step_s.append(secs)
+        sample = "the full small configuration (2^20 keys, capacity 2^21): insert+contains+erase wall time"
+        config = {"workload": "unordered_set<uint32_t>, capacity 2^21, 2^20 uniform keys; insert + contains "
+                              "(50% hits) + erase half, per step", "capacity": 1 << 21, "keys": 1 << 20,
+                  "finds": 1 << 20, "erases": 1 << 19}
+        std_line = None
+    else:
+        k = args.keys_log2 if args.ref_full else args.ref_keys_log2
+        for i in range(args.warmup + args.steps):
+            mops, kind, used, sample, detail, secs = cpu_sample_run(threads, keys_log2=k, reps=1)
+            if i >= args.warmup:
+                vals.append(mops)
+                step_s.append(secs)
+        n = 1 << k
+        config = {"workload": f"voxel-block unordered_map<uint64_t,uint32_t>, capacity 2^{k + 1}, 2^{k} keys; "
+                              f"insert+find(70% hits)+erase(25%) per step",
+                  "capacity": 2 * n, "keys": n, "finds": n, "erases": n // 4,
+                  "native_arm_workload": f"the same generator at 2^{args.keys_log2} keys, capacity "
+                                         f"2^{args.keys_log2 + 1}" + (" (this run)" if args.ref_full else
+                                                                      " (this run times a sample of it)")}
+        std_line = std_map_line(k) if k <= 24 else None
     value = statistics.median(vals)
-    n = 1 << args.keys_log2
-    full_ops = n + n + n // 4
+    config.update({"parallelism": f"host threads ({used})", "l2": "not applicable (host)", "sampled": sample})
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
-        # the full-size step at the sampled rate (each timed step is a 2^18-key sample of it)
-        "ms_per_step": full_ops / (value * 1e6) * 1e3,
+        "ms_per_step": statistics.median(step_s) * 1e3,
         "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u64", "data": "synthetic",
-        "config": {"workload": f"voxel-block unordered_map<uint64_t,uint32_t>, capacity 2^{args.keys_log2 + 1}, "
-                               f"2^{args.keys_log2} keys; clear+insert+find(70% hits)+erase(25%) per step",
-                   "capacity": 2 * n, "keys": n, "finds": n, "erases": n // 4,
-                   "parallelism": f"host threads ({threads})", "l2": "not applicable (host)",
-                   "sampled": sample},
+        "vs_baseline": None, "dtype": "u64" if args.workload != "small" else "u32", "data": "synthetic",
+        "config": config,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": used, "kind": kind, "sample": sample,
-                         "std_unordered_map": std_map_line(18)},
+                         "std_unordered_map": std_line},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "phases_s": detail,
     }
@@ -275,7 +339,6 @@ def reference_arm(args):
 def native_arm(args):
     import torch
     import stdgpu_gb300 as sg
-    from stdgpu_gb300 import workloads as W
 
     ws, rank, local = dist_info()
     if ws > 1:
@@ -284,26 +347,16 @@ def native_arm(args):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
 
-    n = 1 << args.keys_log2
-    cap = 1 << (args.keys_log2 + 1)
-    w = W.voxel_map(n, hit_frac=HIT_FRAC, erase_frac=ERASE_FRAC, seed=0)
-    n_q, n_e = len(w.queries), len(w.erase)
+    from stdgpu_gb300.voxel_step import VoxelStep
 
-    # value_type array: pair<const uint64_t, uint32_t> = 16 bytes (key, value, 4 bytes padding)
-    pairs_np = np.zeros((n, 2), np.uint64)
-    pairs_np[:, 0] = w.keys
-    pairs_np[:, 1] = w.values.astype(np.uint64)
-    to_dev = lambda a: torch.from_numpy(a.view(np.int64)).to(dev)
-    pairs = to_dev(pairs_np.reshape(-1))
-    queries = to_dev(w.queries)
-    erase = to_dev(w.erase)
-    out_vals = torch.empty(n_q, dtype=torch.int32, device=dev)
-    out_found = torch.empty(n_q, dtype=torch.uint8, device=dev)
-
-    table = sg.unordered_map.createDeviceObject(cap, key="u64", mapped="u32")
-    lib = sg.load()
+    vs = VoxelStep(args.keys_log2, dev, hit_frac=HIT_FRAC, erase_frac=ERASE_FRAC, seed=0)
+    w = vs.w
+    n, cap, n_q, n_e = vs.n, vs.capacity, vs.n_q, vs.n_e
+    pairs_np = vs.pairs_np
+    pairs, queries, erase = vs.pairs, vs.queries, vs.erase
+    out_vals, out_found = vs.out_vals, vs.out_found
+    table, lib, h = vs.table, vs.lib, vs.h
     from ctypes import c_void_p
-    h = table._h
     stream = torch.cuda.current_stream(dev)
     sp = c_void_p(stream.cuda_stream)
 
@@ -312,21 +365,7 @@ def native_arm(args):
             raise RuntimeError(f"{what} failed with status {status}")
 
     def step(ev=None):
-        if ev is not None:
-            ev[0].record(stream)
-        call(lib.sg_unordered_clear(h, sp), "clear")
-        if ev is not None:
-            ev[1].record(stream)
-        call(lib.sg_unordered_insert(h, c_void_p(pairs.data_ptr()), n, None, sp), "insert")
-        if ev is not None:
-            ev[2].record(stream)
-        call(lib.sg_unordered_find(h, c_void_p(queries.data_ptr()), n_q, c_void_p(out_vals.data_ptr()),
-                                   c_void_p(out_found.data_ptr()), sp), "find")
-        if ev is not None:
-            ev[3].record(stream)
-        call(lib.sg_unordered_erase(h, c_void_p(erase.data_ptr()), n_e, None, sp), "erase")
-        if ev is not None:
-            ev[4].record(stream)
+        vs.step(stream, ev)
 
     # the random-read ceiling of this GPU's memory, on a buffer the size of the table (untimed, before the run)
     from ctypes import byref, c_double
@@ -339,14 +378,11 @@ def native_arm(args):
                            "32- and 64-byte reads complete at the same rate, so a probe kernel that reads one "
                            "group line per key is bound by this count, not by bytes"}
 
-    # correctness guard on the timed configuration (one untimed pass)
-    step()
-    torch.cuda.synchronize(dev)
-    size = table.size()
-    found = int(out_found.sum())
-    expect_found = int(w.query_hit.sum())
-    if size != n - n_e or found != expect_found:
-        raise RuntimeError(f"wrong results: size {size} (want {n - n_e}), found {found} (want {expect_found})")
+    # correctness guard on the timed configuration (one untimed pass): sizes after every call, every found
+    # flag and value, and the final contents compared element by element with an independent computation
+    guard = vs.checked_step(stream)
+    checked_found = out_found.cpu().numpy().astype(bool)
+    checked_vals = out_vals.cpu()
 
     for _ in range(args.warmup):
         step()
@@ -427,8 +463,11 @@ def native_arm(args):
                 fn()
             b.record(stream)
             torch.cuda.synchronize(dev)
-            if int(found_h.sum()) != expect_found or table.size() != n - n_e:
-                raise RuntimeError("e2e results wrong")
+            got = found_h.numpy().astype(bool)
+            gm = torch.from_numpy(got)
+            if (not np.array_equal(got, checked_found) or not torch.equal(vals_h[gm], checked_vals[gm])
+                    or table.size() != n - n_e):
+                raise RuntimeError("e2e results differ from the checked device-resident step")
             found_h.zero_()
             return a.elapsed_time(b) / args.steps
 
@@ -488,9 +527,9 @@ def native_arm(args):
 
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        mops, kind, used, sample, _ = cpu_sample_run(1, keys_log2=21, reps=1)
+        mops, kind, used, sample, _, _ = cpu_sample_run(1, keys_log2=CPU_BASELINE_KEYS_LOG2, reps=1)
         cpu = {"value": mops, "unit": UNIT, "cores": used, "kind": kind, "sample": sample,
-               "std_unordered_map": std_map_line(21)}
+               "std_unordered_map": std_map_line(CPU_BASELINE_KEYS_LOG2)}
 
     if rank == 0:
         line = {
@@ -502,6 +541,8 @@ def native_arm(args):
                        "capacity": cap, "keys": n, "finds": n_q, "erases": n_e, "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "inputs larger than L2 (no flush)"},
             "phases_ms": med,
+            "guard": {"checked": "sizes after each call; found flags and values of all queries; final contents",
+                      "insert_launches": guard["insert_launches"], "erase_launches": guard["erase_launches"]},
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
@@ -509,7 +550,7 @@ def native_arm(args):
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
-    sg.unordered_base.destroyDeviceObject(table)
+    vs.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
 

@@ -646,21 +646,23 @@ load_homes(const dview& t, const tile_lanes& L, uint64_t hash, bool probe, uint3
 // Insert step.  Per key, from its home group: present (nothing to do), or a claim of the first erased
 // slot of the group (when the group also has a never-used slot) else of the first never-used slot, made
 // by the key's own lane with one compare-and-swap -- 32 claims in flight per warp.
-template <int KIND, bool AOS>
+// The step over keys already in registers (key / val of lane element i, meaningful when valid; hashes as
+// in the loading steps below).
+template <int KIND>
 SG_D void
-insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in1, int64_t i, bool valid,
-            uint8_t* out_flags, step_counts& c, const uint64_t* hashes = nullptr)
+insert_kv_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K key,
+               typename kind_consts<KIND>::V val, int64_t i, bool valid, uint8_t* out_flags, step_counts& c,
+               const uint64_t* hashes = nullptr)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
     using V = typename C::V;
     constexpr uint32_t G = C::slots_per_group;
     constexpr uint32_t S = sector_consts<KIND>::slots;
-    K key = C::empty_key;
-    V val{};
-    if (valid)
+    if (!valid)
     {
-        load_input<KIND, AOS>(in0, in1, i, key, val);
+        key = C::empty_key;
+        val = V{};
     }
     const bool special = valid && key >= C::tomb_key;
     int res = special ? special_insert<KIND>(t, key, val) : 0;
@@ -772,6 +774,20 @@ insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in
     }
 }
 
+template <int KIND, bool AOS>
+SG_D void
+insert_step(const dview& t, const tile_lanes& L, const void* in0, const void* in1, int64_t i, bool valid,
+            uint8_t* out_flags, step_counts& c, const uint64_t* hashes = nullptr)
+{
+    typename kind_consts<KIND>::K key = kind_consts<KIND>::empty_key;
+    typename kind_consts<KIND>::V val{};
+    if (valid)
+    {
+        load_input<KIND, AOS>(in0, in1, i, key, val);
+    }
+    insert_kv_step<KIND>(t, L, key, val, i, valid, out_flags, c, hashes);
+}
+
 // Locates the slot of each lane's key (-1 when absent); with WANT_VALUE the mapped value comes back in
 // val.  Keys not decided in their home group (group full of other keys) continue with tile_find.
 template <int KIND, bool WANT_VALUE>
@@ -843,13 +859,16 @@ locate_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K k
 // Erase step: every lane locates its key, then swaps its slot to the erased marker.
 template <int KIND>
 SG_D void
-erase_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool valid, uint8_t* out_flags,
-           step_counts& c, const uint64_t* hashes = nullptr)
+erase_key_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K key, int64_t i, bool valid,
+               uint8_t* out_flags, step_counts& c, const uint64_t* hashes = nullptr)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
     using V = typename C::V;
-    const K key = valid ? __ldcs(reinterpret_cast<const K*>(keys) + i) : C::empty_key;
+    if (!valid)
+    {
+        key = C::empty_key;
+    }
     const bool special = valid && key >= C::tomb_key;
     int res = 0;
     if (special)
@@ -875,16 +894,29 @@ erase_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, boo
     }
 }
 
+template <int KIND>
+SG_D void
+erase_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool valid, uint8_t* out_flags,
+           step_counts& c, const uint64_t* hashes = nullptr)
+{
+    using K = typename kind_consts<KIND>::K;
+    const K key = valid ? __ldcs(reinterpret_cast<const K*>(keys) + i) : kind_consts<KIND>::empty_key;
+    erase_key_step<KIND>(t, L, key, i, valid, out_flags, c, hashes);
+}
+
 // Find / contains step.
 template <int KIND, bool WANT_VALUES>
 SG_D void
-find_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool valid, void* out_vals,
-          uint8_t* out_found, const uint64_t* hashes = nullptr)
+find_key_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K key, int64_t i, bool valid,
+              void* out_vals, uint8_t* out_found, const uint64_t* hashes = nullptr)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
     using V = typename C::V;
-    const K key = valid ? __ldcs(reinterpret_cast<const K*>(keys) + i) : C::empty_key;
+    if (!valid)
+    {
+        key = C::empty_key;
+    }
     const bool special = valid && key >= C::tomb_key;
     V val{};
     bool found = special ? special_find<KIND>(t, key, val) : false;
@@ -911,6 +943,16 @@ find_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool
             }
         }
     }
+}
+
+template <int KIND, bool WANT_VALUES>
+SG_D void
+find_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool valid, void* out_vals,
+          uint8_t* out_found, const uint64_t* hashes = nullptr)
+{
+    using K = typename kind_consts<KIND>::K;
+    const K key = valid ? __ldcs(reinterpret_cast<const K*>(keys) + i) : kind_consts<KIND>::empty_key;
+    find_key_step<KIND, WANT_VALUES>(t, L, key, i, valid, out_vals, out_found, hashes);
 }
 
 } // namespace detail

@@ -23,6 +23,7 @@
 #include "stdgpu_gb300.h"
 #include "stdgpu_gb300/detail/layout.cuh"
 #include "stdgpu_gb300/device.cuh"
+#include "bulk_stage.cuh"
 #include "table_core.cuh"
 
 namespace sg
@@ -391,6 +392,52 @@ ordered_chunk(const part_layout& pl, unsigned long long c, int64_t& first, int64
     return true;
 }
 
+// L2 prefetch ahead of the ordered insert.  Chunk (p, j) -- the j-th of the `per` chunks of partition p --
+// is mapped onto the j-th of `per` equal slices of partition p's home-group range, so the claims, which run
+// through the chunks in order, sweep the slot array front to back.  The block that claims chunk c issues a
+// bulk L2 prefetch (cp.async.bulk.prefetch.L2, the TMA unit's L2 fill) of chunk c + SG_ORDERED_PREFETCH's
+// slice: partitions ahead of the claim front arrive in L2 as sequential lines instead of each insert's
+// random line read, and the dirty lines leave L2 in about the same order.  0 turns it off.
+#ifndef SG_ORDERED_PREFETCH
+#define SG_ORDERED_PREFETCH 0
+#endif
+
+SG_D void
+prefetch_l2_bulk(const char* p, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// Warp 0 of the calling block prefetches slice j of partition p's groups (p < parts); every address lies in
+// the slot array, and every piece starts on a group boundary and is a whole number of groups.
+template <int CHUNK>
+SG_D void
+prefetch_chunk_slice(const dview& t, const part_layout& pl, unsigned long long c)
+{
+    const unsigned long long per = pl.cap / CHUNK;
+    const unsigned long long p = c / per;
+    if (p >= static_cast<unsigned long long>(pl.parts))
+    {
+        return;
+    }
+    const unsigned long long j = c - p * per;
+    const unsigned long long b_lo = p << pl.shift;
+    const unsigned long long b_hi = (p + 1) << pl.shift;
+    const unsigned long long g_lo = (b_lo * t.num_groups) >> t.bits;
+    const unsigned long long g_hi = (b_hi * t.num_groups) >> t.bits;
+    const unsigned long long ng = g_hi - g_lo;
+    const unsigned long long s_lo = g_lo + ng * j / per;
+    const unsigned long long s_hi = g_lo + ng * (j + 1) / per;
+    const unsigned long long span = s_hi - s_lo; // groups of the slice
+    const int lane = threadIdx.x & 31;
+    const unsigned long long a = s_lo + span * lane / 32;
+    const unsigned long long b = s_lo + span * (lane + 1) / 32;
+    if (b > a && b <= t.num_groups)
+    {
+        prefetch_l2_bulk(t.slots + (a << 7), static_cast<uint32_t>((b - a) << 7));
+    }
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, SG_ORDERED_MIN_BLOCKS)
 k_insert_ordered(dview t, const void* in0, part_layout pl, unsigned long long* next_chunk)
@@ -414,7 +461,8 @@ k_insert_ordered(dview t, const void* in0, part_layout pl, unsigned long long* n
         }
         __syncthreads();
         int64_t first, last;
-        const bool more = ordered_chunk<kOrderedChunk>(pl, s_claim, first, last);
+        const unsigned long long cur = s_claim;
+        const bool more = ordered_chunk<kOrderedChunk>(pl, cur, first, last);
         __syncthreads();
         if (!more)
         {
@@ -424,6 +472,14 @@ k_insert_ordered(dview t, const void* in0, part_layout pl, unsigned long long* n
         {
             claimed = atomicAdd(next_chunk, 1ull);
         }
+#if SG_ORDERED_PREFETCH > 0
+        if (warp == 0)
+        {
+            prefetch_chunk_slice<kOrderedChunk>(t, pl, cur + SG_ORDERED_PREFETCH);
+        }
+#else
+        (void)cur;
+#endif
         for (int64_t base = first + warp * 32; base < last; base += kThreads)
         {
             const int64_t i = base + L.lane;
@@ -484,6 +540,188 @@ k_erase_ordered(dview t, const void* keys, part_layout pl, unsigned long long* n
     block_add<2>(v, dst);
 }
 
+// Ordered insert / erase with the input staged in shared memory.  The block's chunks are copied from the
+// partitioned scratch array into a double buffer by bulk copies (cp.async.bulk, completed on an mbarrier):
+// thread 0 stages chunk k + 1 while the warps probe chunk k, so every warp finds its 32 elements in shared
+// memory when it reaches them and issues its home-group loads without first waiting for the input.
+#ifndef SG_ORDERED_STAGE
+#define SG_ORDERED_STAGE 0
+#endif
+#ifndef SG_STAGE_ITERS
+#define SG_STAGE_ITERS 4
+#endif
+constexpr int kStageChunk = SG_STAGE_ITERS * kThreads;
+
+template <int KIND, bool ERASE>
+struct staged_elem
+{
+    using type = typename std::conditional<ERASE, typename kind_consts<KIND>::K, typename slot_image<KIND>::type>::type;
+};
+
+// key / mapped value of a value_type image (padding ignored)
+template <int KIND>
+SG_D void
+unpack_element(const typename slot_image<KIND>::type& e, typename kind_consts<KIND>::K& key,
+               typename kind_consts<KIND>::V& val)
+{
+    constexpr int sb = kind_consts<KIND>::slot_bytes;
+    if constexpr (sb == 16)
+    {
+        key = key_in_lane<KIND>(e, 0);
+        val = value_in_lane<KIND>(e, 0);
+    }
+    else if constexpr (sb == 8)
+    {
+        const uint4 q = make_uint4(e.x, e.y, 0u, 0u);
+        key = key_in_lane<KIND>(q, 0);
+        val = value_in_lane<KIND>(q, 0);
+    }
+    else
+    {
+        key = static_cast<typename kind_consts<KIND>::K>(e);
+        val = typename kind_consts<KIND>::V{};
+    }
+}
+
+template <int KIND, bool ERASE, int CHUNK>
+__global__ void __launch_bounds__(kThreads, SG_ORDERED_MIN_BLOCKS)
+k_ordered_staged(dview t, const void* in, part_layout pl, unsigned long long* next_chunk)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    using E = typename staged_elem<KIND, ERASE>::type;
+    static_assert(2 * CHUNK * sizeof(E) <= 40 * 1024, "staging buffers exceed the static shared memory budget");
+    __shared__ __align__(128) E buf[2][CHUNK];
+    __shared__ __align__(8) uint64_t full[2];
+    __shared__ long long s_first[2];
+    __shared__ long long s_last[2];
+    const tile_lanes L;
+    const int warp = threadIdx.x >> 5;
+    const E* src = static_cast<const E*>(in);
+    step_counts c;
+
+    // thread 0: chunk ch into buffer b.  Its range goes to s_first / s_last (s_first = -1 past the last chunk);
+    // every call completes one phase of full[b], by the copy's bytes or, with nothing to copy, a plain arrival.
+    // The copy is rounded up to 16 bytes; the rounded tail stays inside the chunk's region, whose capacity is
+    // a whole number of chunks.
+    auto stage = [&](unsigned long long ch, int b) {
+        int64_t first, last;
+        if (!ordered_chunk<CHUNK>(pl, ch, first, last))
+        {
+            first = last = -1;
+        }
+        s_first[b] = first;
+        s_last[b] = last;
+        if (last > first)
+        {
+            const uint32_t bytes = static_cast<uint32_t>(((last - first) * static_cast<int64_t>(sizeof(E)) + 15) & ~15ll);
+            mbar_arrive_expect(&full[b], bytes);
+            bulk_to_shared(&buf[b][0], src + first, bytes, &full[b]);
+        }
+        else
+        {
+            mbar_arrive(&full[b]);
+        }
+    };
+
+    unsigned long long claimed = 0;
+    if (threadIdx.x == 0)
+    {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        fence_async_shared();
+        stage(atomicAdd(next_chunk, 1ull), 0);
+        claimed = atomicAdd(next_chunk, 1ull);
+    }
+    __syncthreads();
+    for (int k = 0;; ++k)
+    {
+        const int b = k & 1;
+        const long long first = s_first[b];
+        const long long last = s_last[b];
+        if (first < 0)
+        {
+            break;
+        }
+        if (threadIdx.x == 0)
+        {
+            // buffer b ^ 1 was released by the barrier that ended the previous chunk
+            stage(claimed, b ^ 1);
+            claimed = atomicAdd(next_chunk, 1ull);
+        }
+#if SG_ORDERED_PREFETCH > 0
+        if (!ERASE && warp == 0)
+        {
+            // chunk index of this buffer: the block's claims are consecutive in `next_chunk` order only per
+            // block, so the slice ahead is keyed on the chunk's own position
+            const unsigned long long per = pl.cap / CHUNK;
+            const unsigned long long cidx = static_cast<unsigned long long>(first / pl.cap) * per +
+                                            static_cast<unsigned long long>(first % pl.cap) / CHUNK;
+            if (first < static_cast<long long>(pl.parts) * pl.cap)
+            {
+                prefetch_chunk_slice<CHUNK>(t, pl, cidx + SG_ORDERED_PREFETCH);
+            }
+        }
+#endif
+        const bool ok = mbar_wait(&full[b], static_cast<uint32_t>(k >> 1) & 1u);
+        if (__syncthreads_or(!ok))
+        {
+            if (threadIdx.x == 0)
+            {
+                atomicOr(&t.hdr->error, kErrStageWait);
+                // the copy just staged into the other buffer, and a late one into this buffer
+                mbar_wait(&full[b ^ 1], static_cast<uint32_t>((k + 1) >> 1) & 1u);
+                mbar_wait(&full[b], static_cast<uint32_t>(k >> 1) & 1u);
+            }
+            break;
+        }
+        for (long long base = first + warp * 32; base < last; base += kThreads)
+        {
+            const long long i = base + L.lane;
+            const bool valid = i < last;
+            K key = C::empty_key;
+            V val{};
+            if (valid)
+            {
+                if constexpr (ERASE)
+                {
+                    key = buf[b][i - first];
+                }
+                else
+                {
+                    unpack_element<KIND>(buf[b][i - first], key, val);
+                }
+            }
+            if constexpr (ERASE)
+            {
+                erase_key_step<KIND>(t, L, key, i, valid, nullptr, c);
+            }
+            else
+            {
+                insert_kv_step<KIND>(t, L, key, val, i, valid, nullptr, c);
+            }
+        }
+        __syncthreads(); // buffer b is read; thread 0 may stage into it in the next iteration
+    }
+    if constexpr (ERASE)
+    {
+        unsigned long long v[2] = { 0ull - c.done, c.done - c.oob };
+        unsigned long long* const dst[2] = { &t.hdr->size, &t.hdr->tombstones };
+        block_add<2>(v, dst);
+    }
+    else
+    {
+        if (c.retry != 0)
+        {
+            atomicOr(&t.hdr->error, kErrRetry);
+        }
+        unsigned long long v[3] = { c.done, c.refused, 0ull - c.reused };
+        unsigned long long* const dst[3] = { &t.hdr->size, &t.hdr->refused, &t.hdr->tombstones };
+        block_add<3>(v, dst);
+    }
+}
+
 // Bulk erase: src/stdgpu/impl/unordered_base_detail.cuh:1045-1066 (erase_from_key :497-522).
 template <int KIND>
 __global__ void __launch_bounds__(kThreads, SG_BULK_MIN_BLOCKS)
@@ -520,6 +758,103 @@ k_find(dview t, const void* keys, int64_t n, void* out_vals, uint8_t* out_found,
     {
         const int64_t i = base + L.lane;
         find_step<KIND, WANT_VALUES>(t, L, keys, i, i < n, out_vals, out_found, hashes);
+    }
+}
+
+// Bulk find / contains with the query keys staged in shared memory: each warp keeps a ring of
+// SG_FIND_STAGES stages of its next 32 keys, filled by bulk copies that lane 0 issues SG_FIND_STAGES
+// iterations ahead, so the home-group loads of an iteration start without waiting for its keys.  A
+// partial last tile of 32 is loaded directly.  Keys must be 16-byte aligned (checked by the caller).
+#ifndef SG_FIND_STAGE
+#define SG_FIND_STAGE 0
+#endif
+#ifndef SG_FIND_STAGES
+#define SG_FIND_STAGES 4
+#endif
+
+template <int KIND, bool WANT_VALUES>
+__global__ void __launch_bounds__(kThreads, SG_FIND_MIN_BLOCKS)
+k_find_staged(dview t, const void* keys, int64_t n, void* out_vals, uint8_t* out_found)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    constexpr int ST = SG_FIND_STAGES;
+    constexpr int W = kThreads / 32;
+    __shared__ __align__(128) K ring[W][ST][32];
+    __shared__ __align__(8) uint64_t bars[W][ST];
+    const tile_lanes L;
+    const int w = threadIdx.x >> 5;
+    const int64_t gwarp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    const K* src = static_cast<const K*>(keys);
+    // lane 0: the 32 keys of iteration `it` into stage s -- a bulk copy when all 32 are in range, else a plain
+    // arrival (the lanes then load their keys themselves); either completes one phase of bars[w][s]
+    auto issue = [&](int64_t it, int st) {
+        const int64_t base = (gwarp + it * nwarps) * 32;
+        if (base + 32 <= n)
+        {
+            mbar_arrive_expect(&bars[w][st], 32 * sizeof(K));
+            bulk_to_shared(&ring[w][st][0], src + base, 32 * sizeof(K), &bars[w][st]);
+        }
+        else
+        {
+            mbar_arrive(&bars[w][st]);
+        }
+    };
+    if (L.lane == 0)
+    {
+        for (int st = 0; st < ST; ++st)
+        {
+            mbar_init(&bars[w][st], 1);
+        }
+        fence_async_shared();
+        for (int st = 0; st < ST; ++st)
+        {
+            if ((gwarp + st * nwarps) * 32 < n)
+            {
+                issue(st, st);
+            }
+        }
+    }
+    __syncwarp();
+    for (int64_t it = 0;; ++it)
+    {
+        const int64_t base = (gwarp + it * nwarps) * 32;
+        if (base >= n)
+        {
+            break;
+        }
+        const int st = static_cast<int>(it % ST);
+        const bool ok = mbar_wait(&bars[w][st], static_cast<uint32_t>(it / ST) & 1u);
+        if (__any_sync(0xffffffffu, !ok))
+        {
+            if (L.lane == 0)
+            {
+                atomicOr(&t.hdr->error, kErrStageWait);
+                for (int64_t j = it; j < it + ST; ++j) // copies still in flight, this one included
+                {
+                    if ((gwarp + j * nwarps) * 32 < n)
+                    {
+                        mbar_wait(&bars[w][j % ST], static_cast<uint32_t>(j / ST) & 1u);
+                    }
+                }
+            }
+            break;
+        }
+        const int64_t i = base + L.lane;
+        const bool valid = i < n;
+        K key = C::empty_key;
+        if (valid)
+        {
+            key = base + 32 <= n ? ring[w][st][L.lane] : __ldcs(src + i);
+        }
+        __syncwarp();
+        if (L.lane == 0 && (gwarp + (it + ST) * nwarps) * 32 < n)
+        {
+            fence_async_shared();
+            issue(it + ST, st);
+        }
+        find_key_step<KIND, WANT_VALUES>(t, L, key, i, valid, out_vals, out_found);
     }
 }
 
@@ -927,6 +1262,15 @@ ensure_part_scratch(sg_unordered* t, int64_t bytes)
         return e == cudaErrorMemoryAllocation ? SG_ERR_OOM : SG_ERR_CUDA;
     }
     t->part_scratch_bytes = bytes;
+    if (reinterpret_cast<uintptr_t>(t->part_scratch) % 16 != 0)
+    {
+        // the staged kernels copy chunks of the array with 16-byte-aligned bulk copies; an allocator that
+        // returned less alignment gets the direct kernels instead
+        sg::detail::dev_free(t->part_scratch);
+        t->part_scratch = nullptr;
+        t->part_scratch_bytes = 0;
+        return SG_ERR_OOM;
+    }
     return SG_OK;
 }
 
@@ -997,10 +1341,11 @@ struct do_insert
         part_layout pl{};
         unsigned long long* next_chunk = nullptr;
         sg_status st = SG_ERR_OOM;
+        constexpr int kChunk = SG_ORDERED_STAGE ? kStageChunk : kOrderedChunk;
         if (hashes == nullptr && use_partitioned_insert(t, n, flags))
         {
-            st = aos ? partition_into_scratch<KIND, true, kOrderedChunk>(t, in0, in1, n, s, &pl, &next_chunk)
-                     : partition_into_scratch<KIND, false, kOrderedChunk>(t, in0, in1, n, s, &pl, &next_chunk);
+            st = aos ? partition_into_scratch<KIND, true, kChunk>(t, in0, in1, n, s, &pl, &next_chunk)
+                     : partition_into_scratch<KIND, false, kChunk>(t, in0, in1, n, s, &pl, &next_chunk);
             if (st != SG_OK && st != SG_ERR_OOM)
             {
                 return st;
@@ -1011,10 +1356,19 @@ struct do_insert
         const unsigned int* gate = nullptr;
         if (st == SG_OK)
         {
-            static const int max_grid = persistent_grid(k_insert_ordered<KIND>, kThreads);
-            k_insert_ordered<KIND><<<grid_for(n, kOrderedChunk, max_grid), kThreads, 0, s>>>(view_of(t),
-                                                                                            t->part_scratch, pl,
-                                                                                            next_chunk);
+            if constexpr (SG_ORDERED_STAGE)
+            {
+                static const int max_grid = persistent_grid(k_ordered_staged<KIND, false, kChunk>, kThreads);
+                k_ordered_staged<KIND, false, kChunk><<<grid_for(n, kChunk, max_grid), kThreads, 0, s>>>(
+                        view_of(t), t->part_scratch, pl, next_chunk);
+            }
+            else
+            {
+                static const int max_grid = persistent_grid(k_insert_ordered<KIND>, kThreads);
+                k_insert_ordered<KIND><<<grid_for(n, kChunk, max_grid), kThreads, 0, s>>>(view_of(t),
+                                                                                         t->part_scratch, pl,
+                                                                                         next_chunk);
+            }
             SG_LAUNCH_CHECK();
             gate = pl.lost;
         }
@@ -1055,9 +1409,18 @@ struct do_erase
         const unsigned int* gate = nullptr;
         if (st == SG_OK)
         {
-            static const int g_ordered = persistent_grid(k_erase_ordered<KIND>, kThreads);
-            k_erase_ordered<KIND><<<grid_for(n, kEraseChunk, g_ordered), kThreads, 0, s>>>(view_of(t), t->part_scratch,
-                                                                                           pl, next_chunk);
+            if constexpr (SG_ORDERED_STAGE)
+            {
+                static const int g_ordered = persistent_grid(k_ordered_staged<KIND, true, kEraseChunk>, kThreads);
+                k_ordered_staged<KIND, true, kEraseChunk><<<grid_for(n, kEraseChunk, g_ordered), kThreads, 0, s>>>(
+                        view_of(t), t->part_scratch, pl, next_chunk);
+            }
+            else
+            {
+                static const int g_ordered = persistent_grid(k_erase_ordered<KIND>, kThreads);
+                k_erase_ordered<KIND><<<grid_for(n, kEraseChunk, g_ordered), kThreads, 0, s>>>(
+                        view_of(t), t->part_scratch, pl, next_chunk);
+            }
             SG_LAUNCH_CHECK();
             gate = pl.lost;
         }
@@ -1075,6 +1438,23 @@ struct do_find
     run(sg_unordered* t, const void* keys, int64_t n, void* vals, uint8_t* found, cudaStream_t s,
         const uint64_t* hashes = nullptr)
     {
+        if (SG_FIND_STAGE && hashes == nullptr && reinterpret_cast<uintptr_t>(keys) % 16 == 0)
+        {
+            if (vals != nullptr)
+            {
+                static const int max_grid = persistent_grid(k_find_staged<KIND, true>, kThreads);
+                k_find_staged<KIND, true><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n,
+                                                                                              vals, found);
+            }
+            else
+            {
+                static const int max_grid = persistent_grid(k_find_staged<KIND, false>, kThreads);
+                k_find_staged<KIND, false><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), keys, n,
+                                                                                               vals, found);
+            }
+            SG_LAUNCH_CHECK();
+            return SG_OK;
+        }
         if (vals != nullptr)
         {
             static const int max_grid = persistent_grid(k_find<KIND, true>, kThreads);

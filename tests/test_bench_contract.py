@@ -21,6 +21,10 @@ def test_reference_arm_line_has_the_contract_keys():
     assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
     assert d["unit"] == "Mops/s" and d["scaling"] == "weak"
     assert {"workload", "capacity", "keys", "finds", "erases"} <= set(d["config"])
+    # ms_per_step is the measured step of the sample the config names (one step here: exactly the value)
+    c = d["config"]
+    ops = c["keys"] + c["finds"] + c["erases"]
+    assert abs(ops / (d["ms_per_step"] * 1e3) - d["value"]) <= 1e-6 * d["value"]
     cb = d["cpu_baseline"]
     assert {"value", "unit", "cores", "kind", "sample"} <= set(cb) and cb["kind"] in ("reference", "port")
     # the std::unordered_map sanity line (one host thread, same sample)
