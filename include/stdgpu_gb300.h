@@ -88,6 +88,9 @@ typedef struct sg_unordered_view
     int64_t bucket_count;
     int32_t bucket_bits;     /* log2(bucket_count) */
     int32_t kind;
+    uint32_t* insert_locks;  /* device stripe locks of the native device inserts, lock_mask + 1 of them (a power
+                                of two); nullable: device inserts then claim never-used slots only */
+    int64_t lock_mask;
 } sg_unordered_view;
 
 /* ---------------- device memory ---------------- */
@@ -297,10 +300,12 @@ SG_API sg_status sg_batch_info(const sg_table_batch* batch, int64_t* out_storage
 /* ---------------- served request stream (no counterpart in the reference) ---------------- */
 
 /* A scheduler thread keeps tables of one kind resident and executes submitted requests with
- * continuous batching: each free launch slot takes, from every table with pending requests and
- * nothing in flight, its run of consecutive same-operation requests; all runs of one operation share
- * one segmented launch, and the launches of a wave run on different streams.  Requests on one table
- * execute in submission order.  Tables are admitted, and grown (rehashed to twice the capacity)
+ * continuous batching: whenever launches complete or requests arrive, every table with pending requests
+ * and nothing in flight contributes its run of consecutive same-operation requests.  Small runs of one
+ * operation share one segmented launch on a high-priority stream; a run of many keys (sg_server_set_policy)
+ * runs as its own launches, cut into chunks, on a low-priority stream, with a cap on how many such runs
+ * are in flight, so small requests of other tables are not held behind it.  Each launch completes its own
+ * requests.  Requests on one table execute in submission order.  Tables are admitted, and grown (rehashed to twice the capacity)
  * before an insert run would pass 85 % of max_size(), only while the HBM budget allows; otherwise
  * the table admission or the request is refused with SG_ERR_BUDGET -- nothing spills to host memory.
  * Within one run of same-operation requests the per-key inserted / erased flags of a key repeated in
@@ -355,6 +360,10 @@ SG_API sg_status sg_server_submit_many(sg_server* server, const sg_request* requ
 /* While paused, submitted requests queue and no new launch starts (launches in flight finish);
  * resuming lets the queued requests coalesce into the next waves. */
 SG_API sg_status sg_server_set_paused(sg_server* server, int32_t paused);
+/* Request-size policy: a table's run of same-operation requests with at least direct_keys keys runs as
+ * its own launches of at most chunk_keys keys each, with at most max_direct (1..16) such runs in flight;
+ * defaults 65536, 524288 and 2. */
+SG_API sg_status sg_server_set_policy(sg_server* server, int64_t direct_keys, int64_t chunk_keys, int32_t max_direct);
 /* Waits (timeout_ms < 0: no limit) for a ticket; out_request_status: SG_OK or SG_ERR_BUDGET (refused). */
 SG_API sg_status sg_server_wait(sg_server* server, int64_t ticket, int32_t timeout_ms, sg_status* out_request_status);
 /* Waits for every submitted request. */
@@ -375,7 +384,21 @@ typedef struct sg_vector_view
     int64_t capacity;
     int32_t elem_bytes;
     int32_t pad;
+    void* slot_state; /* device, one 16-bit word per element: (epoch << 1) | occupied, written by device calls */
+    void* sync;       /* device: the epoch of the last bulk call and the size it left (sg_vector_sync) */
 } sg_vector_view;
+
+/* Device-call state of a vector.  Device push_back and pop_back may share a launch: each takes its position
+ * from the counter, then waits (bounded) until its slot is free (push) or written (pop), as the reference's
+ * per-slot occupied bit and lock do (vector_detail.cuh:181-299).  A slot word whose epoch is not the
+ * current one has not been touched since the last bulk call and reads as occupied exactly when its index
+ * is below base_size, so bulk calls never touch the slot words: each ends by advancing the epoch. */
+typedef struct sg_vector_sync
+{
+    uint32_t epoch;     /* 1 .. 32767 */
+    uint32_t error;     /* bit 0: a device wait gave up */
+    int64_t base_size;  /* size() after the last bulk call */
+} sg_vector_sync;
 
 /* vector::createDeviceObject(capacity): src/stdgpu/impl/vector_detail.cuh (createDeviceObject) */
 SG_API sg_status sg_vector_create(int32_t elem_bytes, int64_t capacity, sg_vector** out);
@@ -412,7 +435,23 @@ typedef struct sg_deque_view
     int64_t capacity;
     int32_t elem_bytes;
     int32_t pad;
+    void* slot_state; /* device, one 16-bit word per slot: (epoch << 1) | occupied, written by device calls */
+    void* sync;       /* device sg_deque_sync */
 } sg_deque_view;
+
+/* Device-call state of a deque.  The device calls (push_back, push_front, pop_front, pop_back, in any mix
+ * in one launch) take their ticket from the counters and then wait (bounded) on the slot's word until the
+ * slot is free (push) or written (pop), the reference's per-slot occupied bit
+ * (src/stdgpu/impl/deque_detail.cuh:202-446).  A word of another epoch has not been touched since the last
+ * bulk call: its slot is occupied exactly when its ticket lay in [base_begin, base_end) after that call.
+ * Device calls set `dirty`; the next bulk call first rebuilds the turn words its own kernels wait on. */
+typedef struct sg_deque_sync
+{
+    uint32_t epoch; /* 1 .. 32767 */
+    uint32_t dirty;
+    uint64_t base_begin;
+    uint64_t base_end;
+} sg_deque_sync;
 
 /* deque::createDeviceObject(capacity): src/stdgpu/impl/deque_detail.cuh (createDeviceObject) */
 SG_API sg_status sg_deque_create(int32_t elem_bytes, int64_t capacity, sg_deque** out);
@@ -443,17 +482,19 @@ SG_API sg_status sg_deque_view_of(const sg_deque* dq, sg_deque_view* out);
 SG_API sg_status sg_bitset_count(const uint32_t* blocks, int64_t nbits, void* stream, int64_t* out_count);
 
 /* Allocation-free form of sg_bitset_count.  It has no counterpart in the reference.
- * For callers that must not allocate device memory: code that runs while a CUDA graph is being captured
- * in global mode (where cudaMalloc fails), processes whose device memory is owned by another allocator
- * with a budget fixed up front, and latency-critical paths that cannot take an allocation's implicit
- * synchronisation.  sg_bitset_count allocates its per-block partial sums on first use; this entry point
+ * For callers that must not allocate device memory: processes whose device memory is owned by another
+ * allocator with a budget fixed up front (a framework's pool that leaves nothing for a library to
+ * cudaMalloc), and latency-critical paths that cannot take the device-wide synchronisation that
+ * cudaMalloc / cudaFree imply.  sg_bitset_count allocates its per-block partial sums on first use; this entry point
  * keeps them in a fixed array compiled into the library instead (64 KiB, present on every GPU that
  * loads the library until the process exits) and calls no allocator.  The count is written to
  * out_count, which is DEVICE memory owned by the caller; the call is asynchronous on `stream`.
  * Limit: nbits <= 2^34 (2 GiB of blocks); larger inputs return SG_ERR_BAD_ARG.  All calls on a device
  * share the array, so two calls whose kernels overlap on the GPU (unordered streams) race and give
  * wrong counts: order them on one stream or with events.  The first call on each device looks up the
- * array's device address (cudaGetSymbolAddress); make that first call before any stream capture. */
+ * array's device address (cudaGetSymbolAddress); make that first call before any stream capture.  The
+ * address is kept for the life of the process: after a cudaDeviceReset of that device (which also ends
+ * every other allocation of this library there) the entry point must not be called again. */
 SG_API sg_status sg_bitset_count_noalloc(const uint32_t* blocks, int64_t nbits, int64_t* out_count, void* stream);
 
 /* ---------------- library ---------------- */

@@ -5,11 +5,19 @@
 // groups with 16-byte loads through L2.
 //
 // Concurrency within one launch:
-//  * insert / emplace claim only never-used slots (compare-and-swap on the key
-//    word), so inserts may run concurrently with each other and with erase:
-//    a key is stored at most once and exactly one of several concurrent inserts
-//    of the same key reports success.  Erased slots are reclaimed by the bulk
-//    insert entry point (sg_unordered_insert), which runs alone on a table.
+//  * insert / emplace take the stripe lock of the key's home group (the
+//    table's insert_locks; a bounded wait), scan the probe sequence for the
+//    key up to the first group holding a never-used slot, and claim the first
+//    free slot -- erased or never used -- with a compare-and-swap over the
+//    whole slot.  All inserts of one key share the lock, so they never scan and
+//    claim at the same time: a key is stored at most once and exactly one of
+//    several concurrent inserts of an absent key reports success, while erases
+//    (which take no lock) run in the same launch and free slots that the next
+//    inserts reuse -- as the reference's device insert, which locks the bucket
+//    (src/stdgpu/impl/unordered_base_detail.cuh:708-809, 958-994).  A view
+//    without insert_locks falls back to claiming never-used slots only, which
+//    needs no lock.  Device calls and the bulk entry points must not run on a
+//    table at the same time.
 //  * erase marks the slot erased (compare-and-swap key -> erased marker);
 //    exactly one of several concurrent erases of a key reports success.
 //  * insert writes the key and its mapped value with one compare-and-swap over
@@ -202,8 +210,155 @@ struct unordered_ref
         return true;
     }
 
+    // Stripe lock of home group g (bounded wait with back-off; false when it gave up).
+    __device__ bool
+    lock_group(int64_t g) const
+    {
+        unsigned int* l = v.insert_locks + (static_cast<uint64_t>(g) & static_cast<uint64_t>(v.lock_mask));
+        unsigned int backoff = 32;
+        for (long long polls = 0; polls < detail::kWaitLimit; ++polls)
+        {
+            if (atomicCAS(l, 0u, 1u) == 0u)
+            {
+                __threadfence();
+                return true;
+            }
+            __nanosleep(backoff);
+            backoff = backoff < 256 ? backoff * 2 : 256;
+        }
+        return false;
+    }
+
+    __device__ void
+    unlock_group(int64_t g) const
+    {
+        __threadfence();
+        atomicExch(v.insert_locks + (static_cast<uint64_t>(g) & static_cast<uint64_t>(v.lock_mask)), 0u);
+    }
+
+    // The slot's current bytes as four words (unused words all ones).
+    __device__ void
+    read_slot(int64_t slot, uint32_t (&w)[4]) const
+    {
+        w[0] = w[1] = w[2] = w[3] = ~0u;
+        if constexpr (C::slot_bytes == 16)
+        {
+            const uint4 d = __ldcg(reinterpret_cast<const uint4*>(slot_ptr(slot)));
+            w[0] = d.x;
+            w[1] = d.y;
+            w[2] = d.z;
+            w[3] = d.w;
+        }
+        else if constexpr (C::slot_bytes == 8)
+        {
+            const uint2 d = __ldcg(reinterpret_cast<const uint2*>(slot_ptr(slot)));
+            w[0] = d.x;
+            w[1] = d.y;
+        }
+        else
+        {
+            w[0] = __ldcg(reinterpret_cast<const unsigned int*>(slot_ptr(slot)));
+        }
+    }
+
+    // Insert under the home group's stripe lock: erased slots are reused.  Returns the slot, or -1 (present,
+    // refused -- no free slot in the table --, or the lock wait gave up, which sets an error bit).
+    __device__ int64_t
+    insert_slot_locked(key_type key, mapped_type mapped) const
+    {
+        const int64_t home = home_group(key);
+        if (!lock_group(home))
+        {
+            atomicOr(&header()->error, detail::kErrRetry);
+            return -1;
+        }
+        int64_t result = -1;
+        bool refused = false;
+        for (int attempt = 0; attempt < 65536; ++attempt)
+        {
+            // the key along its probe sequence, up to the first group holding a never-used slot, and the first
+            // free slot (erased below max_size(), or never used) on the way
+            int64_t g = home;
+            int64_t target = -1;
+            bool target_tomb = false;
+            bool present = false;
+            for (int64_t probes = 0; probes < v.num_groups && !present; ++probes)
+            {
+                const uint4* p = group_ptr(g);
+                bool any_empty = false;
+#pragma unroll
+                for (int l = 0; l < detail::kTileLanes; ++l)
+                {
+                    const uint4 d = __ldcg(p + l);
+#pragma unroll
+                    for (int s = 0; s < SPL; ++s)
+                    {
+                        const key_type k = detail::key_in_lane<KIND>(d, s);
+                        const int64_t slot = g * G + l * SPL + s;
+                        present |= k == key;
+                        any_empty |= k == C::empty_key;
+                        if (target < 0 && (k == C::empty_key || (k == C::tomb_key && slot < v.total_count)))
+                        {
+                            target = slot;
+                            target_tomb = k == C::tomb_key;
+                        }
+                    }
+                }
+                if (any_empty)
+                {
+                    break;
+                }
+                g = detail::next_group(g, v.num_groups);
+            }
+            if (present)
+            {
+                break;
+            }
+            if (target < 0)
+            {
+                refused = true;
+                break;
+            }
+            uint32_t image[4];
+            if (target_tomb)
+            {
+                read_slot(target, image);
+                if (detail::key_in_lane<KIND>(make_uint4(image[0], image[1], image[2], image[3]), 0) != C::tomb_key)
+                {
+                    continue; // taken since the scan: scan again
+                }
+            }
+            else
+            {
+                image[0] = image[1] = image[2] = image[3] = ~0u;
+            }
+            key_type old;
+            if (detail::claim_slot_image<KIND>(slot_ptr(target), image, key, mapped, old))
+            {
+                atomicAdd(&header()->size, 1ull);
+                if (target_tomb)
+                {
+                    atomicAdd(&header()->tombstones, ~0ull);
+                }
+                result = target;
+                break;
+            }
+            if (old == key)
+            {
+                break;
+            }
+            // another key took the slot: scan again
+        }
+        unlock_group(home);
+        if (refused)
+        {
+            atomicAdd(&header()->refused, 1ull);
+        }
+        return result;
+    }
+
     // insert(value) / emplace(key, mapped): the slot this call stored the key in, or -1 when the key
-    // was already present or no never-used slot was left (the reference returns (end(), false)).
+    // was already present or no free slot was left (the reference returns (end(), false)).
     __device__ int64_t
     insert_slot(key_type key, mapped_type mapped = mapped_type{}) const
     {
@@ -219,6 +374,10 @@ struct unordered_ref
             atomicExch(&header()->special_state[s], 1u);
             atomicAdd(&header()->size, 1ull);
             return special_slot(key);
+        }
+        if (v.insert_locks != nullptr)
+        {
+            return insert_slot_locked(key, mapped);
         }
         int64_t g = home_group(key);
         int64_t steps = 0;

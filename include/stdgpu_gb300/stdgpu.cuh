@@ -681,8 +681,12 @@ struct device_range_of
 };
 
 // stdgpu::vector<T> (src/stdgpu/vector.cuh) for 4/8-byte T: the reference's host calls over the C ABI and
-// its device calls on the vector's view.  Device push_back is warp-aggregated like the bulk kernel;
-// push_back and pop_back do not share a launch (a pop may read a slot whose push has not written it yet).
+// its device calls on the vector's view.  Device push_back is warp-aggregated like the bulk kernel, and
+// device push_back and pop_back may share a launch: each takes its position from the counter and then
+// waits (bounded) on the slot's word until the slot is free (push) or written (pop) -- the reference's
+// per-slot occupied bit (vector_detail.cuh:181-299), kept as (epoch << 1) | occupied so that bulk calls,
+// which end by advancing the epoch, never touch the slot words (sg_vector_sync).  Device calls and bulk
+// calls on one vector must not run at the same time.
 template <typename T, typename Allocator = safe_device_allocator<T>>
 class vector
 {
@@ -796,10 +800,12 @@ public:
             return true;
         }
         long long n = -1;
+        sg_vector_sync sy{};
         const bool ok = cudaMemcpyAsync(&n, _view.size, sizeof(n), cudaMemcpyDeviceToHost, policy.stream) == cudaSuccess &&
+                        cudaMemcpyAsync(&sy, _view.sync, sizeof(sy), cudaMemcpyDeviceToHost, policy.stream) == cudaSuccess &&
                         cudaStreamSynchronize(policy.stream) == cudaSuccess;
         detail::gb300_check(ok ? SG_OK : SG_ERR_CUDA, "vector::valid");
-        return n >= 0 && n <= _view.capacity;
+        return n >= 0 && n <= _view.capacity && sy.error == 0u;
     }
 
     // device_begin() / device_end() / device_range(): the stored elements [data(), data() + size())
@@ -859,8 +865,58 @@ public:
         detail::gb300_check(sg_vector_erase(_handle, end - begin, policy.stream), "vector::erase");
     }
 
+    // Slot word protocol of the device calls.  A word of another epoch has not been touched since the last
+    // bulk call: its slot is occupied exactly when it lies below the size that call left.
+    __device__ bool
+    slot_occupied(long long pos, uint32_t epoch, long long base) const
+    {
+        unsigned short w;
+        asm volatile("ld.acquire.gpu.global.u16 %0, [%1];"
+                     : "=h"(w)
+                     : "l"(static_cast<unsigned short*>(_view.slot_state) + pos)
+                     : "memory");
+        return (static_cast<uint32_t>(w) >> 1) == epoch ? (w & 1u) != 0u : pos < base;
+    }
+
+    __device__ void
+    set_slot(long long pos, uint32_t epoch, bool occupied) const
+    {
+        const unsigned short w = static_cast<unsigned short>((epoch << 1) | (occupied ? 1u : 0u));
+        asm volatile("st.release.gpu.global.u16 [%0], %1;" ::"l"(static_cast<unsigned short*>(_view.slot_state) + pos),
+                     "h"(w)
+                     : "memory");
+    }
+
+    // Waits until slot pos is occupied (want == true) or free; false when the wait ran out (~1 s), which sets
+    // the error bit that valid() reports.
+    __device__ bool
+    wait_slot(long long pos, bool want, uint32_t epoch, long long base) const
+    {
+        unsigned backoff = 32;
+        for (long long polls = 0; polls < ::sg::detail::kWaitLimit; ++polls)
+        {
+            if (slot_occupied(pos, epoch, base) == want)
+            {
+                return true;
+            }
+            __nanosleep(backoff);
+            backoff = backoff < 256 ? backoff * 2 : 256;
+        }
+        atomicOr(&static_cast<sg_vector_sync*>(_view.sync)->error, 1u);
+        return false;
+    }
+
+    __device__ void
+    sync_state(uint32_t& epoch, long long& base) const
+    {
+        const sg_vector_sync* sy = static_cast<const sg_vector_sync*>(_view.sync);
+        epoch = *reinterpret_cast<const volatile uint32_t*>(&sy->epoch);
+        base = *reinterpret_cast<const volatile long long*>(&sy->base_size);
+    }
+
     // Device push_back (src/stdgpu/impl/vector_detail.cuh:181-238): the calling lanes that are active
-    // together reserve their positions with one atomic per warp.
+    // together reserve their positions with one atomic per warp; each then waits until its slot is free (a
+    // pop_back of the same launch may still be reading it) and writes.
     __device__ bool
     push_back(const T& element) const
     {
@@ -884,7 +940,15 @@ public:
         {
             return false;
         }
+        uint32_t epoch;
+        long long start;
+        sync_state(epoch, start);
+        if (!wait_slot(pos, false, epoch, start))
+        {
+            return false;
+        }
         data()[pos] = element;
+        set_slot(pos, epoch, true);
         return true;
     }
 
@@ -896,7 +960,8 @@ public:
     }
 
     // Device pop_back (src/stdgpu/impl/vector_detail.cuh:240-299): takes the last element, or fails on an
-    // empty vector.  The count is taken down with a bounded compare-and-swap loop.
+    // empty vector.  The count is taken down with a bounded compare-and-swap loop; the pop then waits until
+    // its slot is written (a push_back of the same launch may not have stored it yet), reads it and frees it.
     __device__ pair<T, bool>
     pop_back() const
     {
@@ -913,7 +978,16 @@ public:
                                                                     static_cast<unsigned long long>(n - 1)));
             if (seen == cur)
             {
-                return pair<T, bool>(data()[n - 1], true);
+                uint32_t epoch;
+                long long start;
+                sync_state(epoch, start);
+                if (!wait_slot(n - 1, true, epoch, start))
+                {
+                    return pair<T, bool>(T{}, false);
+                }
+                const T x = *reinterpret_cast<volatile T*>(data() + (n - 1));
+                set_slot(n - 1, epoch, false);
+                return pair<T, bool>(x, true);
             }
             cur = seen;
         }
@@ -952,10 +1026,14 @@ private:
     Allocator _allocator{};
 };
 
-// stdgpu::deque<T> (src/stdgpu/deque.cuh) for 4/8-byte T.  Device push_back / pop_front may run
-// concurrently in one kernel (the ring's turn words order a pop after the push of its ticket, with
-// bounded waits: a wait that runs out sets the deque's error bit, which size() reports, and the call fails);
-// host bulk calls cover push_back / pop_front mixes, push_front and pop_back.
+// stdgpu::deque<T> (src/stdgpu/deque.cuh) for 4/8-byte T.  Device push_back, push_front, pop_front and
+// pop_back may run in any mix in one kernel: each takes its ticket from the counters (size guards the
+// capacity, avail the elements) and then waits on its slot's word until the slot is free (push) or written
+// (pop), the reference's per-slot occupied bit (deque_detail.cuh:202-446); the waits are bounded (one that
+// runs out sets the deque's error bit, which size() reports, and the call fails).  The host bulk calls
+// (push_back / pop_front mixes, push_front, pop_back) keep turn words of their own, rebuilt from the tickets
+// after device calls ran (sg_deque_sync).  Device calls and bulk calls on one deque must not run at the same
+// time.
 template <typename T, typename Allocator = safe_device_allocator<T>>
 class deque
 {
@@ -1085,6 +1163,14 @@ public:
         detail::gb300_check(sg_deque_clear(_handle, policy.stream), "deque::clear");
     }
 
+    // the C-ABI handle, for the sg_deque_* entry points (for example sg_deque_ops, a bulk push_back /
+    // pop_front mix)
+    sg_deque*
+    native_handle() const noexcept
+    {
+        return _handle;
+    }
+
     // host bulk forms (device pointers): push_front / pop_back of n elements, as sequences of calls
     void
     push_front(const T* values, index_t n, std::uint8_t* ok = nullptr,
@@ -1099,9 +1185,79 @@ public:
         detail::gb300_check(sg_deque_pop_back(_handle, n, popped, ok, policy.stream), "deque::pop_back");
     }
 
-    // device push_back (src/stdgpu/impl/deque_detail.cuh:202-258)
+private:
+    // Slot words of the device calls: (epoch << 1) | occupied.  A word of another epoch has not been touched
+    // since the last bulk call; its slot is occupied exactly when the ticket mapping to it lay in
+    // [base_begin, base_end) after that call.
     __device__ bool
-    push_back(const T& element) const
+    slot_occupied(long long pos, uint32_t epoch, unsigned long long b0, unsigned long long e0) const
+    {
+        unsigned short w;
+        asm volatile("ld.acquire.gpu.global.u16 %0, [%1];"
+                     : "=h"(w)
+                     : "l"(static_cast<unsigned short*>(_view.slot_state) + pos)
+                     : "memory");
+        if ((static_cast<uint32_t>(w) >> 1) == epoch)
+        {
+            return (w & 1u) != 0u;
+        }
+        const unsigned long long cap = static_cast<unsigned long long>(_view.capacity);
+        const unsigned long long from_b = (static_cast<unsigned long long>(pos) + cap - b0 % cap) % cap;
+        return from_b < e0 - b0;
+    }
+
+    __device__ void
+    set_slot(long long pos, uint32_t epoch, bool occupied) const
+    {
+        const unsigned short w = static_cast<unsigned short>((epoch << 1) | (occupied ? 1u : 0u));
+        asm volatile("st.release.gpu.global.u16 [%0], %1;" ::"l"(static_cast<unsigned short*>(_view.slot_state) + pos),
+                     "h"(w)
+                     : "memory");
+    }
+
+    // Waits until the slot is occupied (want) or free; false after ~1 s, which sets the deque's error bit
+    // (size() then reports SG_ERR_RETRY_EXHAUSTED).
+    __device__ bool
+    wait_slot(long long pos, bool want) const
+    {
+        const sg_deque_sync* sy = static_cast<const sg_deque_sync*>(_view.sync);
+        const uint32_t epoch = *reinterpret_cast<const volatile uint32_t*>(&sy->epoch);
+        const unsigned long long b0 = *reinterpret_cast<const volatile unsigned long long*>(&sy->base_begin);
+        const unsigned long long e0 = *reinterpret_cast<const volatile unsigned long long*>(&sy->base_end);
+        unsigned backoff = 32;
+        for (long long polls = 0; polls < ::sg::detail::kWaitLimit; ++polls)
+        {
+            if (slot_occupied(pos, epoch, b0, e0) == want)
+            {
+                return true;
+            }
+            __nanosleep(backoff);
+            backoff = backoff < 256 ? backoff * 2 : 256;
+        }
+        atomicOr(&counters()->error, ::sg::detail::kDequeErrWait);
+        return false;
+    }
+
+    __device__ uint32_t
+    current_epoch() const
+    {
+        return *reinterpret_cast<const volatile uint32_t*>(&static_cast<const sg_deque_sync*>(_view.sync)->epoch);
+    }
+
+    // the next bulk call must rebuild its turn words
+    __device__ void
+    mark_dirty() const
+    {
+        uint32_t* dirty = &static_cast<sg_deque_sync*>(_view.sync)->dirty;
+        if (*reinterpret_cast<volatile uint32_t*>(dirty) == 0u)
+        {
+            atomicExch(dirty, 1u);
+        }
+    }
+
+    // A push's reservation: size guards the capacity (taken first); false when full.
+    __device__ bool
+    reserve_push() const
     {
         auto* c = counters();
         const long long cap = _view.capacity;
@@ -1114,17 +1270,99 @@ public:
             atomicAdd(reinterpret_cast<unsigned long long*>(&c->size), ~0ull);
             return false;
         }
-        const unsigned long long tk = atomicAdd(&c->end, 1ull);
-        const long long pos = static_cast<long long>(tk % static_cast<unsigned long long>(cap));
-        unsigned* seq = static_cast<unsigned*>(_view.seq);
-        if (!sg::detail::wait_turn(seq + pos, static_cast<unsigned>(tk), &c->error))
+        return true;
+    }
+
+    // A pop's reservation: avail guards the elements (taken first); false when empty.
+    __device__ bool
+    reserve_pop() const
+    {
+        auto* c = counters();
+        if (*reinterpret_cast<volatile long long*>(&c->avail) <= 0) // preemptive empty() check
+        {
+            return false;
+        }
+        if (static_cast<long long>(atomicAdd(reinterpret_cast<unsigned long long*>(&c->avail), ~0ull)) <= 0)
+        {
+            atomicAdd(reinterpret_cast<unsigned long long*>(&c->avail), 1ull);
+            return false;
+        }
+        return true;
+    }
+
+    __device__ bool
+    push_at(unsigned long long tk, const T& element) const
+    {
+        auto* c = counters();
+        const long long pos = static_cast<long long>(tk % static_cast<unsigned long long>(_view.capacity));
+        mark_dirty();
+        if (!wait_slot(pos, false))
         {
             return false;
         }
         static_cast<T*>(_view.data)[pos] = element;
-        sg::detail::store_turn(seq + pos, static_cast<unsigned>(tk + 1));
+        set_slot(pos, current_epoch(), true);
         atomicAdd(reinterpret_cast<unsigned long long*>(&c->avail), 1ull);
         return true;
+    }
+
+    __device__ pair<T, bool>
+    pop_at(unsigned long long tk) const
+    {
+        auto* c = counters();
+        const long long pos = static_cast<long long>(tk % static_cast<unsigned long long>(_view.capacity));
+        mark_dirty();
+        if (!wait_slot(pos, true))
+        {
+            return pair<T, bool>(T{}, false);
+        }
+        const T v = *reinterpret_cast<volatile T*>(static_cast<T*>(_view.data) + pos);
+        set_slot(pos, current_epoch(), false);
+        atomicAdd(reinterpret_cast<unsigned long long*>(&c->size), ~0ull);
+        return pair<T, bool>(v, true);
+    }
+
+public:
+    // device push_back (src/stdgpu/impl/deque_detail.cuh:202-258): a ticket from end (end moves up), then the
+    // slot is written once free
+    __device__ bool
+    push_back(const T& element) const
+    {
+        if (!reserve_push())
+        {
+            return false;
+        }
+        return push_at(atomicAdd(&counters()->end, 1ull), element);
+    }
+
+    // device push_front (src/stdgpu/impl/deque_detail.cuh:315-386): a ticket below begin (begin moves down)
+    __device__ bool
+    push_front(const T& element) const
+    {
+        if (!reserve_push())
+        {
+            return false;
+        }
+        return push_at(atomicAdd(&counters()->begin, ~0ull) - 1ull, element);
+    }
+
+    template <typename... Args>
+    __device__ bool
+    emplace_front(Args&&... args) const
+    {
+        return push_front(T(static_cast<Args&&>(args)...));
+    }
+
+    // device pop_back (src/stdgpu/impl/deque_detail.cuh:260-313): the ticket below end (end moves down), read
+    // once written
+    __device__ pair<T, bool>
+    pop_back() const
+    {
+        if (!reserve_pop())
+        {
+            return pair<T, bool>(T{}, false);
+        }
+        return pop_at(atomicAdd(&counters()->end, ~0ull) - 1ull);
     }
 
     template <typename... Args>
@@ -1164,32 +1402,15 @@ public:
         return static_cast<T*>(_view.data)[(c->end + cap - 1) % cap];
     }
 
-    // device pop_front (src/stdgpu/impl/deque_detail.cuh:388-446)
+    // device pop_front (src/stdgpu/impl/deque_detail.cuh:388-446): the ticket at begin (begin moves up)
     __device__ pair<T, bool>
     pop_front() const
     {
-        auto* c = counters();
-        if (*reinterpret_cast<volatile long long*>(&c->avail) <= 0) // preemptive empty() check
+        if (!reserve_pop())
         {
             return pair<T, bool>(T{}, false);
         }
-        if (static_cast<long long>(atomicAdd(reinterpret_cast<unsigned long long*>(&c->avail), ~0ull)) <= 0)
-        {
-            atomicAdd(reinterpret_cast<unsigned long long*>(&c->avail), 1ull);
-            return pair<T, bool>(T{}, false);
-        }
-        const unsigned long long tk = atomicAdd(&c->begin, 1ull);
-        const long long cap = _view.capacity;
-        const long long pos = static_cast<long long>(tk % static_cast<unsigned long long>(cap));
-        unsigned* seq = static_cast<unsigned*>(_view.seq);
-        if (!sg::detail::wait_turn(seq + pos, static_cast<unsigned>(tk + 1), &c->error))
-        {
-            return pair<T, bool>(T{}, false);
-        }
-        const T v = *reinterpret_cast<volatile T*>(static_cast<T*>(_view.data) + pos);
-        sg::detail::store_turn(seq + pos, static_cast<unsigned>(tk + static_cast<unsigned long long>(cap)));
-        atomicAdd(reinterpret_cast<unsigned long long*>(&c->size), ~0ull);
-        return pair<T, bool>(v, true);
+        return pop_at(atomicAdd(&counters()->begin, 1ull));
     }
 
 private:

@@ -46,17 +46,19 @@ class sg_unordered_view(ctypes.Structure):
         ("bucket_count", c_int64),
         ("bucket_bits", c_int32),
         ("kind", c_int32),
+        ("insert_locks", c_void_p),
+        ("lock_mask", c_int64),
     ]
 
 
 class sg_vector_view(ctypes.Structure):
     _fields_ = [("data", c_void_p), ("size", c_void_p), ("capacity", c_int64), ("elem_bytes", c_int32),
-                ("pad", c_int32)]
+                ("pad", c_int32), ("slot_state", c_void_p), ("sync", c_void_p)]
 
 
 class sg_deque_view(ctypes.Structure):
     _fields_ = [("data", c_void_p), ("seq", c_void_p), ("counters", c_void_p), ("capacity", c_int64),
-                ("elem_bytes", c_int32), ("pad", c_int32)]
+                ("elem_bytes", c_int32), ("pad", c_int32), ("slot_state", c_void_p), ("sync", c_void_p)]
 
 
 class sg_request(ctypes.Structure):
@@ -129,6 +131,7 @@ SIGNATURES = {
     "sg_server_submit": (c_int32, [c_void_p, POINTER(sg_request), POINTER(c_int64)]),
     "sg_server_submit_many": (c_int32, [c_void_p, POINTER(sg_request), c_int32, POINTER(c_int64)]),
     "sg_server_set_paused": (c_int32, [c_void_p, c_int32]),
+    "sg_server_set_policy": (c_int32, [c_void_p, c_int64, c_int64, c_int32]),
     "sg_server_wait": (c_int32, [c_void_p, c_int64, c_int32, POINTER(c_int32)]),
     "sg_server_drain": (c_int32, [c_void_p, c_int32]),
     "sg_server_get_stats": (c_int32, [c_void_p, POINTER(sg_server_stats)]),

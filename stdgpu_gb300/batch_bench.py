@@ -5,7 +5,8 @@ Per-table key counts are lognormal (median 2048, sigma 1.5, clipped to 64..26214
 are half stored keys, half fresh.  One step = clear + insert + contains over every table, run three
 ways on the same GB300:
 
-* plain:   one createDeviceObject per table, then 3 calls per table per step (clear, insert, contains)
+* plain:   one createDeviceObject per table, then 3 calls per table per step (clear, insert, contains),
+           issued from a C++ loop over the C ABI
 * batched: one batch object, 3 batched calls per step (each one persistent launch plus a tile count)
 * graph:   the batched step captured once in a CUDA graph and replayed
 
@@ -20,6 +21,7 @@ from ctypes import c_void_p
 import numpy as np
 import torch
 
+from . import comparators as P
 from . import containers as C
 from . import workloads as W
 
@@ -92,35 +94,12 @@ def time_graph(batch: C.table_batch, d_keys, d_q, d_off, out, steps: int, warmup
 
 
 def time_plain(caps, d_keys, d_q, offsets, out, steps: int, warmup: int) -> tuple[float, float]:
-    """Plain per-table C-ABI calls on the current stream.  Returns (GPU ms per step, host ms per step)."""
-    lib = C.N.load()
+    """Plain per-table C-ABI calls (clear, insert, contains per table) on the current stream, from a C++ loop
+    (comparators.plain_tables_steps).  Returns (GPU ms per step, host ms per step)."""
     tables = [C.unordered_set.createDeviceObject(int(c), key="u64") for c in caps]
     st = torch.cuda.current_stream()
-    sp = c_void_p(st.cuda_stream)
-    kp = d_keys.data_ptr()
-    qp = d_q.data_ptr()
-    op = out.data_ptr()
-    ranges = [(int(offsets[t]), int(offsets[t + 1] - offsets[t])) for t in range(len(caps))]
-
-    def step():
-        for t, (lo, n) in zip(tables, ranges):
-            lib.sg_unordered_clear(t._h, sp)
-            lib.sg_unordered_insert_kv(t._h, c_void_p(kp + 8 * lo), None, n, None, sp)
-            lib.sg_unordered_contains(t._h, c_void_p(qp + 8 * lo), n, c_void_p(op + lo), sp)
-
-    for _ in range(warmup):
-        step()
-    torch.cuda.synchronize()
-    a = torch.cuda.Event(enable_timing=True)
-    b = torch.cuda.Event(enable_timing=True)
-    t0 = time.perf_counter()
-    a.record(st)
-    for _ in range(steps):
-        step()
-    b.record(st)
-    torch.cuda.synchronize()
-    host_ms = (time.perf_counter() - t0) * 1e3 / steps
-    gpu_ms = a.elapsed_time(b) / steps
+    P.plain_tables_steps(tables, d_keys, d_q, offsets, 8, out, warmup, st)
+    gpu_ms, host_ms = P.plain_tables_steps(tables, d_keys, d_q, offsets, 8, out, steps, st)
     for t in tables:
         C.unordered_base.destroyDeviceObject(t)
     return gpu_ms, host_ms

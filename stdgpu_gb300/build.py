@@ -42,6 +42,27 @@ def _run(cmd: list[str]) -> str:
     return r.stdout + r.stderr
 
 
+# the plain-call comparators (host C++ over the C ABI; stdgpu_gb300/comparators)
+COMPARATORS_SRC = PKG / "comparators" / "plain_calls.cpp"
+COMPARATORS_LIB = "libsg_plain_calls.so"
+
+
+def build_comparators() -> Path:
+    """Compile the plain-call comparator library against the product library (g++, static CUDA runtime)."""
+    out = OUT / COMPARATORS_LIB
+    lib = library_path()
+    if out.exists() and out.stat().st_mtime >= max(COMPARATORS_SRC.stat().st_mtime, lib.stat().st_mtime,
+                                                    (INCLUDE / "stdgpu_gb300.h").stat().st_mtime):
+        return out
+    cuda = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
+    tmp = OUT / (COMPARATORS_LIB + ".tmp")
+    _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fvisibility=hidden", "-I", str(INCLUDE),
+          "-I", str(cuda / "include"), str(COMPARATORS_SRC), "-o", str(tmp), "-L", str(OUT), "-lstdgpu_gb300",
+          "-Wl,-rpath,$ORIGIN", "-L", str(cuda / "lib64"), "-lcudart_static", "-ldl", "-lpthread", "-lrt"])
+    os.replace(tmp, out)
+    return out
+
+
 def _deps() -> list[Path]:
     return list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.rglob("*.h")) + \
         list(INCLUDE.rglob("*.cuh")) + [Path(__file__)]
@@ -62,6 +83,7 @@ def is_current() -> bool:
 def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     """Compile every translation unit for sm_103a and link the shared library."""
     if not force and is_current():
+        build_comparators()
         return library_path()
     OUT.mkdir(exist_ok=True)
     extra = ["-Xptxas", "-v"] if verbose_ptxas else []
@@ -81,6 +103,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
     os.replace(tmp, library_path())
     if verbose_ptxas:
         (OUT / "ptxas.log").write_text("\n".join(logs))
+    build_comparators()
     return library_path()
 
 

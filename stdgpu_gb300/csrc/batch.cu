@@ -262,7 +262,10 @@ struct sg_table_batch
     long long* sizes_dev;    // device, n
     long long* sizes_host;   // pinned, n
     int64_t arena_bytes;
+    unsigned int* locks;     // stripe locks of native device inserts, shared by the batch's tables
 };
+
+constexpr int64_t kBatchInsertLocks = int64_t{ 1 } << 16;
 
 namespace
 {
@@ -480,6 +483,14 @@ sg_batch_create(int32_t kind, int32_t n_tables, const int64_t* capacities, void*
     {
         e = cudaMallocHost(&b->sizes_host, sizeof(long long) * n_tables);
     }
+    if (e == cudaSuccess)
+    {
+        e = sg::detail::dev_malloc(&b->locks, sizeof(unsigned int) * kBatchInsertLocks);
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaMemsetAsync(b->locks, 0, sizeof(unsigned int) * kBatchInsertLocks, as_stream(stream));
+    }
     if (e != cudaSuccess)
     {
         sg_batch_destroy(b);
@@ -531,6 +542,7 @@ sg_batch_destroy(sg_table_batch* b)
     sg::detail::dev_free(b->chunks);
     sg::detail::dev_free(b->prefix);
     sg::detail::dev_free(b->sizes_dev);
+    sg::detail::dev_free(b->locks);
     if (b->sizes_host != nullptr)
     {
         cudaFreeHost(b->sizes_host);
@@ -651,6 +663,8 @@ sg_batch_view_of(const sg_table_batch* b, int32_t table, sg_unordered_view* out)
     out->bucket_count = b->bucket_counts[table];
     out->bucket_bits = v.bits;
     out->kind = b->kind;
+    out->insert_locks = b->locks;
+    out->lock_mask = kBatchInsertLocks - 1;
     return SG_OK;
 }
 

@@ -368,6 +368,18 @@ k_vector_clamp(long long* size, int64_t cap, int64_t minus)
     *size = s < 0 ? 0 : s;
 }
 
+// End of every bulk call: size clamped into [0, capacity], the device calls' epoch advanced and the size
+// it starts from recorded (sg_vector_sync).
+__global__ void
+k_vector_epoch(long long* size, int64_t cap, sg_vector_sync* sync, uint32_t epoch)
+{
+    long long s = *size;
+    s = s < 0 ? 0 : (s > cap ? cap : s);
+    *size = s;
+    sync->base_size = s;
+    sync->epoch = epoch;
+}
+
 template <typename T>
 __global__ void
 k_vector_pop_back(const T* data, const long long* size, int64_t n, T* out_values, uint8_t* out_ok)
@@ -387,6 +399,48 @@ k_vector_pop_back(const T* data, const long long* size, int64_t n, T* out_values
             out_ok[i] = static_cast<uint8_t>(ok);
         }
     }
+}
+
+// Before a bulk call: when device calls ran since the last bulk call (they keep per-slot occupied words,
+// not turn words), every slot's turn word is rebuilt from the tickets -- a slot holding ticket t (t in
+// [begin, end)) gets t + 1, a free slot the ticket of the next push_back that maps to it.
+__global__ void
+k_deque_rebuild_turns(unsigned* seq, const deque_counters* c, const sg_deque_sync* sync, int64_t cap)
+{
+    if (*reinterpret_cast<const volatile uint32_t*>(&sync->dirty) == 0u)
+    {
+        return;
+    }
+    const unsigned long long b = c->begin;
+    const unsigned long long e = c->end;
+    const unsigned long long ucap = static_cast<unsigned long long>(cap);
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < cap; i += stride)
+    {
+        const unsigned long long ui = static_cast<unsigned long long>(i);
+        const unsigned long long from_b = (ui + ucap - b % ucap) % ucap; // tickets t = b + from_b map to slot i
+        unsigned v;
+        if (from_b < e - b)
+        {
+            v = static_cast<unsigned>(b + from_b + 1ull);
+        }
+        else
+        {
+            v = static_cast<unsigned>(e + (ui + ucap - e % ucap) % ucap);
+        }
+        seq[i] = v;
+    }
+}
+
+// After the rebuild, and at the end of every bulk call: the device calls' epoch advanced and the tickets
+// it starts from recorded; dirty cleared.
+__global__ void
+k_deque_epoch(const deque_counters* c, sg_deque_sync* sync, uint32_t epoch)
+{
+    sync->base_begin = c->begin;
+    sync->base_end = c->end;
+    sync->epoch = epoch;
+    sync->dirty = 0u;
 }
 
 __global__ void
@@ -604,6 +658,9 @@ struct sg_vector
     void* data;
     long long* size;
     long long* host;
+    uint16_t* slot_state;   // device calls' per-slot words (sg_vector_sync)
+    sg_vector_sync* sync;
+    uint32_t epoch;         // host copy of sync->epoch
 };
 
 struct sg_deque
@@ -614,6 +671,9 @@ struct sg_deque
     unsigned* seq;
     deque_counters* counters;
     deque_counters* host;
+    uint16_t* slot_state; // device calls' per-slot words (sg_deque_sync)
+    sg_deque_sync* sync;
+    uint32_t epoch;       // host copy of sync->epoch
 };
 
 namespace
@@ -635,6 +695,33 @@ count_scratch g_count_scratch[64];
 namespace
 {
 
+// Every bulk call on a deque runs between these two: the turn words rebuilt if device calls ran since the
+// last bulk call, and afterwards the device calls' epoch advanced (slot words cleared when it wraps).
+sg_status
+deque_bulk_begin(sg_deque* d, cudaStream_t s)
+{
+    static const int mg = persistent_grid(k_deque_rebuild_turns, kCThreads);
+    k_deque_rebuild_turns<<<grid_for(d->capacity, kCThreads, mg), kCThreads, 0, s>>>(d->seq, d->counters, d->sync,
+                                                                                     d->capacity);
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+}
+
+sg_status
+deque_bulk_end(sg_deque* d, cudaStream_t s)
+{
+    uint32_t e = d->epoch + 1;
+    if (e > 32767u)
+    {
+        SG_CUDA_TRY(cudaMemsetAsync(d->slot_state, 0, static_cast<size_t>(d->capacity) * sizeof(uint16_t), s));
+        e = 1;
+    }
+    d->epoch = e;
+    k_deque_epoch<<<1, 1, 0, s>>>(d->counters, d->sync, e);
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+}
+
 template <bool FRONT_PUSH>
 sg_status
 deque_end_ops(sg_deque* d, const void* values, int64_t n, void* out_popped, uint8_t* out_ok, void* stream)
@@ -648,6 +735,11 @@ deque_end_ops(sg_deque* d, const void* values, int64_t n, void* out_popped, uint
         return SG_OK;
     }
     cudaStream_t s = as_stream(stream);
+    sg_status st = deque_bulk_begin(d, s);
+    if (st != SG_OK)
+    {
+        return st;
+    }
     k_deque_reserve_end<FRONT_PUSH><<<1, 1, 0, s>>>(d->counters, d->capacity, n);
     SG_LAUNCH_CHECK();
     const int g = grid_for(n, kCThreads, 4096);
@@ -663,6 +755,27 @@ deque_end_ops(sg_deque* d, const void* values, int64_t n, void* out_popped, uint
                 static_cast<unsigned long long*>(d->data), d->seq, d->counters, d->capacity,
                 static_cast<const unsigned long long*>(values), n, static_cast<unsigned long long*>(out_popped), out_ok);
     }
+    SG_LAUNCH_CHECK();
+    return deque_bulk_end(d, s);
+}
+
+} // namespace
+
+namespace
+{
+
+// Ends a bulk call on v: the next epoch (1 .. 32767; slot words are cleared when it wraps).
+sg_status
+vector_next_epoch(sg_vector* v, cudaStream_t s)
+{
+    uint32_t e = v->epoch + 1;
+    if (e > 32767u)
+    {
+        SG_CUDA_TRY(cudaMemsetAsync(v->slot_state, 0, static_cast<size_t>(v->capacity) * sizeof(uint16_t), s));
+        e = 1;
+    }
+    v->epoch = e;
+    k_vector_epoch<<<1, 1, 0, s>>>(v->size, v->capacity, v->sync, e);
     SG_LAUNCH_CHECK();
     return SG_OK;
 }
@@ -699,6 +812,24 @@ sg_vector_create(int32_t elem_bytes, int64_t capacity, sg_vector** out)
     {
         e = cudaMallocHost(&v->host, sizeof(long long));
     }
+    if (e == cudaSuccess)
+    {
+        e = sg::detail::dev_malloc(&v->slot_state, static_cast<size_t>(capacity) * sizeof(uint16_t));
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaMemset(v->slot_state, 0, static_cast<size_t>(capacity) * sizeof(uint16_t));
+    }
+    if (e == cudaSuccess)
+    {
+        e = sg::detail::dev_malloc(&v->sync, sizeof(sg_vector_sync));
+    }
+    if (e == cudaSuccess)
+    {
+        const sg_vector_sync init{ 1u, 0u, 0 };
+        v->epoch = 1;
+        e = cudaMemcpy(v->sync, &init, sizeof(init), cudaMemcpyHostToDevice);
+    }
     if (e != cudaSuccess)
     {
         sg_vector_destroy(v);
@@ -719,6 +850,8 @@ sg_vector_destroy(sg_vector* v)
     cudaDeviceSynchronize();
     sg::detail::dev_free(v->data);
     sg::detail::dev_free(v->size);
+    sg::detail::dev_free(v->slot_state);
+    sg::detail::dev_free(v->sync);
     if (v->host != nullptr)
     {
         cudaFreeHost(v->host);
@@ -755,7 +888,7 @@ sg_vector_push_back(sg_vector* v, const void* values, const uint8_t* pred, int64
                 static_cast<const unsigned long long*>(values), pred, n, out_pushed);
     }
     SG_LAUNCH_CHECK();
-    return SG_OK;
+    return vector_next_epoch(v, s);
 }
 
 sg_status
@@ -781,7 +914,7 @@ sg_vector_clear(sg_vector* v, void* stream)
         return SG_ERR_BAD_ARG;
     }
     SG_CUDA_TRY(cudaMemsetAsync(v->size, 0, sizeof(long long), as_stream(stream)));
-    return SG_OK;
+    return vector_next_epoch(v, as_stream(stream));
 }
 
 sg_status
@@ -813,7 +946,7 @@ sg_vector_pop_back(sg_vector* v, int64_t n, void* out_values, uint8_t* out_ok, v
     SG_LAUNCH_CHECK();
     k_vector_clamp<<<1, 1, 0, s>>>(v->size, v->capacity, n);
     SG_LAUNCH_CHECK();
-    return SG_OK;
+    return vector_next_epoch(v, s);
 }
 
 sg_status
@@ -838,8 +971,9 @@ sg_vector_insert(sg_vector* v, const void* values, int64_t n, void* stream)
                                 static_cast<size_t>(n) * v->elem_bytes, cudaMemcpyDeviceToDevice, s));
     *v->host = size + n;
     SG_CUDA_TRY(cudaMemcpyAsync(v->size, v->host, sizeof(long long), cudaMemcpyHostToDevice, s));
+    const sg_status e = vector_next_epoch(v, s);
     SG_CUDA_TRY(cudaStreamSynchronize(s));
-    return SG_OK;
+    return e;
 }
 
 sg_status
@@ -862,8 +996,9 @@ sg_vector_erase(sg_vector* v, int64_t n, void* stream)
     cudaStream_t s = as_stream(stream);
     *v->host = size - n;
     SG_CUDA_TRY(cudaMemcpyAsync(v->size, v->host, sizeof(long long), cudaMemcpyHostToDevice, s));
+    const sg_status e = vector_next_epoch(v, s);
     SG_CUDA_TRY(cudaStreamSynchronize(s));
-    return SG_OK;
+    return e;
 }
 
 sg_status
@@ -878,6 +1013,8 @@ sg_vector_view_of(const sg_vector* v, sg_vector_view* out)
     out->capacity = v->capacity;
     out->elem_bytes = v->elem_bytes;
     out->pad = 0;
+    out->slot_state = v->slot_state;
+    out->sync = v->sync;
     return SG_OK;
 }
 
@@ -909,6 +1046,22 @@ sg_deque_create(int32_t elem_bytes, int64_t capacity, sg_deque** out)
     {
         e = cudaMallocHost(&d->host, sizeof(deque_counters));
     }
+    if (e == cudaSuccess)
+    {
+        e = sg::detail::dev_malloc(&d->slot_state, static_cast<size_t>(capacity) * sizeof(uint16_t));
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaMemset(d->slot_state, 0, static_cast<size_t>(capacity) * sizeof(uint16_t));
+    }
+    if (e == cudaSuccess)
+    {
+        e = sg::detail::dev_malloc(&d->sync, sizeof(sg_deque_sync));
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaMemset(d->sync, 0, sizeof(sg_deque_sync));
+    }
     if (e != cudaSuccess)
     {
         sg_deque_destroy(d);
@@ -936,6 +1089,8 @@ sg_deque_destroy(sg_deque* d)
     sg::detail::dev_free(d->data);
     sg::detail::dev_free(d->seq);
     sg::detail::dev_free(d->counters);
+    sg::detail::dev_free(d->slot_state);
+    sg::detail::dev_free(d->sync);
     if (d->host != nullptr)
     {
         cudaFreeHost(d->host);
@@ -955,7 +1110,7 @@ sg_deque_clear(sg_deque* d, void* stream)
     static const int mg = persistent_grid(k_deque_reset, kCThreads);
     k_deque_reset<<<grid_for(d->capacity, kCThreads, mg), kCThreads, 0, s>>>(d->seq, d->counters, d->capacity);
     SG_LAUNCH_CHECK();
-    return SG_OK;
+    return deque_bulk_end(d, s);
 }
 
 sg_status
@@ -983,6 +1138,11 @@ sg_deque_ops(sg_deque* d, const uint8_t* is_push, const void* values, int64_t n,
         return SG_OK;
     }
     cudaStream_t s = as_stream(stream);
+    sg_status st = deque_bulk_begin(d, s);
+    if (st != SG_OK)
+    {
+        return st;
+    }
     if (d->elem_bytes == 4)
     {
         static const int mg = persistent_grid(k_deque_ops<uint32_t>, kCThreads);
@@ -999,7 +1159,7 @@ sg_deque_ops(sg_deque* d, const uint8_t* is_push, const void* values, int64_t n,
                 out_ok);
     }
     SG_LAUNCH_CHECK();
-    return SG_OK;
+    return deque_bulk_end(d, s);
 }
 
 sg_status
@@ -1065,6 +1225,8 @@ sg_deque_view_of(const sg_deque* d, sg_deque_view* out)
     out->capacity = d->capacity;
     out->elem_bytes = d->elem_bytes;
     out->pad = 0;
+    out->slot_state = d->slot_state;
+    out->sync = d->sync;
     return SG_OK;
 }
 

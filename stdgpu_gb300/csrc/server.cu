@@ -224,8 +224,15 @@ namespace
 
 using clock_type = std::chrono::steady_clock;
 
-constexpr int kSlotSegments = 4096;          // segments one launch slot can carry
-constexpr int64_t kDirectKeys = int64_t{ 1 } << 16; // requests this large run as their own single-table launch
+constexpr int kSlotSegments = 4096; // segments one packed launch can carry
+// Request-size policy defaults (sg_server_set_policy): a table's run of same-operation requests with at
+// least kDefaultDirectKeys keys runs as its own launches on a low-priority stream, cut into launches of at
+// most kDefaultChunkKeys keys, with at most kDefaultMaxDirect such runs in flight; smaller runs are packed
+// into one segmented launch per operation on a high-priority stream.
+constexpr int64_t kDefaultDirectKeys = int64_t{ 1 } << 16;
+constexpr int64_t kDefaultChunkKeys = int64_t{ 1 } << 19;
+constexpr int kDefaultMaxDirect = 2;
+constexpr int kMaxDirectLimit = 16;
 
 struct request_rec
 {
@@ -247,7 +254,8 @@ struct table_rec
     bool busy = false;
 };
 
-// Device and pinned host memory of one in-flight launch group (a wave).
+// One segmented launch of small runs of one operation: its descriptors (device and pinned host), its
+// completion event and what completes with it.
 struct launch_slot
 {
     seg_desc* d_segs = nullptr;
@@ -260,6 +268,15 @@ struct launch_slot
     std::vector<int32_t> tables;
 };
 
+// One table's run of large requests, launched chunk by chunk on one low-priority stream.
+struct direct_unit
+{
+    cudaEvent_t done = nullptr;
+    bool in_use = false;
+    std::vector<int64_t> tickets;
+    int32_t table = -1;
+};
+
 } // namespace
 
 struct sg_server
@@ -268,9 +285,15 @@ struct sg_server
     int64_t budget = 0;
     int64_t used = 0;
     int grid_cap = 0;
-    std::vector<cudaStream_t> streams;
-    int next_stream = 0;
+    std::vector<cudaStream_t> hi_streams; // packed launches (greatest priority)
+    std::vector<cudaStream_t> lo_streams; // large runs (least priority)
+    int next_hi = 0;
+    int next_lo = 0;
     std::vector<launch_slot> slots;
+    std::vector<direct_unit> units;
+    int64_t direct_keys = kDefaultDirectKeys;
+    int64_t chunk_keys = kDefaultChunkKeys;
+    int max_direct = kDefaultMaxDirect;
     std::mutex m;
     std::condition_variable cv_work;
     std::condition_variable cv_done;
@@ -298,8 +321,14 @@ struct sg_server
     }
 
     void run();
+    void finish(const std::vector<int64_t>& tickets, clock_type::time_point now);
     bool complete_finished();
-    bool form_wave();
+    bool any_in_flight() const;
+    bool any_event_done();
+    bool dispatch();
+    bool admit_insert_run(table_rec& t, size_t take, int64_t run_keys);
+    bool launch_direct(int32_t table, const std::vector<int64_t>& tickets);
+    bool launch_packed(launch_slot& sl, int op, const std::vector<std::pair<int32_t, int64_t>>& run);
     sg_status grow(table_rec& t, int64_t need);
 };
 
@@ -327,9 +356,47 @@ kernel_view(sg_unordered* h)
                   static_cast<uint32_t>(v.num_groups), static_cast<uint32_t>(v.total_count), v.bucket_bits };
 }
 
+int
+key_bytes_of_kind(int32_t kind)
+{
+    return (kind == SG_SET_U32 || kind == SG_MAP_U32_U32 || kind == SG_MAP_U32_U64) ? 4 : 8;
+}
+
+int
+mapped_bytes_of_kind(int32_t kind)
+{
+    return kind == SG_MAP_U64_U32 || kind == SG_MAP_U32_U32 ? 4 : (kind == SG_MAP_U64_U64 || kind == SG_MAP_U32_U64 ? 8 : 0);
+}
+
+template <typename T>
+T*
+advance(T* p, int64_t bytes)
+{
+    return p == nullptr ? nullptr
+                        : reinterpret_cast<T*>(reinterpret_cast<typename std::conditional<std::is_const<T>::value,
+                                                                                          const char, char>::type*>(p) +
+                                               bytes);
+}
+
 } // namespace
 
-// Completes every wave whose event has fired.  Caller holds the lock.
+// Marks the requests done at `now`.  Caller holds the lock.
+void
+sg_server::finish(const std::vector<int64_t>& tickets, clock_type::time_point now)
+{
+    for (int64_t tk : tickets)
+    {
+        request_rec& r = rec(tk);
+        r.done = true;
+        r.t_done = now;
+        latencies_us.push_back(std::chrono::duration<double, std::micro>(now - r.t_submit).count());
+        keys_done += r.r.n;
+    }
+    t_last = now;
+}
+
+// Completes every launch whose event has fired: its requests are done and its tables free again.  Caller
+// holds the lock.
 bool
 sg_server::complete_finished()
 {
@@ -340,15 +407,7 @@ sg_server::complete_finished()
         {
             continue;
         }
-        const auto now = clock_type::now();
-        for (int64_t tk : sl.tickets)
-        {
-            request_rec& r = rec(tk);
-            r.done = true;
-            r.t_done = now;
-            latencies_us.push_back(std::chrono::duration<double, std::micro>(now - r.t_submit).count());
-            keys_done += r.r.n;
-        }
+        finish(sl.tickets, clock_type::now());
         for (int32_t t : sl.tables)
         {
             auto it = tables.find(t);
@@ -357,13 +416,69 @@ sg_server::complete_finished()
                 it->second.busy = false;
             }
         }
-        t_last = now;
         sl.tickets.clear();
         sl.tables.clear();
         sl.in_use = false;
         any = true;
     }
+    for (auto& u : units)
+    {
+        if (!u.in_use || cudaEventQuery(u.done) != cudaSuccess)
+        {
+            continue;
+        }
+        finish(u.tickets, clock_type::now());
+        auto it = tables.find(u.table);
+        if (it != tables.end())
+        {
+            it->second.busy = false;
+        }
+        u.tickets.clear();
+        u.in_use = false;
+        any = true;
+    }
     return any;
+}
+
+bool
+sg_server::any_in_flight() const
+{
+    for (const auto& sl : slots)
+    {
+        if (sl.in_use)
+        {
+            return true;
+        }
+    }
+    for (const auto& u : units)
+    {
+        if (u.in_use)
+        {
+            return true;
+        }
+    }
+    return false;
+}
+
+// Only the scheduler thread touches the events; safe without the lock.
+bool
+sg_server::any_event_done()
+{
+    for (auto& sl : slots)
+    {
+        if (sl.in_use && cudaEventQuery(sl.done) == cudaSuccess)
+        {
+            return true;
+        }
+    }
+    for (auto& u : units)
+    {
+        if (u.in_use && cudaEventQuery(u.done) == cudaSuccess)
+        {
+            return true;
+        }
+    }
+    return false;
 }
 
 // Grows table t (rehash into a table of twice the capacity, until `need` elements fit under 85 %
@@ -383,7 +498,6 @@ sg_server::grow(table_rec& t, int64_t need)
             return SG_ERR_BUDGET;
         }
     } while (need > ms * 85 / 100);
-    const int64_t elem = slot_bytes_of_kind(kind);
     int64_t cur = 0;
     sg_status st = sg_unordered_size(t.h, nullptr, &cur);
     if (st != SG_OK)
@@ -424,7 +538,6 @@ sg_server::grow(table_rec& t, int64_t need)
     }
     sg::detail::dev_free(keys);
     sg::detail::dev_free(vals);
-    (void)elem;
     if (st != SG_OK)
     {
         sg_unordered_destroy(nh);
@@ -441,205 +554,254 @@ sg_server::grow(table_rec& t, int64_t need)
     return SG_OK;
 }
 
-// Forms and launches one wave if a slot is free and some table has runnable requests.  Caller holds
-// the lock.
+// Before an insert run of `take` requests and run_keys keys: grows the table if the run could pass 85 % of
+// max_size().  When the budget does not allow it, the run's requests complete with SG_ERR_BUDGET (nothing
+// spills) and false is returned.  Caller holds the lock.
 bool
-sg_server::form_wave()
+sg_server::admit_insert_run(table_rec& t, size_t take, int64_t run_keys)
 {
-    launch_slot* sl = nullptr;
-    for (auto& s : slots)
+    if (t.size_bound + run_keys > t.max_size * 85 / 100)
     {
-        if (!s.in_use)
+        int64_t exact = 0;
+        if (sg_unordered_size(t.h, nullptr, &exact) == SG_OK)
         {
-            sl = &s;
+            t.size_bound = exact;
+        }
+        if (t.size_bound + run_keys > t.max_size * 85 / 100 && grow(t, t.size_bound + run_keys) != SG_OK)
+        {
+            const auto now = clock_type::now();
+            for (size_t k = 0; k < take; ++k)
+            {
+                request_rec& r = rec(t.fifo.front());
+                r.status = SG_ERR_BUDGET;
+                r.done = true;
+                r.t_done = now;
+                ++refused_budget;
+                t.fifo.pop_front();
+            }
+            cv_done.notify_all();
+            return false;
+        }
+    }
+    t.size_bound += run_keys;
+    return true;
+}
+
+// A table's run of large requests: each request is cut into launches of at most chunk_keys keys on one
+// low-priority stream (in request order, so the table sees them in submission order); the unit's event
+// completes the run.  Caller holds the lock and has checked that a unit is free.
+bool
+sg_server::launch_direct(int32_t table, const std::vector<int64_t>& tickets)
+{
+    direct_unit* u = nullptr;
+    for (auto& x : units)
+    {
+        if (!x.in_use)
+        {
+            u = &x;
             break;
         }
     }
-    if (sl == nullptr)
+    if (u == nullptr)
     {
         return false;
     }
-    // runs[op] = (table, ticket) pairs, in table order then FIFO order
-    std::vector<std::pair<int32_t, int64_t>> runs[3];
-    int nseg = 0;
-    for (auto& kv : tables)
+    sg_unordered* h = tables[table].h;
+    cudaStream_t s = lo_streams[next_lo];
+    next_lo = (next_lo + 1) % static_cast<int>(lo_streams.size());
+    const int kb = key_bytes_of_kind(kind);
+    const int mb = mapped_bytes_of_kind(kind);
+    bool ok = true;
+    for (int64_t tk : tickets)
     {
-        table_rec& t = kv.second;
-        if (t.busy || t.fifo.empty())
+        const sg_request& r = rec(tk).r;
+        for (int64_t off = 0; off < r.n && ok; off += chunk_keys)
         {
-            continue;
-        }
-        const int op = rec(t.fifo.front()).r.op;
-        int64_t run_keys = 0;
-        size_t take = 0;
-        while (take < t.fifo.size() && rec(t.fifo[take]).r.op == op && nseg + static_cast<int>(take) < kSlotSegments)
-        {
-            run_keys += rec(t.fifo[take]).r.n;
-            ++take;
-        }
-        if (take == 0)
-        {
-            continue;
-        }
-        if (op == SG_SERVER_INSERT && t.size_bound + run_keys > t.max_size * 85 / 100)
-        {
-            int64_t exact = 0;
-            if (sg_unordered_size(t.h, nullptr, &exact) == SG_OK)
+            const int64_t len = r.n - off < chunk_keys ? r.n - off : chunk_keys;
+            sg_status st = SG_OK;
+            if (r.op == SG_SERVER_INSERT)
             {
-                t.size_bound = exact;
+                st = sg_unordered_insert_kv(h, advance(r.keys, off * kb), advance(r.mapped, off * mb), len,
+                                            advance(r.out_flags, off), s);
             }
-            if (t.size_bound + run_keys > t.max_size * 85 / 100 && grow(t, t.size_bound + run_keys) != SG_OK)
+            else if (r.op == SG_SERVER_FIND)
             {
-                // refuse the run rather than spill: these requests complete with SG_ERR_BUDGET
-                const auto now = clock_type::now();
-                for (size_t k = 0; k < take; ++k)
-                {
-                    request_rec& r = rec(t.fifo.front());
-                    r.status = SG_ERR_BUDGET;
-                    r.done = true;
-                    r.t_done = now;
-                    ++refused_budget;
-                    t.fifo.pop_front();
-                }
-                continue;
+                st = sg_unordered_find(h, advance(r.keys, off * kb), len, advance(r.out_mapped, off * mb),
+                                       advance(r.out_flags, off), s);
             }
+            else
+            {
+                st = sg_unordered_erase(h, advance(r.keys, off * kb), len, advance(r.out_flags, off), s);
+            }
+            ok = st == SG_OK;
+            ++launches;
         }
-        if (op == SG_SERVER_INSERT)
-        {
-            t.size_bound += run_keys;
-        }
-        for (size_t k = 0; k < take; ++k)
-        {
-            runs[op].push_back({ kv.first, t.fifo.front() });
-            t.fifo.pop_front();
-        }
-        nseg += static_cast<int>(take);
-        t.busy = true;
-        sl->tables.push_back(kv.first);
-    }
-    if (nseg == 0)
-    {
-        if (!sl->tables.empty())
-        {
-            sl->tables.clear();
-        }
-        cv_done.notify_all();
-        return false;
-    }
-    // large requests run as their own single-table launches; the rest are packed into one segmented
-    // launch per operation (descriptors: op 0 first, then 1, then 2)
-    std::vector<std::pair<int32_t, int64_t>> direct;
-    for (int op = 0; op < 3; ++op)
-    {
-        std::vector<std::pair<int32_t, int64_t>> packed;
-        for (const auto& tr : runs[op])
-        {
-            (rec(tr.second).r.n >= kDirectKeys ? direct : packed).push_back(tr);
-        }
-        runs[op].swap(packed);
-    }
-    int base = 0;
-    int op_first[3], op_count[3];
-    int64_t op_tiles[3];
-    for (int op = 0; op < 3; ++op)
-    {
-        op_first[op] = base;
-        op_count[op] = static_cast<int>(runs[op].size());
-        int64_t tiles = 0;
-        for (const auto& tr : runs[op])
-        {
-            const request_rec& r = rec(tr.second);
-            seg_desc& d = sl->h_segs[base];
-            d.view = kernel_view(tables[tr.first].h);
-            d.in0 = r.r.keys;
-            d.in1 = r.r.mapped;
-            d.out_vals = r.r.out_mapped;
-            d.out_flags = r.r.out_flags;
-            d.n = r.r.n;
-            sl->h_prefix[base + op] = tiles; // per-op prefix arrays are laid out back to back
-            tiles += (r.r.n + 31) / 32;
-            sl->tickets.push_back(tr.second);
-            ++base;
-        }
-        sl->h_prefix[base + op] = tiles;
-        op_tiles[op] = tiles;
-    }
-    cudaStream_t s0 = streams[next_stream];
-    next_stream = (next_stream + 1) % static_cast<int>(streams.size());
-    bool ok = cudaMemcpyAsync(sl->d_segs, sl->h_segs, sizeof(seg_desc) * base, cudaMemcpyHostToDevice, s0) ==
-                      cudaSuccess &&
-              cudaMemcpyAsync(sl->d_prefix, sl->h_prefix, sizeof(int64_t) * (base + 3), cudaMemcpyHostToDevice, s0) ==
-                      cudaSuccess;
-    cudaEvent_t staged = nullptr;
-    cudaEventCreateWithFlags(&staged, cudaEventDisableTiming);
-    cudaEventRecord(staged, s0);
-    std::vector<cudaStream_t> used_streams;
-    for (int op = 0; op < 3 && ok; ++op)
-    {
-        if (op_count[op] == 0)
-        {
-            continue;
-        }
-        cudaStream_t s = streams[next_stream];
-        next_stream = (next_stream + 1) % static_cast<int>(streams.size());
-        cudaStreamWaitEvent(s, staged, 0);
-        ok = launch_segments_kind(kind, op, sl->d_segs + op_first[op], sl->d_prefix + op_first[op] + op,
-                                  op_count[op], op_tiles[op], grid_cap, s) == SG_OK;
-        used_streams.push_back(s);
-        ++launches;
-    }
-    for (const auto& tr : direct)
-    {
         if (!ok)
         {
-            break;
+            rec(tk).status = SG_ERR_CUDA;
         }
-        const request_rec& r = rec(tr.second);
-        sg_unordered* h = tables[tr.first].h;
-        cudaStream_t s = streams[next_stream];
-        next_stream = (next_stream + 1) % static_cast<int>(streams.size());
-        sg_status st = SG_OK;
-        if (r.r.op == SG_SERVER_INSERT)
-        {
-            st = sg_unordered_insert_kv(h, r.r.keys, r.r.mapped, r.r.n, r.r.out_flags, s);
-        }
-        else if (r.r.op == SG_SERVER_FIND)
-        {
-            st = sg_unordered_find(h, r.r.keys, r.r.n, r.r.out_mapped, r.r.out_flags, s);
-        }
-        else
-        {
-            st = sg_unordered_erase(h, r.r.keys, r.r.n, r.r.out_flags, s);
-        }
-        ok = st == SG_OK;
-        sl->tickets.push_back(tr.second);
-        used_streams.push_back(s);
-        ++launches;
     }
-    // the wave is done when every stream it used is done
-    for (cudaStream_t s : used_streams)
+    cudaEventRecord(u->done, s);
+    u->tickets = tickets;
+    u->table = table;
+    u->in_use = true;
+    return true;
+}
+
+// One segmented launch of small runs of operation `op` on a high-priority stream.  Caller holds the lock.
+bool
+sg_server::launch_packed(launch_slot& sl, int op, const std::vector<std::pair<int32_t, int64_t>>& run)
+{
+    int64_t tiles = 0;
+    int nseg = 0;
+    for (const auto& tr : run)
     {
-        if (s != s0)
+        const request_rec& r = rec(tr.second);
+        seg_desc& d = sl.h_segs[nseg];
+        d.view = kernel_view(tables[tr.first].h);
+        d.in0 = r.r.keys;
+        d.in1 = r.r.mapped;
+        d.out_vals = r.r.out_mapped;
+        d.out_flags = r.r.out_flags;
+        d.n = r.r.n;
+        sl.h_prefix[nseg] = tiles;
+        tiles += (r.r.n + 31) / 32;
+        sl.tickets.push_back(tr.second);
+        if (sl.tables.empty() || sl.tables.back() != tr.first)
         {
-            cudaEvent_t e = nullptr;
-            cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
-            cudaEventRecord(e, s);
-            cudaStreamWaitEvent(s0, e, 0);
-            cudaEventDestroy(e);
+            sl.tables.push_back(tr.first);
         }
+        ++nseg;
     }
-    cudaEventRecord(sl->done, s0);
-    cudaEventDestroy(staged);
-    sl->in_use = true;
-    ++waves;
+    sl.h_prefix[nseg] = tiles;
+    cudaStream_t s = hi_streams[next_hi];
+    next_hi = (next_hi + 1) % static_cast<int>(hi_streams.size());
+    bool ok = cudaMemcpyAsync(sl.d_segs, sl.h_segs, sizeof(seg_desc) * nseg, cudaMemcpyHostToDevice, s) ==
+                      cudaSuccess &&
+              cudaMemcpyAsync(sl.d_prefix, sl.h_prefix, sizeof(int64_t) * (nseg + 1), cudaMemcpyHostToDevice, s) ==
+                      cudaSuccess;
+    ok = ok && launch_segments_kind(kind, op, sl.d_segs, sl.d_prefix, nseg, tiles, grid_cap, s) == SG_OK;
+    ++launches;
+    cudaEventRecord(sl.done, s);
+    sl.in_use = true;
     if (!ok)
     {
-        for (int64_t tk : sl->tickets)
+        for (int64_t tk : sl.tickets)
         {
             rec(tk).status = SG_ERR_CUDA;
         }
     }
     return true;
+}
+
+// One scheduling round.  Tables with pending requests and nothing in flight are taken oldest request
+// first; each contributes its run of consecutive same-operation requests.  A run of at least direct_keys
+// keys becomes a direct unit while fewer than max_direct are in flight (else the table waits); smaller
+// runs join the round's packed launch of their operation, when a launch slot is free for it.  Caller
+// holds the lock.  Returns true when something was launched.
+bool
+sg_server::dispatch()
+{
+    std::vector<std::pair<int64_t, int32_t>> cand;
+    for (auto& kv : tables)
+    {
+        if (!kv.second.busy && !kv.second.fifo.empty())
+        {
+            cand.push_back({ kv.second.fifo.front(), kv.first });
+        }
+    }
+    if (cand.empty())
+    {
+        return false;
+    }
+    std::sort(cand.begin(), cand.end());
+    int direct_busy = 0;
+    for (const auto& u : units)
+    {
+        direct_busy += u.in_use ? 1 : 0;
+    }
+    launch_slot* op_slot[3] = { nullptr, nullptr, nullptr };
+    std::vector<std::pair<int32_t, int64_t>> packed[3];
+    int packed_segs[3] = { 0, 0, 0 };
+    bool launched = false;
+    for (const auto& c : cand)
+    {
+        table_rec& t = tables[c.second];
+        const int op = rec(t.fifo.front()).r.op;
+        size_t take = 0;
+        int64_t run_keys = 0;
+        while (take < t.fifo.size() && rec(t.fifo[take]).r.op == op && take < static_cast<size_t>(kSlotSegments))
+        {
+            run_keys += rec(t.fifo[take]).r.n;
+            ++take;
+        }
+        const bool big = run_keys >= direct_keys;
+        if (big && direct_busy >= max_direct)
+        {
+            continue;
+        }
+        if (!big)
+        {
+            if (packed_segs[op] + static_cast<int>(take) > kSlotSegments)
+            {
+                continue;
+            }
+            if (op_slot[op] == nullptr)
+            {
+                for (auto& sl : slots)
+                {
+                    if (!sl.in_use && &sl != op_slot[0] && &sl != op_slot[1] && &sl != op_slot[2])
+                    {
+                        op_slot[op] = &sl;
+                        break;
+                    }
+                }
+                if (op_slot[op] == nullptr)
+                {
+                    continue;
+                }
+            }
+        }
+        if (op == SG_SERVER_INSERT && !admit_insert_run(t, take, run_keys))
+        {
+            continue;
+        }
+        std::vector<int64_t> tk;
+        tk.reserve(take);
+        for (size_t k = 0; k < take; ++k)
+        {
+            tk.push_back(t.fifo.front());
+            t.fifo.pop_front();
+        }
+        t.busy = true;
+        if (big)
+        {
+            launch_direct(c.second, tk);
+            ++direct_busy;
+            launched = true;
+        }
+        else
+        {
+            for (int64_t x : tk)
+            {
+                packed[op].push_back({ c.second, x });
+            }
+            packed_segs[op] += static_cast<int>(take);
+        }
+    }
+    for (int op = 0; op < 3; ++op)
+    {
+        if (!packed[op].empty())
+        {
+            launch_packed(*op_slot[op], op, packed[op]);
+            launched = true;
+        }
+    }
+    if (launched)
+    {
+        ++waves;
+    }
+    return launched;
 }
 
 void
@@ -649,55 +811,25 @@ sg_server::run()
     std::unique_lock<std::mutex> lock(m);
     while (true)
     {
-        const bool finished = complete_finished();
-        if (finished)
+        if (complete_finished())
         {
             cv_done.notify_all();
         }
-        bool launched = false;
-        while (!paused && form_wave())
+        const bool launched = !paused && dispatch();
+        const bool in_flight = any_in_flight();
+        if (stop && !in_flight)
         {
-            launched = true;
-        }
-        if (stop)
-        {
-            bool idle = true;
-            for (auto& s : slots)
-            {
-                idle = idle && !s.in_use;
-            }
-            if (idle)
-            {
-                break;
-            }
-        }
-        bool in_flight = false;
-        for (auto& s : slots)
-        {
-            in_flight = in_flight || s.in_use;
+            break;
         }
         if (in_flight)
         {
-            // Spin outside the lock until a wave completes or a request arrives; only this thread
-            // touches the slots' events.  After ~200 us of spinning, yield the core between polls.
+            // Spin outside the lock until a launch completes or a request arrives; only this thread
+            // touches the events.  After ~200 us of spinning, yield the core between polls.
             const uint64_t seen = submissions.load(std::memory_order_acquire);
             lock.unlock();
             const auto t0 = clock_type::now();
-            while (true)
+            while (!any_event_done() && submissions.load(std::memory_order_acquire) == seen)
             {
-                bool ready = false;
-                for (auto& sl : slots)
-                {
-                    if (sl.in_use && cudaEventQuery(sl.done) == cudaSuccess)
-                    {
-                        ready = true;
-                        break;
-                    }
-                }
-                if (ready || submissions.load(std::memory_order_acquire) != seen)
-                {
-                    break;
-                }
                 if (clock_type::now() - t0 > std::chrono::microseconds(200))
                 {
                     std::this_thread::yield();
@@ -735,18 +867,35 @@ sg_server_create(int32_t kind, int64_t hbm_budget_bytes, int32_t n_streams, int3
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, srv->device);
     srv->grid_cap = sms * 8;
-    srv->streams.resize(n_streams);
-    for (auto& s : srv->streams)
+    int least = 0, greatest = 0;
+    cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    srv->hi_streams.resize(n_streams);
+    for (auto& s : srv->hi_streams)
     {
-        cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, greatest);
+    }
+    srv->lo_streams.resize(n_streams);
+    for (auto& s : srv->lo_streams)
+    {
+        cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, least);
+    }
+    srv->units.resize(kMaxDirectLimit);
+    for (auto& u : srv->units)
+    {
+        if (cudaEventCreateWithFlags(&u.done, cudaEventDisableTiming) != cudaSuccess)
+        {
+            cudaGetLastError();
+            sg_server_destroy(srv);
+            return SG_ERR_OOM;
+        }
     }
     srv->slots.resize(n_slots);
     for (auto& sl : srv->slots)
     {
         if (sg::detail::dev_malloc(&sl.d_segs, sizeof(seg_desc) * kSlotSegments) != cudaSuccess ||
-            sg::detail::dev_malloc(&sl.d_prefix, sizeof(int64_t) * (kSlotSegments + 3)) != cudaSuccess ||
+            sg::detail::dev_malloc(&sl.d_prefix, sizeof(int64_t) * (kSlotSegments + 1)) != cudaSuccess ||
             cudaMallocHost(&sl.h_segs, sizeof(seg_desc) * kSlotSegments) != cudaSuccess ||
-            cudaMallocHost(&sl.h_prefix, sizeof(int64_t) * (kSlotSegments + 3)) != cudaSuccess ||
+            cudaMallocHost(&sl.h_prefix, sizeof(int64_t) * (kSlotSegments + 1)) != cudaSuccess ||
             cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess)
         {
             cudaGetLastError();
@@ -797,11 +946,38 @@ sg_server_destroy(sg_server* srv)
             cudaEventDestroy(sl.done);
         }
     }
-    for (auto& s : srv->streams)
+    for (auto& u : srv->units)
     {
-        cudaStreamDestroy(s);
+        if (u.done != nullptr)
+        {
+            cudaEventDestroy(u.done);
+        }
+    }
+    for (auto* v : { &srv->hi_streams, &srv->lo_streams })
+    {
+        for (auto& s : *v)
+        {
+            if (s != nullptr)
+            {
+                cudaStreamDestroy(s);
+            }
+        }
     }
     delete srv;
+    return SG_OK;
+}
+
+sg_status
+sg_server_set_policy(sg_server* srv, int64_t direct_keys, int64_t chunk_keys, int32_t max_direct)
+{
+    if (srv == nullptr || direct_keys < 1 || chunk_keys < 1 || max_direct < 1 || max_direct > kMaxDirectLimit)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    std::lock_guard<std::mutex> lock(srv->m);
+    srv->direct_keys = direct_keys;
+    srv->chunk_keys = chunk_keys;
+    srv->max_direct = max_direct;
     return SG_OK;
 }
 

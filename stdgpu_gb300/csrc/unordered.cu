@@ -1120,6 +1120,8 @@ struct sg_unordered
     bool custom_hash;           // buckets come from caller-supplied hashes (the *_hashed entry points)
     char* part_scratch;         // partitioned bulk insert: value_type elements, then 2 x kPartMax counters
     int64_t part_scratch_bytes;
+    unsigned int* locks;        // stripe locks of the native device inserts (include/stdgpu_gb300/device.cuh)
+    int64_t lock_count;
 };
 
 namespace
@@ -1148,7 +1150,21 @@ public_view(const sg_unordered* t)
     v.bucket_count = t->bucket_count;
     v.bucket_bits = t->bits;
     v.kind = t->kind;
+    v.insert_locks = t->locks;
+    v.lock_mask = t->lock_count - 1;
     return v;
+}
+
+// Stripe locks of the native device inserts: one per 16 probe groups, a power of two in [256, 2^22].
+int64_t
+insert_lock_count(int64_t num_groups)
+{
+    int64_t n = 256;
+    while (n < num_groups / 16 && n < (int64_t{ 1 } << 22))
+    {
+        n <<= 1;
+    }
+    return n;
 }
 
 void
@@ -1167,7 +1183,7 @@ fill_geometry(int32_t kind, int64_t capacity, sg_geometry* g)
     g->slots_per_group = spg;
     const int64_t nchunks = (g->max_size + kRangeChunk - 1) / kRangeChunk;
     g->storage_bytes = (g->num_groups + 1) * kGroupBytes + static_cast<int64_t>(sizeof(table_header)) +
-                       (nchunks + 1) * 4;
+                       (nchunks + 1) * 4 + insert_lock_count(g->num_groups) * 4;
 }
 
 // Kernel dispatch over the six kinds.
@@ -1625,6 +1641,15 @@ sg_unordered_create(int32_t kind, int64_t capacity, void* stream, sg_unordered**
     {
         e = cudaMallocHost(&t->host_hdr, sizeof(table_header));
     }
+    if (e == cudaSuccess)
+    {
+        t->lock_count = insert_lock_count(t->num_groups);
+        e = sg::detail::dev_malloc(&t->locks, static_cast<size_t>(t->lock_count) * sizeof(unsigned int));
+    }
+    if (e == cudaSuccess)
+    {
+        e = cudaMemsetAsync(t->locks, 0, static_cast<size_t>(t->lock_count) * sizeof(unsigned int), as_stream(stream));
+    }
     if (e != cudaSuccess)
     {
         sg_unordered_destroy(t);
@@ -1668,6 +1693,10 @@ sg_unordered_destroy(sg_unordered* t)
     if (t->part_scratch != nullptr)
     {
         sg::detail::dev_free(t->part_scratch);
+    }
+    if (t->locks != nullptr)
+    {
+        sg::detail::dev_free(t->locks);
     }
     if (t->host_hdr != nullptr)
     {

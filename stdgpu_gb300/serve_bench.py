@@ -6,7 +6,10 @@ keys drawn Zipf(0.99) over a 2^30-rank universe per table (rank -> key by a seed
 mix, salted per table); values are a hash of the key.  HBM budget 120 GB.  Measured:
 
 * saturated throughput: all requests submitted back to back, server vs serial plain calls (one
-  request at a time, each a C-ABI call on the table's own object followed by a stream sync);
+  request at a time, each a C-ABI call on the table's own object followed by a stream sync, driven from
+  a C++ loop);
+* the speed-up ceiling: the serial calls once more without synchronisation, each timed on the device;
+  the device time of the requests large enough to fill the GPU on their own bounds any schedule;
 * latency under load: Poisson arrivals at a rate that keeps the device >= 80 % busy (80 % of the
   server's saturated request rate), p50 / p99 of submission-to-completion for the server and for the
   serial path fed the same arrivals.
@@ -24,6 +27,7 @@ import numpy as np
 import torch
 
 from . import _native as N
+from . import comparators as P
 from . import containers as C
 from . import server as S
 from . import workloads as W
@@ -90,34 +94,41 @@ def run_server(caps, staged, arrivals=None, budget=120 << 30):
     return wall, st, statuses, final_caps, sizes
 
 
-def run_serial(caps, staged, arrivals=None):
-    lib = N.load()
+def run_serial(caps, staged, arrivals=None, sync_each: bool = True, kernel_times: bool = False):
+    """The plain path from a C++ loop over the C ABI (comparators.serial_replay): each request is one call on
+    its table's own object; with sync_each the stream is synchronised after every request (the serial
+    plain path), without it the calls run back to back (the device time of the same kernels)."""
     tables = [C.unordered_map.createDeviceObject(int(c), key="u64", mapped="u64") for c in caps]
-    stream = torch.cuda.current_stream()
-    sp = c_void_p(stream.cuda_stream)
+    reqs = [N.sg_request(t, op, k.numel(), k.data_ptr(), v.data_ptr() if v is not None else None,
+                         ov.data_ptr() if ov is not None else None, of.data_ptr())
+            for t, op, k, v, ov, of in staged]
     torch.cuda.synchronize()
-    lat = []
-    t0 = time.perf_counter()
-    for i, (t, op, k, v, ov, of) in enumerate(staged):
-        arrive = t0 + (arrivals[i] if arrivals is not None else 0.0)
-        while arrivals is not None and time.perf_counter() < arrive:
-            pass
-        h = tables[t]._h
-        n = k.numel()
-        if op == S.INSERT:
-            lib.sg_unordered_insert_kv(h, c_void_p(k.data_ptr()), c_void_p(v.data_ptr()), n,
-                                       c_void_p(of.data_ptr()), sp)
-        elif op == S.FIND:
-            lib.sg_unordered_find(h, c_void_p(k.data_ptr()), n, c_void_p(ov.data_ptr()), c_void_p(of.data_ptr()), sp)
-        else:
-            lib.sg_unordered_erase(h, c_void_p(k.data_ptr()), n, c_void_p(of.data_ptr()), sp)
-        stream.synchronize()
-        lat.append((time.perf_counter() - arrive) * 1e6)
-    wall = time.perf_counter() - t0
+    lat, ker, wall = P.serial_replay(tables, reqs, arrivals, sync_each=sync_each, kernel_times=kernel_times)
     sizes = [tb.size() for tb in tables]
     for tb in tables:
         C.unordered_base.destroyDeviceObject(tb)
-    return wall, np.array(lat), sizes
+    return wall, lat, ker, sizes
+
+
+def ceiling(staged, kernel_us, serial_s: float, direct_keys: int = 1 << 16) -> dict:
+    """Upper bound of the speed-up any scheduler can reach over the serial path on this stream.  A request
+    of at least direct_keys keys fills the GPU by itself (each such launch is a persistent grid over every
+    SM), so overlapping it with other work cannot shorten it much; the device time of those requests,
+    measured back to back, is a floor under any schedule's wall time, and serial / floor bounds the
+    speed-up.  Small requests are assumed to overlap completely."""
+    n = np.array([k.numel() for _, _, k, _, _, _ in staged])
+    big = n >= direct_keys
+    k_us = np.asarray(kernel_us, dtype=np.float64)
+    floor_s = float(k_us[big].sum()) * 1e-6
+    return {
+        "direct_keys": direct_keys,
+        "keys_in_large_requests": float(n[big].sum() / n.sum()),
+        "large_requests": int(big.sum()),
+        "device_time_all_s": float(k_us.sum()) * 1e-6,
+        "device_time_large_s": floor_s,
+        "serial_s": serial_s,
+        "speedup_ceiling": serial_s / floor_s if floor_s > 0 else None,
+    }
 
 
 def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22) -> dict:
@@ -128,13 +139,17 @@ def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22) -> dict:
     wall_srv, st_sat, statuses, final_caps, sizes_srv = run_server(caps, staged)
     refused = sum(1 for s in statuses if s != N.SG_OK)
     # serial plain calls on tables presized to the final capacities
-    wall_ser, lat_ser_sat, sizes_ser = run_serial(final_caps, staged)
+    wall_ser, lat_ser_sat, _, sizes_ser = run_serial(final_caps, staged)
+    # the same calls back to back (no host synchronisation), each timed on the device: the speed-up ceiling
+    wall_stream, _, ker_us, _ = run_serial(final_caps, staged, sync_each=False, kernel_times=True)
+    bound = ceiling(staged, ker_us, wall_ser)
+    bound["stream_no_sync_s"] = wall_stream
     # Poisson arrivals at `load` x the server's saturated request rate
     rate = load * len(staged) / wall_srv
     rng = np.random.default_rng(seed + 1)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(staged)))
     wall_srv_l, st_load, _, _, _ = run_server(caps, staged, arrivals)
-    wall_ser_l, lat_ser_load, _ = run_serial(final_caps, staged, arrivals)
+    wall_ser_l, lat_ser_load, _, _ = run_serial(final_caps, staged, arrivals)
     return {
         "request_keys": [min_n, max_n],
         "tables": len(caps), "requests": len(staged), "keys": keys_total,
@@ -153,5 +168,7 @@ def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22) -> dict:
             "server_wall_s": wall_srv_l, "serial_wall_s": wall_ser_l,
             "server_keys_per_s": keys_total / wall_srv_l, "serial_keys_per_s": keys_total / wall_ser_l,
         },
+        "ceiling": bound,
+        "serial_driver": "C++ loop over the C ABI (stdgpu_gb300/comparators/plain_calls.cpp)",
         "final_sizes_agree": bool(sizes_srv == sizes_ser),
     }

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <random>
 #include <set>
+#include <string>
 #include <unordered_set>
 #include <vector>
 
@@ -25,6 +26,12 @@ check(bool ok, const char* name)
     {
         ++failures;
     }
+}
+
+static void
+check(bool ok, const std::string& name)
+{
+    check(ok, name.c_str());
 }
 
 template <typename T>
@@ -162,6 +169,85 @@ k_push_if(stdgpu::vector<std::uint32_t> v, int n, int* pushed)
     if (i < n && (i % 3) == 0)
     {
         pushed[i] = v.push_back(static_cast<std::uint32_t>(i));
+    }
+}
+
+// vector.inc:1022-1056 simultaneous_push_back_and_pop_back: every thread pushes its value, pops one element
+// and pushes what it popped into a second vector, all in one launch
+__global__ void
+vector_push_then_pop(stdgpu::vector<int> pool, stdgpu::vector<int> validation, const int* values, int n)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        pool.push_back(values[i]);
+        const auto popped = pool.pop_back();
+        if (popped.second)
+        {
+            validation.push_back(popped.first);
+        }
+    }
+}
+
+// deque.inc:1494-1700 simultaneous_*: every thread pushes its value at one end, pops one element from one
+// end and pushes what it popped into a second deque; mode bit 0: push_front (else push_back), bit 1:
+// pop_front (else pop_back)
+__global__ void
+deque_push_then_pop(stdgpu::deque<int> pool, stdgpu::deque<int> validation, const int* values, int n, int mode)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        if (mode & 1)
+        {
+            pool.push_front(values[i]);
+        }
+        else
+        {
+            pool.push_back(values[i]);
+        }
+        const auto popped = (mode & 2) ? pool.pop_front() : pool.pop_back();
+        if (popped.second)
+        {
+            if (mode & 1)
+            {
+                validation.push_front(popped.first);
+            }
+            else
+            {
+                validation.push_back(popped.first);
+            }
+        }
+    }
+}
+
+// one device call per thread: 0 push_back, 1 push_front, 2 emplace_front, 3 pop_back, 4 pop_front
+__global__ void
+deque_calls(stdgpu::deque<int> d, const int* values, int n, int op, int* ok)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        bool r = false;
+        switch (op)
+        {
+            case 0:
+                r = d.push_back(values[i]);
+                break;
+            case 1:
+                r = d.push_front(values[i]);
+                break;
+            case 2:
+                r = d.emplace_front(values[i]);
+                break;
+            case 3:
+                r = d.pop_back().second;
+                break;
+            default:
+                r = d.pop_front().second;
+                break;
+        }
+        ok[i] = r ? 1 : 0;
     }
 }
 
@@ -617,6 +703,172 @@ main()
         cudaFree(d_h);
         cudaFree(d_out);
         cudaFree(d_ok);
+    }
+
+    // vector: push_back and pop_back in one launch (vector.inc:1022-1056, N = 100000), then the same on a
+    // vector that a bulk call left non-empty, and a second launch on the result
+    {
+        using ivec = stdgpu::vector<int>;
+        const int N = 100000;
+        ivec pool = ivec::createDeviceObject(N);
+        ivec validation = ivec::createDeviceObject(N);
+        std::vector<int> h(N);
+        for (int i = 0; i < N; ++i)
+        {
+            h[i] = i + 1;
+        }
+        int* d_v = to_device(h);
+        vector_push_then_pop<<<(N + 127) / 128, 128>>>(pool, validation, d_v, N);
+        std::vector<int> got = to_host(validation.data(), N);
+        std::sort(got.begin(), got.end());
+        check(pool.size() == 0 && pool.empty() && !pool.full() && pool.valid() && validation.size() == N &&
+                      validation.full() && validation.valid() && got == h,
+              "vector simultaneous_push_back_and_pop_back");
+        // the pool starts from 5000 elements inserted by a bulk call: the launch's pops may take those too
+        pool.insert(pool.device_end(), d_v, d_v + 5000);
+        validation.clear();
+        vector_push_then_pop<<<(N / 2 + 127) / 128, 128>>>(pool, validation, d_v + 5000, N / 2);
+        const int left = pool.size();
+        std::vector<int> all = to_host(validation.data(), validation.size());
+        std::vector<int> rest = to_host(pool.data(), left);
+        all.insert(all.end(), rest.begin(), rest.end());
+        std::sort(all.begin(), all.end());
+        std::vector<int> want(h.begin(), h.begin() + 5000 + N / 2);
+        check(left == 5000 && validation.size() == N / 2 && all == want && pool.valid() && validation.valid(),
+              "vector push_back and pop_back in one launch after a bulk insert: every element kept once");
+        ivec::destroyDeviceObject(pool);
+        ivec::destroyDeviceObject(validation);
+        cudaFree(d_v);
+    }
+
+    // deque: the reference's simultaneous_* scenarios (deque.inc:1494-1700, N = 100000) for all four pairs
+    // of ends, the *_some / *_all / *_too_many scenarios of push_front, emplace_front and pop_back
+    // (deque.inc:284-345, 962-1245), push_front_circular (deque.inc:1298-1336), and a bulk call after
+    // device calls (turn words rebuilt)
+    {
+        using idq = stdgpu::deque<int>;
+        const int N = 100000;
+        std::vector<int> h(N);
+        for (int i = 0; i < N; ++i)
+        {
+            h[i] = i + 1;
+        }
+        int* d_v = to_device(h);
+        const char* names[4] = { "deque simultaneous_push_back_and_pop_back", "deque simultaneous_push_front_and_pop_back",
+                                 "deque simultaneous_push_back_and_pop_front",
+                                 "deque simultaneous_push_front_and_pop_front" };
+        for (int mode = 0; mode < 4; ++mode)
+        {
+            idq pool = idq::createDeviceObject(N);
+            idq validation = idq::createDeviceObject(N);
+            deque_push_then_pop<<<(N + 127) / 128, 128>>>(pool, validation, d_v, N, mode);
+            auto r = validation.device_range();
+            std::vector<int> got = to_host(r.begin(), r.size());
+            std::sort(got.begin(), got.end());
+            check(pool.size() == 0 && pool.empty() && !pool.full() && pool.valid() && validation.size() == N &&
+                          validation.full() && validation.valid() && got == h,
+                  names[mode]);
+            idq::destroyDeviceObject(pool);
+            idq::destroyDeviceObject(validation);
+        }
+        int* d_ok = nullptr;
+        cudaMalloc(&d_ok, sizeof(int) * N);
+        auto ok_count = [&](int n) {
+            long long c = 0;
+            for (int x : to_host(d_ok, n))
+            {
+                c += x;
+            }
+            return c;
+        };
+        // push_front / emplace_front: some, all, too many
+        for (int op = 1; op <= 2; ++op)
+        {
+            const int M = 10000;
+            const int sizes[3] = { M / 2, M, M + 500 };
+            for (int k = 0; k < 3; ++k)
+            {
+                idq d = idq::createDeviceObject(M);
+                deque_calls<<<(sizes[k] + 127) / 128, 128>>>(d, d_v, sizes[k], op, d_ok);
+                const int want = sizes[k] < M ? sizes[k] : M;
+                auto r = d.device_range();
+                std::vector<int> got = to_host(r.begin(), r.size());
+                std::sort(got.begin(), got.end());
+                bool vals = static_cast<int>(got.size()) == want;
+                for (int i = 0; vals && i + 1 < want; ++i)
+                {
+                    vals = got[i] < got[i + 1] && got[i] >= 1 && got[i + 1] <= sizes[k];
+                }
+                check(ok_count(sizes[k]) == want && d.size() == want && d.valid() && vals,
+                      std::string(op == 1 ? "deque push_front" : "deque emplace_front") +
+                              (k == 0 ? "_some" : k == 1 ? "_all" : "_too_many"));
+                idq::destroyDeviceObject(d);
+            }
+        }
+        // pop_back: some, all, too many, from a deque filled by push_back 1..M; the back elements go first
+        {
+            const int M = 10000;
+            const int pops[3] = { M / 3, M, M + 700 };
+            for (int k = 0; k < 3; ++k)
+            {
+                idq d = idq::createDeviceObject(M);
+                deque_calls<<<(M + 127) / 128, 128>>>(d, d_v, M, 0, d_ok);
+                deque_calls<<<(pops[k] + 127) / 128, 128>>>(d, d_v, pops[k], 3, d_ok);
+                const int taken = pops[k] < M ? pops[k] : M;
+                auto r = d.device_range();
+                std::vector<int> left = to_host(r.begin(), r.size());
+                std::sort(left.begin(), left.end());
+                std::vector<int> want(h.begin(), h.begin() + (M - taken));
+                check(ok_count(pops[k]) == taken && d.size() == M - taken && d.valid() && left == want,
+                      std::string("deque pop_back") + (k == 0 ? "_some" : k == 1 ? "_all" : "_too_many"));
+                idq::destroyDeviceObject(d);
+            }
+        }
+        // push_front_circular: fill 1..M, pop_back M/3, pop_front M/3, push_front 2M/3 new values
+        {
+            const int M = 10000;
+            const int n_pop = M / 3;
+            const int n_push = 2 * n_pop;
+            idq d = idq::createDeviceObject(M);
+            deque_calls<<<(M + 127) / 128, 128>>>(d, d_v, M, 0, d_ok);
+            deque_calls<<<(n_pop + 127) / 128, 128>>>(d, d_v, n_pop, 3, d_ok);
+            deque_calls<<<(n_pop + 127) / 128, 128>>>(d, d_v, n_pop, 4, d_ok);
+            deque_calls<<<(n_push + 127) / 128, 128>>>(d, d_v + M - n_pop, n_push, 1, d_ok);
+            auto r = d.device_range();
+            std::vector<int> got = to_host(r.begin(), r.size());
+            std::sort(got.begin(), got.end());
+            std::vector<int> want;
+            for (int i = 0; i < M - 2 * n_pop; ++i)
+            {
+                want.push_back(n_pop + 1 + i);
+            }
+            for (int i = 0; i < n_push; ++i)
+            {
+                want.push_back(M - n_pop + 1 + i);
+            }
+            std::sort(want.begin(), want.end());
+            check(d.size() == M - 2 * n_pop + n_push && d.valid() && got == want, "deque push_front_circular");
+            // a bulk call after the device calls: pop_front of everything through the host, front to back
+            std::uint8_t* d_bok = nullptr;
+            int* d_pop = nullptr;
+            const int n_all = M - 2 * n_pop + n_push;
+            cudaMalloc(&d_bok, n_all);
+            cudaMalloc(&d_pop, sizeof(int) * n_all);
+            std::vector<std::uint8_t> is_push(n_all, 0);
+            std::uint8_t* d_is_push = to_device(is_push);
+            check(sg_deque_ops(d.native_handle(), d_is_push, nullptr, n_all, d_pop, d_bok, nullptr) == SG_OK,
+                  "deque bulk call after device calls: accepted");
+            const std::vector<int> front_to_back = to_host(d_pop, n_all);
+            check(count_ok(d_bok, n_all) == n_all && d.size() == 0 && d.valid() &&
+                          front_to_back == to_host(r.begin(), r.size()),
+                  "deque bulk pop_front after device calls: every element, front to back");
+            cudaFree(d_bok);
+            cudaFree(d_pop);
+            cudaFree(d_is_push);
+            idq::destroyDeviceObject(d);
+        }
+        cudaFree(d_ok);
+        cudaFree(d_v);
     }
 
     // deque: device emplace_back, front / back / at / operator[], device_range, valid, max_size

@@ -15,6 +15,7 @@ CUSTOM = ROOT / "tests" / "cpp" / "custom_key_test.cu"
 WIDE = ROOT / "tests" / "cpp" / "wide_key_test.cu"
 WIDE_GOLDEN = ROOT / "tests" / "cpp" / "wide_golden_test.cu"
 ROUTING = ROOT / "tests" / "cpp" / "routing_check.cu"
+CHURN = ROOT / "tests" / "cpp" / "device_churn_test.cu"
 GOLDEN = ROOT / "tests" / "golden"
 OUT = ROOT / "tests" / "cpp" / "_build"
 
@@ -119,3 +120,50 @@ def test_element_types_route_to_the_intended_storage():
     keys of up to 8 bytes, the wide tables for the rest (static_asserts in tests/cpp/routing_check.cu)."""
     stdgpu_gb300.load()
     _compile(src=ROUTING)
+
+
+def test_device_churn_program_compiles_for_sm103a():
+    stdgpu_gb300.load()
+    _compile(src=CHURN)
+
+
+@pytest.mark.gpu
+def test_device_insert_erase_churn_reuses_erased_slots(tmp_path):
+    """Device-only insert / erase churn on tiny tables for hundreds of launches: per-key outcomes and sizes
+    equal a std::unordered_set / std::unordered_map model after every launch, no insert of an absent key is
+    refused below max_size() (erased slots are reused), racing inserts and erases of one key keep at most
+    one copy.  The set churn's launches are then replayed on the oracle restatement (and on the reference
+    library where it is built) launch by launch, with equal per-key outcomes and sizes."""
+    import numpy as np
+
+    import oracle as O
+    from gpu_util import per_key_success
+
+    stdgpu_gb300.load()
+    exe = _compile(src=CHURN)
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=600)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "ALL PASS" in r.stdout
+    cap, launches = np.fromfile(tmp_path / "header.bin", dtype=np.int64)
+    meta = np.fromfile(tmp_path / "meta.bin", dtype=np.int32).reshape(-1, 2)
+    keys = np.fromfile(tmp_path / "keys.bin", dtype=np.uint64)
+    ok = np.fromfile(tmp_path / "ok.bin", dtype=np.uint8)
+    assert len(meta) == launches
+    tables = [O.PortTable(O.SET_U64, int(cap))]
+    if O.ref_available():
+        O.ref_set_threads(1)
+        tables.append(O.RefTable(O.SET_U64, int(cap)))
+    pos = 0
+    for n, n_ins in meta:
+        k, f = keys[pos: pos + n], ok[pos: pos + n]
+        pos += n
+        for t in tables:
+            fi = t.insert(k[:n_ins], flags=True)
+            fe = t.erase(k[n_ins:], flags=True)
+            assert per_key_success(k[:n_ins], f[:n_ins]) == per_key_success(k[:n_ins], fi)
+            assert per_key_success(k[n_ins:], f[n_ins:]) == per_key_success(k[n_ins:], fe)
+    sizes = {t.size() for t in tables}
+    assert len(sizes) == 1
+    for t in tables:
+        t.close()

@@ -1,9 +1,9 @@
 """The allocation-free bitset count, called through the C ABI, against the allocating one.
 
-sg_bitset_count_noalloc serves callers that must not allocate device memory (for example code that
-runs while a CUDA graph is captured in global mode, or a process whose device memory belongs to
-another allocator with a fixed budget): it keeps its per-block partial sums in a fixed array inside
-the library instead of allocating them.  Two calls in a row must give the same counts as
+sg_bitset_count_noalloc serves callers that must not allocate device memory (a process whose device
+memory belongs to another allocator with a fixed budget, or a latency-critical path that cannot take
+the device-wide synchronisation of cudaMalloc / cudaFree): it keeps its per-block partial sums in a
+fixed array inside the library instead of allocating them.  Two calls in a row must give the same counts as
 sg_bitset_count (integer work: exact), the second with fewer chunks than the first so that stale
 partial sums left in the shared array by the first call would show; sizes beyond the array's limit
 are refused.  This file is collected last and passes alone in a fresh process as well.
