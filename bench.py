@@ -13,8 +13,10 @@ larger than L2, so no flush is needed between steps.
 
 e2e: the same step through the C ABI's host-buffer entry points (sg_unordered_*_host):
 every step copies its inputs host->device from pinned memory and the find results
-device->host, in chunks overlapped with the kernels.  serial_copies: the same with
-whole-array copies before and after the device-pointer calls.
+device->host, in chunks overlapped with the kernels; the host inputs are static, so the
+stager is told so (sg_stager_set_inputs_ready) and a call's uploads start while the previous
+call's kernels run.  ordered_uploads: the same with uploads in stream order (the stager's
+default).  serial_copies: whole-array copies before and after the device-pointer calls.
 
 --impl reference: the reference's own CPU implementation (stdgpu 1.3.0,
 OpenMP backend, built under oracle/_ref) on a bounded sample of the same
@@ -471,6 +473,10 @@ def native_arm(args):
             found_h.zero_()
             return a.elapsed_time(b) / args.steps
 
+        # uploads in stream order (the stager's default), then with the inputs declared ready: the host
+        # buffers are static here, so the uploads of a call may start while the previous call's kernels run
+        ordered_ms = slowest_rank_ms(time_steps(e2e_step), ws, dev)
+        stager.set_inputs_ready(True)
         e2e_ms = slowest_rank_ms(time_steps(e2e_step), ws, dev)
         serial_ms = slowest_rank_ms(time_steps(e2e_serial_step), ws, dev)
         # one more, untimed step with events between the calls: where the e2e time goes
@@ -488,8 +494,11 @@ def native_arm(args):
         link_ms = max(h2d / link["h2d_gbs"], d2h / link["d2h_gbs"]) / 1e6
         link.update({"bound_ms": link_ms, "frac": link_ms / e2e_ms})
         e2e = {"value": ops_per_step * ws / (e2e_ms * 1e-3) / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms, "api": f"sg_unordered_*_host (pipelined, 2^{args.e2e_chunk_log2}-element chunks, {args.e2e_buffers} buffers)", "link": link,
-               "phases_ms": e2e_phase_ms,
+               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
+               "api": f"sg_unordered_*_host (pipelined, 2^{args.e2e_chunk_log2}-element chunks, {args.e2e_buffers} "
+                      f"buffers, sg_stager_set_inputs_ready)", "link": link,
+               "phases_ms": e2e_phase_ms, "inputs_ready": True,
+               "ordered_uploads": {"value": ops_per_step * ws / (ordered_ms * 1e-3) / 1e6, "ms_per_step": ordered_ms},
                "serial_copies": {"value": ops_per_step * ws / (serial_ms * 1e-3) / 1e6, "ms_per_step": serial_ms}}
 
     # ---------------- roofline of the dominant kernel
@@ -508,13 +517,16 @@ def native_arm(args):
             traffic = json.loads(tf.read_text()).get(dominant)
         except (ValueError, AttributeError):
             traffic = None
-    phase_kernels = {"insert": "k_part_scatter + k_insert_ordered (+ the gated direct k_insert, which exits at once "
-                               "unless the scatter left elements out); partitioned bulk insert, chosen automatically "
-                               "at this size",
-                     "find": "k_find", "erase": "k_part_scatter + k_erase_ordered (+ the gated direct k_erase); "
+    phase_kernels = {"insert": "k_part_scatter + k_ordered_staged<insert> (input chunks staged in shared memory by "
+                               "bulk copies; + the gated direct k_insert, which exits at once unless the scatter "
+                               "left elements out); partitioned bulk insert, chosen automatically at this size",
+                     "find": "k_find", "erase": "k_part_scatter + k_ordered_staged<erase> (+ the gated direct k_erase); "
                                                  "partitioned bulk erase, chosen automatically at this size"}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "frac_of_nominal": achieved / NOMINAL_HBM_GBS, "traffic": traffic, "kernel": dominant, "kernels": phase_kernels[dominant], "peak_source": peak_src,
+                "frac_of_nominal": achieved / NOMINAL_HBM_GBS, "traffic": traffic,
+                "traffic_source": "committed profile profiles/dram_traffic.json (ncu DRAM bytes of the same phase "
+                                  "from the launch list of this command; not measured in this run)",
+                "kernel": dominant, "kernels": phase_kernels[dominant], "peak_source": peak_src,
                 "bytes_per_op": BYTES_PER_OP[dominant],
                 "per_kernel": {k: {"ms": med[k], "mops": counts[k] / (med[k] * 1e-3) / 1e6,
                                    "gbs": BYTES_PER_OP[k] * counts[k] / (med[k] * 1e-3) / 1e9,

@@ -246,6 +246,11 @@ typedef struct sg_stager sg_stager;
 /* chunk_elems in [1, 2^30], n_buffers in [2, 8]; holds n_buffers x 33 x chunk_elems device bytes. */
 SG_API sg_status sg_stager_create(int64_t chunk_elems, int32_t n_buffers, sg_stager** out);
 SG_API sg_status sg_stager_destroy(sg_stager* stager);
+/* inputs_ready != 0: a call's host->device copies start when the call is made instead of after the work
+ * already queued on the caller's stream (the kernels still run in stream order), so the link keeps busy
+ * while earlier calls finish.  The caller vouches that no work queued before a call writes that call's
+ * host inputs (for example a download into the same host buffer).  Default 0. */
+SG_API sg_status sg_stager_set_inputs_ready(sg_stager* stager, int32_t inputs_ready);
 /* sg_unordered_insert / insert_kv / erase / find / contains with host buffers (outputs nullable); the
  * find form writes 0 as the mapped value of an absent key. */
 SG_API sg_status sg_unordered_insert_host(sg_unordered* table, sg_stager* stager, const void* values, int64_t n,
@@ -361,9 +366,11 @@ SG_API sg_status sg_server_submit_many(sg_server* server, const sg_request* requ
  * resuming lets the queued requests coalesce into the next waves. */
 SG_API sg_status sg_server_set_paused(sg_server* server, int32_t paused);
 /* Request-size policy: a table's run of same-operation requests with at least direct_keys keys runs as
- * its own launches of at most chunk_keys keys each, with at most max_direct (1..16) such runs in flight;
- * defaults 65536, 524288 and 2. */
-SG_API sg_status sg_server_set_policy(sg_server* server, int64_t direct_keys, int64_t chunk_keys, int32_t max_direct);
+ * its own launches of at most chunk_keys keys each on one of direct_streams (1..n_streams) low-priority
+ * streams, with at most max_direct (1..16) such runs issued and not complete; defaults 65536, 4194304, 4
+ * and 1 (large runs back to back in arrival order of their oldest requests). */
+SG_API sg_status sg_server_set_policy(sg_server* server, int64_t direct_keys, int64_t chunk_keys, int32_t max_direct,
+                                      int32_t direct_streams);
 /* Waits (timeout_ms < 0: no limit) for a ticket; out_request_status: SG_OK or SG_ERR_BUDGET (refused). */
 SG_API sg_status sg_server_wait(sg_server* server, int64_t ticket, int32_t timeout_ms, sg_status* out_request_status);
 /* Waits for every submitted request. */

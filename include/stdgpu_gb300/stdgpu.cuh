@@ -1163,6 +1163,14 @@ public:
         detail::gb300_check(sg_deque_clear(_handle, policy.stream), "deque::clear");
     }
 
+    // data() (src/stdgpu/deque.cuh): the ring's storage; element i sits at slot (front ticket + i) mod
+    // capacity(), which is i on a deque that never wrapped or moved its front
+    __host__ __device__ T*
+    data() const
+    {
+        return static_cast<T*>(_view.data);
+    }
+
     // the C-ABI handle, for the sg_deque_* entry points (for example sg_deque_ops, a bulk push_back /
     // pop_front mix)
     sg_deque*

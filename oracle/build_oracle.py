@@ -11,10 +11,12 @@
    (Release defaults, src/stdgpu/CMakeLists.txt:10-22).  Thrust comes from the
    CUDA toolkit's CCCL headers.
 
-The reference tree is read from ``$STDGPU_REFERENCE`` (default
-``/root/reference``) and staged into the git-ignored ``oracle/_ref/src`` so that
-the same recipe can rebuild the checker on an aarch64 machine where only the
-staged copy exists.  Nothing here is part of the product library.
+The reference tree is read from the ``ref_root`` argument of ``build_reference``,
+else from ``$STDGPU_REFERENCE``, else from REFERENCE_MOUNT (where the build
+container mounts the reference checkout, read-only); it is staged into the
+git-ignored ``oracle/_ref/src`` so that the same recipe can rebuild the checker on
+a machine where only the staged copy exists (the GPU host).  Nothing here is part
+of the product library.
 """
 
 from __future__ import annotations
@@ -28,6 +30,8 @@ from concurrent.futures import ThreadPoolExecutor
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
+# the read-only reference checkout of the build container, the last place this recipe looks
+REFERENCE_MOUNT = Path("/root/reference")
 REF_OUT = HERE / "_ref"
 PORT_OUT = HERE / "_build"
 STAGE = REF_OUT / "src"
@@ -108,9 +112,11 @@ def stage_reference(ref_root: Path) -> None:
     (dst / "config.h").write_text(CONFIG_H)
 
 
-def build_reference(jobs: int = 8) -> Path | None:
+def build_reference(jobs: int = 8, ref_root: Path | str | None = None) -> Path | None:
     """Stage (when the reference tree is present) and compile libsgref.so."""
-    ref_root = Path(os.environ.get("STDGPU_REFERENCE", "/root/reference"))
+    if ref_root is None:
+        ref_root = os.environ.get("STDGPU_REFERENCE") or REFERENCE_MOUNT
+    ref_root = Path(ref_root)
     if (ref_root / "src" / "stdgpu").is_dir():
         stage_reference(ref_root)
     if not (STAGE / "stdgpu" / "config.h").exists():

@@ -107,6 +107,7 @@ SIGNATURES = {
     "sg_unordered_geometry_for": (c_int32, [c_int32, c_int64, POINTER(sg_geometry)]),
     "sg_stager_create": (c_int32, [c_int64, c_int32, POINTER(c_void_p)]),
     "sg_stager_destroy": (c_int32, [c_void_p]),
+    "sg_stager_set_inputs_ready": (c_int32, [c_void_p, c_int32]),
     "sg_unordered_insert_host": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_unordered_insert_kv_host": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_unordered_erase_host": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
@@ -131,7 +132,7 @@ SIGNATURES = {
     "sg_server_submit": (c_int32, [c_void_p, POINTER(sg_request), POINTER(c_int64)]),
     "sg_server_submit_many": (c_int32, [c_void_p, POINTER(sg_request), c_int32, POINTER(c_int64)]),
     "sg_server_set_paused": (c_int32, [c_void_p, c_int32]),
-    "sg_server_set_policy": (c_int32, [c_void_p, c_int64, c_int64, c_int32]),
+    "sg_server_set_policy": (c_int32, [c_void_p, c_int64, c_int64, c_int32, c_int32]),
     "sg_server_wait": (c_int32, [c_void_p, c_int64, c_int32, POINTER(c_int32)]),
     "sg_server_drain": (c_int32, [c_void_p, c_int32]),
     "sg_server_get_stats": (c_int32, [c_void_p, POINTER(sg_server_stats)]),

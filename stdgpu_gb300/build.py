@@ -77,34 +77,55 @@ def is_current() -> bool:
     if not lib.exists() or os.environ.get("STDGPU_GB300_NVCC_FLAGS"):
         return False
     t = lib.stat().st_mtime
-    return all(p.stat().st_mtime <= t for p in _deps())
+    deps = _deps() + ([TUNING] if TUNING.exists() else [])
+    return all(p.stat().st_mtime <= t for p in deps)
 
 
-def build(force: bool = False, verbose_ptxas: bool = False) -> Path:
-    """Compile every translation unit for sm_103a and link the shared library."""
-    if not force and is_current():
+# launch shapes of the single-table kernels chosen by stdgpu_gb300/autotune_single.py (compile-time macros)
+TUNING = PKG / "tuning" / "single_table.json"
+
+
+def tuned_flags() -> list[str]:
+    """-D flags of the recorded best single-table launch shapes (none when no record exists)."""
+    if not TUNING.exists():
+        return []
+    import json
+    best = json.loads(TUNING.read_text()).get("best", {})
+    return [f"-D{k}={int(v)}" for k, v in sorted(best.items())]
+
+
+def build(force: bool = False, verbose_ptxas: bool = False, flags: list[str] | None = None,
+          out_lib: Path | None = None) -> Path:
+    """Compile every translation unit for sm_103a and link the shared library.  `flags` replaces the recorded
+    launch shapes (autotuning builds its candidates this way, into `out_lib`)."""
+    if flags is None and out_lib is None and not force and is_current():
         build_comparators()
         return library_path()
     OUT.mkdir(exist_ok=True)
     extra = ["-Xptxas", "-v"] if verbose_ptxas else []
+    extra += tuned_flags() if flags is None else list(flags)
     # optional extra compiler flags, e.g. -DSG_BULK_MIN_BLOCKS=3
     extra += os.environ.get("STDGPU_GB300_NVCC_FLAGS", "").split()
     cmds = []
     objs = []
+    obj_dir = OUT if out_lib is None else out_lib.parent / (out_lib.stem + "_obj")
+    obj_dir.mkdir(parents=True, exist_ok=True)
     for src in SOURCES:
-        obj = OUT / (Path(src).stem + ".o")
+        obj = obj_dir / (Path(src).stem + ".o")
         objs.append(obj)
         cmds.append([nvcc(), *ARCH_FLAGS, *NVCC_FLAGS, *extra, "-I", str(INCLUDE), "-I", str(CSRC),
                      "-c", str(CSRC / src), "-o", str(obj)])
     with ThreadPoolExecutor(max_workers=len(cmds)) as ex:
         logs = list(ex.map(_run, cmds))
-    tmp = OUT / (LIB_NAME + ".tmp")
+    target = library_path() if out_lib is None else out_lib
+    tmp = target.parent / (target.name + ".tmp")
     _run([nvcc(), *ARCH_FLAGS, "-shared", "-o", str(tmp), *[str(o) for o in objs], "-lcudart"])
-    os.replace(tmp, library_path())
+    os.replace(tmp, target)
     if verbose_ptxas:
-        (OUT / "ptxas.log").write_text("\n".join(logs))
-    build_comparators()
-    return library_path()
+        (obj_dir / "ptxas.log").write_text("\n".join(logs))
+    if out_lib is None:
+        build_comparators()
+    return target
 
 
 if __name__ == "__main__":

@@ -70,6 +70,11 @@ class stager:
         self.chunk_elems = int(chunk_elems)
         self.buffers = int(buffers)
 
+    def set_inputs_ready(self, ready: bool = True) -> None:
+        """Uploads start when a call is made, not after the stream's earlier work (sg_stager_set_inputs_ready);
+        the caller vouches that no earlier work writes the call's host inputs."""
+        N.check(N.load().sg_stager_set_inputs_ready(self._h, int(bool(ready))), "stager::set_inputs_ready")
+
     def close(self) -> None:
         if self._h:
             N.check(N.load().sg_stager_destroy(self._h), "stager::destroy")

@@ -226,12 +226,16 @@ using clock_type = std::chrono::steady_clock;
 
 constexpr int kSlotSegments = 4096; // segments one packed launch can carry
 // Request-size policy defaults (sg_server_set_policy): a table's run of same-operation requests with at
-// least kDefaultDirectKeys keys runs as its own launches on a low-priority stream, cut into launches of at
-// most kDefaultChunkKeys keys, with at most kDefaultMaxDirect such runs in flight; smaller runs are packed
-// into one segmented launch per operation on a high-priority stream.
+// least kDefaultDirectKeys keys runs as its own launches (cut into launches of at most kDefaultChunkKeys
+// keys) on one of kDefaultDirectStreams low-priority streams, at most kDefaultMaxDirect such runs issued and
+// not yet complete; smaller runs are packed into one segmented launch per operation on a high-priority
+// stream.  With one direct stream the large runs execute back to back in the order their oldest requests
+// arrived, as a serial caller would run them but without a host round trip between them, while small
+// requests of other tables run beside them.
 constexpr int64_t kDefaultDirectKeys = int64_t{ 1 } << 16;
-constexpr int64_t kDefaultChunkKeys = int64_t{ 1 } << 19;
-constexpr int kDefaultMaxDirect = 2;
+constexpr int64_t kDefaultChunkKeys = int64_t{ 1 } << 22;
+constexpr int kDefaultMaxDirect = 4;
+constexpr int kDefaultDirectStreams = 1;
 constexpr int kMaxDirectLimit = 16;
 
 struct request_rec
@@ -294,6 +298,7 @@ struct sg_server
     int64_t direct_keys = kDefaultDirectKeys;
     int64_t chunk_keys = kDefaultChunkKeys;
     int max_direct = kDefaultMaxDirect;
+    int direct_streams = kDefaultDirectStreams;
     std::mutex m;
     std::condition_variable cv_work;
     std::condition_variable cv_done;
@@ -607,8 +612,10 @@ sg_server::launch_direct(int32_t table, const std::vector<int64_t>& tickets)
         return false;
     }
     sg_unordered* h = tables[table].h;
+    const int nlo = direct_streams < static_cast<int>(lo_streams.size()) ? direct_streams
+                                                                        : static_cast<int>(lo_streams.size());
+    next_lo = (next_lo + 1) % nlo;
     cudaStream_t s = lo_streams[next_lo];
-    next_lo = (next_lo + 1) % static_cast<int>(lo_streams.size());
     const int kb = key_bytes_of_kind(kind);
     const int mb = mapped_bytes_of_kind(kind);
     bool ok = true;
@@ -968,9 +975,11 @@ sg_server_destroy(sg_server* srv)
 }
 
 sg_status
-sg_server_set_policy(sg_server* srv, int64_t direct_keys, int64_t chunk_keys, int32_t max_direct)
+sg_server_set_policy(sg_server* srv, int64_t direct_keys, int64_t chunk_keys, int32_t max_direct,
+                     int32_t direct_streams)
 {
-    if (srv == nullptr || direct_keys < 1 || chunk_keys < 1 || max_direct < 1 || max_direct > kMaxDirectLimit)
+    if (srv == nullptr || direct_keys < 1 || chunk_keys < 1 || max_direct < 1 || max_direct > kMaxDirectLimit ||
+        direct_streams < 1 || direct_streams > static_cast<int32_t>(srv->lo_streams.size()))
     {
         return SG_ERR_BAD_ARG;
     }
@@ -978,6 +987,7 @@ sg_server_set_policy(sg_server* srv, int64_t direct_keys, int64_t chunk_keys, in
     srv->direct_keys = direct_keys;
     srv->chunk_keys = chunk_keys;
     srv->max_direct = max_direct;
+    srv->direct_streams = direct_streams;
     return SG_OK;
 }
 

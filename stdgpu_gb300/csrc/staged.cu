@@ -10,8 +10,9 @@
 // previous chunk's kernel and download finished), so at most B chunks are in flight.
 //
 // Ordering seen by the caller: every copy of a call starts after the work already queued on the
-// caller's stream, and the caller's stream waits for the call's last download, so a call behaves like
-// one stream-ordered operation.  The host buffers must stay valid until then; with pinned memory
+// caller's stream (unless the caller declared its inputs ready, sg_stager_set_inputs_ready: then the
+// uploads start at once and only the kernels keep stream order), and the caller's stream waits for the
+// call's last download, so a call behaves like one stream-ordered operation.  The host buffers must stay valid until then; with pinned memory
 // (cudaHostAlloc / cudaHostRegister) the copies are asynchronous, with pageable memory they still work
 // but do not overlap the kernels.
 #include <cuda_runtime.h>
@@ -54,6 +55,7 @@ struct sg_stager
     cudaEvent_t ready[kMaxBuffers] = {};
     cudaEvent_t used[kMaxBuffers] = {};
     cudaEvent_t freed[kMaxBuffers] = {};
+    bool inputs_ready = false; // uploads need not wait for the caller's earlier work
 };
 
 namespace
@@ -107,8 +109,11 @@ staged(sg_stager* sg, cudaStream_t s, int64_t n, host_in in0, host_in in1, host_
         return SG_ERR_BAD_ARG;
     }
     const bool any_out = out0.ptr != nullptr || out1.ptr != nullptr;
-    SG_CUDA_TRY(cudaEventRecord(sg->start, s));
-    SG_CUDA_TRY(cudaStreamWaitEvent(sg->up, sg->start, 0));
+    if (!sg->inputs_ready)
+    {
+        SG_CUDA_TRY(cudaEventRecord(sg->start, s));
+        SG_CUDA_TRY(cudaStreamWaitEvent(sg->up, sg->start, 0));
+    }
     for (int64_t off = 0; off < n; off += sg->chunk)
     {
         const int64_t m = n - off < sg->chunk ? n - off : sg->chunk;
@@ -290,6 +295,17 @@ sg_stager_destroy(sg_stager* sg)
     }
     sg::detail::dev_free(sg->mem);
     delete sg;
+    return SG_OK;
+}
+
+sg_status
+sg_stager_set_inputs_ready(sg_stager* sg, int32_t inputs_ready)
+{
+    if (sg == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    sg->inputs_ready = inputs_ready != 0;
     return SG_OK;
 }
 

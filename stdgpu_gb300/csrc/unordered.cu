@@ -545,7 +545,7 @@ k_erase_ordered(dview t, const void* keys, part_layout pl, unsigned long long* n
 // thread 0 stages chunk k + 1 while the warps probe chunk k, so every warp finds its 32 elements in shared
 // memory when it reaches them and issues its home-group loads without first waiting for the input.
 #ifndef SG_ORDERED_STAGE
-#define SG_ORDERED_STAGE 0
+#define SG_ORDERED_STAGE 1
 #endif
 #ifndef SG_STAGE_ITERS
 #define SG_STAGE_ITERS 4

@@ -185,3 +185,25 @@ def run(full: bool = True) -> dict:
         return {"map": m, "vector": vector_part(), "deque": deque_part(), "bitset": bitset_part()}
     return {"map": map_part(capacity_log2=22, batch_log2=18, rounds=2), "vector": vector_part(22),
             "deque": deque_part(20), "bitset": bitset_part(26)}
+
+
+if __name__ == "__main__":
+    # one part at a chosen size, e.g. for a profiler capture of its kernel:
+    #   python -m stdgpu_gb300.large_bench --part bitset --log2 31
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--part", choices=["map", "vector", "deque", "bitset"], required=True)
+    ap.add_argument("--log2", type=int, required=True,
+                    help="map: capacity; vector: threads; deque: operations; bitset: bits (log2)")
+    a = ap.parse_args()
+    if a.part == "map":
+        r = map_part(capacity_log2=a.log2, batch_log2=max(10, a.log2 - 6), rounds=2)
+    elif a.part == "vector":
+        r = vector_part(a.log2)
+    elif a.part == "deque":
+        r = deque_part(a.log2)
+    else:
+        r = bitset_part(a.log2)
+    print(json.dumps(r))

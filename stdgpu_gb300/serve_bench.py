@@ -10,9 +10,9 @@ mix, salted per table); values are a hash of the key.  HBM budget 120 GB.  Measu
   a C++ loop);
 * the speed-up ceiling: the serial calls once more without synchronisation, each timed on the device;
   the device time of the requests large enough to fill the GPU on their own bounds any schedule;
-* latency under load: Poisson arrivals at a rate that keeps the device >= 80 % busy (80 % of the
-  server's saturated request rate), p50 / p99 of submission-to-completion for the server and for the
-  serial path fed the same arrivals.
+* latency under load: Poisson arrivals at 80 % of the serial path's saturated request rate (the device is
+  at least that busy under the serial path), p50 / p99 of submission-to-completion for the server and
+  for the serial path fed the same arrivals.
 
 The serial path's tables are created at the capacity each table reaches in the server run, so it
 pays no rehash.
@@ -39,9 +39,9 @@ def zipf_ranks(rng, n, universe=2**30, s=0.99):
     return np.floor((1.0 + u * (universe ** a - 1.0)) ** (1.0 / a)).astype(np.uint64)
 
 
-def make_stream(n_tables=256, n_requests=600, seed=0, min_n=1 << 10, max_n=1 << 22):
+def make_stream(n_tables=256, n_requests=600, seed=0, min_n=1 << 10, max_n=1 << 22, cap_log2=(16, 24)):
     rng = np.random.default_rng(seed)
-    caps = np.exp(rng.uniform(np.log(2**16), np.log(2**24), size=n_tables)).astype(np.int64)
+    caps = np.exp(rng.uniform(np.log(2 ** cap_log2[0]), np.log(2 ** cap_log2[1]), size=n_tables)).astype(np.int64)
     salts = W.mix64(np.arange(n_tables, dtype=np.uint64) + np.uint64(12345))
     reqs = []
     for _ in range(n_requests):
@@ -66,8 +66,10 @@ def stage(reqs):
     return out
 
 
-def run_server(caps, staged, arrivals=None, budget=120 << 30):
+def run_server(caps, staged, arrivals=None, budget=120 << 30, policy: dict | None = None):
     srv = S.server(key="u64", mapped="u64", budget_bytes=budget, n_streams=8, n_slots=16)
+    if policy:
+        srv.set_policy(**policy)
     for t, c in enumerate(caps):
         if srv.admit(t, int(c)) != N.SG_OK:
             raise RuntimeError("budget too small for the initial tables")
@@ -131,12 +133,12 @@ def ceiling(staged, kernel_us, serial_s: float, direct_keys: int = 1 << 16) -> d
     }
 
 
-def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22) -> dict:
+def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22, policy: dict | None = None) -> dict:
     caps, reqs = make_stream(n_requests=n_requests, seed=seed, min_n=min_n, max_n=max_n)
     staged = stage(reqs)
     keys_total = int(sum(len(r[2]) for r in reqs))
     # saturated server (also gives the capacity each table grows to)
-    wall_srv, st_sat, statuses, final_caps, sizes_srv = run_server(caps, staged)
+    wall_srv, st_sat, statuses, final_caps, sizes_srv = run_server(caps, staged, policy=policy)
     refused = sum(1 for s in statuses if s != N.SG_OK)
     # serial plain calls on tables presized to the final capacities
     wall_ser, lat_ser_sat, _, sizes_ser = run_serial(final_caps, staged)
@@ -144,11 +146,12 @@ def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22) -> dict:
     wall_stream, _, ker_us, _ = run_serial(final_caps, staged, sync_each=False, kernel_times=True)
     bound = ceiling(staged, ker_us, wall_ser)
     bound["stream_no_sync_s"] = wall_stream
-    # Poisson arrivals at `load` x the server's saturated request rate
-    rate = load * len(staged) / wall_srv
+    # Poisson arrivals at `load` x the serial path's saturated request rate: the device is at least that busy
+    # under the serial path, and both paths see the same arrivals
+    rate = load * len(staged) / wall_ser
     rng = np.random.default_rng(seed + 1)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(staged)))
-    wall_srv_l, st_load, _, _, _ = run_server(caps, staged, arrivals)
+    wall_srv_l, st_load, _, _, _ = run_server(caps, staged, arrivals, policy=policy)
     wall_ser_l, lat_ser_load, _, _ = run_serial(final_caps, staged, arrivals)
     return {
         "request_keys": [min_n, max_n],
@@ -160,8 +163,9 @@ def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22) -> dict:
             "server_requests_per_s": len(staged) / wall_srv, "serial_requests_per_s": len(staged) / wall_ser,
             "speedup": wall_ser / wall_srv, "waves": st_sat["waves"], "launches": st_sat["launches"],
         },
+        "policy": policy or "default",
         "under_load": {
-            "arrival_rate_per_s": rate, "load_vs_server_capacity": load,
+            "arrival_rate_per_s": rate, "load_vs_serial_capacity": load,
             "server_p50_us": st_load["p50_us"], "server_p99_us": st_load["p99_us"],
             "serial_p50_us": float(np.percentile(lat_ser_load, 50)),
             "serial_p99_us": float(np.percentile(lat_ser_load, 99)),
@@ -172,3 +176,25 @@ def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22) -> dict:
         "serial_driver": "C++ loop over the C ABI (stdgpu_gb300/comparators/plain_calls.cpp)",
         "final_sizes_agree": bool(sizes_srv == sizes_ser),
     }
+
+
+if __name__ == "__main__":
+    # the server alone on a chosen stream, e.g. for a profiler capture of its segmented launches:
+    #   python -m stdgpu_gb300.serve_bench --tables 64 --requests 400 --max-log2 14 --cap-log2 16 20
+    import argparse
+    import json
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--tables", type=int, default=256)
+    ap.add_argument("--requests", type=int, default=600)
+    ap.add_argument("--min-log2", type=int, default=10)
+    ap.add_argument("--max-log2", type=int, default=22)
+    ap.add_argument("--cap-log2", type=int, nargs=2, default=[16, 24])
+    a = ap.parse_args()
+    caps, reqs = make_stream(n_tables=a.tables, n_requests=a.requests, min_n=1 << a.min_log2, max_n=1 << a.max_log2,
+                             cap_log2=tuple(a.cap_log2))
+    staged = stage(reqs)
+    wall, st, statuses, _, _ = run_server(caps, staged)
+    keys = int(sum(len(r[2]) for r in reqs))
+    print(json.dumps({"server_s": wall, "keys_per_s": keys / wall, "launches": st["launches"],
+                      "refused": sum(1 for x in statuses if x != N.SG_OK)}))

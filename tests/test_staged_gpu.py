@@ -26,14 +26,18 @@ def cpu(a: np.ndarray) -> torch.Tensor:
     return torch.from_numpy(np.ascontiguousarray(a).view(v).copy())
 
 
-@pytest.mark.parametrize("chunk,buffers", [(1000, 2), (4096, 3), (1 << 20, 4)])
-def test_map_host_calls_match_oracle(chunk, buffers):
+@pytest.mark.parametrize("chunk,buffers,ready", [(1000, 2, False), (4096, 3, False), (1 << 20, 4, False),
+                                                  (1000, 2, True), (4096, 3, True)])
+def test_map_host_calls_match_oracle(chunk, buffers, ready):
+    """With inputs declared ready the uploads of a call overlap the previous call's kernels; the results are
+    the same."""
     rng = np.random.default_rng(chunk)
     n = 50_000 + 123  # ragged last chunk
     keys = rng.integers(0, 2**63, size=n, dtype=np.uint64)
     keys[::7] = keys[::5][: len(keys[::7])]  # duplicates inside one call
     vals = rng.integers(0, 2**32, size=n, dtype=np.uint64).astype(np.uint32)
     st = sg.stager(chunk, buffers)
+    st.set_inputs_ready(ready)
     t = sg.unordered_map.createDeviceObject(1 << 17, key="u64", mapped="u32")
     port = O.PortTable(O.MAP_U64_U32, 1 << 17)
     flags = torch.zeros(n, dtype=torch.uint8).pin_memory()
