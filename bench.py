@@ -72,6 +72,8 @@ def parse_args(argv=None):
     p.add_argument("--keys-log2", type=int, default=KEYS_LOG2, help="2^k keys (default: the full workload)")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-other-configs", action="store_true",
+                   help="skip the small / batched / served configurations that follow the voxel step")
     p.add_argument("--workload", choices=["voxel", "batched", "serve", "large", "small"], default="voxel",
                    help="voxel: the headline map workload; batched: 4096 small sets, batched vs plain calls; "
                         "serve: request stream over 256 resident maps, continuous batching vs serial calls; "
@@ -537,6 +539,12 @@ def native_arm(args):
         ceiling["per_kernel_frac"] = {k: counts[k] / (med[k] * 1e-3) / ceiling["reads_per_s"] for k in counts}
         roofline["access_ceiling"] = ceiling
 
+    others = None
+    if rank == 0 and ws == 1 and not args.no_other_configs:
+        vs.close()
+        vs = None
+        others = other_configs(args)
+
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         mops, kind, used, sample, _, _ = cpu_sample_run(1, keys_log2=CPU_BASELINE_KEYS_LOG2, reps=1)
@@ -560,11 +568,98 @@ def native_arm(args):
             "e2e": e2e,
             "gpu_launches": launches,
             "clocks": clocks,
+            "other_configs": others,
         }
         print(json.dumps(line), flush=True)
-    vs.close()
+    if vs is not None:
+        vs.close()
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def batched_cpu_sample(threads: int, n_tables: int = 256) -> dict:
+    """The reference (or the oracle restatement) on the first n_tables tables of the many-small-tables
+    workload: per table createDeviceObject(capacity), insert of its keys, contains of its queries."""
+    import oracle as O
+    from stdgpu_gb300 import batch_bench
+
+    counts, caps, keys, queries, offsets = batch_bench.make_workload()
+    kind = "reference" if O.ref_available() else "port"
+    if kind == "reference":
+        O.ref_set_threads(threads)
+        make = lambda c: O.RefTable(O.SET_U64, int(c))
+    else:
+        threads = 1
+        make = lambda c: O.PortTable(O.SET_U64, int(c))
+    secs, ops, hits = 0.0, 0, 0
+    for t in range(n_tables):
+        a, b = int(offsets[t]), int(offsets[t + 1])
+        tab = make(caps[t])
+        t0 = time.perf_counter()
+        tab.insert(keys[a:b])
+        f = tab.contains(queries[a:b])
+        secs += time.perf_counter() - t0
+        hits += int(f.sum())
+        ops += 2 * (b - a)
+        tab.close()
+    return {"value": ops / secs / 1e6, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"the first {n_tables} of the 4096 tables ({ops // 2} keys): insert + contains per table, "
+                      f"wall time of the calls (table creation excluded); {hits} hits"}
+
+
+def other_configs(args) -> dict:
+    """The other benchmark configurations, each run once on this GPU after the voxel step, so that one
+    invocation records them all: the L2-resident small set (with the reference's CPU time of the same
+    configuration), the 4096 many-small-tables step (batched and graph forms against the plain per-table
+    calls from a C++ loop), and the served request stream (server against serial plain calls).  A part that
+    fails reports why instead of its numbers."""
+    import torch
+
+    from stdgpu_gb300 import batch_bench, serve_bench, small_bench
+
+    def small():
+        r = small_bench.run(steps=20, warmup=5)
+        out = {"value": r["graph_mops"], "unit": UNIT, "ms_per_step": r["graph_ms"], "detail": r,
+               "roofline": {"bound": "l2", "note": "the 13.7 MB table stays in the 129 MB L2; HBM fraction not "
+                                                   "meaningful, launch overhead and L2 latency bound the step"}}
+        cpu = []
+        for th in (1, os.cpu_count() or 1):
+            mops, kind, used, phases, secs = small_cpu_run(th)
+            cpu.append({"value": mops, "unit": UNIT, "cores": used, "kind": kind, "step_s": secs,
+                        "sample": "the full small configuration (2^20 keys, capacity 2^21): insert + contains + "
+                                  "erase wall time"})
+        out["cpu_baseline"] = cpu
+        return out
+
+    def batched():
+        r = batch_bench.run(steps=max(args.steps, 5), warmup=max(args.warmup, 3))
+        return {"value": r["graph_mops"], "unit": UNIT, "ms_per_step": r["graph_ms"],
+                "plain_calls": {"value": r["plain_mops"], "ms_per_step": r["plain_ms"],
+                                "driver": "C++ loop over the C ABI, 3 calls per table per step"},
+                "speedup_vs_plain": r["speedup_graph"], "detail": r,
+                "cpu_baseline": batched_cpu_sample(1)}
+
+    def serve():
+        r = serve_bench.run(n_requests=args.requests)
+        sat, ul = r["saturated"], r["under_load"]
+        return {"value": sat["server_keys_per_s"] / 1e6, "unit": "M keys/s",
+                "serial_plain_calls": {"value": sat["serial_keys_per_s"] / 1e6, "unit": "M keys/s",
+                                       "driver": r["serial_driver"]},
+                "speedup_vs_serial": sat["speedup"], "speedup_ceiling": r["ceiling"]["speedup_ceiling"],
+                "p50_us": ul["server_p50_us"], "p99_us": ul["server_p99_us"],
+                "serial_p50_us": ul["serial_p50_us"], "serial_p99_us": ul["serial_p99_us"], "detail": r}
+
+    out = {}
+    for name, fn in (("small", small), ("batched", batched), ("serve", serve)):
+        t0 = time.perf_counter()
+        try:
+            out[name] = fn()
+        except Exception as ex:  # one configuration's failure never costs the headline its line
+            out[name] = {"unavailable": f"{type(ex).__name__}: {str(ex)[:300]}"}
+        out[name]["wall_s"] = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+    return out
 
 
 def batched_arm(args):

@@ -310,9 +310,12 @@ SG_API sg_status sg_batch_info(const sg_table_batch* batch, int64_t* out_storage
  * operation share one segmented launch on a high-priority stream; a run of many keys (sg_server_set_policy)
  * runs as its own launches, cut into chunks, on a low-priority stream, with a cap on how many such runs
  * are in flight, so small requests of other tables are not held behind it.  Each launch completes its own
- * requests.  Requests on one table execute in submission order.  Tables are admitted, and grown (rehashed to twice the capacity)
- * before an insert run would pass 85 % of max_size(), only while the HBM budget allows; otherwise
- * the table admission or the request is refused with SG_ERR_BUDGET -- nothing spills to host memory.
+ * requests.  Requests on one table execute in submission order.  Tables are admitted, and grown (rehashed
+ * into a table of the next doubling of the capacity that holds the run, on the device with no host round
+ * trip, while the table's later requests wait) before an insert run would pass 85 % of max_size(), only
+ * while the HBM budget allows; otherwise the table admission or the request is refused with SG_ERR_BUDGET
+ * -- nothing spills to host memory.  The storage a grow replaced counts against the budget until the
+ * server is next idle (or the budget needs it).
  * Within one run of same-operation requests the per-key inserted / erased flags of a key repeated in
  * several requests may fall on any of them (as for duplicates within one bulk call). */
 typedef struct sg_server sg_server;
@@ -376,6 +379,9 @@ SG_API sg_status sg_server_wait(sg_server* server, int64_t ticket, int32_t timeo
 /* Waits for every submitted request. */
 SG_API sg_status sg_server_drain(sg_server* server, int32_t timeout_ms);
 SG_API sg_status sg_server_get_stats(sg_server* server, sg_server_stats* out);
+/* Latency of a completed request (submission to completion, microseconds); SG_ERR_BAD_ARG for an unknown
+ * ticket, SG_ERR_RETRY_EXHAUSTED while it is not complete. */
+SG_API sg_status sg_server_request_latency(sg_server* server, int64_t ticket, double* out_us);
 /* Waits for the table's requests, then size(). */
 SG_API sg_status sg_server_table_size(sg_server* server, int32_t table, int64_t* out_size);
 SG_API sg_status sg_server_table_view(sg_server* server, int32_t table, sg_unordered_view* out);

@@ -136,6 +136,7 @@ SIGNATURES = {
     "sg_server_wait": (c_int32, [c_void_p, c_int64, c_int32, POINTER(c_int32)]),
     "sg_server_drain": (c_int32, [c_void_p, c_int32]),
     "sg_server_get_stats": (c_int32, [c_void_p, POINTER(sg_server_stats)]),
+    "sg_server_request_latency": (c_int32, [c_void_p, c_int64, POINTER(ctypes.c_double)]),
     "sg_server_table_size": (c_int32, [c_void_p, c_int32, POINTER(c_int64)]),
     "sg_server_table_view": (c_int32, [c_void_p, c_int32, POINTER(sg_unordered_view)]),
     "sg_vector_create": (c_int32, [c_int32, c_int64, POINTER(c_void_p)]),

@@ -168,6 +168,88 @@ k_segments(const seg_desc* segs, const int64_t* prefix, int32_t nseg)
     }
 }
 
+// Grow of a table without a host round trip: every element of src (its regular slots, then the two
+// out-of-band slots of the tail group) is inserted into the empty, larger table dst by the bulk insert
+// step, 32 consecutive slots of src per warp step.  src is read only; nothing else runs on either table
+// meanwhile.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads)
+k_migrate(dview src, dview dst)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    using V = typename C::V;
+    constexpr int64_t sb = C::slot_bytes;
+    const tile_lanes L;
+    const int64_t regular = static_cast<int64_t>(src.num_groups) * C::slots_per_group;
+    const int64_t n = regular + 2;
+    const int64_t warp = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    step_counts c;
+    for (int64_t base = warp * 32; base < n; base += nwarps * 32)
+    {
+        const int64_t i = base + L.lane;
+        bool valid = false;
+        K key = C::empty_key;
+        V val{};
+        if (i < regular)
+        {
+            key = __ldcs(reinterpret_cast<const K*>(src.slots + i * sb));
+            valid = key < C::tomb_key; // neither never used nor erased
+        }
+        else if (i < n)
+        {
+            const int s = static_cast<int>(i - regular);
+            valid = src.hdr->special_state[s] == 1u;
+            key = s == 0 ? C::empty_key : C::tomb_key;
+        }
+        if constexpr (kind_traits<KIND>::is_map)
+        {
+            if (valid)
+            {
+                val = __ldcs(reinterpret_cast<const V*>(src.slots + i * sb + kind_traits<KIND>::val_offset));
+            }
+        }
+        insert_kv_step<KIND>(dst, L, key, val, i, valid, nullptr, c);
+    }
+    unsigned long long v[2] = { c.done, c.refused };
+    unsigned long long* const dst_counts[2] = { &dst.hdr->size, &dst.hdr->refused };
+    block_add<2>(v, dst_counts);
+}
+
+sg_status
+launch_migrate(int kind, const dview& src, const dview& dst, int grid_cap, cudaStream_t s)
+{
+    const int64_t slots = static_cast<int64_t>(src.num_groups) * (kGroupBytes / 4) + 2; // at most 32 per group
+    const int64_t want = (slots + kThreads - 1) / kThreads;
+    const int grid = static_cast<int>(want < grid_cap ? (want < 1 ? 1 : want) : grid_cap);
+    switch (kind)
+    {
+        case 0:
+            k_migrate<0><<<grid, kThreads, 0, s>>>(src, dst);
+            break;
+        case 1:
+            k_migrate<1><<<grid, kThreads, 0, s>>>(src, dst);
+            break;
+        case 2:
+            k_migrate<2><<<grid, kThreads, 0, s>>>(src, dst);
+            break;
+        case 3:
+            k_migrate<3><<<grid, kThreads, 0, s>>>(src, dst);
+            break;
+        case 4:
+            k_migrate<4><<<grid, kThreads, 0, s>>>(src, dst);
+            break;
+        case 5:
+            k_migrate<5><<<grid, kThreads, 0, s>>>(src, dst);
+            break;
+        default:
+            return SG_ERR_BAD_ARG;
+    }
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+}
+
 template <int KIND>
 sg_status
 launch_segments(int op, const seg_desc* segs, const int64_t* prefix, int32_t nseg, int64_t tiles, int grid_cap,
@@ -272,13 +354,25 @@ struct launch_slot
     std::vector<int32_t> tables;
 };
 
-// One table's run of large requests, launched chunk by chunk on one low-priority stream.
+// One table's run of large requests, launched chunk by chunk on one low-priority stream; or one table's
+// grow (retire: the storage it replaced, released once the server is idle).
 struct direct_unit
 {
     cudaEvent_t done = nullptr;
     bool in_use = false;
     std::vector<int64_t> tickets;
     int32_t table = -1;
+    sg_unordered* retire = nullptr;
+    int64_t retire_bytes = 0;
+};
+
+// What admit_insert_run decided for an insert run.
+enum admit_result
+{
+    kAdmitRun,     // launch it
+    kAdmitGrowing, // the table's grow was launched; the run waits for it
+    kAdmitWait,    // no unit free for the grow; try again next round
+    kAdmitRefused  // refused by the budget (its requests are complete)
 };
 
 } // namespace
@@ -291,6 +385,8 @@ struct sg_server
     int grid_cap = 0;
     std::vector<cudaStream_t> hi_streams; // packed launches (greatest priority)
     std::vector<cudaStream_t> lo_streams; // large runs (least priority)
+    cudaStream_t grow_stream = nullptr;   // grows (least priority)
+    std::vector<std::pair<sg_unordered*, int64_t>> graveyard; // storage replaced by grows, and its bytes
     int next_hi = 0;
     int next_lo = 0;
     std::vector<launch_slot> slots;
@@ -331,10 +427,12 @@ struct sg_server
     bool any_in_flight() const;
     bool any_event_done();
     bool dispatch();
-    bool admit_insert_run(table_rec& t, size_t take, int64_t run_keys);
+    admit_result admit_insert_run(int32_t table, table_rec& t, size_t take, int64_t run_keys);
     bool launch_direct(int32_t table, const std::vector<int64_t>& tickets);
     bool launch_packed(launch_slot& sl, int op, const std::vector<std::pair<int32_t, int64_t>>& run);
-    sg_status grow(table_rec& t, int64_t need);
+    direct_unit* free_unit();
+    sg_status grow(int32_t table, table_rec& t, int64_t need, direct_unit& u);
+    void release_graveyard();
 };
 
 namespace
@@ -438,6 +536,12 @@ sg_server::complete_finished()
         {
             it->second.busy = false;
         }
+        if (u.retire != nullptr)
+        {
+            graveyard.push_back({ u.retire, u.retire_bytes });
+            u.retire = nullptr;
+            u.retire_bytes = 0;
+        }
         u.tickets.clear();
         u.in_use = false;
         any = true;
@@ -486,10 +590,40 @@ sg_server::any_event_done()
     return false;
 }
 
-// Grows table t (rehash into a table of twice the capacity, until `need` elements fit under 85 %
-// of max_size) when the budget allows.  Caller holds the lock; the table has nothing in flight.
+// A direct unit not in use, or nullptr.
+direct_unit*
+sg_server::free_unit()
+{
+    for (auto& x : units)
+    {
+        if (!x.in_use)
+        {
+            return &x;
+        }
+    }
+    return nullptr;
+}
+
+// Releases the storage that grows replaced.  cudaFree waits for the whole device, so this runs only when
+// nothing of the server is in flight, or when the budget needs the bytes back.  Caller holds the lock.
+void
+sg_server::release_graveyard()
+{
+    for (auto& g : graveyard)
+    {
+        sg_unordered_destroy(g.first);
+        used -= g.second;
+    }
+    graveyard.clear();
+}
+
+// Grows table t to the first doubling of its capacity under which `need` elements stay below 85 % of
+// max_size(), when the budget allows.  Asynchronous: the new table is created and filled from the old one
+// by k_migrate on the grow stream, the unit's event completes the grow, and until then the table is busy,
+// so its requests keep their order.  The old storage stays counted against the budget until it is
+// released.  Caller holds the lock; the table has nothing in flight.
 sg_status
-sg_server::grow(table_rec& t, int64_t need)
+sg_server::grow(int32_t table, table_rec& t, int64_t need, direct_unit& u)
 {
     int64_t cap = t.capacity;
     int64_t ms = 0;
@@ -503,67 +637,53 @@ sg_server::grow(table_rec& t, int64_t need)
             return SG_ERR_BUDGET;
         }
     } while (need > ms * 85 / 100);
-    int64_t cur = 0;
-    sg_status st = sg_unordered_size(t.h, nullptr, &cur);
-    if (st != SG_OK)
+    if (used + bytes > budget && !graveyard.empty())
     {
-        return st;
+        release_graveyard();
     }
-    const int64_t temp = (cur + 2) * 16;
-    if (used + bytes + temp > budget)
+    if (used + bytes > budget)
     {
         return SG_ERR_BUDGET;
     }
     sg_unordered* nh = nullptr;
-    st = sg_unordered_create(kind, cap, nullptr, &nh);
+    sg_status st = sg_unordered_create(kind, cap, grow_stream, &nh);
     if (st != SG_OK)
     {
         return st;
     }
-    void* keys = nullptr;
-    void* vals = nullptr;
-    if (sg::detail::dev_malloc(&keys, static_cast<size_t>((cur + 2) * 8)) != cudaSuccess ||
-        sg::detail::dev_malloc(&vals, static_cast<size_t>((cur + 2) * 8)) != cudaSuccess)
+    st = launch_migrate(kind, kernel_view(t.h), kernel_view(nh), grid_cap, grow_stream);
+    if (st == SG_OK && cudaEventRecord(u.done, grow_stream) != cudaSuccess)
     {
-        sg::detail::dev_free(keys);
+        st = SG_ERR_CUDA;
+    }
+    if (st != SG_OK)
+    {
+        cudaStreamSynchronize(grow_stream);
         sg_unordered_destroy(nh);
         cudaGetLastError();
-        return SG_ERR_OOM;
-    }
-    int64_t n = 0;
-    const bool is_map = kind >= SG_MAP_U64_U32;
-    st = sg_unordered_range_copy(t.h, keys, is_map ? vals : nullptr, nullptr, &n);
-    if (st == SG_OK && n > 0)
-    {
-        st = sg_unordered_insert_kv(nh, keys, is_map ? vals : nullptr, n, nullptr, nullptr);
-    }
-    if (st == SG_OK)
-    {
-        st = cudaDeviceSynchronize() == cudaSuccess ? SG_OK : SG_ERR_CUDA;
-    }
-    sg::detail::dev_free(keys);
-    sg::detail::dev_free(vals);
-    if (st != SG_OK)
-    {
-        sg_unordered_destroy(nh);
         return st;
     }
-    sg_unordered_destroy(t.h);
-    used += bytes - t.bytes;
+    u.tickets.clear();
+    u.table = table;
+    u.in_use = true;
+    u.retire = t.h;
+    u.retire_bytes = t.bytes;
+    used += bytes;
     t.h = nh;
     t.capacity = cap;
     t.max_size = ms;
     t.bytes = bytes;
-    t.size_bound = n;
+    t.busy = true;
     ++rehashes;
     return SG_OK;
 }
 
-// Before an insert run of `take` requests and run_keys keys: grows the table if the run could pass 85 % of
-// max_size().  When the budget does not allow it, the run's requests complete with SG_ERR_BUDGET (nothing
-// spills) and false is returned.  Caller holds the lock.
-bool
-sg_server::admit_insert_run(table_rec& t, size_t take, int64_t run_keys)
+// Before an insert run of `take` requests and run_keys keys: if the run could pass 85 % of max_size(), the
+// table's exact size is read and, if that does not rule it out, the table grows first (the run waits for
+// the grow).  When the budget does not allow the grow, the run's requests complete with SG_ERR_BUDGET
+// (nothing spills).  Caller holds the lock.
+admit_result
+sg_server::admit_insert_run(int32_t table, table_rec& t, size_t take, int64_t run_keys)
 {
     if (t.size_bound + run_keys > t.max_size * 85 / 100)
     {
@@ -572,8 +692,17 @@ sg_server::admit_insert_run(table_rec& t, size_t take, int64_t run_keys)
         {
             t.size_bound = exact;
         }
-        if (t.size_bound + run_keys > t.max_size * 85 / 100 && grow(t, t.size_bound + run_keys) != SG_OK)
+        if (t.size_bound + run_keys > t.max_size * 85 / 100)
         {
+            direct_unit* u = free_unit();
+            if (u == nullptr)
+            {
+                return kAdmitWait;
+            }
+            if (grow(table, t, t.size_bound + run_keys, *u) == SG_OK)
+            {
+                return kAdmitGrowing;
+            }
             const auto now = clock_type::now();
             for (size_t k = 0; k < take; ++k)
             {
@@ -585,11 +714,11 @@ sg_server::admit_insert_run(table_rec& t, size_t take, int64_t run_keys)
                 t.fifo.pop_front();
             }
             cv_done.notify_all();
-            return false;
+            return kAdmitRefused;
         }
     }
     t.size_bound += run_keys;
-    return true;
+    return kAdmitRun;
 }
 
 // A table's run of large requests: each request is cut into launches of at most chunk_keys keys on one
@@ -598,15 +727,7 @@ sg_server::admit_insert_run(table_rec& t, size_t take, int64_t run_keys)
 bool
 sg_server::launch_direct(int32_t table, const std::vector<int64_t>& tickets)
 {
-    direct_unit* u = nullptr;
-    for (auto& x : units)
-    {
-        if (!x.in_use)
-        {
-            u = &x;
-            break;
-        }
-    }
+    direct_unit* u = free_unit();
     if (u == nullptr)
     {
         return false;
@@ -725,7 +846,7 @@ sg_server::dispatch()
     int direct_busy = 0;
     for (const auto& u : units)
     {
-        direct_busy += u.in_use ? 1 : 0;
+        direct_busy += u.in_use && u.retire == nullptr ? 1 : 0; // grows do not count
     }
     launch_slot* op_slot[3] = { nullptr, nullptr, nullptr };
     std::vector<std::pair<int32_t, int64_t>> packed[3];
@@ -769,9 +890,17 @@ sg_server::dispatch()
                 }
             }
         }
-        if (op == SG_SERVER_INSERT && !admit_insert_run(t, take, run_keys))
+        if (op == SG_SERVER_INSERT)
         {
-            continue;
+            const admit_result a = admit_insert_run(c.second, t, take, run_keys);
+            if (a == kAdmitGrowing)
+            {
+                launched = true;
+            }
+            if (a != kAdmitRun)
+            {
+                continue;
+            }
         }
         std::vector<int64_t> tk;
         tk.reserve(take);
@@ -824,6 +953,10 @@ sg_server::run()
         }
         const bool launched = !paused && dispatch();
         const bool in_flight = any_in_flight();
+        if (!in_flight && !graveyard.empty())
+        {
+            release_graveyard();
+        }
         if (stop && !in_flight)
         {
             break;
@@ -886,6 +1019,7 @@ sg_server_create(int32_t kind, int64_t hbm_budget_bytes, int32_t n_streams, int3
     {
         cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, least);
     }
+    cudaStreamCreateWithPriority(&srv->grow_stream, cudaStreamNonBlocking, least);
     srv->units.resize(kMaxDirectLimit);
     for (auto& u : srv->units)
     {
@@ -932,6 +1066,7 @@ sg_server_destroy(sg_server* srv)
         srv->worker.join();
     }
     cudaDeviceSynchronize();
+    srv->release_graveyard();
     for (auto& kv : srv->tables)
     {
         sg_unordered_destroy(kv.second.h);
@@ -959,6 +1094,10 @@ sg_server_destroy(sg_server* srv)
         {
             cudaEventDestroy(u.done);
         }
+    }
+    if (srv->grow_stream != nullptr)
+    {
+        cudaStreamDestroy(srv->grow_stream);
     }
     for (auto* v : { &srv->hi_streams, &srv->lo_streams })
     {
@@ -1208,6 +1347,27 @@ sg_server_get_stats(sg_server* srv, sg_server_stats* out)
     out->refused_budget = srv->refused_budget;
     out->rehashes = srv->rehashes;
     out->hbm_used_bytes = srv->used;
+    return SG_OK;
+}
+
+sg_status
+sg_server_request_latency(sg_server* srv, int64_t ticket, double* out_us)
+{
+    if (srv == nullptr || out_us == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    std::lock_guard<std::mutex> lock(srv->m);
+    if (ticket < srv->ticket_base || ticket >= srv->ticket_base + static_cast<int64_t>(srv->reqs.size()))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    const request_rec& r = srv->rec(ticket);
+    if (!r.done)
+    {
+        return SG_ERR_RETRY_EXHAUSTED;
+    }
+    *out_us = std::chrono::duration<double, std::micro>(r.t_done - r.t_submit).count();
     return SG_OK;
 }
 

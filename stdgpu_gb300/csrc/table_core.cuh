@@ -894,6 +894,54 @@ erase_key_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::
     }
 }
 
+// Erase step whose compare-and-swap result is consumed one step later: the swap of step k stays in flight
+// while step k + 1 issues its home-group loads, so a warp waits once per step instead of twice.  For calls
+// without per-key flags; the caller adds the last step's result with erase_pending_done.
+template <int KIND>
+struct erase_pending
+{
+    typename kind_consts<KIND>::K key{};
+    typename kind_consts<KIND>::K old{};
+    bool live = false;
+};
+
+template <int KIND>
+SG_D unsigned int
+erase_pending_done(const erase_pending<KIND>& p)
+{
+    return p.live && p.old == p.key ? 1u : 0u;
+}
+
+template <int KIND>
+SG_D void
+erase_key_step_deferred(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K key, bool valid,
+                        step_counts& c, erase_pending<KIND>& pend)
+{
+    using C = kind_consts<KIND>;
+    using V = typename C::V;
+    if (!valid)
+    {
+        key = C::empty_key;
+    }
+    const bool special = valid && key >= C::tomb_key;
+    if (special)
+    {
+        const unsigned int r = static_cast<unsigned int>(special_erase<KIND>(t, key));
+        c.oob += r;
+        c.done += r;
+    }
+    const bool probe = valid && !special;
+    V dummy{};
+    const int32_t my_slot = locate_step<KIND, false>(t, L, key, static_cast<uint64_t>(key), probe, dummy);
+    c.done += erase_pending_done<KIND>(pend);
+    pend.live = my_slot >= 0;
+    pend.key = key;
+    if (pend.live)
+    {
+        pend.old = cas_key<KIND>(t, static_cast<uint32_t>(my_slot), key, C::tomb_key);
+    }
+}
+
 template <int KIND>
 SG_D void
 erase_step(const dview& t, const tile_lanes& L, const void* keys, int64_t i, bool valid, uint8_t* out_flags,

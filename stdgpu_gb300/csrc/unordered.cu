@@ -123,6 +123,13 @@ constexpr int kPartMax = 256;
 #define SG_PART_PER 4
 #endif
 constexpr int kPartPer = SG_PART_PER; // elements per thread per scatter round
+// the same for elements of at most 8 bytes (bare keys of an erase, set keys): a tile of more elements gives
+// each partition's run more bytes per tile and spreads the tile's fixed steps over more elements
+#ifndef SG_PART_PER_NARROW
+#define SG_PART_PER_NARROW 4
+#endif
+template <int KIND>
+constexpr int part_per = kind_consts<KIND>::slot_bytes <= 8 ? SG_PART_PER_NARROW : kPartPer;
 
 template <int KIND, bool AOS>
 SG_D typename kind_consts<KIND>::K
@@ -208,12 +215,12 @@ struct part_layout
     unsigned int* lost;  // set when an element found no room
 };
 
-// One pass over the input: each block takes kPartPer x kThreads elements, ranks them per partition in
+// One pass over the input: each block takes PER x kThreads elements, ranks them per partition in
 // shared memory, reserves one range per partition (and one in the overflow region for what a partition
 // has no room for), sorts the elements by partition in shared memory and writes each partition's run with
 // consecutive threads, so stores reach L2 as whole lines rather than one request per element (random small
 // writes cost as many requests as random line reads).
-template <int KIND, bool AOS>
+template <int KIND, bool AOS, int PER>
 __global__ void __launch_bounds__(kThreads, 6)
 k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, part_layout pl, void* out)
 {
@@ -221,7 +228,7 @@ k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, part_layou
     using K = typename C::K;
     using V = typename C::V;
     using E = typename slot_image<KIND>::type;
-    constexpr int kTileElems = kPartPer * kThreads;
+    constexpr int kTileElems = PER * kThreads;
     __shared__ E stage[kTileElems];
     __shared__ uint8_t spid[kTileElems];
     __shared__ unsigned int cnt[kPartMax];
@@ -238,11 +245,11 @@ k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, part_layou
             cnt[p] = 0u;
         }
         __syncthreads();
-        E elem[kPartPer];
-        uint32_t pid[kPartPer];
-        uint32_t rank[kPartPer];
+        E elem[PER];
+        uint32_t pid[PER];
+        uint32_t rank[PER];
 #pragma unroll
-        for (int j = 0; j < kPartPer; ++j)
+        for (int j = 0; j < PER; ++j)
         {
             const int64_t i = tile + j * kThreads + threadIdx.x;
             pid[j] = 0u;
@@ -305,7 +312,7 @@ k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, part_layou
         }
         __syncthreads();
 #pragma unroll
-        for (int j = 0; j < kPartPer; ++j)
+        for (int j = 0; j < PER; ++j)
         {
             const int64_t i = tile + j * kThreads + threadIdx.x;
             if (i < n)
@@ -550,6 +557,10 @@ k_erase_ordered(dview t, const void* keys, part_layout pl, unsigned long long* n
 #ifndef SG_STAGE_ITERS
 #define SG_STAGE_ITERS 4
 #endif
+// ordered erase: consume each compare-and-swap one warp step later (erase_key_step_deferred)
+#ifndef SG_ERASE_DEFER
+#define SG_ERASE_DEFER 0
+#endif
 constexpr int kStageChunk = SG_STAGE_ITERS * kThreads;
 
 template <int KIND, bool ERASE>
@@ -600,6 +611,7 @@ k_ordered_staged(dview t, const void* in, part_layout pl, unsigned long long* ne
     const int warp = threadIdx.x >> 5;
     const E* src = static_cast<const E*>(in);
     step_counts c;
+    erase_pending<KIND> pend;
 
     // thread 0: chunk ch into buffer b.  Its range goes to s_first / s_last (s_first = -1 past the last chunk);
     // every call completes one phase of full[b], by the copy's bytes or, with nothing to copy, a plain arrival.
@@ -695,7 +707,11 @@ k_ordered_staged(dview t, const void* in, part_layout pl, unsigned long long* ne
             }
             if constexpr (ERASE)
             {
+#if SG_ERASE_DEFER
+                erase_key_step_deferred<KIND>(t, L, key, valid, c, pend);
+#else
                 erase_key_step<KIND>(t, L, key, i, valid, nullptr, c);
+#endif
             }
             else
             {
@@ -706,6 +722,7 @@ k_ordered_staged(dview t, const void* in, part_layout pl, unsigned long long* ne
     }
     if constexpr (ERASE)
     {
+        c.done += erase_pending_done<KIND>(pend);
         unsigned long long v[2] = { 0ull - c.done, c.done - c.oob };
         unsigned long long* const dst[2] = { &t.hdr->size, &t.hdr->tombstones };
         block_add<2>(v, dst);
@@ -1308,7 +1325,8 @@ partition_into_scratch(sg_unordered* t, const void* in0, const void* in1, int64_
     const auto round_up = [](int64_t x, int64_t m) { return (x + m - 1) / m * m; };
     const int64_t mean = (n + parts - 1) / parts;
     const int64_t cap = round_up(mean + mean / 16 + 2 * CHUNK, CHUNK);
-    const int64_t ocap = round_up(n / 16 + kPartPer * kThreads, CHUNK);
+    constexpr int PER = part_per<PKIND>;
+    const int64_t ocap = round_up(n / 16 + PER * kThreads, CHUNK);
     const int64_t ebytes = round_up((parts * cap + ocap) * kind_consts<PKIND>::slot_bytes, 256);
     constexpr int64_t kControlBytes = 2048; // fill[kPartMax], ofill, lost, then the 8-byte chunk counter
     sg_status st = ensure_part_scratch(t, ebytes + kControlBytes);
@@ -1321,8 +1339,8 @@ partition_into_scratch(sg_unordered* t, const void* in0, const void* in1, int64_
     *pl = part_layout{ parts,   shift,          static_cast<unsigned int>(cap), static_cast<unsigned int>(ocap),
                        control, control + kPartMax, control + kPartMax + 1 };
     *next_chunk = reinterpret_cast<unsigned long long*>(control + kPartMax + 2);
-    static const int g_scatter = persistent_grid(k_part_scatter<PKIND, AOS>, kThreads);
-    k_part_scatter<PKIND, AOS><<<grid_for(n, kThreads * kPartPer, g_scatter), kThreads, 0, s>>>(
+    static const int g_scatter = persistent_grid(k_part_scatter<PKIND, AOS, PER>, kThreads);
+    k_part_scatter<PKIND, AOS, PER><<<grid_for(n, kThreads * PER, g_scatter), kThreads, 0, s>>>(
             in0, in1, n, t->bits, *pl, t->part_scratch);
     SG_LAUNCH_CHECK();
     return SG_OK;

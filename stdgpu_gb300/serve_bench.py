@@ -87,6 +87,7 @@ def run_server(caps, staged, arrivals=None, budget=120 << 30, policy: dict | Non
     statuses = [srv.wait(tk) for tk in tickets]
     wall = time.perf_counter() - t0
     st = srv.stats()
+    st["latency_us"] = [srv.latency_us(tk) for tk in tickets]
     final_caps = []
     for t in range(len(caps)):
         v = srv.table_view(t)
@@ -133,6 +134,18 @@ def ceiling(staged, kernel_us, serial_s: float, direct_keys: int = 1 << 16) -> d
     }
 
 
+def tail_requests(staged, lat_server, lat_serial, k: int = 8) -> dict:
+    """The k slowest requests under load on each path: operation, keys and both latencies (microseconds)."""
+    ops = {S.INSERT: "insert", S.FIND: "find", S.ERASE: "erase"}
+    ls, lp = np.asarray(lat_server, dtype=np.float64), np.asarray(lat_serial, dtype=np.float64)
+
+    def rows(order):
+        return [{"op": ops[staged[i][1]], "keys": int(staged[i][2].numel()), "server_us": round(float(ls[i]), 1),
+                 "serial_us": round(float(lp[i]), 1)} for i in order[:k]]
+
+    return {"server": rows(np.argsort(-ls)), "serial": rows(np.argsort(-lp))}
+
+
 def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22, policy: dict | None = None) -> dict:
     caps, reqs = make_stream(n_requests=n_requests, seed=seed, min_n=min_n, max_n=max_n)
     staged = stage(reqs)
@@ -173,6 +186,7 @@ def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22, policy: 
             "server_keys_per_s": keys_total / wall_srv_l, "serial_keys_per_s": keys_total / wall_ser_l,
         },
         "ceiling": bound,
+        "tail": tail_requests(staged, st_load["latency_us"], lat_ser_load),
         "serial_driver": "C++ loop over the C ABI (stdgpu_gb300/comparators/plain_calls.cpp)",
         "final_sizes_agree": bool(sizes_srv == sizes_ser),
     }

@@ -6,7 +6,7 @@ requests and keeps each request's device buffers alive until it completes.
 
 from __future__ import annotations
 
-from ctypes import byref, c_int32, c_int64, c_void_p
+from ctypes import byref, c_double, c_int32, c_int64, c_void_p
 
 import torch
 
@@ -95,6 +95,12 @@ class server:
         s = N.sg_server_stats()
         N.check(N.load().sg_server_get_stats(self._h, byref(s)), "server::stats")
         return {f: getattr(s, f) for f, _ in N.sg_server_stats._fields_}
+
+    def latency_us(self, ticket: int) -> float:
+        """Submission-to-completion latency of a completed request (sg_server_request_latency)."""
+        x = c_double()
+        N.check(N.load().sg_server_request_latency(self._h, int(ticket), byref(x)), "server::latency")
+        return x.value
 
     def table_size(self, table: int) -> int:
         n = c_int64()

@@ -145,3 +145,59 @@ def test_growth_under_budget_keeps_contents():
     assert np.array_equal(host(ov, np.uint64), everything * np.uint64(3))
     assert srv.table_size(7) == len(everything)
     srv.close()
+
+
+def test_growth_moves_out_of_band_keys_and_skips_erased_slots():
+    """A grow rebuilds the table on the device: erased slots stay behind, the two out-of-band keys (all
+    ones and all ones minus one) move with their values, and the latency of every request is reported."""
+    srv = S.server(key="u64", mapped="u64", budget_bytes=4 << 30, n_streams=2, n_slots=4)
+    assert srv.admit(3, 1 << 10) == N.SG_OK
+    rng = np.random.default_rng(11)
+    keys = rng.integers(1, 2**62, size=700, dtype=np.uint64)
+    keys[:2] = [np.uint64(2**64 - 1), np.uint64(2**64 - 2)]
+    port = O.PortTable(O.MAP_U64_U64, 1 << 16)
+    tickets = [srv.submit(3, S.INSERT, dev(keys), dev(keys ^ np.uint64(5)), None, None)]
+    port.insert(keys, keys ^ np.uint64(5))
+    gone = keys[1:300:3]  # one out-of-band key and about a hundred others
+    tickets.append(srv.submit(3, S.ERASE, dev(gone), None, None, None))
+    port.erase(gone)
+    more = rng.integers(1, 2**62, size=3000, dtype=np.uint64)
+    tickets.append(srv.submit(3, S.INSERT, dev(more), dev(more ^ np.uint64(5)), None, None))
+    port.insert(more, more ^ np.uint64(5))
+    assert all(srv.wait(t) == N.SG_OK for t in tickets)
+    assert srv.stats()["rehashes"] >= 1
+    assert all(srv.latency_us(t) > 0 for t in tickets)
+    probe = np.concatenate([keys, more, rng.integers(1, 2**62, size=500, dtype=np.uint64)])
+    ov, of = srv.new_outputs(len(probe))
+    tk = srv.submit(3, S.FIND, dev(probe), None, ov, of)
+    assert srv.wait(tk) == N.SG_OK
+    want_vals, want_found = port.find(probe)
+    got_found = of.cpu().numpy().astype(bool)
+    assert np.array_equal(got_found, want_found.astype(bool))
+    assert np.array_equal(host(ov, np.uint64)[got_found], want_vals[got_found])
+    assert srv.table_size(3) == port.size()
+    srv.close()
+
+
+def test_back_to_back_grows_release_replaced_storage_for_the_budget():
+    """Two grows of one table in one burst: the storage the first grow replaced is still held when the second
+    needs room, and the budget only allows the second once it is released."""
+    c = 1 << 12
+    geo = [sg.geometry_for(N.MAP_U64_U64, c << k) for k in range(3)]
+    s = [g.storage_bytes for g in geo]
+    budget = s[1] + s[2] + s[0] // 2  # the three never fit at once
+    srv = S.server(key="u64", mapped="u64", budget_bytes=budget, n_streams=2, n_slots=4)
+    assert srv.admit(0, c) == N.SG_OK
+    rng = np.random.default_rng(12)
+    ms0 = geo[0].max_size
+    k1 = rng.integers(1, 2**62, size=ms0 * 9 // 10, dtype=np.uint64)  # past 85 % of the first max_size
+    k2 = rng.integers(1, 2**62, size=ms0, dtype=np.uint64)  # then past 85 % of the second's
+    tickets = srv.submit_many([(0, S.INSERT, dev(k1), dev(k1), None, None),
+                               (0, S.FIND, dev(k1), None, *srv.new_outputs(len(k1))),
+                               (0, S.INSERT, dev(k2), dev(k2), None, None)])
+    assert [srv.wait(t) for t in tickets] == [N.SG_OK] * 3
+    st = srv.stats()
+    assert st["rehashes"] == 2 and st["refused_budget"] == 0
+    assert st["hbm_used_bytes"] <= budget
+    assert srv.table_size(0) == len(np.unique(np.concatenate([k1, k2])))
+    srv.close()
