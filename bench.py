@@ -429,23 +429,24 @@ def native_arm(args):
 
         e2e_phase_ms = {"clear": [], "insert_host": [], "find_host": [], "erase_host": []}
 
+        e2e_host_ms = {}
+
         def e2e_step(ev=None):
-            # the host-buffer entry points: chunked copies in, kernels, results out, overlapped
+            # the host-buffer entry points: chunked copies in, kernels, results out, overlapped; with events,
+            # the host time of each call is kept too (a call blocks the host while its staging buffers cycle)
+            calls = (("clear", lambda: lib.sg_unordered_clear(h, sp)),
+                     ("insert_host", lambda: lib.sg_unordered_insert_host(h, stager._h, hp(pairs_h), n, None, sp)),
+                     ("find_host", lambda: lib.sg_unordered_find_host(h, stager._h, hp(queries_h), n_q, hp(vals_h),
+                                                                      hp(found_h), sp)),
+                     ("erase_host", lambda: lib.sg_unordered_erase_host(h, stager._h, hp(erase_h), n_e, None, sp)))
             if ev is not None:
                 ev[0].record(stream)
-            call(lib.sg_unordered_clear(h, sp), "clear")
-            if ev is not None:
-                ev[1].record(stream)
-            call(lib.sg_unordered_insert_host(h, stager._h, hp(pairs_h), n, None, sp), "insert_host")
-            if ev is not None:
-                ev[2].record(stream)
-            call(lib.sg_unordered_find_host(h, stager._h, hp(queries_h), n_q, hp(vals_h), hp(found_h), sp),
-                 "find_host")
-            if ev is not None:
-                ev[3].record(stream)
-            call(lib.sg_unordered_erase_host(h, stager._h, hp(erase_h), n_e, None, sp), "erase_host")
-            if ev is not None:
-                ev[4].record(stream)
+            for k, (name, fn) in enumerate(calls):
+                t0 = time.perf_counter()
+                call(fn(), name)
+                if ev is not None:
+                    e2e_host_ms[name] = (time.perf_counter() - t0) * 1e3
+                    ev[k + 1].record(stream)
 
         def e2e_serial_step():
             # the same step as separate whole-array copies around the device-pointer calls
@@ -499,7 +500,7 @@ def native_arm(args):
                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms,
                "api": f"sg_unordered_*_host (pipelined, 2^{args.e2e_chunk_log2}-element chunks, {args.e2e_buffers} "
                       f"buffers, sg_stager_set_inputs_ready)", "link": link,
-               "phases_ms": e2e_phase_ms, "inputs_ready": True,
+               "phases_ms": e2e_phase_ms, "phases_host_ms": e2e_host_ms, "inputs_ready": True,
                "ordered_uploads": {"value": ops_per_step * ws / (ordered_ms * 1e-3) / 1e6, "ms_per_step": ordered_ms},
                "serial_copies": {"value": ops_per_step * ws / (serial_ms * 1e-3) / 1e6, "ms_per_step": serial_ms}}
 
