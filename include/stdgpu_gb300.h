@@ -351,6 +351,8 @@ typedef struct sg_server_stats
     int64_t refused_budget;
     int64_t rehashes;
     int64_t hbm_used_bytes;
+    double grow_host_us;     /* scheduler time spent launching grows (allocation of the new table included) */
+    double max_grow_host_us; /* the longest of them */
 } sg_server_stats;
 
 SG_API sg_status sg_server_create(int32_t kind, int64_t hbm_budget_bytes, int32_t n_streams, int32_t n_slots,

@@ -27,7 +27,7 @@ def load() -> ctypes.CDLL:
                                              c_int32, c_void_p, POINTER(c_double), POINTER(c_double)]
         L.sgc_serial_replay.restype = c_int32
         L.sgc_serial_replay.argtypes = [c_void_p, c_void_p, c_int64, c_void_p, c_int32, c_void_p, c_void_p,
-                                        c_void_p, POINTER(c_double)]
+                                        c_void_p, POINTER(c_double), c_int32, POINTER(c_int64)]
         _lib = L
     return _lib
 
@@ -50,9 +50,11 @@ def plain_tables_steps(tables, keys, queries, offsets: np.ndarray, key_bytes: in
     return g.value, w.value
 
 
-def serial_replay(tables, requests, arrivals=None, sync_each: bool = True, stream=None, kernel_times=False):
-    """One request at a time on plain tables from a C++ loop.  requests: sequence of N.sg_request.  Returns
-    (latencies_us or None, kernel_us or None, wall_s)."""
+def serial_replay(tables, requests, arrivals=None, sync_each: bool = True, stream=None, kernel_times=False,
+                  grow_kind: int | None = None):
+    """One request at a time on plain tables from a C++ loop.  requests: sequence of N.sg_request.  With
+    grow_kind (the tables' kind) the loop grows a table before an insert as the server does.  Returns
+    (latencies_us or None, kernel_us or None, wall_s, rehashes)."""
     import torch
     n = len(requests)
     arr = (N.sg_request * n)(*requests)
@@ -63,10 +65,12 @@ def serial_replay(tables, requests, arrivals=None, sync_each: bool = True, strea
     if arrv is not None and len(arrv) < n:
         raise ValueError("one arrival time per request expected")
     wall = c_double()
+    grown = c_int64()
     st = stream if stream is not None else torch.cuda.current_stream()
     N.check(load().sgc_serial_replay(c_void_p(h.ctypes.data), ctypes.cast(arr, c_void_p), n,
                                      None if arrv is None else c_void_p(arrv.ctypes.data), int(bool(sync_each)),
                                      c_void_p(st.cuda_stream), c_void_p(lat.ctypes.data),
-                                     None if ker is None else c_void_p(ker.ctypes.data), ctypes.byref(wall)),
+                                     None if ker is None else c_void_p(ker.ctypes.data), ctypes.byref(wall),
+                                     -1 if grow_kind is None else int(grow_kind), ctypes.byref(grown)),
             "serial_replay")
-    return (lat if sync_each else None), ker, wall.value
+    return (lat if sync_each else None), ker, wall.value, grown.value

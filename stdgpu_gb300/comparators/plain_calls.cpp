@@ -7,6 +7,7 @@
 
 #include <chrono>
 #include <cstdint>
+#include <unordered_map>
 #include <vector>
 
 #include "stdgpu_gb300.h"
@@ -26,6 +27,49 @@ const char*
 at(const void* base, int64_t elem, int64_t bytes)
 {
     return static_cast<const char*>(base) + elem * bytes;
+}
+
+// The server's growth policy on a plain table, before an insert of n keys: bound is an upper bound of the
+// table's size (exact after a read, plus the keys inserted since).
+sg_status
+grow_before_insert(sg_unordered* h, int32_t kind, int64_t n, void* stream, int64_t& bound, int64_t& grown)
+{
+    sg_geometry g{};
+    sg_status st = sg_unordered_geometry(h, &g);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    if (bound + n > g.max_size * 85 / 100)
+    {
+        st = sg_unordered_size(h, stream, &bound);
+        if (st != SG_OK)
+        {
+            return st;
+        }
+        if (bound + n > g.max_size * 85 / 100)
+        {
+            int64_t cap = g.capacity;
+            sg_geometry ng{};
+            do
+            {
+                cap *= 2;
+                st = sg_unordered_geometry_for(kind, cap, &ng);
+                if (st != SG_OK)
+                {
+                    return st;
+                }
+            } while (bound + n > ng.max_size * 85 / 100);
+            st = sg_unordered_rehash(h, cap, stream);
+            if (st != SG_OK)
+            {
+                return st;
+            }
+            ++grown;
+        }
+    }
+    bound += n;
+    return SG_OK;
 }
 
 } // namespace
@@ -107,9 +151,14 @@ sgc_plain_tables_steps(sg_unordered* const* tables, int64_t n_tables, const void
 //   sync_each == 0: back to back without synchronisation (the device time of the stream's kernels).
 // kernel_us (nullable): each request's device time from CUDA events around its call.  wall_s: wall time of
 // the whole stream.
+//   grow_kind >= 0 (the tables' kind): before an insert that could take its table past 85 % of max_size(),
+//                   the table's size is read and, where needed, the table is rehashed (sg_unordered_rehash)
+//                   to the first doubling of its capacity that holds the insert -- the growth policy of the
+//                   server, as a plain caller applies it; *rehashes counts them (nullable).
 SGC_API sg_status
 sgc_serial_replay(sg_unordered* const* tables, const sg_request* reqs, int64_t n, const double* arrivals_s,
-                  int32_t sync_each, void* stream, double* latencies_us, float* kernel_us, double* wall_s)
+                  int32_t sync_each, void* stream, double* latencies_us, float* kernel_us, double* wall_s,
+                  int32_t grow_kind, int64_t* rehashes)
 {
     if (tables == nullptr || (n > 0 && reqs == nullptr) || n < 0)
     {
@@ -140,6 +189,8 @@ sgc_serial_replay(sg_unordered* const* tables, const sg_request* reqs, int64_t n
         return SG_ERR_CUDA;
     }
     sg_status st = SG_OK;
+    std::unordered_map<int32_t, int64_t> size_bound; // per table: exact after a read, plus keys inserted since
+    int64_t grown = 0;
     const auto t0 = clock_type::now();
     for (int64_t i = 0; i < n && st == SG_OK; ++i)
     {
@@ -158,6 +209,14 @@ sgc_serial_replay(sg_unordered* const* tables, const sg_request* reqs, int64_t n
             cudaEventRecord(ev[2 * i], s);
         }
         sg_unordered* h = tables[r.table];
+        if (r.op == SG_SERVER_INSERT && grow_kind >= 0)
+        {
+            st = grow_before_insert(h, grow_kind, r.n, stream, size_bound[r.table], grown);
+        }
+        if (st != SG_OK)
+        {
+            break;
+        }
         if (r.op == SG_SERVER_INSERT)
         {
             st = sg_unordered_insert_kv(h, r.keys, r.mapped, r.n, r.out_flags, stream);
@@ -199,6 +258,10 @@ sgc_serial_replay(sg_unordered* const* tables, const sg_request* reqs, int64_t n
     if (wall_s != nullptr)
     {
         *wall_s = std::chrono::duration<double>(t1 - t0).count();
+    }
+    if (rehashes != nullptr)
+    {
+        *rehashes = grown;
     }
     for (int64_t i = 0; i < static_cast<int64_t>(ev.size()) / 2; ++i)
     {

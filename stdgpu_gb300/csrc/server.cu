@@ -407,6 +407,8 @@ struct sg_server
     int64_t waves = 0;
     int64_t refused_budget = 0;
     int64_t rehashes = 0;
+    double grow_host_us = 0.0;
+    double max_grow_host_us = 0.0;
     clock_type::time_point t_first{}, t_last{};
     bool any_done = false;
     bool stop = false;
@@ -625,6 +627,18 @@ sg_server::release_graveyard()
 sg_status
 sg_server::grow(int32_t table, table_rec& t, int64_t need, direct_unit& u)
 {
+    const auto t0 = clock_type::now();
+    struct timer
+    {
+        sg_server* s;
+        clock_type::time_point t0;
+        ~timer()
+        {
+            const double us = std::chrono::duration<double, std::micro>(clock_type::now() - t0).count();
+            s->grow_host_us += us;
+            s->max_grow_host_us = us > s->max_grow_host_us ? us : s->max_grow_host_us;
+        }
+    } tm{ this, t0 };
     int64_t cap = t.capacity;
     int64_t ms = 0;
     int64_t bytes = 0;
@@ -1347,6 +1361,8 @@ sg_server_get_stats(sg_server* srv, sg_server_stats* out)
     out->refused_budget = srv->refused_budget;
     out->rehashes = srv->rehashes;
     out->hbm_used_bytes = srv->used;
+    out->grow_host_us = srv->grow_host_us;
+    out->max_grow_host_us = srv->max_grow_host_us;
     return SG_OK;
 }
 

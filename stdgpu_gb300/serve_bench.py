@@ -7,15 +7,14 @@ mix, salted per table); values are a hash of the key.  HBM budget 120 GB.  Measu
 
 * saturated throughput: all requests submitted back to back, server vs serial plain calls (one
   request at a time, each a C-ABI call on the table's own object followed by a stream sync, driven from
-  a C++ loop);
-* the speed-up ceiling: the serial calls once more without synchronisation, each timed on the device;
-  the device time of the requests large enough to fill the GPU on their own bounds any schedule;
+  a C++ loop).  Two serial paths: `serial` starts from the admitted capacities and rehashes a table
+  before an insert that needs room, by the server's growth policy; `serial_presized` runs on tables
+  created at the capacities the server's tables ended with, so it never rehashes (its best case);
+* the speed-up ceiling: the presized serial calls once more without synchronisation, each timed on the
+  device; the device time of the requests large enough to fill the GPU on their own bounds any schedule;
 * latency under load: Poisson arrivals at 80 % of the serial path's saturated request rate (the device is
   at least that busy under the serial path), p50 / p99 of submission-to-completion for the server and
-  for the serial path fed the same arrivals.
-
-The serial path's tables are created at the capacity each table reaches in the server run, so it
-pays no rehash.
+  for both serial paths fed the same arrivals.
 """
 
 from __future__ import annotations
@@ -97,20 +96,24 @@ def run_server(caps, staged, arrivals=None, budget=120 << 30, policy: dict | Non
     return wall, st, statuses, final_caps, sizes
 
 
-def run_serial(caps, staged, arrivals=None, sync_each: bool = True, kernel_times: bool = False):
+def run_serial(caps, staged, arrivals=None, sync_each: bool = True, kernel_times: bool = False, grow: bool = False):
     """The plain path from a C++ loop over the C ABI (comparators.serial_replay): each request is one call on
     its table's own object; with sync_each the stream is synchronised after every request (the serial
-    plain path), without it the calls run back to back (the device time of the same kernels)."""
+    plain path), without it the calls run back to back (the device time of the same kernels).  With grow
+    the loop rehashes a table before an insert that needs room, by the server's policy (the tables then
+    start at the admitted capacities); without it the tables must already be large enough."""
     tables = [C.unordered_map.createDeviceObject(int(c), key="u64", mapped="u64") for c in caps]
     reqs = [N.sg_request(t, op, k.numel(), k.data_ptr(), v.data_ptr() if v is not None else None,
                          ov.data_ptr() if ov is not None else None, of.data_ptr())
             for t, op, k, v, ov, of in staged]
     torch.cuda.synchronize()
-    lat, ker, wall = P.serial_replay(tables, reqs, arrivals, sync_each=sync_each, kernel_times=kernel_times)
+    lat, ker, wall, rehashes = P.serial_replay(tables, reqs, arrivals, sync_each=sync_each,
+                                               kernel_times=kernel_times,
+                                               grow_kind=N.MAP_U64_U64 if grow else None)
     sizes = [tb.size() for tb in tables]
     for tb in tables:
         C.unordered_base.destroyDeviceObject(tb)
-    return wall, lat, ker, sizes
+    return wall, lat, ker, sizes, rehashes
 
 
 def ceiling(staged, kernel_us, serial_s: float, direct_keys: int = 1 << 16) -> dict:
@@ -147,48 +150,59 @@ def tail_requests(staged, lat_server, lat_serial, k: int = 8) -> dict:
 
 
 def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22, policy: dict | None = None) -> dict:
+    """The server against two serial plain paths on the same request stream: `serial` starts from the
+    admitted capacities and grows its tables by the server's policy (what a plain caller must do), and
+    `serial_presized` runs on tables created at the capacities the server's tables ended with (no rehash
+    at all: the best case of the plain path, which needs the stream's future)."""
     caps, reqs = make_stream(n_requests=n_requests, seed=seed, min_n=min_n, max_n=max_n)
     staged = stage(reqs)
     keys_total = int(sum(len(r[2]) for r in reqs))
     # saturated server (also gives the capacity each table grows to)
     wall_srv, st_sat, statuses, final_caps, sizes_srv = run_server(caps, staged, policy=policy)
     refused = sum(1 for s in statuses if s != N.SG_OK)
-    # serial plain calls on tables presized to the final capacities
-    wall_ser, lat_ser_sat, _, sizes_ser = run_serial(final_caps, staged)
-    # the same calls back to back (no host synchronisation), each timed on the device: the speed-up ceiling
-    wall_stream, _, ker_us, _ = run_serial(final_caps, staged, sync_each=False, kernel_times=True)
-    bound = ceiling(staged, ker_us, wall_ser)
+    wall_ser, _, _, sizes_ser, ser_rehashes = run_serial(caps, staged, grow=True)
+    wall_pre, _, _, sizes_pre, _ = run_serial(final_caps, staged)
+    # the presized calls back to back (no host synchronisation), each timed on the device: the ceiling
+    wall_stream, _, ker_us, _, _ = run_serial(final_caps, staged, sync_each=False, kernel_times=True)
+    bound = ceiling(staged, ker_us, wall_pre)
     bound["stream_no_sync_s"] = wall_stream
     # Poisson arrivals at `load` x the serial path's saturated request rate: the device is at least that busy
-    # under the serial path, and both paths see the same arrivals
+    # under the serial path, and every path sees the same arrivals
     rate = load * len(staged) / wall_ser
     rng = np.random.default_rng(seed + 1)
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(staged)))
     wall_srv_l, st_load, _, _, _ = run_server(caps, staged, arrivals, policy=policy)
-    wall_ser_l, lat_ser_load, _, _ = run_serial(final_caps, staged, arrivals)
+    wall_ser_l, lat_ser_load, _, _, _ = run_serial(caps, staged, arrivals, grow=True)
+    wall_pre_l, lat_pre_load, _, _, _ = run_serial(final_caps, staged, arrivals)
+    pct = lambda a, q: float(np.percentile(a, q))
     return {
         "request_keys": [min_n, max_n],
         "tables": len(caps), "requests": len(staged), "keys": keys_total,
-        "refused_requests": refused, "rehashes": st_sat["rehashes"], "hbm_used_bytes": st_sat["hbm_used_bytes"],
+        "refused_requests": refused, "rehashes": st_sat["rehashes"], "serial_rehashes": ser_rehashes,
+        "hbm_used_bytes": st_sat["hbm_used_bytes"],
         "saturated": {
-            "server_s": wall_srv, "serial_s": wall_ser,
+            "server_s": wall_srv, "serial_s": wall_ser, "serial_presized_s": wall_pre,
             "server_keys_per_s": keys_total / wall_srv, "serial_keys_per_s": keys_total / wall_ser,
+            "serial_presized_keys_per_s": keys_total / wall_pre,
             "server_requests_per_s": len(staged) / wall_srv, "serial_requests_per_s": len(staged) / wall_ser,
-            "speedup": wall_ser / wall_srv, "waves": st_sat["waves"], "launches": st_sat["launches"],
+            "speedup": wall_ser / wall_srv, "speedup_vs_presized": wall_pre / wall_srv,
+            "waves": st_sat["waves"], "launches": st_sat["launches"],
+            "grow_host_us": st_sat.get("grow_host_us"), "max_grow_host_us": st_sat.get("max_grow_host_us"),
         },
         "policy": policy or "default",
         "under_load": {
             "arrival_rate_per_s": rate, "load_vs_serial_capacity": load,
             "server_p50_us": st_load["p50_us"], "server_p99_us": st_load["p99_us"],
-            "serial_p50_us": float(np.percentile(lat_ser_load, 50)),
-            "serial_p99_us": float(np.percentile(lat_ser_load, 99)),
-            "server_wall_s": wall_srv_l, "serial_wall_s": wall_ser_l,
+            "serial_p50_us": pct(lat_ser_load, 50), "serial_p99_us": pct(lat_ser_load, 99),
+            "serial_presized_p50_us": pct(lat_pre_load, 50), "serial_presized_p99_us": pct(lat_pre_load, 99),
+            "server_wall_s": wall_srv_l, "serial_wall_s": wall_ser_l, "serial_presized_wall_s": wall_pre_l,
             "server_keys_per_s": keys_total / wall_srv_l, "serial_keys_per_s": keys_total / wall_ser_l,
         },
         "ceiling": bound,
         "tail": tail_requests(staged, st_load["latency_us"], lat_ser_load),
+        "tail_vs_presized": tail_requests(staged, st_load["latency_us"], lat_pre_load),
         "serial_driver": "C++ loop over the C ABI (stdgpu_gb300/comparators/plain_calls.cpp)",
-        "final_sizes_agree": bool(sizes_srv == sizes_ser),
+        "final_sizes_agree": bool(sizes_srv == sizes_ser == sizes_pre),
     }
 
 
