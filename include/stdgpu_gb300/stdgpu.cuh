@@ -19,6 +19,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <exception>
+#include <functional>
 #include <type_traits>
 
 #include "../stdgpu_gb300.h"
@@ -521,31 +522,56 @@ struct fits_word_table
                                          mapped_fits_word<T>::value>
 {
 };
+
+// Whether keys may compare by their bytes: the default comparison (equal_to<Key>, equal_to<void>,
+// std::equal_to<Key>) of a key type whose equal values have equal object bytes (integers, enums, pointers
+// and padding-free aggregates of them; not floating point, not types with padding).  Such keys use the
+// library's kernels; every other key compares through KeyEqual in the header tables of wide_key.cuh.  A
+// class key compared by default must have an operator== that compares all of its members.
+template <typename Key, typename KeyEqual>
+struct bytes_compare
+  : std::integral_constant<bool, (std::is_same<KeyEqual, equal_to<Key>>::value ||
+                                  std::is_same<KeyEqual, equal_to<void>>::value ||
+                                  std::is_same<KeyEqual, std::equal_to<Key>>::value) &&
+                                         std::has_unique_object_representations<Key>::value>
+{
+};
+
+// The wide tables' comparison for KeyEqual: void (bytes) where bytes_compare holds.
+template <typename Key, typename KeyEqual>
+using wide_key_equal = std::conditional_t<bytes_compare<Key, KeyEqual>::value, void, KeyEqual>;
+
+// Storage of unordered_map<Key, T, Hash, KeyEqual> / unordered_set (T = void): the library's kinds, the
+// word-keyed custom path, or the wide header tables.
+template <typename Key, typename T, typename Hash, typename KeyEqual, typename Derived>
+using map_storage = std::conditional_t<
+        is_native_table<Key, T, Hash>::value && bytes_compare<Key, KeyEqual>::value, native_map<Key, T, Derived>,
+        std::conditional_t<fits_word_table<Key, T>::value && bytes_compare<Key, KeyEqual>::value,
+                           custom_map<Key, T, Hash, Derived>,
+                           wide_map<Key, T, Hash, Derived, wide_key_equal<Key, KeyEqual>>>>;
+template <typename Key, typename Hash, typename KeyEqual, typename Derived>
+using set_storage = std::conditional_t<
+        is_native_table<Key, void, Hash>::value && bytes_compare<Key, KeyEqual>::value, native_set<Key, Derived>,
+        std::conditional_t<fits_word_table<Key, void>::value && bytes_compare<Key, KeyEqual>::value,
+                           custom_set<Key, Hash, Derived>, wide_set<Key, Hash, Derived, wide_key_equal<Key, KeyEqual>>>>;
 } // namespace detail
 } // namespace stdgpu
 
 namespace stdgpu
 {
 
-// stdgpu::unordered_map<Key, T, Hash>: integer keys with the default hash and integer mapped values use the
-// library's precompiled kernels; other keys of at most 8 bytes (short3, vec3int16, packed coordinates) with a
-// user Hash and a 4/8-byte mapped type go through the word-keyed path of custom_key.cuh; every other element
-// type (a 3 x int32 key, an empty or 16-byte mapped type, a type with a destructor) through wide_key.cuh.
+// stdgpu::unordered_map<Key, T, Hash, KeyEqual>: integer keys with the default hash and integer mapped values
+// use the library's precompiled kernels; other keys of at most 8 bytes (short3, vec3int16, packed coordinates)
+// with a user Hash and a 4/8-byte mapped type go through the word-keyed path of custom_key.cuh; every other
+// element type (a 3 x int32 key, an empty or 16-byte mapped type, a type with a destructor) through
+// wide_key.cuh.  Keys compared by a user KeyEqual, or whose bytes do not decide their equality (floating
+// point, padding), also take wide_key.cuh, which calls KeyEqual on every probe (detail::bytes_compare).
 template <typename Key, typename T, typename Hash = hash<Key>, typename KeyEqual = equal_to<Key>,
           typename Allocator = safe_device_allocator<pair<const Key, T>>>
 class unordered_map
-  : public std::conditional_t<
-            detail::is_native_table<Key, T, Hash>::value,
-            detail::native_map<Key, T, unordered_map<Key, T, Hash, KeyEqual, Allocator>>,
-            std::conditional_t<detail::fits_word_table<Key, T>::value,
-                               detail::custom_map<Key, T, Hash, unordered_map<Key, T, Hash, KeyEqual, Allocator>>,
-                               detail::wide_map<Key, T, Hash, unordered_map<Key, T, Hash, KeyEqual, Allocator>>>>
+  : public detail::map_storage<Key, T, Hash, KeyEqual, unordered_map<Key, T, Hash, KeyEqual, Allocator>>
 {
-    using base = std::conditional_t<
-            detail::is_native_table<Key, T, Hash>::value,
-            detail::native_map<Key, T, unordered_map>,
-            std::conditional_t<detail::fits_word_table<Key, T>::value, detail::custom_map<Key, T, Hash, unordered_map>,
-                               detail::wide_map<Key, T, Hash, unordered_map>>>;
+    using base = detail::map_storage<Key, T, Hash, KeyEqual, unordered_map>;
 
 public:
     using key_equal = KeyEqual;
@@ -595,19 +621,9 @@ private:
 // stdgpu::unordered_set<Key, Hash>
 template <typename Key, typename Hash = hash<Key>, typename KeyEqual = equal_to<Key>,
           typename Allocator = safe_device_allocator<Key>>
-class unordered_set
-  : public std::conditional_t<
-            detail::is_native_table<Key, void, Hash>::value,
-            detail::native_set<Key, unordered_set<Key, Hash, KeyEqual, Allocator>>,
-            std::conditional_t<detail::fits_word_table<Key, void>::value,
-                               detail::custom_set<Key, Hash, unordered_set<Key, Hash, KeyEqual, Allocator>>,
-                               detail::wide_set<Key, Hash, unordered_set<Key, Hash, KeyEqual, Allocator>>>>
+class unordered_set : public detail::set_storage<Key, Hash, KeyEqual, unordered_set<Key, Hash, KeyEqual, Allocator>>
 {
-    using base = std::conditional_t<detail::is_native_table<Key, void, Hash>::value,
-                                    detail::native_set<Key, unordered_set>,
-                                    std::conditional_t<detail::fits_word_table<Key, void>::value,
-                                                       detail::custom_set<Key, Hash, unordered_set>,
-                                                       detail::wide_set<Key, Hash, unordered_set>>>;
+    using base = detail::set_storage<Key, Hash, KeyEqual, unordered_set>;
 
 public:
     using key_equal = KeyEqual;

@@ -18,8 +18,13 @@
 // inserted, so a lookup stops at the first group with a never-used slot; a bulk insert may take an erased
 // slot of that group, a device insert only never-used slots (it may run beside device erases).
 //
-// Keys compare equal when their bytes do (as for the word-sized custom keys); the mapped value of a key
-// claimed in the same launch as a lookup of it may not be written yet when the lookup reads it.
+// Keys compare with KeyEqual, as the reference compares them on every probe
+// (src/stdgpu/impl/unordered_base_detail.cuh:661, :673): a probe accepts a stored key when KeyEqual holds for
+// it and the probed key, a lost claim whose winner holds an equal key means present, and an erase swaps out
+// the stored word it found.  KeyEqual = void compares the key bytes (the default comparison of keys whose
+// equal values have equal bytes).  Keys whose bytes fill their word with all ones or all ones minus one
+// (the two reserved patterns, held out of band) compare by their bytes.  The mapped value of a key claimed
+// in the same launch as a lookup of it may not be written yet when the lookup reads it.
 #ifndef STDGPU_GB300_WIDE_KEY_CUH
 #define STDGPU_GB300_WIDE_KEY_CUH
 
@@ -219,11 +224,12 @@ word_in(unsigned long long a, unsigned long long b, int j)
 }
 
 // Kernel view of a wide table (trivially copyable, passed by value).
-template <typename Key, typename T, typename Hash>
+template <typename Key, typename T, typename Hash, typename KeyEqual = void>
 struct wide_ref
 {
     using key_type = Key;
     using hasher = Hash;
+    using key_equal = KeyEqual;
     using W = wide_word_of<Key>;
     using WW = wide_word<W>;
     static constexpr int G = 128 / static_cast<int>(sizeof(W)); // slots per probe group
@@ -256,6 +262,20 @@ struct wide_ref
     home(std::uint64_t hash) const
     {
         return sg::detail::group_of_bucket(sg::detail::fibonacci_bucket(hash, bucket_bits), bucket_bits, num_groups);
+    }
+
+    // Whether stored key word x holds a key equal to the key of word w.
+    __host__ __device__ static bool
+    same(const W& x, const W& w)
+    {
+        if constexpr (std::is_void<KeyEqual>::value)
+        {
+            return x == w;
+        }
+        else
+        {
+            return KeyEqual{}(from_wide<Key>(x), from_wide<Key>(w));
+        }
     }
 
     __host__ __device__ static int
@@ -384,10 +404,26 @@ struct wide_ref
         {
             return special_state(sp) == 1u ? special_base() + sp : -1;
         }
-        return find_if(hash, [&](const W& x) { return x == w; });
+        return find_if(hash, [&](const W& x) { return same(x, w); });
     }
 
-    // Heterogeneous lookup: a value equal (operator==) to the stored Key, hashed like it.
+    // Whether stored Key k equals heterogeneous key kl: KeyEqual where it takes the pair (a transparent
+    // KeyEqual), else operator==.
+    template <typename KeyLike>
+    __host__ __device__ static bool
+    same_like(const Key& k, const KeyLike& kl)
+    {
+        if constexpr (!std::is_void<KeyEqual>::value && std::is_invocable<KeyEqual, const Key&, const KeyLike&>::value)
+        {
+            return KeyEqual{}(k, kl);
+        }
+        else
+        {
+            return k == kl;
+        }
+    }
+
+    // Heterogeneous lookup: a value equal to the stored Key, hashed like it.
     template <typename KeyLike>
     __device__ std::int64_t
     find_like(const KeyLike& k, std::uint64_t hash) const
@@ -396,13 +432,13 @@ struct wide_ref
         {
             for (int s = 0; s < 2; ++s)
             {
-                if (special_state(s) == 1u && from_wide<Key>(s == 0 ? WW::empty() : WW::tomb()) == k)
+                if (special_state(s) == 1u && same_like(from_wide<Key>(s == 0 ? WW::empty() : WW::tomb()), k))
                 {
                     return special_base() + s;
                 }
             }
         }
-        return find_if(hash, [&](const W& x) { return from_wide<Key>(x) == k; });
+        return find_if(hash, [&](const W& x) { return same_like(from_wide<Key>(x), k); });
     }
 
     __device__ void
@@ -459,7 +495,7 @@ struct wide_ref
         {
             for (int tries = 0;; ++tries)
             {
-                const group_masks m = scan(g, [&](const W& x) { return x == w; });
+                const group_masks m = scan(g, [&](const W& x) { return same(x, w); });
                 if (m.match != 0u)
                 {
                     return { g * G + (__ffs(m.match) - 1), false };
@@ -482,7 +518,7 @@ struct wide_ref
                     construct(slot, mapped);
                     return { slot, true };
                 }
-                if (old == w)
+                if (old != WW::empty() && old != WW::tomb() && same(old, w))
                 {
                     return { slot, false };
                 }
@@ -509,8 +545,15 @@ struct wide_ref
             atomicExch(&hdr->special_state[sp], 0u);
             return true;
         }
-        const std::int64_t slot = find_if(hash, [&](const W& x) { return x == w; });
-        if (slot < 0 || WW::cas(keys + slot, w, WW::tomb()) != w)
+        const std::int64_t slot = find_if(hash, [&](const W& x) { return same(x, w); });
+        if (slot < 0)
+        {
+            return false;
+        }
+        // the word found there: the key's own bytes, or an equal key's
+        const W stored = std::is_void<KeyEqual>::value ? w : WW::load(keys + slot);
+        if (stored == WW::empty() || stored == WW::tomb() || !same(stored, w) ||
+            WW::cas(keys + slot, stored, WW::tomb()) != stored)
         {
             return false;
         }
@@ -821,13 +864,13 @@ wide_alloc(P** p, std::size_t bytes)
     return cudaMalloc(reinterpret_cast<void**>(p), bytes > 0 ? bytes : 1) == cudaSuccess;
 }
 
-template <typename Key, typename T, typename Hash, typename Value, typename Derived>
+template <typename Key, typename T, typename Hash, typename Value, typename Derived, typename KeyEqual = void>
 class wide_unordered
 {
     static_assert(sizeof(Key) <= 16, "a key type of at most 16 bytes");
 
 public:
-    using ref_type = wide_ref<Key, T, Hash>;
+    using ref_type = wide_ref<Key, T, Hash, KeyEqual>;
     using W = typename ref_type::W;
     using value_store = typename ref_type::value_store;
     using key_type = Key;
@@ -1159,10 +1202,10 @@ protected:
     std::int32_t* _range = nullptr;
 };
 
-template <typename Key, typename T, typename Hash, typename Derived>
-class wide_map : public wide_unordered<Key, T, Hash, pair<const Key, T>, Derived>
+template <typename Key, typename T, typename Hash, typename Derived, typename KeyEqual = void>
+class wide_map : public wide_unordered<Key, T, Hash, pair<const Key, T>, Derived, KeyEqual>
 {
-    using base = wide_unordered<Key, T, Hash, pair<const Key, T>, Derived>;
+    using base = wide_unordered<Key, T, Hash, pair<const Key, T>, Derived, KeyEqual>;
 
 public:
     using mapped_type = T;
@@ -1186,10 +1229,10 @@ public:
 #endif
 };
 
-template <typename Key, typename Hash, typename Derived>
-class wide_set : public wide_unordered<Key, void, Hash, Key, Derived>
+template <typename Key, typename Hash, typename Derived, typename KeyEqual = void>
+class wide_set : public wide_unordered<Key, void, Hash, Key, Derived, KeyEqual>
 {
-    using base = wide_unordered<Key, void, Hash, Key, Derived>;
+    using base = wide_unordered<Key, void, Hash, Key, Derived, KeyEqual>;
 
 public:
     using typename base::iterator;

@@ -1,7 +1,8 @@
 // Compile-time check of which storage each element type takes in the C++ API (include/stdgpu_gb300/stdgpu.cuh):
 // integer keys with the default hash and integer mapped values -> the library's precompiled kinds; other
 // trivially copyable keys of at most 8 bytes with a 4/8-byte trivially copyable mapped type -> the word-keyed
-// custom path; everything else -> the wide tables.  Builds to a program that does nothing.
+// custom path; everything else -> the wide tables, and so do keys compared by a user KeyEqual or whose bytes do
+// not decide equality (floating point, padding).  Builds to a program that does nothing.
 #include <cstdint>
 #include <type_traits>
 
@@ -79,7 +80,36 @@ static_assert(routes_to<w3, wide_map<std::uint64_t, key16, hash<std::uint64_t>, 
 static_assert(routes_to<w4, wide_map<std::uint32_t, with_destructor, hash<std::uint32_t>, w4>>,
               "mapped type with a destructor");
 static_assert(routes_to<w5, wide_map<vec3i32_key, empty_tag, any_hash, w5>>, "empty mapped type");
-static_assert(routes_to<w6, wide_set<with_destructor, any_hash, w6>>, "key with a destructor");
+// a key that is not trivially copyable compares through its KeyEqual
+static_assert(routes_to<w6, wide_set<with_destructor, any_hash, w6, equal_to<with_destructor>>>,
+              "key with a destructor");
+
+// keys whose bytes do not decide equality, or a user KeyEqual: the wide tables, comparing with KeyEqual
+struct x_only_equal
+{
+    template <typename K>
+    __host__ __device__ bool
+    operator()(const K& a, const K& b) const
+    {
+        return a.x == b.x;
+    }
+};
+struct padded_key
+{
+    std::uint32_t x;
+    std::uint16_t y; // two bytes of padding follow
+};
+using e1 = unordered_set<short3_key, any_hash, x_only_equal>;
+using e2 = unordered_map<float, std::uint32_t, any_hash>;
+using e3 = unordered_map<padded_key, std::uint64_t, any_hash>;
+using e4 = unordered_set<std::uint64_t, hash<std::uint64_t>, std::equal_to<std::uint64_t>>;
+using e5 = unordered_set<std::uint64_t, hash<std::uint64_t>, equal_to<>>;
+static_assert(routes_to<e1, wide_set<short3_key, any_hash, e1, x_only_equal>>, "user KeyEqual");
+static_assert(routes_to<e2, wide_map<float, std::uint32_t, any_hash, e2, equal_to<float>>>, "floating-point key");
+static_assert(routes_to<e3, wide_map<padded_key, std::uint64_t, any_hash, e3, equal_to<padded_key>>>,
+              "key with padding");
+static_assert(routes_to<e4, native_set<std::uint64_t, e4>>, "std::equal_to on an integer key compares bytes");
+static_assert(routes_to<e5, native_set<std::uint64_t, e5>>, "equal_to<void> on an integer key compares bytes");
 
 // the allocator parameter and get_allocator()
 using a1 = unordered_map<std::uint64_t, std::uint32_t, hash<std::uint64_t>, equal_to<std::uint64_t>,

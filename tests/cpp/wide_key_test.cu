@@ -147,8 +147,9 @@ using wide_payload_map = stdgpu::unordered_map<key128, payload, key128_hash>;
 using u64_payload_map = stdgpu::unordered_map<std::uint64_t, payload>;
 using counted_map = stdgpu::unordered_map<std::uint32_t, counted>;
 
-static_assert(std::is_base_of<stdgpu::detail::wide_set<vec3int32, vec_hash, nontrivial_set>, nontrivial_set>::value,
-              "a 12-byte key takes the wide path");
+static_assert(std::is_base_of<stdgpu::detail::wide_set<vec3int32, vec_hash, nontrivial_set, stdgpu::equal_to<vec3int32>>,
+                              nontrivial_set>::value,
+              "a 12-byte key that is not trivially copyable takes the wide path and compares with its operator==");
 static_assert(std::is_base_of<stdgpu::detail::wide_map<std::uint64_t, payload, stdgpu::hash<std::uint64_t>,
                                                        u64_payload_map>,
                               u64_payload_map>::value,

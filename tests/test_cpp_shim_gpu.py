@@ -16,6 +16,7 @@ WIDE = ROOT / "tests" / "cpp" / "wide_key_test.cu"
 WIDE_GOLDEN = ROOT / "tests" / "cpp" / "wide_golden_test.cu"
 ROUTING = ROOT / "tests" / "cpp" / "routing_check.cu"
 CHURN = ROOT / "tests" / "cpp" / "device_churn_test.cu"
+KEY_EQUAL = ROOT / "tests" / "cpp" / "key_equal_test.cu"
 GOLDEN = ROOT / "tests" / "golden"
 OUT = ROOT / "tests" / "cpp" / "_build"
 
@@ -167,3 +168,20 @@ def test_device_insert_erase_churn_reuses_erased_slots(tmp_path):
     assert len(sizes) == 1
     for t in tables:
         t.close()
+
+
+def test_key_equal_program_compiles_for_sm103a():
+    stdgpu_gb300.load()
+    _compile(src=KEY_EQUAL)
+
+
+@pytest.mark.gpu
+def test_keys_compare_with_key_equal_on_gpu():
+    """Keys equal under KeyEqual are one key (a tagged key compared by one field; float keys, +0.0 == -0.0):
+    bulk and device calls against std::unordered_set / std::unordered_map with the same Hash and KeyEqual."""
+    stdgpu_gb300.load()
+    exe = _compile(src=KEY_EQUAL)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "ALL PASS" in r.stdout
