@@ -107,6 +107,21 @@ SG_API sg_status sg_set_device_allocator(sg_device_alloc_fn alloc, sg_device_fre
 /* Number of device allocations the library holds (all containers, staging and scratch buffers). */
 SG_API int64_t sg_live_device_allocations(void);
 
+/* An allocator of one table's device storage: the reference's Allocator argument of
+ * createDeviceObject(capacity, allocator) (src/stdgpu/impl/unordered_base_detail.cuh:1254-1308 allocates
+ * the table's arrays through it with allocator_traits).  Every device allocation the table makes in its
+ * life -- slots, header, counters, bulk-call scratch, the storage a rehash rebuilds -- goes through
+ * alloc / release with ctx (a release is preceded by a device synchronisation, as cudaFree is), and
+ * release_ctx (nullable) is called with ctx once the table is destroyed.  The memory must be device memory
+ * of the current device.  These allocations are not counted by sg_live_device_allocations. */
+typedef struct sg_allocator
+{
+    sg_device_alloc_fn alloc;
+    sg_device_free_fn release;
+    void* ctx;
+    void (*release_ctx)(void* ctx);
+} sg_allocator;
+
 /* ---------------- unordered_set / unordered_map ---------------- */
 
 /* createDeviceObject(capacity): src/stdgpu/impl/unordered_base_detail.cuh:1254-1308,
@@ -116,6 +131,10 @@ SG_API sg_status sg_unordered_create(int32_t kind, int64_t capacity, void* strea
 
 /* destroyDeviceObject: src/stdgpu/impl/unordered_base_detail.cuh:1310-1348 */
 SG_API sg_status sg_unordered_destroy(sg_unordered* table);
+/* createDeviceObject(capacity, allocator): sg_unordered_create (custom_hash = 0) or sg_unordered_create_hashed
+ * (custom_hash = 1) with the table's storage taken from `allocator` (copied; alloc and release non-null). */
+SG_API sg_status sg_unordered_create_with_allocator(int32_t kind, int64_t capacity, int32_t custom_hash,
+                                                    const sg_allocator* allocator, void* stream, sg_unordered** out);
 
 /* insert(begin, end) with begin pointing at value_type elements:
  * src/stdgpu/impl/unordered_base_detail.cuh:996-1017 (per element :967-994).

@@ -312,6 +312,24 @@ public:
         return d;
     }
 
+    // createDeviceObject(capacity, allocator): every device block of the object from `alloc`
+    static Derived
+    create_with_allocator(execution::device_policy policy, const index_t& capacity, const sg_allocator& alloc)
+    {
+        Derived d;
+        const sg_status st = sg_unordered_create_with_allocator(kind, capacity, 1, &alloc, policy.stream, &d._handle);
+        if (st != SG_OK && alloc.release_ctx != nullptr)
+        {
+            alloc.release_ctx(alloc.ctx);
+        }
+        gb300_check(st, "createDeviceObject");
+        d._alloc = alloc;
+        gb300_check(sg_unordered_view_of(d._handle, &d._view), "createDeviceObject");
+        d._range = own_alloc<std::int32_t>(alloc, sizeof(std::int32_t) * (d._view.total_count + 2));
+        gb300_check(d._range != nullptr ? SG_OK : SG_ERR_OOM, "createDeviceObject");
+        return d;
+    }
+
     static void
     destroyDeviceObject(Derived& d)
     {
@@ -323,12 +341,21 @@ public:
     {
         if (d._handle != nullptr)
         {
+            if (d._alloc.alloc != nullptr)
+            {
+                cudaDeviceSynchronize();
+                d._alloc.release(d._range, d._alloc.ctx); // before the table drops the allocator's context
+            }
+            else
+            {
+                cudaFree(d._range);
+            }
             gb300_check(sg_unordered_destroy(d._handle), "destroyDeviceObject");
-            cudaFree(d._range);
         }
         d._handle = nullptr;
         d._range = nullptr;
         d._view = sg_unordered_view{};
+        d._alloc = sg_allocator{};
     }
 
     // insert(begin, end) over value_type elements (device memory): unordered_base_detail.cuh:996-1017
@@ -593,6 +620,7 @@ protected:
     sg_unordered* _handle = nullptr;
     sg_unordered_view _view{};
     std::int32_t* _range = nullptr;
+    sg_allocator _alloc{}; // the object's own allocator (createDeviceObject(capacity, allocator)), or none
 };
 
 template <typename Key, typename T, typename Hash, typename Derived>

@@ -20,7 +20,10 @@
 #include <cstdio>
 #include <exception>
 #include <functional>
+#include <memory>
+#include <mutex>
 #include <type_traits>
+#include <unordered_map>
 
 #include "../stdgpu_gb300.h"
 #include "device.cuh"
@@ -98,9 +101,11 @@ struct pair
 };
 
 // stdgpu::safe_device_allocator<T> (src/stdgpu/memory.h:340-420): device memory through cudaMalloc / cudaFree.
-// The containers accept an allocator type parameter, as the reference's do, for source compatibility; their
-// storage itself goes through the library's allocator pair (sg_set_device_allocator, one per process), and
-// get_allocator() returns a default-constructed allocator of the given type.
+// The containers take an allocator type parameter, as the reference's do.  With this default type a
+// container's storage goes through the library's allocator pair (sg_set_device_allocator, one per process);
+// an unordered_map / unordered_set created with another allocator (createDeviceObject(capacity, allocator))
+// takes all of its device storage from that allocator (detail::allocator_bridge), and get_allocator()
+// returns it.
 template <typename T>
 struct safe_device_allocator
 {
@@ -128,6 +133,89 @@ struct safe_device_allocator
         cudaFree(p);
     }
 };
+
+namespace detail
+{
+template <typename Allocator>
+struct is_safe_device_allocator : std::false_type
+{
+};
+template <typename T>
+struct is_safe_device_allocator<safe_device_allocator<T>> : std::true_type
+{
+};
+
+// The sg_allocator of a C++ Allocator: byte blocks through std::allocator_traits of the allocator rebound to
+// char, as the reference allocates its arrays (src/stdgpu/impl/memory_detail.h, allocator_traits); the
+// context owns a copy of the allocator and the size of every block it handed out (deallocate takes it) and
+// is deleted with the table (release_ctx).
+template <typename Allocator>
+struct allocator_bridge
+{
+    using bytes = typename std::allocator_traits<Allocator>::template rebind_alloc<char>;
+    using traits = std::allocator_traits<bytes>;
+
+    bytes a;
+    std::mutex m;
+    std::unordered_map<void*, std::size_t> sizes;
+
+    explicit allocator_bridge(const Allocator& x)
+      : a(x)
+    {
+    }
+
+    static void*
+    alloc(std::size_t n, void* c)
+    {
+        auto* x = static_cast<allocator_bridge*>(c);
+        char* p = traits::allocate(x->a, static_cast<typename traits::size_type>(n));
+        if (p != nullptr)
+        {
+            std::lock_guard<std::mutex> lock(x->m);
+            x->sizes[p] = n;
+        }
+        return p;
+    }
+
+    static void
+    release(void* p, void* c)
+    {
+        auto* x = static_cast<allocator_bridge*>(c);
+        std::size_t n = 0;
+        {
+            std::lock_guard<std::mutex> lock(x->m);
+            auto it = x->sizes.find(p);
+            if (it == x->sizes.end())
+            {
+                return;
+            }
+            n = it->second;
+            x->sizes.erase(it);
+        }
+        traits::deallocate(x->a, static_cast<char*>(p), static_cast<typename traits::size_type>(n));
+    }
+
+    static void
+    drop(void* c)
+    {
+        delete static_cast<allocator_bridge*>(c);
+    }
+
+    static sg_allocator
+    make(const Allocator& x)
+    {
+        return sg_allocator{ &alloc, &release, new allocator_bridge(x), &drop };
+    }
+};
+
+// A block of an object's own allocator (nullptr when its alloc is empty or fails).
+template <typename P>
+inline P*
+own_alloc(const sg_allocator& a, std::size_t bytes)
+{
+    return a.alloc != nullptr ? static_cast<P*>(a.alloc(bytes > 0 ? bytes : 1, a.ctx)) : nullptr;
+}
+} // namespace detail
 
 // Execution policies: the reference's execution::device plus a stream-carrying policy.
 namespace execution
@@ -228,6 +316,24 @@ public:
         return d;
     }
 
+    // createDeviceObject(capacity, allocator): every device block of the object from `alloc`
+    static Derived
+    create_with_allocator(execution::device_policy policy, const index_t& capacity, const sg_allocator& alloc)
+    {
+        Derived d;
+        const sg_status st = sg_unordered_create_with_allocator(kind, capacity, 0, &alloc, policy.stream, &d._handle);
+        if (st != SG_OK && alloc.release_ctx != nullptr)
+        {
+            alloc.release_ctx(alloc.ctx);
+        }
+        gb300_check(st, "createDeviceObject");
+        d._alloc = alloc;
+        gb300_check(sg_unordered_view_of(d._handle, &d._view), "createDeviceObject");
+        d._range = own_alloc<std::int32_t>(alloc, sizeof(std::int32_t) * (d._view.total_count + 2));
+        gb300_check(d._range != nullptr ? SG_OK : SG_ERR_OOM, "createDeviceObject");
+        return d;
+    }
+
     // destroyDeviceObject: src/stdgpu/impl/unordered_base_detail.cuh:1310-1348
     static void
     destroyDeviceObject(Derived& d)
@@ -240,12 +346,21 @@ public:
     {
         if (d._handle != nullptr)
         {
+            if (d._alloc.alloc != nullptr)
+            {
+                cudaDeviceSynchronize();
+                d._alloc.release(d._range, d._alloc.ctx); // before the table drops the allocator's context
+            }
+            else
+            {
+                cudaFree(d._range);
+            }
             gb300_check(sg_unordered_destroy(d._handle), "destroyDeviceObject");
-            cudaFree(d._range);
         }
         d._handle = nullptr;
         d._range = nullptr;
         d._view = sg_unordered_view{};
+        d._alloc = sg_allocator{};
     }
 
     // insert(begin, end) over value_type elements: unordered_base_detail.cuh:996-1017
@@ -426,6 +541,7 @@ protected:
     sg_unordered* _handle = nullptr;
     sg_unordered_view _view{};
     std::int32_t* _range = nullptr;
+    sg_allocator _alloc{}; // the object's own allocator (createDeviceObject(capacity, allocator)), or none
 };
 } // namespace detail
 
@@ -590,7 +706,10 @@ public:
     static unordered_map
     createDeviceObject(execution::device_policy policy, const index_t& capacity, const Allocator& allocator)
     {
-        unordered_map m = base::createDeviceObject(policy, capacity);
+        unordered_map m = detail::is_safe_device_allocator<Allocator>::value
+                                  ? base::createDeviceObject(policy, capacity)
+                                  : base::create_with_allocator(policy, capacity,
+                                                                detail::allocator_bridge<Allocator>::make(allocator));
         m._allocator = allocator;
         return m;
     }
@@ -640,7 +759,10 @@ public:
     static unordered_set
     createDeviceObject(execution::device_policy policy, const index_t& capacity, const Allocator& allocator)
     {
-        unordered_set m = base::createDeviceObject(policy, capacity);
+        unordered_set m = detail::is_safe_device_allocator<Allocator>::value
+                                  ? base::createDeviceObject(policy, capacity)
+                                  : base::create_with_allocator(policy, capacity,
+                                                                detail::allocator_bridge<Allocator>::make(allocator));
         m._allocator = allocator;
         return m;
     }

@@ -889,9 +889,28 @@ public:
     static Derived
     createDeviceObject(execution::device_policy policy, const index_t& capacity)
     {
+        return create_impl(policy, capacity, sg_allocator{});
+    }
+
+    // createDeviceObject(capacity, allocator): every device block of the object from `alloc`
+    static Derived
+    create_with_allocator(execution::device_policy policy, const index_t& capacity, const sg_allocator& alloc)
+    {
+        return create_impl(policy, capacity, alloc);
+    }
+
+    static Derived
+    create_impl(execution::device_policy policy, const index_t& capacity, const sg_allocator& alloc)
+    {
         sg_geometry geo{};
-        gb300_check(sg_unordered_geometry_for(SG_SET_U32, capacity, &geo), "createDeviceObject");
+        const sg_status gst = sg_unordered_geometry_for(SG_SET_U32, capacity, &geo);
+        if (gst != SG_OK && alloc.release_ctx != nullptr)
+        {
+            alloc.release_ctx(alloc.ctx);
+        }
+        gb300_check(gst, "createDeviceObject");
         Derived d;
+        d._alloc = alloc;
         ref_type& t = d._t;
         t.max_size = geo.max_size;
         t.bucket_count = geo.bucket_count;
@@ -901,11 +920,11 @@ public:
             ++t.bucket_bits;
         }
         const std::int64_t slots = t.end_slot();
-        bool ok = wide_alloc(&t.keys, sizeof(W) * slots) && wide_alloc(&t.hdr, sizeof(wide_header)) &&
-                  wide_alloc(&d._range, sizeof(std::int32_t) * (geo.max_size + 2));
+        bool ok = d.block(&t.keys, sizeof(W) * slots) && d.block(&t.hdr, sizeof(wide_header)) &&
+                  d.block(&d._range, sizeof(std::int32_t) * (geo.max_size + 2));
         if (ok && ref_type::has_values)
         {
-            ok = wide_alloc(&t.values, sizeof(value_store) * slots);
+            ok = d.block(&t.values, sizeof(value_store) * slots);
         }
         if (!ok)
         {
@@ -1150,15 +1169,55 @@ protected:
         return ref_type::has_values && !std::is_trivially_destructible<value_store>::value;
     }
 
+    // a device block of this object: its own allocator's, else cudaMalloc
+    template <typename P>
+    bool
+    block(P** p, std::size_t bytes)
+    {
+        if (_alloc.alloc != nullptr)
+        {
+            *p = own_alloc<P>(_alloc, bytes);
+            return *p != nullptr;
+        }
+        return wide_alloc(p, bytes);
+    }
+
+    void
+    unblock(void* p)
+    {
+        if (p == nullptr)
+        {
+            return;
+        }
+        if (_alloc.alloc != nullptr)
+        {
+            _alloc.release(p, _alloc.ctx);
+        }
+        else
+        {
+            cudaFree(p);
+        }
+    }
+
+    // frees every block and drops the allocator's context
     static void
     free_all(Derived& d)
     {
-        cudaFree(d._t.keys);
-        cudaFree(d._t.values);
-        cudaFree(d._t.hdr);
-        cudaFree(d._range);
+        if (d._alloc.alloc != nullptr)
+        {
+            cudaDeviceSynchronize(); // as cudaFree does, before the allocator may hand the memory on
+        }
+        d.unblock(d._t.keys);
+        d.unblock(d._t.values);
+        d.unblock(d._t.hdr);
+        d.unblock(d._range);
+        if (d._alloc.release_ctx != nullptr)
+        {
+            d._alloc.release_ctx(d._alloc.ctx);
+        }
         d._t = ref_type{};
         d._range = nullptr;
+        d._alloc = sg_allocator{};
     }
 
     wide_header
@@ -1200,6 +1259,7 @@ protected:
 
     ref_type _t{};
     std::int32_t* _range = nullptr;
+    sg_allocator _alloc{}; // the object's own allocator (createDeviceObject(capacity, allocator)), or none
 };
 
 template <typename Key, typename T, typename Hash, typename Derived, typename KeyEqual = void>

@@ -24,6 +24,10 @@ SG_ERR_NO_DEVICE = 7
 SET_U32, SET_U64, MAP_U64_U32, MAP_U64_U64, MAP_U32_U32, MAP_U32_U64 = range(6)
 
 
+class sg_allocator(ctypes.Structure):
+    _fields_ = [("alloc", c_void_p), ("release", c_void_p), ("ctx", c_void_p), ("release_ctx", c_void_p)]
+
+
 class sg_geometry(ctypes.Structure):
     _fields_ = [
         ("capacity", c_int64),
@@ -79,6 +83,8 @@ SIGNATURES = {
     "sg_set_device_allocator": (c_int32, [c_void_p, c_void_p, c_void_p]),
     "sg_live_device_allocations": (c_int64, []),
     "sg_unordered_create": (c_int32, [c_int32, c_int64, c_void_p, POINTER(c_void_p)]),
+    "sg_unordered_create_with_allocator": (c_int32, [c_int32, c_int64, c_int32, POINTER(sg_allocator), c_void_p,
+                                                   POINTER(c_void_p)]),
     "sg_unordered_destroy": (c_int32, [c_void_p]),
     "sg_unordered_insert": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),
     "sg_unordered_insert_kv": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p]),

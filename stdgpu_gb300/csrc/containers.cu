@@ -86,19 +86,26 @@ scan_counts(unsigned* cnt, int lane)
 
 // ---------------------------------------------------------------- vector
 
+// Bulk push_back: element i pushes values[i] where pred[i] != 0 (every element without pred).  Per tile the
+// selected values are loaded before the tile's reservation, so their loads are in flight while warp 0 scans
+// the counts and adds the tile's total to the size; a reservation past capacity fails the tile's elements
+// there, as the reference's push_back fails past capacity() (its size is clamped when read,
+// vector_detail.cuh:484-511).  Two count buffers alternate between tiles, so a tile needs two barriers.
 template <typename T>
 __global__ void __launch_bounds__(kCThreads)
 k_vector_push_back(T* data, long long* size, int64_t cap, const T* values, const uint8_t* pred, int64_t n,
                    uint8_t* out_pushed)
 {
-    __shared__ unsigned cnt[kCounts];
-    __shared__ long long s_base;
+    __shared__ unsigned cnt[2][kCounts];
+    __shared__ long long s_base[2];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
+    int buf = 0;
     for (int64_t tile = static_cast<int64_t>(blockIdx.x) * kTileElems; tile < n;
-         tile += static_cast<int64_t>(gridDim.x) * kTileElems)
+         tile += static_cast<int64_t>(gridDim.x) * kTileElems, buf ^= 1)
     {
         unsigned masks[kItems];
+        T vals[kItems];
 #pragma unroll
         for (int j = 0; j < kItems; ++j)
         {
@@ -107,46 +114,42 @@ k_vector_push_back(T* data, long long* size, int64_t cap, const T* values, const
             masks[j] = __ballot_sync(0xffffffffu, want);
             if (lane == 0)
             {
-                cnt[j * kWarps + warp] = __popc(masks[j]);
+                cnt[buf][j * kWarps + warp] = __popc(masks[j]);
             }
+            vals[j] = want ? ld_stream(values + i) : T{};
         }
         __syncthreads();
         if (warp == 0)
         {
-            const unsigned total = scan_counts(cnt, lane);
+            const unsigned total = scan_counts(cnt[buf], lane);
             if (lane == 0)
             {
-                // preemptive full() check, then one reservation for the tile (vector_detail.cuh:186-195)
-                long long b = -1;
-                if (total > 0)
-                {
-                    const long long cur = *reinterpret_cast<volatile long long*>(size);
-                    b = cur >= cap ? -1
-                                   : static_cast<long long>(atomicAdd(reinterpret_cast<unsigned long long*>(size),
-                                                                      static_cast<unsigned long long>(total)));
-                }
-                s_base = b;
+                // one reservation for the tile (vector_detail.cuh:186-195)
+                s_base[buf] = total > 0 ? static_cast<long long>(atomicAdd(reinterpret_cast<unsigned long long*>(size),
+                                                                           static_cast<unsigned long long>(total)))
+                                        : -1;
             }
         }
         __syncthreads();
-        const long long base = s_base;
+        const long long base = s_base[buf];
 #pragma unroll
         for (int j = 0; j < kItems; ++j)
         {
             const int64_t i = tile + j * kCThreads + threadIdx.x;
             const bool want = (masks[j] >> lane) & 1u;
-            const long long pos = base + cnt[j * kWarps + warp] + __popc(masks[j] & lanemask_lt());
+            const long long pos = base + cnt[buf][j * kWarps + warp] + __popc(masks[j] & lanemask_lt());
             const bool ok = want && base >= 0 && pos < cap;
             if (ok)
             {
-                data[pos] = ld_stream(values + i);
+                data[pos] = vals[j];
             }
             if (i < n && out_pushed != nullptr)
             {
                 out_pushed[i] = static_cast<uint8_t>(ok);
             }
         }
-        __syncthreads(); // cnt and s_base are rewritten by the next tile
+        // no barrier: the next tile fills the other count buffer, and the one after passes two barriers
+        // that every warp reaches only after reading this tile's counts
     }
 }
 

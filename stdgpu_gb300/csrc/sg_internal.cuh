@@ -100,6 +100,43 @@ dev_free(void* p)
     a.live.fetch_sub(1);
 }
 
+// One object's own allocator (sg_unordered_create_with_allocator); alloc == nullptr: the process-wide pair.
+struct object_allocator
+{
+    sg_device_alloc_fn alloc = nullptr;
+    sg_device_free_fn release = nullptr;
+    void* ctx = nullptr;
+};
+
+template <typename T>
+inline cudaError_t
+obj_malloc(const object_allocator& oa, T** p, size_t bytes)
+{
+    if (oa.alloc == nullptr)
+    {
+        return dev_malloc(p, bytes);
+    }
+    void* q = oa.alloc(bytes > 0 ? bytes : 1, oa.ctx);
+    *p = static_cast<T*>(q);
+    return q == nullptr ? cudaErrorMemoryAllocation : cudaSuccess;
+}
+
+inline void
+obj_free(const object_allocator& oa, void* p)
+{
+    if (p == nullptr)
+    {
+        return;
+    }
+    if (oa.alloc == nullptr)
+    {
+        dev_free(p);
+        return;
+    }
+    cudaDeviceSynchronize(); // as cudaFree does, before the caller's release may hand the memory on
+    oa.release(p, oa.ctx);
+}
+
 // Blocks per SM at which `kernel` is resident with `threads` threads, times the SM count.
 template <typename Kernel>
 int

@@ -1139,6 +1139,8 @@ struct sg_unordered
     int64_t part_scratch_bytes;
     unsigned int* locks;        // stripe locks of the native device inserts (include/stdgpu_gb300/device.cuh)
     int64_t lock_count;
+    object_allocator oa;           // the table's own allocator (sg_unordered_create_with_allocator), or none
+    void (*release_ctx)(void* ctx); // called with oa.ctx when the table is destroyed (nullable)
 };
 
 namespace
@@ -1283,11 +1285,11 @@ ensure_part_scratch(sg_unordered* t, int64_t bytes)
     {
         // a launch queued earlier may still read the old array
         SG_CUDA_TRY(cudaDeviceSynchronize());
-        sg::detail::dev_free(t->part_scratch);
+        sg::detail::obj_free(t->oa, t->part_scratch);
         t->part_scratch = nullptr;
         t->part_scratch_bytes = 0;
     }
-    const cudaError_t e = sg::detail::dev_malloc(&t->part_scratch, static_cast<size_t>(bytes));
+    const cudaError_t e = sg::detail::obj_malloc(t->oa, &t->part_scratch, static_cast<size_t>(bytes));
     if (e != cudaSuccess)
     {
         cudaGetLastError();
@@ -1299,7 +1301,7 @@ ensure_part_scratch(sg_unordered* t, int64_t bytes)
     {
         // the staged kernels copy chunks of the array with 16-byte-aligned bulk copies; an allocator that
         // returned less alignment gets the direct kernels instead
-        sg::detail::dev_free(t->part_scratch);
+        sg::detail::obj_free(t->oa, t->part_scratch);
         t->part_scratch = nullptr;
         t->part_scratch_bytes = 0;
         return SG_ERR_OOM;
@@ -1612,8 +1614,11 @@ sg_unordered_geometry_for(int32_t kind, int64_t capacity, sg_geometry* out)
     return SG_OK;
 }
 
+namespace
+{
+
 sg_status
-sg_unordered_create(int32_t kind, int64_t capacity, void* stream, sg_unordered** out)
+create_table(int32_t kind, int64_t capacity, const object_allocator& oa, void* stream, sg_unordered** out)
 {
     if (out == nullptr)
     {
@@ -1646,14 +1651,15 @@ sg_unordered_create(int32_t kind, int64_t capacity, void* stream, sg_unordered**
     t->bits = log2_exact(g.bucket_count);
     t->nchunks = (t->total + kRangeChunk - 1) / kRangeChunk;
     t->device = dev;
-    cudaError_t e = sg::detail::dev_malloc(&t->slots, static_cast<size_t>((t->num_groups + 1) * kGroupBytes));
+    t->oa = oa;
+    cudaError_t e = sg::detail::obj_malloc(t->oa, &t->slots, static_cast<size_t>((t->num_groups + 1) * kGroupBytes));
     if (e == cudaSuccess)
     {
-        e = sg::detail::dev_malloc(&t->hdr, sizeof(table_header));
+        e = sg::detail::obj_malloc(t->oa, &t->hdr, sizeof(table_header));
     }
     if (e == cudaSuccess)
     {
-        e = sg::detail::dev_malloc(&t->chunk_counts, static_cast<size_t>(t->nchunks + 1) * sizeof(unsigned int));
+        e = sg::detail::obj_malloc(t->oa, &t->chunk_counts, static_cast<size_t>(t->nchunks + 1) * sizeof(unsigned int));
     }
     if (e == cudaSuccess)
     {
@@ -1662,7 +1668,7 @@ sg_unordered_create(int32_t kind, int64_t capacity, void* stream, sg_unordered**
     if (e == cudaSuccess)
     {
         t->lock_count = insert_lock_count(t->num_groups);
-        e = sg::detail::dev_malloc(&t->locks, static_cast<size_t>(t->lock_count) * sizeof(unsigned int));
+        e = sg::detail::obj_malloc(t->oa, &t->locks, static_cast<size_t>(t->lock_count) * sizeof(unsigned int));
     }
     if (e == cudaSuccess)
     {
@@ -1684,6 +1690,34 @@ sg_unordered_create(int32_t kind, int64_t capacity, void* stream, sg_unordered**
     return SG_OK;
 }
 
+} // namespace
+
+sg_status
+sg_unordered_create(int32_t kind, int64_t capacity, void* stream, sg_unordered** out)
+{
+    return create_table(kind, capacity, object_allocator{}, stream, out);
+}
+
+sg_status
+sg_unordered_create_with_allocator(int32_t kind, int64_t capacity, int32_t custom_hash, const sg_allocator* allocator,
+                                   void* stream, sg_unordered** out)
+{
+    if (allocator == nullptr || allocator->alloc == nullptr || allocator->release == nullptr || out == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    const sg_status st =
+            create_table(kind, capacity, object_allocator{ allocator->alloc, allocator->release, allocator->ctx }, stream,
+                         out);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    (*out)->custom_hash = custom_hash != 0;
+    (*out)->release_ctx = allocator->release_ctx;
+    return SG_OK;
+}
+
 sg_status
 sg_unordered_destroy(sg_unordered* t)
 {
@@ -1698,27 +1732,31 @@ sg_unordered_destroy(sg_unordered* t)
     }
     if (t->slots != nullptr)
     {
-        sg::detail::dev_free(t->slots);
+        sg::detail::obj_free(t->oa, t->slots);
     }
     if (t->hdr != nullptr)
     {
-        sg::detail::dev_free(t->hdr);
+        sg::detail::obj_free(t->oa, t->hdr);
     }
     if (t->chunk_counts != nullptr)
     {
-        sg::detail::dev_free(t->chunk_counts);
+        sg::detail::obj_free(t->oa, t->chunk_counts);
     }
     if (t->part_scratch != nullptr)
     {
-        sg::detail::dev_free(t->part_scratch);
+        sg::detail::obj_free(t->oa, t->part_scratch);
     }
     if (t->locks != nullptr)
     {
-        sg::detail::dev_free(t->locks);
+        sg::detail::obj_free(t->oa, t->locks);
     }
     if (t->host_hdr != nullptr)
     {
         cudaFreeHost(t->host_hdr);
+    }
+    if (t->release_ctx != nullptr)
+    {
+        t->release_ctx(t->oa.ctx);
     }
     delete t;
     return e == cudaSuccess ? SG_OK : SG_ERR_CUDA;
@@ -1863,7 +1901,7 @@ sg_unordered_rehash(sg_unordered* t, int64_t new_capacity, void* stream)
     char* buf = nullptr;
     const int64_t cap = n + 2;
     const int64_t kbytes = ((cap * kb + 255) / 256) * 256;
-    if (sg::detail::dev_malloc(&buf, static_cast<size_t>(kbytes + cap * (mb > 0 ? mb : 1))) != cudaSuccess)
+    if (sg::detail::obj_malloc(t->oa, &buf, static_cast<size_t>(kbytes + cap * (mb > 0 ? mb : 1))) != cudaSuccess)
     {
         cudaGetLastError();
         return SG_ERR_OOM;
@@ -1873,7 +1911,7 @@ sg_unordered_rehash(sg_unordered* t, int64_t new_capacity, void* stream)
     st = sg_unordered_range_copy(t, buf, mb > 0 ? buf + kbytes : nullptr, stream, &copied);
     if (st == SG_OK)
     {
-        st = sg_unordered_create(t->kind, new_capacity, stream, &fresh);
+        st = create_table(t->kind, new_capacity, t->oa, stream, &fresh);
     }
     if (st == SG_OK && copied > 0)
     {
@@ -1884,7 +1922,7 @@ sg_unordered_rehash(sg_unordered* t, int64_t new_capacity, void* stream)
     {
         st = sg_unordered_status(fresh, stream, &refused, nullptr);
     }
-    sg::detail::dev_free(buf);
+    sg::detail::obj_free(t->oa, buf);
     if (st != SG_OK)
     {
         if (fresh != nullptr)
@@ -1899,6 +1937,8 @@ sg_unordered_rehash(sg_unordered* t, int64_t new_capacity, void* stream)
     *t = *fresh;
     *fresh = tmp;
     t->insert_mode = mode;
+    t->release_ctx = tmp.release_ctx; // the handle keeps its allocator's context; the old storage leaves alone
+    fresh->release_ctx = nullptr;
     return sg_unordered_destroy(fresh);
 }
 

@@ -17,6 +17,7 @@ WIDE_GOLDEN = ROOT / "tests" / "cpp" / "wide_golden_test.cu"
 ROUTING = ROOT / "tests" / "cpp" / "routing_check.cu"
 CHURN = ROOT / "tests" / "cpp" / "device_churn_test.cu"
 KEY_EQUAL = ROOT / "tests" / "cpp" / "key_equal_test.cu"
+ALLOCATOR = ROOT / "tests" / "cpp" / "allocator_test.cu"
 GOLDEN = ROOT / "tests" / "golden"
 OUT = ROOT / "tests" / "cpp" / "_build"
 
@@ -181,6 +182,23 @@ def test_keys_compare_with_key_equal_on_gpu():
     bulk and device calls against std::unordered_set / std::unordered_map with the same Hash and KeyEqual."""
     stdgpu_gb300.load()
     exe = _compile(src=KEY_EQUAL)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    print(r.stdout)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "ALL PASS" in r.stdout
+
+
+def test_allocator_program_compiles_for_sm103a():
+    stdgpu_gb300.load()
+    _compile(src=ALLOCATOR)
+
+
+@pytest.mark.gpu
+def test_user_allocator_holds_every_block_on_gpu():
+    """createDeviceObject(capacity, allocator) with a counting device allocator on the three storage paths:
+    every block from it, tables working, every block returned by destroyDeviceObject."""
+    stdgpu_gb300.load()
+    exe = _compile(src=ALLOCATOR)
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     print(r.stdout)
     assert r.returncode == 0, r.stdout + r.stderr
