@@ -338,6 +338,7 @@ struct table_rec
     int64_t size_bound = 0; // upper bound of size(): exact after a check, plus keys inserted since
     std::deque<int64_t> fifo;
     bool busy = false;
+    bool grow_failed = false; // the last grow could not allocate: the waiting insert run is refused
 };
 
 // One segmented launch of small runs of one operation: its descriptors (device and pinned host), its
@@ -364,6 +365,20 @@ struct direct_unit
     int32_t table = -1;
     sg_unordered* retire = nullptr;
     int64_t retire_bytes = 0;
+    // a grow the grow thread has not launched yet (its event is not recorded): written by the grow thread,
+    // read by the scheduler's event polling outside the lock
+    std::atomic<bool> pending{ false };
+};
+
+// A grow handed to the grow thread: the new table's capacity and bytes, the storage it replaces.
+struct grow_job
+{
+    int32_t table = -1;
+    direct_unit* unit = nullptr;
+    int64_t capacity = 0;
+    int64_t max_size = 0;
+    int64_t bytes = 0;
+    sg_unordered* old = nullptr;
 };
 
 // What admit_insert_run decided for an insert run.
@@ -412,9 +427,13 @@ struct sg_server
     clock_type::time_point t_first{}, t_last{};
     bool any_done = false;
     bool stop = false;
+    bool stop_grows = false;
     bool paused = false;
     std::atomic<uint64_t> submissions{ 0 }; // bumped by every submit: wakes the scheduler's spin
     std::thread worker;
+    std::thread grower; // creates and fills grown tables, so the scheduler keeps launching meanwhile
+    std::deque<grow_job> grow_jobs;
+    std::condition_variable cv_grow;
     int device = 0;
 
     request_rec&
@@ -424,6 +443,7 @@ struct sg_server
     }
 
     void run();
+    void run_grows();
     void finish(const std::vector<int64_t>& tickets, clock_type::time_point now);
     bool complete_finished();
     bool any_in_flight() const;
@@ -434,6 +454,8 @@ struct sg_server
     bool launch_packed(launch_slot& sl, int op, const std::vector<std::pair<int32_t, int64_t>>& run);
     direct_unit* free_unit();
     sg_status grow(int32_t table, table_rec& t, int64_t need, direct_unit& u);
+    void grow_done(const grow_job& job, sg_unordered* nh);
+    void refuse_run(table_rec& t, size_t take);
     void release_graveyard();
 };
 
@@ -528,7 +550,7 @@ sg_server::complete_finished()
     }
     for (auto& u : units)
     {
-        if (!u.in_use || cudaEventQuery(u.done) != cudaSuccess)
+        if (!u.in_use || u.pending || cudaEventQuery(u.done) != cudaSuccess)
         {
             continue;
         }
@@ -584,7 +606,7 @@ sg_server::any_event_done()
     }
     for (auto& u : units)
     {
-        if (u.in_use && cudaEventQuery(u.done) == cudaSuccess)
+        if (u.in_use && !u.pending && cudaEventQuery(u.done) == cudaSuccess)
         {
             return true;
         }
@@ -620,25 +642,15 @@ sg_server::release_graveyard()
 }
 
 // Grows table t to the first doubling of its capacity under which `need` elements stay below 85 % of
-// max_size(), when the budget allows.  Asynchronous: the new table is created and filled from the old one
-// by k_migrate on the grow stream, the unit's event completes the grow, and until then the table is busy,
-// so its requests keep their order.  The old storage stays counted against the budget until it is
+// max_size(), when the budget allows.  Asynchronous: the grow thread creates the new table and fills it
+// from the old one by k_migrate on the grow stream, the unit's event completes the grow, and until then
+// the table is busy, so its requests keep their order; the scheduler goes on with other tables while the
+// new storage is allocated.  The new bytes are counted at once, the old ones until the old storage is
 // released.  Caller holds the lock; the table has nothing in flight.
 sg_status
 sg_server::grow(int32_t table, table_rec& t, int64_t need, direct_unit& u)
 {
     const auto t0 = clock_type::now();
-    struct timer
-    {
-        sg_server* s;
-        clock_type::time_point t0;
-        ~timer()
-        {
-            const double us = std::chrono::duration<double, std::micro>(clock_type::now() - t0).count();
-            s->grow_host_us += us;
-            s->max_grow_host_us = us > s->max_grow_host_us ? us : s->max_grow_host_us;
-        }
-    } tm{ this, t0 };
     int64_t cap = t.capacity;
     int64_t ms = 0;
     int64_t bytes = 0;
@@ -659,37 +671,109 @@ sg_server::grow(int32_t table, table_rec& t, int64_t need, direct_unit& u)
     {
         return SG_ERR_BUDGET;
     }
-    sg_unordered* nh = nullptr;
-    sg_status st = sg_unordered_create(kind, cap, grow_stream, &nh);
-    if (st != SG_OK)
-    {
-        return st;
-    }
-    st = launch_migrate(kind, kernel_view(t.h), kernel_view(nh), grid_cap, grow_stream);
-    if (st == SG_OK && cudaEventRecord(u.done, grow_stream) != cudaSuccess)
-    {
-        st = SG_ERR_CUDA;
-    }
-    if (st != SG_OK)
-    {
-        cudaStreamSynchronize(grow_stream);
-        sg_unordered_destroy(nh);
-        cudaGetLastError();
-        return st;
-    }
+    grow_jobs.push_back(grow_job{ table, &u, cap, ms, bytes, t.h });
     u.tickets.clear();
     u.table = table;
     u.in_use = true;
-    u.retire = t.h;
-    u.retire_bytes = t.bytes;
+    u.pending = true;
     used += bytes;
-    t.h = nh;
-    t.capacity = cap;
-    t.max_size = ms;
-    t.bytes = bytes;
     t.busy = true;
     ++rehashes;
+    cv_grow.notify_one();
+    const double us = std::chrono::duration<double, std::micro>(clock_type::now() - t0).count();
+    grow_host_us += us;
+    max_grow_host_us = us > max_grow_host_us ? us : max_grow_host_us;
     return SG_OK;
+}
+
+// The grow thread: for each job, the new table and the migrate launch on the grow stream, then the unit's
+// event; the job's table is busy meanwhile, so nothing else touches its storage.
+void
+sg_server::run_grows()
+{
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lock(m);
+    while (true)
+    {
+        cv_grow.wait(lock, [&] { return stop_grows || !grow_jobs.empty(); });
+        if (grow_jobs.empty())
+        {
+            return;
+        }
+        const grow_job job = grow_jobs.front();
+        grow_jobs.pop_front();
+        lock.unlock();
+        sg_unordered* nh = nullptr;
+        sg_status st = sg_unordered_create(kind, job.capacity, grow_stream, &nh);
+        if (st == SG_OK)
+        {
+            st = launch_migrate(kind, kernel_view(job.old), kernel_view(nh), grid_cap, grow_stream);
+            if (st == SG_OK && cudaEventRecord(job.unit->done, grow_stream) != cudaSuccess)
+            {
+                st = SG_ERR_CUDA;
+            }
+            if (st != SG_OK)
+            {
+                cudaStreamSynchronize(grow_stream);
+                sg_unordered_destroy(nh);
+                nh = nullptr;
+            }
+        }
+        cudaGetLastError();
+        lock.lock();
+        grow_done(job, nh);
+        lock.unlock();
+        submissions.fetch_add(1, std::memory_order_release); // wakes the scheduler's spin
+        cv_work.notify_one();
+        lock.lock();
+    }
+}
+
+// A grow job's outcome.  Launched: the table takes the new storage and the unit completes with its event,
+// the old storage then retiring.  Failed: the bytes go back, the table is free again and its waiting insert
+// run is refused.  Caller holds the lock.
+void
+sg_server::grow_done(const grow_job& job, sg_unordered* nh)
+{
+    direct_unit& u = *job.unit;
+    table_rec& t = tables[job.table];
+    if (nh != nullptr)
+    {
+        u.retire = job.old;
+        u.retire_bytes = t.bytes;
+        u.pending = false;
+        t.h = nh;
+        t.capacity = job.capacity;
+        t.max_size = job.max_size;
+        t.bytes = job.bytes;
+    }
+    else
+    {
+        used -= job.bytes;
+        --rehashes;
+        u.pending = false;
+        u.in_use = false;
+        t.busy = false;
+        t.grow_failed = true;
+    }
+}
+
+// Completes the first `take` requests of table t with SG_ERR_BUDGET (refused; nothing spills).  Caller holds
+// the lock.
+void
+sg_server::refuse_run(table_rec& t, size_t take)
+{
+    const auto now = clock_type::now();
+    for (size_t k = 0; k < take; ++k)
+    {
+        request_rec& r = rec(t.fifo.front());
+        r.status = SG_ERR_BUDGET;
+        r.done = true;
+        r.t_done = now;
+        ++refused_budget;
+        t.fifo.pop_front();
+    }
+    cv_done.notify_all();
 }
 
 // Before an insert run of `take` requests and run_keys keys: if the run could pass 85 % of max_size(), the
@@ -699,6 +783,13 @@ sg_server::grow(int32_t table, table_rec& t, int64_t need, direct_unit& u)
 admit_result
 sg_server::admit_insert_run(int32_t table, table_rec& t, size_t take, int64_t run_keys)
 {
+    if (t.grow_failed)
+    {
+        // the grow this run waited for could not allocate its table
+        t.grow_failed = false;
+        refuse_run(t, take);
+        return kAdmitRefused;
+    }
     if (t.size_bound + run_keys > t.max_size * 85 / 100)
     {
         int64_t exact = 0;
@@ -717,17 +808,7 @@ sg_server::admit_insert_run(int32_t table, table_rec& t, size_t take, int64_t ru
             {
                 return kAdmitGrowing;
             }
-            const auto now = clock_type::now();
-            for (size_t k = 0; k < take; ++k)
-            {
-                request_rec& r = rec(t.fifo.front());
-                r.status = SG_ERR_BUDGET;
-                r.done = true;
-                r.t_done = now;
-                ++refused_budget;
-                t.fifo.pop_front();
-            }
-            cv_done.notify_all();
+            refuse_run(t, take);
             return kAdmitRefused;
         }
     }
@@ -1034,7 +1115,7 @@ sg_server_create(int32_t kind, int64_t hbm_budget_bytes, int32_t n_streams, int3
         cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, least);
     }
     cudaStreamCreateWithPriority(&srv->grow_stream, cudaStreamNonBlocking, least);
-    srv->units.resize(kMaxDirectLimit);
+    srv->units = std::vector<direct_unit>(kMaxDirectLimit);
     for (auto& u : srv->units)
     {
         if (cudaEventCreateWithFlags(&u.done, cudaEventDisableTiming) != cudaSuccess)
@@ -1058,6 +1139,7 @@ sg_server_create(int32_t kind, int64_t hbm_budget_bytes, int32_t n_streams, int3
             return SG_ERR_OOM;
         }
     }
+    srv->grower = std::thread([srv] { srv->run_grows(); });
     srv->worker = std::thread([srv] { srv->run(); });
     *out = srv;
     return SG_OK;
@@ -1077,7 +1159,16 @@ sg_server_destroy(sg_server* srv)
     srv->cv_work.notify_all();
     if (srv->worker.joinable())
     {
-        srv->worker.join();
+        srv->worker.join(); // returns once nothing is in flight, pending grows included
+    }
+    {
+        std::lock_guard<std::mutex> lock(srv->m);
+        srv->stop_grows = true;
+    }
+    srv->cv_grow.notify_all();
+    if (srv->grower.joinable())
+    {
+        srv->grower.join();
     }
     cudaDeviceSynchronize();
     srv->release_graveyard();

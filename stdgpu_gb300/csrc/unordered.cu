@@ -16,8 +16,10 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <type_traits>
+#include <vector>
 
 #include "sg_internal.cuh"
 #include "stdgpu_gb300.h"
@@ -1117,6 +1119,55 @@ k_range_specials(dview t, const unsigned int* chunk_offsets, int64_t nchunks, co
 
 using namespace sg::detail;
 
+// Pinned host mirrors of table headers, carved from 64 KB pinned pages that are kept for the process's
+// life: a table's creation then costs no cudaMallocHost, which takes tens to hundreds of microseconds and
+// serialises with other host-side CUDA calls.
+class pinned_header_pool
+{
+public:
+    void*
+    get()
+    {
+        std::lock_guard<std::mutex> lock(m_);
+        if (free_.empty())
+        {
+            void* page = nullptr;
+            if (cudaMallocHost(&page, kPage) != cudaSuccess)
+            {
+                cudaGetLastError();
+                return nullptr;
+            }
+            for (size_t off = 0; off + kPiece <= kPage; off += kPiece)
+            {
+                free_.push_back(static_cast<char*>(page) + off);
+            }
+        }
+        void* p = free_.back();
+        free_.pop_back();
+        return p;
+    }
+
+    void
+    put(void* p)
+    {
+        std::lock_guard<std::mutex> lock(m_);
+        free_.push_back(p);
+    }
+
+private:
+    static constexpr size_t kPage = size_t{ 64 } << 10;
+    static constexpr size_t kPiece = (sizeof(sg::detail::table_header) + 63) / 64 * 64;
+    std::mutex m_;
+    std::vector<void*> free_;
+};
+
+inline pinned_header_pool&
+pinned_headers()
+{
+    static pinned_header_pool* pool = new pinned_header_pool; // pages stay mapped until the process exits
+    return *pool;
+}
+
 struct sg_unordered
 {
     int32_t kind;
@@ -1127,6 +1178,7 @@ struct sg_unordered
     int64_t total;
     int64_t num_groups;
     int bits;
+    char* block;                // the one device block of slots, header, counters and locks
     char* slots;
     table_header* hdr;
     unsigned int* chunk_counts; // compaction scratch: one count per kRangeChunk slots, plus one
@@ -1652,23 +1704,25 @@ create_table(int32_t kind, int64_t capacity, const object_allocator& oa, void* s
     t->nchunks = (t->total + kRangeChunk - 1) / kRangeChunk;
     t->device = dev;
     t->oa = oa;
-    cudaError_t e = sg::detail::obj_malloc(t->oa, &t->slots, static_cast<size_t>((t->num_groups + 1) * kGroupBytes));
+    // one device block: slots, then header, compaction counters and stripe locks at 256-byte offsets
+    t->lock_count = insert_lock_count(t->num_groups);
+    const auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+    const size_t off_hdr = up(static_cast<size_t>((t->num_groups + 1) * kGroupBytes));
+    const size_t off_counts = off_hdr + up(sizeof(table_header));
+    const size_t off_locks = off_counts + up(static_cast<size_t>(t->nchunks + 1) * sizeof(unsigned int));
+    const size_t block_bytes = off_locks + static_cast<size_t>(t->lock_count) * sizeof(unsigned int);
+    cudaError_t e = sg::detail::obj_malloc(t->oa, &t->block, block_bytes);
     if (e == cudaSuccess)
     {
-        e = sg::detail::obj_malloc(t->oa, &t->hdr, sizeof(table_header));
-    }
-    if (e == cudaSuccess)
-    {
-        e = sg::detail::obj_malloc(t->oa, &t->chunk_counts, static_cast<size_t>(t->nchunks + 1) * sizeof(unsigned int));
-    }
-    if (e == cudaSuccess)
-    {
-        e = cudaMallocHost(&t->host_hdr, sizeof(table_header));
-    }
-    if (e == cudaSuccess)
-    {
-        t->lock_count = insert_lock_count(t->num_groups);
-        e = sg::detail::obj_malloc(t->oa, &t->locks, static_cast<size_t>(t->lock_count) * sizeof(unsigned int));
+        t->slots = t->block;
+        t->hdr = reinterpret_cast<table_header*>(t->block + off_hdr);
+        t->chunk_counts = reinterpret_cast<unsigned int*>(t->block + off_counts);
+        t->locks = reinterpret_cast<unsigned int*>(t->block + off_locks);
+        t->host_hdr = static_cast<unsigned long long*>(pinned_headers().get());
+        if (t->host_hdr == nullptr)
+        {
+            e = cudaErrorMemoryAllocation;
+        }
     }
     if (e == cudaSuccess)
     {
@@ -1726,33 +1780,21 @@ sg_unordered_destroy(sg_unordered* t)
         return SG_ERR_BAD_ARG;
     }
     cudaError_t e = cudaSuccess;
-    if (t->slots != nullptr || t->hdr != nullptr)
+    if (t->block != nullptr)
     {
         e = cudaDeviceSynchronize();
     }
-    if (t->slots != nullptr)
+    if (t->block != nullptr)
     {
-        sg::detail::obj_free(t->oa, t->slots);
-    }
-    if (t->hdr != nullptr)
-    {
-        sg::detail::obj_free(t->oa, t->hdr);
-    }
-    if (t->chunk_counts != nullptr)
-    {
-        sg::detail::obj_free(t->oa, t->chunk_counts);
+        sg::detail::obj_free(t->oa, t->block);
     }
     if (t->part_scratch != nullptr)
     {
         sg::detail::obj_free(t->oa, t->part_scratch);
     }
-    if (t->locks != nullptr)
-    {
-        sg::detail::obj_free(t->oa, t->locks);
-    }
     if (t->host_hdr != nullptr)
     {
-        cudaFreeHost(t->host_hdr);
+        pinned_headers().put(t->host_hdr);
     }
     if (t->release_ctx != nullptr)
     {
