@@ -261,12 +261,73 @@ struct unordered_ref
         }
     }
 
+    // The key along its probe sequence from group home, up to the first group holding a never-used slot:
+    // true when present; else target = the first free slot on the way (erased below max_size(), or never
+    // used; -1 when there is none) and whether it is an erased one.
+    __device__ bool
+    scan_for_insert(key_type key, int64_t home, int64_t& target, bool& target_tomb) const
+    {
+        int64_t g = home;
+        target = -1;
+        target_tomb = false;
+        for (int64_t probes = 0; probes < v.num_groups; ++probes)
+        {
+            const uint4* p = group_ptr(g);
+            bool any_empty = false;
+            bool present = false;
+#pragma unroll
+            for (int l = 0; l < detail::kTileLanes; ++l)
+            {
+                const uint4 d = __ldcg(p + l);
+#pragma unroll
+                for (int s = 0; s < SPL; ++s)
+                {
+                    const key_type k = detail::key_in_lane<KIND>(d, s);
+                    const int64_t slot = g * G + l * SPL + s;
+                    present |= k == key;
+                    any_empty |= k == C::empty_key;
+                    if (target < 0 && (k == C::empty_key || (k == C::tomb_key && slot < v.total_count)))
+                    {
+                        target = slot;
+                        target_tomb = k == C::tomb_key;
+                    }
+                }
+            }
+            if (present)
+            {
+                return true;
+            }
+            if (any_empty)
+            {
+                break;
+            }
+            g = detail::next_group(g, v.num_groups);
+        }
+        return false;
+    }
+
     // Insert under the home group's stripe lock: erased slots are reused.  Returns the slot, or -1 (present,
-    // refused -- no free slot in the table --, or the lock wait gave up, which sets an error bit).
+    // refused -- no free slot in the table --, or the lock wait gave up, which sets an error bit).  As the
+    // reference checks contains() and full() before it locks (unordered_base_detail.cuh:708-720, :958-994),
+    // a key found present, or a table with no free slot along the key's probe sequence, is decided by one
+    // scan without the lock, so inserts of present keys and inserts into a full table do not queue on it.
     __device__ int64_t
     insert_slot_locked(key_type key, mapped_type mapped) const
     {
         const int64_t home = home_group(key);
+        {
+            int64_t target = -1;
+            bool target_tomb = false;
+            if (scan_for_insert(key, home, target, target_tomb))
+            {
+                return -1; // present
+            }
+            if (target < 0)
+            {
+                atomicAdd(&header()->refused, 1ull);
+                return -1;
+            }
+        }
         if (!lock_group(home))
         {
             atomicOr(&header()->error, detail::kErrRetry);
@@ -276,40 +337,9 @@ struct unordered_ref
         bool refused = false;
         for (int attempt = 0; attempt < 65536; ++attempt)
         {
-            // the key along its probe sequence, up to the first group holding a never-used slot, and the first
-            // free slot (erased below max_size(), or never used) on the way
-            int64_t g = home;
             int64_t target = -1;
             bool target_tomb = false;
-            bool present = false;
-            for (int64_t probes = 0; probes < v.num_groups && !present; ++probes)
-            {
-                const uint4* p = group_ptr(g);
-                bool any_empty = false;
-#pragma unroll
-                for (int l = 0; l < detail::kTileLanes; ++l)
-                {
-                    const uint4 d = __ldcg(p + l);
-#pragma unroll
-                    for (int s = 0; s < SPL; ++s)
-                    {
-                        const key_type k = detail::key_in_lane<KIND>(d, s);
-                        const int64_t slot = g * G + l * SPL + s;
-                        present |= k == key;
-                        any_empty |= k == C::empty_key;
-                        if (target < 0 && (k == C::empty_key || (k == C::tomb_key && slot < v.total_count)))
-                        {
-                            target = slot;
-                            target_tomb = k == C::tomb_key;
-                        }
-                    }
-                }
-                if (any_empty)
-                {
-                    break;
-                }
-                g = detail::next_group(g, v.num_groups);
-            }
+            const bool present = scan_for_insert(key, home, target, target_tomb);
             if (present)
             {
                 break;
