@@ -49,6 +49,28 @@ ld_stream(const T* p)
     return __ldcs(p);
 }
 
+// A ring slot's turn word read without ordering (a fence_gpu after the reads orders what follows), and
+// stored without ordering (a fence_gpu before the stores orders what precedes).
+SG_D unsigned
+load_turn_relaxed(const unsigned* p)
+{
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+SG_D void
+store_turn_relaxed(unsigned* p, unsigned v)
+{
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+SG_D void
+fence_gpu()
+{
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
+
 // ---------------------------------------------------------------- block reservations
 //
 // A block takes a tile of kItems x kCThreads elements, element tile + j * kCThreads + threadIdx.x being
@@ -185,8 +207,14 @@ reserve(long long* counter, long long bound, long long want, bool grow)
 // Mixed launch: element i pushes values[i] when is_push[i] != 0 (or is_push == NULL), else pops.  Each
 // tile reserves its pushes and its pops once; the tile's pushes take consecutive tickets in element
 // order, and so do its pops.
+// resident blocks per SM the mixed deque launch is compiled for (its fast path keeps 8 tickets per thread in
+// registers)
+#ifndef SG_DEQUE_MIN_BLOCKS
+#define SG_DEQUE_MIN_BLOCKS 2
+#endif
+
 template <typename T>
-__global__ void __launch_bounds__(kCThreads)
+__global__ void __launch_bounds__(kCThreads, SG_DEQUE_MIN_BLOCKS)
 k_deque_ops(T* data, unsigned* seq, deque_counters* c, int64_t cap, const uint8_t* is_push, const T* values,
             int64_t n, T* out_popped, uint8_t* out_ok)
 {
@@ -248,27 +276,41 @@ k_deque_ops(T* data, unsigned* seq, deque_counters* c, int64_t cap, const uint8_
         const long long pop_ok = s_pop_ok;
         const unsigned long long push_t0 = s_push_t0;
         const unsigned long long pop_t0 = s_pop_t0;
-#pragma unroll 1
+        // The thread's tickets: slot, the turn that lets the element go on, the turn it leaves.  All turns
+        // are read at once (relaxed, then one fence); when every one of them is already there -- the usual
+        // case, each slot's previous operation having finished in an earlier tile or launch -- the elements
+        // are moved, one fence orders those moves before the turns, and the turns are stored.  Otherwise the
+        // thread takes its elements one by one with bounded waits, each releasing its turn at once, since one
+        // of its elements may wait for a turn another of them leaves.
+        int64_t pos[kItems];
+        unsigned want[kItems];
+        unsigned after[kItems];
+        int kind[kItems]; // 0 none, 1 push, 2 pop
+        T pv[kItems];
+        bool ready = true;
+#pragma unroll
         for (int j = 0; j < kItems; ++j)
         {
             const int64_t i = tile + j * kCThreads + threadIdx.x;
             const unsigned bit = 1u << lane;
             const unsigned pm = mpush[j * kWarps + warp];
             const unsigned qm = mpop[j * kWarps + warp];
-            bool ok = false;
+            kind[j] = 0;
+            pos[j] = 0;
+            want[j] = 0;
+            after[j] = 0;
+            pv[j] = T{};
             if (pm & bit)
             {
                 const long long r = cpush[j * kWarps + warp] + __popc(pm & lanemask_lt());
                 if (r < push_ok)
                 {
                     const unsigned long long tk = push_t0 + static_cast<unsigned long long>(r);
-                    const int64_t pos = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
-                    if (wait_turn(seq + pos, static_cast<unsigned>(tk), &c->error))
-                    {
-                        data[pos] = values[i];
-                        store_turn(seq + pos, static_cast<unsigned>(tk + 1));
-                        ok = true;
-                    }
+                    pos[j] = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
+                    want[j] = static_cast<unsigned>(tk);
+                    after[j] = static_cast<unsigned>(tk + 1);
+                    kind[j] = 1;
+                    pv[j] = ld_stream(values + i);
                 }
             }
             else if (qm & bit)
@@ -277,22 +319,101 @@ k_deque_ops(T* data, unsigned* seq, deque_counters* c, int64_t cap, const uint8_
                 if (r < pop_ok)
                 {
                     const unsigned long long tk = pop_t0 + static_cast<unsigned long long>(r);
-                    const int64_t pos = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
-                    if (wait_turn(seq + pos, static_cast<unsigned>(tk + 1), &c->error))
-                    {
-                        const T v = *reinterpret_cast<volatile T*>(data + pos);
-                        store_turn(seq + pos, static_cast<unsigned>(tk + static_cast<unsigned long long>(cap)));
-                        if (out_popped != nullptr)
-                        {
-                            out_popped[i] = v;
-                        }
-                        ok = true;
-                    }
+                    pos[j] = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
+                    want[j] = static_cast<unsigned>(tk + 1);
+                    after[j] = static_cast<unsigned>(tk + static_cast<unsigned long long>(cap));
+                    kind[j] = 2;
                 }
             }
-            if (i < n && out_ok != nullptr)
+            if (kind[j] != 0)
             {
-                out_ok[i] = static_cast<uint8_t>(ok);
+                const unsigned cur = load_turn_relaxed(seq + pos[j]); // independent loads, all in flight
+                ready = ready & (cur == want[j]);
+            }
+        }
+        if (ready)
+        {
+            fence_gpu(); // the turns read above come before the element accesses below
+#pragma unroll
+            for (int j = 0; j < kItems; ++j)
+            {
+                if (kind[j] == 1)
+                {
+                    data[pos[j]] = pv[j];
+                }
+                else if (kind[j] == 2)
+                {
+                    pv[j] = __ldcg(data + pos[j]);
+                }
+            }
+            fence_gpu(); // the element accesses above come before the turns that hand the slots on
+#pragma unroll
+            for (int j = 0; j < kItems; ++j)
+            {
+                const int64_t i = tile + j * kCThreads + threadIdx.x;
+                if (kind[j] != 0)
+                {
+                    store_turn_relaxed(seq + pos[j], after[j]);
+                }
+                if (kind[j] == 2 && out_popped != nullptr)
+                {
+                    out_popped[i] = pv[j];
+                }
+                if (i < n && out_ok != nullptr)
+                {
+                    out_ok[i] = static_cast<uint8_t>(kind[j] != 0);
+                }
+            }
+        }
+        else
+        {
+            // one by one, the tickets read again from the tile's counts in shared memory (no local arrays)
+#pragma unroll 1
+            for (int j = 0; j < kItems; ++j)
+            {
+                const int64_t i = tile + j * kCThreads + threadIdx.x;
+                const unsigned bit = 1u << lane;
+                const unsigned pm = mpush[j * kWarps + warp];
+                const unsigned qm = mpop[j * kWarps + warp];
+                bool ok = false;
+                if (pm & bit)
+                {
+                    const long long r = cpush[j * kWarps + warp] + __popc(pm & lanemask_lt());
+                    if (r < push_ok)
+                    {
+                        const unsigned long long tk = push_t0 + static_cast<unsigned long long>(r);
+                        const int64_t at = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
+                        if (wait_turn(seq + at, static_cast<unsigned>(tk), &c->error))
+                        {
+                            data[at] = values[i];
+                            store_turn(seq + at, static_cast<unsigned>(tk + 1));
+                            ok = true;
+                        }
+                    }
+                }
+                else if (qm & bit)
+                {
+                    const long long r = cpop[j * kWarps + warp] + __popc(qm & lanemask_lt());
+                    if (r < pop_ok)
+                    {
+                        const unsigned long long tk = pop_t0 + static_cast<unsigned long long>(r);
+                        const int64_t at = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
+                        if (wait_turn(seq + at, static_cast<unsigned>(tk + 1), &c->error))
+                        {
+                            const T v = *reinterpret_cast<volatile T*>(data + at);
+                            store_turn(seq + at, static_cast<unsigned>(tk + static_cast<unsigned long long>(cap)));
+                            if (out_popped != nullptr)
+                            {
+                                out_popped[i] = v;
+                            }
+                            ok = true;
+                        }
+                    }
+                }
+                if (i < n && out_ok != nullptr)
+                {
+                    out_ok[i] = static_cast<uint8_t>(ok);
+                }
             }
         }
         __syncthreads(); // the counts and reservations are rewritten by the next tile
