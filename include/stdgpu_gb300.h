@@ -391,10 +391,14 @@ SG_API sg_status sg_server_submit_many(sg_server* server, const sg_request* requ
 SG_API sg_status sg_server_set_paused(sg_server* server, int32_t paused);
 /* Request-size policy: a table's run of same-operation requests with at least direct_keys keys runs as
  * its own launches of at most chunk_keys keys each on one of direct_streams (1..n_streams) low-priority
- * streams, with at most max_direct (1..16) such runs issued and not complete; defaults 65536, 4194304, 4
- * and 1 (large runs back to back in arrival order of their oldest requests). */
+ * streams, with at most max_direct (1..16) such runs issued and not complete; defaults 65536, 4194304, 8
+ * and 4. */
 SG_API sg_status sg_server_set_policy(sg_server* server, int64_t direct_keys, int64_t chunk_keys, int32_t max_direct,
                                       int32_t direct_streams);
+/* Growing ahead (default on): a table that an insert or erase run left more than half full, with no request
+ * waiting, grows to the next doubling of its capacity while it is idle, within the budget as it stands, so a
+ * later insert does not wait for the rehash. */
+SG_API sg_status sg_server_set_grow_ahead(sg_server* server, int32_t enabled);
 /* Waits (timeout_ms < 0: no limit) for a ticket; out_request_status: SG_OK or SG_ERR_BUDGET (refused). */
 SG_API sg_status sg_server_wait(sg_server* server, int64_t ticket, int32_t timeout_ms, sg_status* out_request_status);
 /* Waits for every submitted request. */

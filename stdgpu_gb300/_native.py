@@ -140,6 +140,7 @@ SIGNATURES = {
     "sg_server_submit_many": (c_int32, [c_void_p, POINTER(sg_request), c_int32, POINTER(c_int64)]),
     "sg_server_set_paused": (c_int32, [c_void_p, c_int32]),
     "sg_server_set_policy": (c_int32, [c_void_p, c_int64, c_int64, c_int32, c_int32]),
+    "sg_server_set_grow_ahead": (c_int32, [c_void_p, c_int32]),
     "sg_server_wait": (c_int32, [c_void_p, c_int64, c_int32, POINTER(c_int32)]),
     "sg_server_drain": (c_int32, [c_void_p, c_int32]),
     "sg_server_get_stats": (c_int32, [c_void_p, POINTER(sg_server_stats)]),

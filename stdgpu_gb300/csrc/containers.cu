@@ -212,6 +212,10 @@ reserve(long long* counter, long long bound, long long want, bool grow)
 #ifndef SG_DEQUE_MIN_BLOCKS
 #define SG_DEQUE_MIN_BLOCKS 2
 #endif
+// 0: every element takes the one-by-one path (for comparison)
+#ifndef SG_DEQUE_FAST
+#define SG_DEQUE_FAST 1
+#endif
 
 template <typename T>
 __global__ void __launch_bounds__(kCThreads, SG_DEQUE_MIN_BLOCKS)
@@ -328,7 +332,7 @@ k_deque_ops(T* data, unsigned* seq, deque_counters* c, int64_t cap, const uint8_
             if (kind[j] != 0)
             {
                 const unsigned cur = load_turn_relaxed(seq + pos[j]); // independent loads, all in flight
-                ready = ready & (cur == want[j]);
+                ready = ready & (cur == want[j]) & (SG_DEQUE_FAST != 0);
             }
         }
         if (ready)

@@ -70,13 +70,17 @@ class server:
             self._live[tk] = it
         return out
 
-    def set_policy(self, direct_keys: int = 1 << 16, chunk_keys: int = 1 << 22, max_direct: int = 4,
-                   direct_streams: int = 1) -> None:
+    def set_policy(self, direct_keys: int = 1 << 16, chunk_keys: int = 1 << 22, max_direct: int = 8,
+                   direct_streams: int = 4) -> None:
         """Runs of at least direct_keys keys run as their own launches of at most chunk_keys keys on one of
         direct_streams low-priority streams, at most max_direct of them issued and not complete
         (sg_server_set_policy)."""
         N.check(N.load().sg_server_set_policy(self._h, int(direct_keys), int(chunk_keys), int(max_direct),
                                               int(direct_streams)), "server::set_policy")
+
+    def set_grow_ahead(self, enabled: bool) -> None:
+        """Growing ahead of idle tables more than half full (sg_server_set_grow_ahead; on by default)."""
+        N.check(N.load().sg_server_set_grow_ahead(self._h, int(bool(enabled))), "server::set_grow_ahead")
 
     def pause(self, paused: bool = True) -> None:
         N.check(N.load().sg_server_set_paused(self._h, int(bool(paused))), "server::pause")
