@@ -612,11 +612,12 @@ def other_configs(args) -> dict:
     """The other benchmark configurations, each run once on this GPU after the voxel step, so that one
     invocation records them all: the L2-resident small set (with the reference's CPU time of the same
     configuration), the 4096 many-small-tables step (batched and graph forms against the plain per-table
-    calls from a C++ loop), and the served request stream (server against serial plain calls).  A part that
-    fails reports why instead of its numbers."""
+    calls from a C++ loop), the served request stream (server against serial plain calls), and the large
+    mixed workload (capacity-2^30 map at three loads, vector, deque, bitset).  A part that fails reports why
+    instead of its numbers."""
     import torch
 
-    from stdgpu_gb300 import batch_bench, serve_bench, small_bench
+    from stdgpu_gb300 import batch_bench, large_bench, serve_bench, small_bench
 
     def small():
         r = small_bench.run(steps=20, warmup=5)
@@ -650,8 +651,13 @@ def other_configs(args) -> dict:
                 "p50_us": ul["server_p50_us"], "p99_us": ul["server_p99_us"],
                 "serial_p50_us": ul["serial_p50_us"], "serial_p99_us": ul["serial_p99_us"], "detail": r}
 
+    def large():
+        r = large_bench.run(full=True)
+        return {"value": r["map"][-2]["find_mops"], "unit": UNIT, "detail": r,
+                "note": "value: find M keys/s of the capacity-2^30 map at 0.9 load; per part in detail"}
+
     out = {}
-    for name, fn in (("small", small), ("batched", batched), ("serve", serve)):
+    for name, fn in (("small", small), ("batched", batched), ("serve", serve), ("large", large)):
         t0 = time.perf_counter()
         try:
             out[name] = fn()

@@ -372,6 +372,7 @@ typedef struct sg_server_stats
     int64_t hbm_used_bytes;
     double grow_host_us;     /* scheduler time spent launching grows (allocation of the new table included) */
     double max_grow_host_us; /* the longest of them */
+    double grow_create_us;   /* the grow thread's time creating the grown tables (their allocation included) */
 } sg_server_stats;
 
 SG_API sg_status sg_server_create(int32_t kind, int64_t hbm_budget_bytes, int32_t n_streams, int32_t n_slots,

@@ -75,7 +75,7 @@ class sg_server_stats(ctypes.Structure):
                 ("p99_us", ctypes.c_double), ("max_us", ctypes.c_double), ("keys_per_s", ctypes.c_double),
                 ("launches", c_int64), ("waves", c_int64), ("refused_budget", c_int64), ("rehashes", c_int64),
                 ("hbm_used_bytes", c_int64), ("grow_host_us", ctypes.c_double),
-                ("max_grow_host_us", ctypes.c_double)]
+                ("max_grow_host_us", ctypes.c_double), ("grow_create_us", ctypes.c_double)]
 
 
 # name -> (restype, argtypes); every symbol the header declares

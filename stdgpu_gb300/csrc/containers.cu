@@ -210,7 +210,7 @@ reserve(long long* counter, long long bound, long long want, bool grow)
 // resident blocks per SM the mixed deque launch is compiled for (its fast path keeps 8 tickets per thread in
 // registers)
 #ifndef SG_DEQUE_MIN_BLOCKS
-#define SG_DEQUE_MIN_BLOCKS 2
+#define SG_DEQUE_MIN_BLOCKS 4
 #endif
 // 0: every element takes the one-by-one path (for comparison)
 #ifndef SG_DEQUE_FAST
@@ -280,41 +280,39 @@ k_deque_ops(T* data, unsigned* seq, deque_counters* c, int64_t cap, const uint8_
         const long long pop_ok = s_pop_ok;
         const unsigned long long push_t0 = s_push_t0;
         const unsigned long long pop_t0 = s_pop_t0;
-        // The thread's tickets: slot, the turn that lets the element go on, the turn it leaves.  All turns
-        // are read at once (relaxed, then one fence); when every one of them is already there -- the usual
-        // case, each slot's previous operation having finished in an earlier tile or launch -- the elements
-        // are moved, one fence orders those moves before the turns, and the turns are stored.  Otherwise the
-        // thread takes its elements one by one with bounded waits, each releasing its turn at once, since one
-        // of its elements may wait for a turn another of them leaves.
-        int64_t pos[kItems];
-        unsigned want[kItems];
-        unsigned after[kItems];
-        int kind[kItems]; // 0 none, 1 push, 2 pop
-        T pv[kItems];
+        // The thread's tickets: slot and low 32 bits of the ticket (a push waits for turn tk and leaves
+        // tk + 1, a pop waits for tk + 1 and leaves tk + capacity; capacity < 2^31).  All turns are read at
+        // once (relaxed, then one fence); when every one of them is already there -- the usual case, each
+        // slot's previous operation having finished in an earlier tile or launch -- the elements are moved,
+        // one fence orders those moves before the turns, and the turns are stored.  Otherwise the thread
+        // takes its elements one by one with bounded waits, each releasing its turn at once, since one of
+        // its elements may wait for a turn another of them leaves.
+        unsigned pos[kItems];
+        unsigned tk32[kItems];
+        unsigned pushes = 0u; // bit j: item j is a push with a ticket
+        unsigned pops = 0u;   // bit j: item j is a pop with a ticket
         bool ready = true;
 #pragma unroll
         for (int j = 0; j < kItems; ++j)
         {
-            const int64_t i = tile + j * kCThreads + threadIdx.x;
             const unsigned bit = 1u << lane;
             const unsigned pm = mpush[j * kWarps + warp];
             const unsigned qm = mpop[j * kWarps + warp];
-            kind[j] = 0;
-            pos[j] = 0;
-            want[j] = 0;
-            after[j] = 0;
-            pv[j] = T{};
+            pos[j] = 0u;
+            tk32[j] = 0u;
+            unsigned want = 0u;
+            bool live = false;
             if (pm & bit)
             {
                 const long long r = cpush[j * kWarps + warp] + __popc(pm & lanemask_lt());
                 if (r < push_ok)
                 {
                     const unsigned long long tk = push_t0 + static_cast<unsigned long long>(r);
-                    pos[j] = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
-                    want[j] = static_cast<unsigned>(tk);
-                    after[j] = static_cast<unsigned>(tk + 1);
-                    kind[j] = 1;
-                    pv[j] = ld_stream(values + i);
+                    pos[j] = static_cast<unsigned>(tk % static_cast<unsigned long long>(cap));
+                    tk32[j] = static_cast<unsigned>(tk);
+                    want = tk32[j];
+                    pushes |= 1u << j;
+                    live = true;
                 }
             }
             else if (qm & bit)
@@ -323,16 +321,17 @@ k_deque_ops(T* data, unsigned* seq, deque_counters* c, int64_t cap, const uint8_
                 if (r < pop_ok)
                 {
                     const unsigned long long tk = pop_t0 + static_cast<unsigned long long>(r);
-                    pos[j] = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
-                    want[j] = static_cast<unsigned>(tk + 1);
-                    after[j] = static_cast<unsigned>(tk + static_cast<unsigned long long>(cap));
-                    kind[j] = 2;
+                    pos[j] = static_cast<unsigned>(tk % static_cast<unsigned long long>(cap));
+                    tk32[j] = static_cast<unsigned>(tk);
+                    want = tk32[j] + 1u;
+                    pops |= 1u << j;
+                    live = true;
                 }
             }
-            if (kind[j] != 0)
+            if (live)
             {
                 const unsigned cur = load_turn_relaxed(seq + pos[j]); // independent loads, all in flight
-                ready = ready & (cur == want[j]) & (SG_DEQUE_FAST != 0);
+                ready = ready & (cur == want) & (SG_DEQUE_FAST != 0);
             }
         }
         if (ready)
@@ -341,31 +340,35 @@ k_deque_ops(T* data, unsigned* seq, deque_counters* c, int64_t cap, const uint8_
 #pragma unroll
             for (int j = 0; j < kItems; ++j)
             {
-                if (kind[j] == 1)
+                const int64_t i = tile + j * kCThreads + threadIdx.x;
+                if (pushes & (1u << j))
                 {
-                    data[pos[j]] = pv[j];
+                    data[pos[j]] = ld_stream(values + i);
                 }
-                else if (kind[j] == 2)
+                else if (pops & (1u << j))
                 {
-                    pv[j] = __ldcg(data + pos[j]);
+                    const T v = __ldcg(data + pos[j]);
+                    if (out_popped != nullptr)
+                    {
+                        out_popped[i] = v;
+                    }
+                }
+                if (i < n && out_ok != nullptr)
+                {
+                    out_ok[i] = static_cast<uint8_t>(((pushes | pops) >> j) & 1u);
                 }
             }
             fence_gpu(); // the element accesses above come before the turns that hand the slots on
 #pragma unroll
             for (int j = 0; j < kItems; ++j)
             {
-                const int64_t i = tile + j * kCThreads + threadIdx.x;
-                if (kind[j] != 0)
+                if (pushes & (1u << j))
                 {
-                    store_turn_relaxed(seq + pos[j], after[j]);
+                    store_turn_relaxed(seq + pos[j], tk32[j] + 1u);
                 }
-                if (kind[j] == 2 && out_popped != nullptr)
+                else if (pops & (1u << j))
                 {
-                    out_popped[i] = pv[j];
-                }
-                if (i < n && out_ok != nullptr)
-                {
-                    out_ok[i] = static_cast<uint8_t>(kind[j] != 0);
+                    store_turn_relaxed(seq + pos[j], tk32[j] + static_cast<unsigned>(cap));
                 }
             }
         }

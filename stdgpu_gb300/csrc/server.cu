@@ -319,6 +319,9 @@ namespace
 using clock_type = std::chrono::steady_clock;
 
 constexpr int kSlotSegments = 4096; // segments one packed launch can carry
+#ifndef SG_SERVER_POOL
+#define SG_SERVER_POOL 1
+#endif
 // Request-size policy defaults (sg_server_set_policy): a table's run of same-operation requests with at
 // least kDefaultDirectKeys keys runs as its own launches (cut into launches of at most kDefaultChunkKeys
 // keys) on one of kDefaultDirectStreams low-priority streams, at most kDefaultMaxDirect such runs issued and
@@ -457,6 +460,14 @@ struct sg_server
     std::deque<grow_job> grow_jobs;
     std::condition_variable cv_grow;
     int device = 0;
+    // The tables' storage: a stream-ordered memory pool that keeps what it frees (release threshold
+    // unlimited), so a grow after the first few takes its block from storage that earlier grows released
+    // instead of mapping new memory.  Each allocation completes on its own idle stream before the table is
+    // used elsewhere; a release follows a device synchronisation, as for every table.
+    cudaMemPool_t pool = nullptr;
+    cudaStream_t alloc_stream = nullptr;
+    sg_allocator table_alloc{};
+    double grow_thread_us = 0.0; // grow thread: time creating tables (allocation included)
 
     request_rec&
     rec(int64_t ticket)
@@ -484,6 +495,39 @@ struct sg_server
 
 namespace
 {
+
+void*
+pool_alloc(size_t bytes, void* ctx)
+{
+    auto* srv = static_cast<sg_server*>(ctx);
+    void* p = nullptr;
+    if (cudaMallocFromPoolAsync(&p, bytes, srv->pool, srv->alloc_stream) != cudaSuccess ||
+        cudaStreamSynchronize(srv->alloc_stream) != cudaSuccess)
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+
+void
+pool_release(void* p, void* ctx)
+{
+    auto* srv = static_cast<sg_server*>(ctx);
+    cudaFreeAsync(p, srv->alloc_stream); // the caller synchronised the device first
+}
+
+// A table of the server's kind and the given capacity, its storage from the server's pool (or the library's
+// allocator when the pool could not be made).
+sg_status
+create_server_table(sg_server* srv, int64_t capacity, void* stream, sg_unordered** out)
+{
+    if (srv->pool == nullptr)
+    {
+        return sg_unordered_create(srv->kind, capacity, stream, out);
+    }
+    return sg_unordered_create_with_allocator(srv->kind, capacity, 0, &srv->table_alloc, stream, out);
+}
 
 int64_t
 table_bytes(int32_t kind, int64_t capacity, int64_t* max_size)
@@ -752,7 +796,9 @@ sg_server::run_grows()
         grow_jobs.pop_front();
         lock.unlock();
         sg_unordered* nh = nullptr;
-        sg_status st = sg_unordered_create(kind, job.capacity, grow_stream, &nh);
+        const auto c0 = clock_type::now();
+        sg_status st = create_server_table(this, job.capacity, grow_stream, &nh);
+        const double create_us = std::chrono::duration<double, std::micro>(clock_type::now() - c0).count();
         if (st == SG_OK)
         {
             st = launch_migrate(kind, kernel_view(job.old), kernel_view(nh), grid_cap, grow_stream);
@@ -769,6 +815,7 @@ sg_server::run_grows()
         }
         cudaGetLastError();
         lock.lock();
+        grow_thread_us += create_us;
         grow_done(job, nh);
         lock.unlock();
         submissions.fetch_add(1, std::memory_order_release); // wakes the scheduler's spin
@@ -1211,6 +1258,26 @@ sg_server_create(int32_t kind, int64_t hbm_budget_bytes, int32_t n_streams, int3
         cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, least);
     }
     cudaStreamCreateWithPriority(&srv->grow_stream, cudaStreamNonBlocking, least);
+#if SG_SERVER_POOL
+    {
+        cudaMemPoolProps props{};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = srv->device;
+        if (cudaMemPoolCreate(&srv->pool, &props) == cudaSuccess)
+        {
+            unsigned long long keep = ~0ull;
+            cudaMemPoolSetAttribute(srv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            cudaStreamCreateWithFlags(&srv->alloc_stream, cudaStreamNonBlocking);
+            srv->table_alloc = sg_allocator{ &pool_alloc, &pool_release, srv, nullptr };
+        }
+        else
+        {
+            srv->pool = nullptr;
+            cudaGetLastError();
+        }
+    }
+#endif
     srv->units = std::vector<direct_unit>(kMaxDirectLimit);
     if (cudaMallocHost(&srv->unit_sizes, sizeof(unsigned long long) * kMaxDirectLimit) != cudaSuccess)
     {
@@ -1283,6 +1350,16 @@ sg_server_destroy(sg_server* srv)
     for (auto& kv : srv->tables)
     {
         sg_unordered_destroy(kv.second.h);
+    }
+    srv->tables.clear();
+    if (srv->alloc_stream != nullptr)
+    {
+        cudaStreamSynchronize(srv->alloc_stream);
+        cudaStreamDestroy(srv->alloc_stream);
+    }
+    if (srv->pool != nullptr)
+    {
+        cudaMemPoolDestroy(srv->pool);
     }
     for (auto& sl : srv->slots)
     {
@@ -1386,7 +1463,7 @@ sg_server_admit_table(sg_server* srv, int32_t table, int64_t capacity)
         return SG_ERR_BUDGET;
     }
     table_rec t;
-    const sg_status st = sg_unordered_create(srv->kind, capacity, nullptr, &t.h);
+    const sg_status st = create_server_table(srv, capacity, nullptr, &t.h);
     if (st != SG_OK)
     {
         return st;
@@ -1582,6 +1659,7 @@ sg_server_get_stats(sg_server* srv, sg_server_stats* out)
     out->hbm_used_bytes = srv->used;
     out->grow_host_us = srv->grow_host_us;
     out->max_grow_host_us = srv->max_grow_host_us;
+    out->grow_create_us = srv->grow_thread_us;
     return SG_OK;
 }
 

@@ -188,6 +188,7 @@ def run(n_requests=600, seed=0, load=0.8, min_n=1 << 10, max_n=1 << 22, policy: 
             "speedup": wall_ser / wall_srv, "speedup_vs_presized": wall_pre / wall_srv,
             "waves": st_sat["waves"], "launches": st_sat["launches"],
             "grow_host_us": st_sat.get("grow_host_us"), "max_grow_host_us": st_sat.get("max_grow_host_us"),
+            "grow_create_us": st_sat.get("grow_create_us"),
         },
         "policy": policy or "default",
         "under_load": {
