@@ -108,6 +108,52 @@ scan_counts(unsigned* cnt, int lane)
 
 // ---------------------------------------------------------------- vector
 
+// Bulk push_back tiles: kVecItems elements per thread (a tile of 4096), so the shared size counter takes one
+// reservation per 4096 elements -- a counter that every tile hits on one address is what bounds this launch
+// at small tiles (2048-element tiles: 1.17 ms for 2^28 threads with values loaded after the reservation,
+// 0.80 ms with them loaded before it).
+#ifndef SG_VEC_ITEMS
+#define SG_VEC_ITEMS 16
+#endif
+constexpr int kVecItems = SG_VEC_ITEMS;
+constexpr int kVecCounts = kVecItems * kWarps;
+constexpr int64_t kVecTileElems = int64_t{ kVecItems } * kCThreads;
+static_assert(kVecCounts % 32 == 0 && kVecCounts <= 32 * 8, "whole counts per lane of the scanning warp");
+
+// Exclusive scan of cnt[0, kVecCounts) in place by one warp (kVecCounts / 32 consecutive counts per lane);
+// returns the total to every lane.
+SG_D unsigned
+scan_vec_counts(unsigned* cnt, int lane)
+{
+    constexpr int per = kVecCounts / 32;
+    unsigned v[per];
+    unsigned sum = 0u;
+#pragma unroll
+    for (int k = 0; k < per; ++k)
+    {
+        v[k] = cnt[per * lane + k];
+        sum += v[k];
+    }
+    unsigned incl = sum;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1)
+    {
+        const unsigned t = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d)
+        {
+            incl += t;
+        }
+    }
+    unsigned run = incl - sum;
+#pragma unroll
+    for (int k = 0; k < per; ++k)
+    {
+        cnt[per * lane + k] = run;
+        run += v[k];
+    }
+    return __shfl_sync(0xffffffffu, incl, 31);
+}
+
 // Bulk push_back: element i pushes values[i] where pred[i] != 0 (every element without pred).  Per tile the
 // selected values are loaded before the tile's reservation, so their loads are in flight while warp 0 scans
 // the counts and adds the tile's total to the size; a reservation past capacity fails the tile's elements
@@ -118,18 +164,18 @@ __global__ void __launch_bounds__(kCThreads)
 k_vector_push_back(T* data, long long* size, int64_t cap, const T* values, const uint8_t* pred, int64_t n,
                    uint8_t* out_pushed)
 {
-    __shared__ unsigned cnt[2][kCounts];
+    __shared__ unsigned cnt[2][kVecCounts];
     __shared__ long long s_base[2];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     int buf = 0;
-    for (int64_t tile = static_cast<int64_t>(blockIdx.x) * kTileElems; tile < n;
-         tile += static_cast<int64_t>(gridDim.x) * kTileElems, buf ^= 1)
+    for (int64_t tile = static_cast<int64_t>(blockIdx.x) * kVecTileElems; tile < n;
+         tile += static_cast<int64_t>(gridDim.x) * kVecTileElems, buf ^= 1)
     {
-        unsigned masks[kItems];
-        T vals[kItems];
+        unsigned masks[kVecItems];
+        T vals[kVecItems];
 #pragma unroll
-        for (int j = 0; j < kItems; ++j)
+        for (int j = 0; j < kVecItems; ++j)
         {
             const int64_t i = tile + j * kCThreads + threadIdx.x;
             const bool want = i < n && (pred == nullptr || pred[i] != 0);
@@ -143,7 +189,7 @@ k_vector_push_back(T* data, long long* size, int64_t cap, const T* values, const
         __syncthreads();
         if (warp == 0)
         {
-            const unsigned total = scan_counts(cnt[buf], lane);
+            const unsigned total = scan_vec_counts(cnt[buf], lane);
             if (lane == 0)
             {
                 // one reservation for the tile (vector_detail.cuh:186-195)
@@ -155,7 +201,7 @@ k_vector_push_back(T* data, long long* size, int64_t cap, const T* values, const
         __syncthreads();
         const long long base = s_base[buf];
 #pragma unroll
-        for (int j = 0; j < kItems; ++j)
+        for (int j = 0; j < kVecItems; ++j)
         {
             const int64_t i = tile + j * kCThreads + threadIdx.x;
             const bool want = (masks[j] >> lane) & 1u;
@@ -1007,14 +1053,14 @@ sg_vector_push_back(sg_vector* v, const void* values, const uint8_t* pred, int64
     if (v->elem_bytes == 4)
     {
         static const int mg = persistent_grid(k_vector_push_back<uint32_t>, kCThreads);
-        k_vector_push_back<uint32_t><<<grid_for(n, static_cast<int>(kTileElems), mg), kCThreads, 0, s>>>(
+        k_vector_push_back<uint32_t><<<grid_for(n, static_cast<int>(kVecTileElems), mg), kCThreads, 0, s>>>(
                 static_cast<uint32_t*>(v->data), v->size, v->capacity, static_cast<const uint32_t*>(values), pred, n,
                 out_pushed);
     }
     else
     {
         static const int mg = persistent_grid(k_vector_push_back<unsigned long long>, kCThreads);
-        k_vector_push_back<unsigned long long><<<grid_for(n, static_cast<int>(kTileElems), mg), kCThreads, 0, s>>>(
+        k_vector_push_back<unsigned long long><<<grid_for(n, static_cast<int>(kVecTileElems), mg), kCThreads, 0, s>>>(
                 static_cast<unsigned long long*>(v->data), v->size, v->capacity,
                 static_cast<const unsigned long long*>(values), pred, n, out_pushed);
     }
