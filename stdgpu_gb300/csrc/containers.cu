@@ -256,7 +256,7 @@ reserve(long long* counter, long long bound, long long want, bool grow)
 // resident blocks per SM the mixed deque launch is compiled for (its fast path keeps 8 tickets per thread in
 // registers)
 #ifndef SG_DEQUE_MIN_BLOCKS
-#define SG_DEQUE_MIN_BLOCKS 4
+#define SG_DEQUE_MIN_BLOCKS 5
 #endif
 // 0: every element takes the one-by-one path (for comparison)
 #ifndef SG_DEQUE_FAST
