@@ -108,12 +108,12 @@ scan_counts(unsigned* cnt, int lane)
 
 // ---------------------------------------------------------------- vector
 
-// Bulk push_back tiles: kVecItems elements per thread (a tile of 4096), so the shared size counter takes one
-// reservation per 4096 elements -- a counter that every tile hits on one address is what bounds this launch
-// at small tiles (2048-element tiles: 1.17 ms for 2^28 threads with values loaded after the reservation,
-// 0.80 ms with them loaded before it).
+// Bulk push_back tiles: kVecItems elements per thread, one reservation on the shared size counter per tile.
+// Measured for 2^28 threads (30 % push) on one box: 8 items (2048-element tiles) 0.80 ms, 12 items 1.31 ms,
+// 16 items 1.33 ms -- larger tiles cost registers and resident warps more than their fewer reservations
+// save; 8 items with the values loaded after the reservation took 1.18 ms.
 #ifndef SG_VEC_ITEMS
-#define SG_VEC_ITEMS 16
+#define SG_VEC_ITEMS 8
 #endif
 constexpr int kVecItems = SG_VEC_ITEMS;
 constexpr int kVecCounts = kVecItems * kWarps;
@@ -254,9 +254,10 @@ reserve(long long* counter, long long bound, long long want, bool grow)
 // tile reserves its pushes and its pops once; the tile's pushes take consecutive tickets in element
 // order, and so do its pops.
 // resident blocks per SM the mixed deque launch is compiled for (its fast path keeps 8 tickets per thread in
-// registers)
+// registers); measured for 2^26 mixed ops: 4 blocks 1.60 ms, 5 blocks 1.40 ms, 6 blocks 1.27 ms, and the
+// one-by-one protocol alone (every element's turn waited for and released in turn) 1.60 ms
 #ifndef SG_DEQUE_MIN_BLOCKS
-#define SG_DEQUE_MIN_BLOCKS 5
+#define SG_DEQUE_MIN_BLOCKS 6
 #endif
 // 0: every element takes the one-by-one path (for comparison)
 #ifndef SG_DEQUE_FAST
