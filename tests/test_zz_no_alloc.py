@@ -38,10 +38,13 @@ def test_noalloc_count_matches_allocating_count_twice():
         nwords = (nbits + 31) // 32
         words = torch.randint(-(2**31), 2**31, (nwords,), dtype=torch.int32, device="cuda", generator=gen)
         out = torch.full((1,), -1, dtype=torch.int64, device="cuda")
+        torch.cuda.synchronize()
+        live = sg.live_device_allocations()
         st = lib.sg_bitset_count_noalloc(ctypes.c_void_p(words.data_ptr()), nbits,
                                          ctypes.c_void_p(out.data_ptr()), stream)
         assert st == N.SG_OK
         torch.cuda.synchronize()
+        assert sg.live_device_allocations() == live  # nothing taken from the library's allocator
         assert int(out.item()) == _count_allocating(lib, words, nbits, stream)
 
 
