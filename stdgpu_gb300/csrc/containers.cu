@@ -109,11 +109,11 @@ scan_counts(unsigned* cnt, int lane)
 // ---------------------------------------------------------------- vector
 
 // Bulk push_back tiles: kVecItems elements per thread, one reservation on the shared size counter per tile.
-// Measured for 2^28 threads (30 % push) on one box: 8 items (2048-element tiles) 0.80 ms, 12 items 1.31 ms,
-// 16 items 1.33 ms -- larger tiles cost registers and resident warps more than their fewer reservations
-// save; 8 items with the values loaded after the reservation took 1.18 ms.
+// Measured for 2^28 threads (30 % push): 4 items (1024-element tiles) 0.69 ms, 8 items 0.80 ms, 12 items
+// 1.31 ms, 16 items 1.33 ms -- larger tiles cost registers and resident warps more than their fewer
+// reservations save; 8 items with the values loaded after the reservation took 1.18 ms.
 #ifndef SG_VEC_ITEMS
-#define SG_VEC_ITEMS 8
+#define SG_VEC_ITEMS 4
 #endif
 constexpr int kVecItems = SG_VEC_ITEMS;
 constexpr int kVecCounts = kVecItems * kWarps;

@@ -201,3 +201,39 @@ def test_back_to_back_grows_release_replaced_storage_for_the_budget():
     assert st["hbm_used_bytes"] <= budget
     assert srv.table_size(0) == len(np.unique(np.concatenate([k1, k2])))
     srv.close()
+
+
+def test_idle_table_past_half_grows_ahead_and_keeps_contents():
+    """An insert that leaves a table more than half full, with nothing else queued for it, lets the idle table
+    grow to the next doubling before another insert arrives; its contents stay, and so does the order of what
+    is submitted meanwhile."""
+    import time as _time
+
+    c = 1 << 12
+    g0 = sg.geometry_for(N.MAP_U64_U64, c)
+    srv = S.server(key="u64", mapped="u64", budget_bytes=4 << 30, n_streams=2, n_slots=4)
+    assert srv.admit(5, c) == N.SG_OK
+    rng = np.random.default_rng(13)
+    keys = np.unique(rng.integers(1, 2**62, size=g0.max_size * 6 // 10, dtype=np.uint64))
+    tk = srv.submit(5, S.INSERT, dev(keys), dev(keys + np.uint64(1)), None, None)
+    assert srv.wait(tk) == N.SG_OK
+    deadline = _time.time() + 10.0
+    while srv.stats()["rehashes"] < 1 and _time.time() < deadline:
+        _time.sleep(0.01)
+    assert srv.stats()["rehashes"] == 1  # grown ahead, with no second insert submitted
+    assert srv.table_view(5).bucket_count > g0.bucket_count
+    ov, of = srv.new_outputs(len(keys))
+    tk = srv.submit(5, S.FIND, dev(keys), None, ov, of)
+    assert srv.wait(tk) == N.SG_OK
+    assert of.cpu().numpy().all()
+    assert np.array_equal(host(ov, np.uint64), keys + np.uint64(1))
+    assert srv.table_size(5) == len(keys)
+    # switched off, a table left the same way stays as it is
+    srv.set_grow_ahead(False)
+    assert srv.admit(6, c) == N.SG_OK
+    tk = srv.submit(6, S.INSERT, dev(keys), dev(keys), None, None)
+    assert srv.wait(tk) == N.SG_OK
+    _time.sleep(0.2)
+    assert srv.stats()["rehashes"] == 1
+    assert srv.table_view(6).bucket_count == g0.bucket_count
+    srv.close()
