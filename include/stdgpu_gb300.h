@@ -441,6 +441,10 @@ typedef struct sg_vector_sync
 
 /* vector::createDeviceObject(capacity): src/stdgpu/impl/vector_detail.cuh (createDeviceObject) */
 SG_API sg_status sg_vector_create(int32_t elem_bytes, int64_t capacity, sg_vector** out);
+/* createDeviceObject(capacity, allocator): sg_vector_create with every device block of the object taken from
+ * `allocator` (sg_allocator; copied; alloc and release non-null, release_ctx called at destroy). */
+SG_API sg_status sg_vector_create_with_allocator(int32_t elem_bytes, int64_t capacity, const sg_allocator* allocator,
+                                       sg_vector** out);
 SG_API sg_status sg_vector_destroy(sg_vector* vec);
 /* Bulk form of the device push_back (src/stdgpu/impl/vector_detail.cuh:181-238): element i is pushed when
  * pred == NULL or pred[i] != 0.  out_pushed (nullable) gets 1 for each element that was stored. */
@@ -494,6 +498,10 @@ typedef struct sg_deque_sync
 
 /* deque::createDeviceObject(capacity): src/stdgpu/impl/deque_detail.cuh (createDeviceObject) */
 SG_API sg_status sg_deque_create(int32_t elem_bytes, int64_t capacity, sg_deque** out);
+/* createDeviceObject(capacity, allocator): sg_deque_create with every device block of the object taken from
+ * `allocator` (sg_allocator; copied; alloc and release non-null, release_ctx called at destroy). */
+SG_API sg_status sg_deque_create_with_allocator(int32_t elem_bytes, int64_t capacity, const sg_allocator* allocator,
+                                       sg_deque** out);
 SG_API sg_status sg_deque_destroy(sg_deque* dq);
 /* Mixed launch: element i does push_back(values[i]) when is_push[i] != 0, else pop_front().
  * deque_detail.cuh:202-258 (push_back) and :388-446 (pop_front).  out_popped / out_ok nullable.

@@ -840,11 +840,27 @@ public:
         return _allocator;
     }
 
-    // createDeviceObject(capacity, allocator): the allocator is kept and returned by get_allocator()
+    // createDeviceObject(capacity, allocator): with an allocator other than the default, every device block of
+    // the vector comes from it (detail::allocator_bridge); get_allocator() returns it
     static vector
     createDeviceObject(const index_t& capacity, const Allocator& allocator)
     {
-        vector x = createDeviceObject(execution::device, capacity);
+        vector x;
+        if constexpr (detail::is_safe_device_allocator<Allocator>::value)
+        {
+            x = createDeviceObject(execution::device, capacity);
+        }
+        else
+        {
+            const sg_allocator a = detail::allocator_bridge<Allocator>::make(allocator);
+            const sg_status st = sg_vector_create_with_allocator(sizeof(T), capacity, &a, &x._handle);
+            if (st != SG_OK)
+            {
+                a.release_ctx(a.ctx);
+            }
+            detail::gb300_check(st, "vector::createDeviceObject");
+            detail::gb300_check(sg_vector_view_of(x._handle, &x._view), "vector::createDeviceObject");
+        }
         x._allocator = allocator;
         return x;
     }
@@ -1187,11 +1203,28 @@ public:
         return _allocator;
     }
 
-    // createDeviceObject(capacity, allocator): the allocator is kept and returned by get_allocator()
+    // createDeviceObject(capacity, allocator): with an allocator other than the default, every device block of
+    // the deque (its ring, and the array device_range() copies into) comes from it; get_allocator() returns it
     static deque
     createDeviceObject(const index_t& capacity, const Allocator& allocator)
     {
-        deque x = createDeviceObject(execution::device, capacity);
+        deque x;
+        if constexpr (detail::is_safe_device_allocator<Allocator>::value)
+        {
+            x = createDeviceObject(execution::device, capacity);
+        }
+        else
+        {
+            const sg_allocator a = detail::allocator_bridge<Allocator>::make(allocator);
+            const sg_status st = sg_deque_create_with_allocator(sizeof(T), capacity, &a, &x._handle);
+            if (st != SG_OK)
+            {
+                a.release_ctx(a.ctx);
+            }
+            detail::gb300_check(st, "deque::createDeviceObject");
+            detail::gb300_check(sg_deque_view_of(x._handle, &x._view), "deque::createDeviceObject");
+            x._alloc = sg_allocator{ a.alloc, a.release, a.ctx, nullptr }; // the deque's handle owns the context
+        }
         x._allocator = allocator;
         return x;
     }
@@ -1220,14 +1253,23 @@ public:
     static void
     destroyDeviceObject(execution::device_policy, deque& d)
     {
+        if (d._range != nullptr && d._alloc.alloc != nullptr)
+        {
+            cudaDeviceSynchronize();
+            d._alloc.release(d._range, d._alloc.ctx); // before the handle drops the allocator's context
+        }
+        else
+        {
+            cudaFree(d._range);
+        }
         if (d._handle != nullptr)
         {
             detail::gb300_check(sg_deque_destroy(d._handle), "deque::destroyDeviceObject");
         }
-        cudaFree(d._range);
         d._handle = nullptr;
         d._view = sg_deque_view{};
         d._range = nullptr;
+        d._alloc = sg_allocator{};
     }
 
     index_t
@@ -1287,8 +1329,15 @@ public:
     {
         if (_range == nullptr && _view.capacity > 0)
         {
-            detail::gb300_check(cudaMalloc(&_range, sizeof(T) * _view.capacity) == cudaSuccess ? SG_OK : SG_ERR_OOM,
-                                "deque::device_range");
+            if (_alloc.alloc != nullptr)
+            {
+                _range = detail::own_alloc<T>(_alloc, sizeof(T) * _view.capacity);
+            }
+            else if (cudaMalloc(&_range, sizeof(T) * _view.capacity) != cudaSuccess)
+            {
+                _range = nullptr;
+            }
+            detail::gb300_check(_range != nullptr ? SG_OK : SG_ERR_OOM, "deque::device_range");
         }
         int64_t n = 0;
         detail::gb300_check(sg_deque_copy_out(_handle, _range, policy.stream, &n), "deque::device_range");
@@ -1570,6 +1619,7 @@ private:
     sg_deque_view _view{};
     Allocator _allocator{};
     T* _range = nullptr;
+    sg_allocator _alloc{}; // the deque's own allocator (createDeviceObject(capacity, allocator)), or none
 };
 
 // stdgpu::queue<T> / stack<T> (src/stdgpu/queue.cuh, stack.cuh): adapters over deque.  queue::push / pop

@@ -148,6 +148,7 @@ SIGNATURES = {
     "sg_server_table_size": (c_int32, [c_void_p, c_int32, POINTER(c_int64)]),
     "sg_server_table_view": (c_int32, [c_void_p, c_int32, POINTER(sg_unordered_view)]),
     "sg_vector_create": (c_int32, [c_int32, c_int64, POINTER(c_void_p)]),
+    "sg_vector_create_with_allocator": (c_int32, [c_int32, c_int64, POINTER(sg_allocator), POINTER(c_void_p)]),
     "sg_vector_pop_back": (c_int32, [c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "sg_vector_insert": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),
     "sg_vector_erase": (c_int32, [c_void_p, c_int64, c_void_p]),
@@ -159,6 +160,7 @@ SIGNATURES = {
     "sg_vector_clear": (c_int32, [c_void_p, c_void_p]),
     "sg_vector_view_of": (c_int32, [c_void_p, POINTER(sg_vector_view)]),
     "sg_deque_create": (c_int32, [c_int32, c_int64, POINTER(c_void_p)]),
+    "sg_deque_create_with_allocator": (c_int32, [c_int32, c_int64, POINTER(sg_allocator), POINTER(c_void_p)]),
     "sg_deque_destroy": (c_int32, [c_void_p]),
     "sg_deque_ops": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "sg_deque_size": (c_int32, [c_void_p, c_void_p, POINTER(c_int64)]),

@@ -839,6 +839,8 @@ struct sg_vector
     uint16_t* slot_state;   // device calls' per-slot words (sg_vector_sync)
     sg_vector_sync* sync;
     uint32_t epoch;         // host copy of sync->epoch
+    object_allocator oa;            // the vector's own allocator (sg_vector_create_with_allocator), or none
+    void (*release_ctx)(void* ctx); // called with oa.ctx when the vector is destroyed (nullable)
 };
 
 struct sg_deque
@@ -852,6 +854,8 @@ struct sg_deque
     uint16_t* slot_state; // device calls' per-slot words (sg_deque_sync)
     sg_deque_sync* sync;
     uint32_t epoch;       // host copy of sync->epoch
+    object_allocator oa;            // the deque's own allocator (sg_deque_create_with_allocator), or none
+    void (*release_ctx)(void* ctx); // called with oa.ctx when the deque is destroyed (nullable)
 };
 
 namespace
@@ -962,8 +966,8 @@ vector_next_epoch(sg_vector* v, cudaStream_t s)
 
 extern "C" {
 
-sg_status
-sg_vector_create(int32_t elem_bytes, int64_t capacity, sg_vector** out)
+static sg_status
+create_vector(int32_t elem_bytes, int64_t capacity, const object_allocator& oa, sg_vector** out)
 {
     if (out == nullptr || (elem_bytes != 4 && elem_bytes != 8) || capacity <= 0)
     {
@@ -977,10 +981,11 @@ sg_vector_create(int32_t elem_bytes, int64_t capacity, sg_vector** out)
     }
     v->elem_bytes = elem_bytes;
     v->capacity = capacity;
-    cudaError_t e = sg::detail::dev_malloc(&v->data, static_cast<size_t>(capacity) * elem_bytes);
+    v->oa = oa;
+    cudaError_t e = sg::detail::obj_malloc(v->oa, &v->data, static_cast<size_t>(capacity) * elem_bytes);
     if (e == cudaSuccess)
     {
-        e = sg::detail::dev_malloc(&v->size, sizeof(long long));
+        e = sg::detail::obj_malloc(v->oa, &v->size, sizeof(long long));
     }
     if (e == cudaSuccess)
     {
@@ -992,7 +997,7 @@ sg_vector_create(int32_t elem_bytes, int64_t capacity, sg_vector** out)
     }
     if (e == cudaSuccess)
     {
-        e = sg::detail::dev_malloc(&v->slot_state, static_cast<size_t>(capacity) * sizeof(uint16_t));
+        e = sg::detail::obj_malloc(v->oa, &v->slot_state, static_cast<size_t>(capacity) * sizeof(uint16_t));
     }
     if (e == cudaSuccess)
     {
@@ -1000,7 +1005,7 @@ sg_vector_create(int32_t elem_bytes, int64_t capacity, sg_vector** out)
     }
     if (e == cudaSuccess)
     {
-        e = sg::detail::dev_malloc(&v->sync, sizeof(sg_vector_sync));
+        e = sg::detail::obj_malloc(v->oa, &v->sync, sizeof(sg_vector_sync));
     }
     if (e == cudaSuccess)
     {
@@ -1019,6 +1024,28 @@ sg_vector_create(int32_t elem_bytes, int64_t capacity, sg_vector** out)
 }
 
 sg_status
+sg_vector_create(int32_t elem_bytes, int64_t capacity, sg_vector** out)
+{
+    return create_vector(elem_bytes, capacity, object_allocator{}, out);
+}
+
+sg_status
+sg_vector_create_with_allocator(int32_t elem_bytes, int64_t capacity, const sg_allocator* allocator, sg_vector** out)
+{
+    if (allocator == nullptr || allocator->alloc == nullptr || allocator->release == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    const sg_status st =
+            create_vector(elem_bytes, capacity, object_allocator{ allocator->alloc, allocator->release, allocator->ctx }, out);
+    if (st == SG_OK)
+    {
+        (*out)->release_ctx = allocator->release_ctx;
+    }
+    return st;
+}
+
+sg_status
 sg_vector_destroy(sg_vector* v)
 {
     if (v == nullptr)
@@ -1026,13 +1053,17 @@ sg_vector_destroy(sg_vector* v)
         return SG_ERR_BAD_ARG;
     }
     cudaDeviceSynchronize();
-    sg::detail::dev_free(v->data);
-    sg::detail::dev_free(v->size);
-    sg::detail::dev_free(v->slot_state);
-    sg::detail::dev_free(v->sync);
+    sg::detail::obj_free(v->oa, v->data);
+    sg::detail::obj_free(v->oa, v->size);
+    sg::detail::obj_free(v->oa, v->slot_state);
+    sg::detail::obj_free(v->oa, v->sync);
     if (v->host != nullptr)
     {
         cudaFreeHost(v->host);
+    }
+    if (v->release_ctx != nullptr)
+    {
+        v->release_ctx(v->oa.ctx);
     }
     delete v;
     return SG_OK;
@@ -1196,8 +1227,8 @@ sg_vector_view_of(const sg_vector* v, sg_vector_view* out)
     return SG_OK;
 }
 
-sg_status
-sg_deque_create(int32_t elem_bytes, int64_t capacity, sg_deque** out)
+static sg_status
+create_deque(int32_t elem_bytes, int64_t capacity, const object_allocator& oa, sg_deque** out)
 {
     if (out == nullptr || (elem_bytes != 4 && elem_bytes != 8) || capacity <= 0 || capacity >= (int64_t{ 1 } << 31))
     {
@@ -1211,14 +1242,15 @@ sg_deque_create(int32_t elem_bytes, int64_t capacity, sg_deque** out)
     }
     d->elem_bytes = elem_bytes;
     d->capacity = capacity;
-    cudaError_t e = sg::detail::dev_malloc(&d->data, static_cast<size_t>(capacity) * elem_bytes);
+    d->oa = oa;
+    cudaError_t e = sg::detail::obj_malloc(d->oa, &d->data, static_cast<size_t>(capacity) * elem_bytes);
     if (e == cudaSuccess)
     {
-        e = sg::detail::dev_malloc(&d->seq, static_cast<size_t>(capacity) * sizeof(unsigned));
+        e = sg::detail::obj_malloc(d->oa, &d->seq, static_cast<size_t>(capacity) * sizeof(unsigned));
     }
     if (e == cudaSuccess)
     {
-        e = sg::detail::dev_malloc(&d->counters, sizeof(deque_counters));
+        e = sg::detail::obj_malloc(d->oa, &d->counters, sizeof(deque_counters));
     }
     if (e == cudaSuccess)
     {
@@ -1226,7 +1258,7 @@ sg_deque_create(int32_t elem_bytes, int64_t capacity, sg_deque** out)
     }
     if (e == cudaSuccess)
     {
-        e = sg::detail::dev_malloc(&d->slot_state, static_cast<size_t>(capacity) * sizeof(uint16_t));
+        e = sg::detail::obj_malloc(d->oa, &d->slot_state, static_cast<size_t>(capacity) * sizeof(uint16_t));
     }
     if (e == cudaSuccess)
     {
@@ -1234,7 +1266,7 @@ sg_deque_create(int32_t elem_bytes, int64_t capacity, sg_deque** out)
     }
     if (e == cudaSuccess)
     {
-        e = sg::detail::dev_malloc(&d->sync, sizeof(sg_deque_sync));
+        e = sg::detail::obj_malloc(d->oa, &d->sync, sizeof(sg_deque_sync));
     }
     if (e == cudaSuccess)
     {
@@ -1257,6 +1289,28 @@ sg_deque_create(int32_t elem_bytes, int64_t capacity, sg_deque** out)
 }
 
 sg_status
+sg_deque_create(int32_t elem_bytes, int64_t capacity, sg_deque** out)
+{
+    return create_deque(elem_bytes, capacity, object_allocator{}, out);
+}
+
+sg_status
+sg_deque_create_with_allocator(int32_t elem_bytes, int64_t capacity, const sg_allocator* allocator, sg_deque** out)
+{
+    if (allocator == nullptr || allocator->alloc == nullptr || allocator->release == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    const sg_status st =
+            create_deque(elem_bytes, capacity, object_allocator{ allocator->alloc, allocator->release, allocator->ctx }, out);
+    if (st == SG_OK)
+    {
+        (*out)->release_ctx = allocator->release_ctx;
+    }
+    return st;
+}
+
+sg_status
 sg_deque_destroy(sg_deque* d)
 {
     if (d == nullptr)
@@ -1264,14 +1318,18 @@ sg_deque_destroy(sg_deque* d)
         return SG_ERR_BAD_ARG;
     }
     cudaDeviceSynchronize();
-    sg::detail::dev_free(d->data);
-    sg::detail::dev_free(d->seq);
-    sg::detail::dev_free(d->counters);
-    sg::detail::dev_free(d->slot_state);
-    sg::detail::dev_free(d->sync);
+    sg::detail::obj_free(d->oa, d->data);
+    sg::detail::obj_free(d->oa, d->seq);
+    sg::detail::obj_free(d->oa, d->counters);
+    sg::detail::obj_free(d->oa, d->slot_state);
+    sg::detail::obj_free(d->oa, d->sync);
     if (d->host != nullptr)
     {
         cudaFreeHost(d->host);
+    }
+    if (d->release_ctx != nullptr)
+    {
+        d->release_ctx(d->oa.ctx);
     }
     delete d;
     return SG_OK;

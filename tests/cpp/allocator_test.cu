@@ -240,6 +240,38 @@ main()
         check(st.live == 0 && st.bytes == 0, "wide map: destroyDeviceObject returns every block");
     }
 
+    // ---- vector and deque
+    {
+        alloc_stats st;
+        using vec_t = stdgpu::vector<std::uint32_t, counting_allocator<std::uint32_t>>;
+        vec_t v = vec_t::createDeviceObject(1 << 16, counting_allocator<std::uint32_t>(&st));
+        check(st.live >= 4 && st.bytes >= (1 << 16) * 4 && sg_live_device_allocations() == lib_before,
+              "vector: data, size and per-slot words from the allocator");
+        std::vector<std::uint32_t> h(5000);
+        for (int i = 0; i < 5000; ++i)
+        {
+            h[i] = static_cast<std::uint32_t>(i * 3);
+        }
+        std::uint32_t* dh = to_device(h);
+        v.insert(v.device_end(), dh, dh + h.size());
+        check(v.size() == 5000 && v.valid(), "vector: insert at the end, size, valid");
+        cudaFree(dh);
+        vec_t::destroyDeviceObject(v);
+        check(st.live == 0 && st.bytes == 0, "vector: destroyDeviceObject returns every block");
+    }
+    {
+        alloc_stats st;
+        using deq_t = stdgpu::deque<std::uint64_t, counting_allocator<std::uint64_t>>;
+        deq_t d = deq_t::createDeviceObject(1 << 14, counting_allocator<std::uint64_t>(&st));
+        check(st.live >= 5 && sg_live_device_allocations() == lib_before,
+              "deque: ring, turn words, counters and per-slot words from the allocator");
+        const long long before_range = st.live;
+        auto r = d.device_range();
+        check(r.size() == 0 && st.live == before_range + 1, "deque: the device_range() array from the allocator too");
+        deq_t::destroyDeviceObject(d);
+        check(st.live == 0 && st.bytes == 0, "deque: destroyDeviceObject returns every block");
+    }
+
     check(sg_live_device_allocations() == lib_before, "the library's own allocator held nothing for these objects");
     if (cudaDeviceSynchronize() != cudaSuccess)
     {
