@@ -410,6 +410,7 @@ SG_API sg_status sg_server_get_stats(sg_server* server, sg_server_stats* out);
 SG_API sg_status sg_server_request_latency(sg_server* server, int64_t ticket, double* out_us);
 /* Waits for the table's requests, then size(). */
 SG_API sg_status sg_server_table_size(sg_server* server, int32_t table, int64_t* out_size);
+/* Waits for the table's requests (and a grow in flight), then its device view. */
 SG_API sg_status sg_server_table_view(sg_server* server, int32_t table, sg_unordered_view* out);
 
 /* ---------------- vector<T> (T = 4 or 8 bytes) ---------------- */

@@ -1691,12 +1691,14 @@ sg_server_table_view(sg_server* srv, int32_t table, sg_unordered_view* out)
     {
         return SG_ERR_BAD_ARG;
     }
-    std::lock_guard<std::mutex> lock(srv->m);
+    std::unique_lock<std::mutex> lock(srv->m);
     auto it = srv->tables.find(table);
     if (it == srv->tables.end())
     {
         return SG_ERR_BAD_ARG;
     }
+    // a grow in flight replaces the storage: the view is taken once the table has settled
+    srv->cv_done.wait(lock, [&] { return !it->second.busy && it->second.fifo.empty(); });
     return sg_unordered_view_of(it->second.h, out);
 }
 
