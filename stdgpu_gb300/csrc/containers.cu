@@ -421,52 +421,74 @@ k_deque_ops(T* data, unsigned* seq, deque_counters* c, int64_t cap, const uint8_
         }
         else
         {
-            // one by one, the tickets read again from the tile's counts in shared memory (no local arrays)
+            // One by one in the order of their turns: a push of ticket t before the pop of t, which comes
+            // before the push of t + capacity.  Every wait is for a turn that precedes the element's own,
+            // so a thread never waits for one of its own later elements (a pop and the push of the same
+            // ticket can fall to one thread when the deque runs near empty inside a tile, and a push and
+            // the pop one lap earlier when the ring wraps inside a tile).
+            unsigned done = 0u;
+            const unsigned live = pushes | pops;
 #pragma unroll 1
+            for (int step = 0; step < kItems; ++step)
+            {
+                int sel = -1;
+                unsigned sel_tk = 0u;
+                unsigned sel_pos = 0u;
+                bool sel_pop = false;
+#pragma unroll
+                for (int j = 0; j < kItems; ++j)
+                {
+                    const bool pj = (pops >> j) & 1u;
+                    // order key: ticket, then push before pop (tickets compared modulo 2^32)
+                    const bool before = sel < 0 || static_cast<int>(tk32[j] - sel_tk) < 0 ||
+                                        (tk32[j] == sel_tk && !pj && sel_pop);
+                    if ((((live & ~done) >> j) & 1u) && before)
+                    {
+                        sel = j;
+                        sel_tk = tk32[j];
+                        sel_pos = pos[j];
+                        sel_pop = pj;
+                    }
+                }
+                if (sel < 0)
+                {
+                    break;
+                }
+                done |= 1u << sel;
+                const int64_t i = tile + static_cast<int64_t>(sel) * kCThreads + threadIdx.x;
+                const unsigned want = sel_pop ? sel_tk + 1u : sel_tk;
+                bool ok = false;
+                if (wait_turn(seq + sel_pos, want, &c->error))
+                {
+                    if (sel_pop)
+                    {
+                        const T v = *reinterpret_cast<volatile T*>(data + sel_pos);
+                        store_turn(seq + sel_pos, sel_tk + static_cast<unsigned>(cap));
+                        if (out_popped != nullptr)
+                        {
+                            out_popped[i] = v;
+                        }
+                    }
+                    else
+                    {
+                        data[sel_pos] = values[i];
+                        store_turn(seq + sel_pos, sel_tk + 1u);
+                    }
+                    ok = true;
+                }
+                if (out_ok != nullptr)
+                {
+                    out_ok[i] = static_cast<uint8_t>(ok);
+                }
+            }
+            // elements without a ticket (refused, or past n)
+#pragma unroll
             for (int j = 0; j < kItems; ++j)
             {
                 const int64_t i = tile + j * kCThreads + threadIdx.x;
-                const unsigned bit = 1u << lane;
-                const unsigned pm = mpush[j * kWarps + warp];
-                const unsigned qm = mpop[j * kWarps + warp];
-                bool ok = false;
-                if (pm & bit)
+                if (!((live >> j) & 1u) && i < n && out_ok != nullptr)
                 {
-                    const long long r = cpush[j * kWarps + warp] + __popc(pm & lanemask_lt());
-                    if (r < push_ok)
-                    {
-                        const unsigned long long tk = push_t0 + static_cast<unsigned long long>(r);
-                        const int64_t at = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
-                        if (wait_turn(seq + at, static_cast<unsigned>(tk), &c->error))
-                        {
-                            data[at] = values[i];
-                            store_turn(seq + at, static_cast<unsigned>(tk + 1));
-                            ok = true;
-                        }
-                    }
-                }
-                else if (qm & bit)
-                {
-                    const long long r = cpop[j * kWarps + warp] + __popc(qm & lanemask_lt());
-                    if (r < pop_ok)
-                    {
-                        const unsigned long long tk = pop_t0 + static_cast<unsigned long long>(r);
-                        const int64_t at = static_cast<int64_t>(tk % static_cast<unsigned long long>(cap));
-                        if (wait_turn(seq + at, static_cast<unsigned>(tk + 1), &c->error))
-                        {
-                            const T v = *reinterpret_cast<volatile T*>(data + at);
-                            store_turn(seq + at, static_cast<unsigned>(tk + static_cast<unsigned long long>(cap)));
-                            if (out_popped != nullptr)
-                            {
-                                out_popped[i] = v;
-                            }
-                            ok = true;
-                        }
-                    }
-                }
-                if (i < n && out_ok != nullptr)
-                {
-                    out_ok[i] = static_cast<uint8_t>(ok);
+                    out_ok[i] = 0u;
                 }
             }
         }
