@@ -115,3 +115,28 @@ def test_queue_and_stack_adapters():
     assert q.size() == 30 and s.size() == 30 and not q.empty()
     sg.queue.destroyDeviceObject(q)
     sg.stack.destroyDeviceObject(s)
+
+
+def test_mixed_launches_on_small_deques_keep_the_multiset():
+    """Mixed push_back / pop_front launches of thousands of operations on deques of 64-1000 elements: the
+    ring wraps inside one tile and runs near empty, so one thread may hold a pop and the push of the same
+    ticket, or a push and the pop one lap earlier.  Every launch keeps the multiset (popped + remaining ==
+    before + pushed), stays within capacity, and leaves no wait error (size() would report it)."""
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    for cap in (64, 100, 1000):
+        d = C.deque.createDeviceObject(cap, elem_bytes=8)
+        for it in range(30):
+            n = int(torch.randint(512, 8192, (1,), generator=gen, device="cuda").item())
+            frac = [0.5, 0.6, 0.4][it % 3]
+            is_push = (torch.rand(n, device="cuda", generator=gen) < frac).to(torch.uint8)
+            vals = torch.randint(0, 1 << 62, (n,), dtype=torch.int64, device="cuda", generator=gen)
+            before = d.to_tensor()
+            popped, ok = d.ops(is_push, vals)
+            size = d.size()
+            after = d.to_tensor()
+            ip, okb = is_push.bool(), ok.bool()
+            lhs = torch.sort(torch.cat([popped[~ip & okb], after])).values
+            rhs = torch.sort(torch.cat([before, vals[ip & okb]])).values
+            assert torch.equal(lhs, rhs), (cap, it)
+            assert size == len(after) <= cap
+        C.deque.destroyDeviceObject(d)
