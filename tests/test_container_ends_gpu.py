@@ -124,7 +124,7 @@ def test_mixed_launches_on_small_deques_keep_the_multiset():
     before + pushed), stays within capacity, and leaves no wait error (size() would report it)."""
     gen = torch.Generator(device="cuda").manual_seed(3)
     for cap in (64, 100, 1000):
-        d = C.deque.createDeviceObject(cap, elem_bytes=8)
+        d = sg.deque.createDeviceObject(cap, elem_bytes=8)
         for it in range(30):
             n = int(torch.randint(512, 8192, (1,), generator=gen, device="cuda").item())
             frac = [0.5, 0.6, 0.4][it % 3]
@@ -139,4 +139,4 @@ def test_mixed_launches_on_small_deques_keep_the_multiset():
             rhs = torch.sort(torch.cat([before, vals[ip & okb]])).values
             assert torch.equal(lhs, rhs), (cap, it)
             assert size == len(after) <= cap
-        C.deque.destroyDeviceObject(d)
+        sg.deque.destroyDeviceObject(d)
