@@ -334,7 +334,9 @@ SG_API sg_status sg_batch_info(const sg_table_batch* batch, int64_t* out_storage
  * trip, while the table's later requests wait) before an insert run would pass 85 % of max_size(), only
  * while the HBM budget allows; otherwise the table admission or the request is refused with SG_ERR_BUDGET
  * -- nothing spills to host memory.  The storage a grow replaced counts against the budget until the
- * server is next idle (or the budget needs it).
+ * server is next idle (or the budget needs it).  Table storage comes from a stream-ordered memory pool the
+ * server owns: what it releases stays mapped in the pool for later tables until the server is destroyed,
+ * so the device memory the process holds follows the largest total the tables reached, not the current one.
  * Within one run of same-operation requests the per-key inserted / erased flags of a key repeated in
  * several requests may fall on any of them (as for duplicates within one bulk call). */
 typedef struct sg_server sg_server;

@@ -322,6 +322,10 @@ constexpr int kSlotSegments = 4096; // segments one packed launch can carry
 #ifndef SG_SERVER_POOL
 #define SG_SERVER_POOL 1
 #endif
+// > 0: a budget / SG_SERVER_POOL_WARM_DIV block is mapped into the pool at creation (0: none)
+#ifndef SG_SERVER_POOL_WARM_DIV
+#define SG_SERVER_POOL_WARM_DIV 0
+#endif
 // Request-size policy defaults (sg_server_set_policy): a table's run of same-operation requests with at
 // least kDefaultDirectKeys keys runs as its own launches (cut into launches of at most kDefaultChunkKeys
 // keys) on one of kDefaultDirectStreams low-priority streams, at most kDefaultMaxDirect such runs issued and
@@ -1270,6 +1274,17 @@ sg_server_create(int32_t kind, int64_t hbm_budget_bytes, int32_t n_streams, int3
             cudaMemPoolSetAttribute(srv->pool, cudaMemPoolAttrReleaseThreshold, &keep);
             cudaStreamCreateWithFlags(&srv->alloc_stream, cudaStreamNonBlocking);
             srv->table_alloc = sg_allocator{ &pool_alloc, &pool_release, srv, nullptr };
+#if SG_SERVER_POOL_WARM_DIV > 0
+            // map part of the budget into the pool up front, so the first grows do not map memory
+            void* warm = nullptr;
+            if (cudaMallocFromPoolAsync(&warm, static_cast<size_t>(hbm_budget_bytes / SG_SERVER_POOL_WARM_DIV), srv->pool,
+                                        srv->alloc_stream) == cudaSuccess)
+            {
+                cudaFreeAsync(warm, srv->alloc_stream);
+            }
+            cudaStreamSynchronize(srv->alloc_stream);
+            cudaGetLastError();
+#endif
         }
         else
         {
