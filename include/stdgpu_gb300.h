@@ -335,8 +335,9 @@ SG_API sg_status sg_batch_info(const sg_table_batch* batch, int64_t* out_storage
  * while the HBM budget allows; otherwise the table admission or the request is refused with SG_ERR_BUDGET
  * -- nothing spills to host memory.  The storage a grow replaced counts against the budget until the
  * server is next idle (or the budget needs it).  Table storage comes from a stream-ordered memory pool the
- * server owns: what it releases stays mapped in the pool for later tables until the server is destroyed,
- * so the device memory the process holds follows the largest total the tables reached, not the current one.
+ * server owns, into which a quarter of the budget is mapped at creation: what the pool releases stays mapped
+ * for later tables until the server is destroyed, so the device memory the process holds is the larger of
+ * that quarter and the largest total the tables reached, and a grow rarely has to map new memory.
  * Within one run of same-operation requests the per-key inserted / erased flags of a key repeated in
  * several requests may fall on any of them (as for duplicates within one bulk call). */
 typedef struct sg_server sg_server;
