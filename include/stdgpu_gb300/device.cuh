@@ -210,25 +210,6 @@ struct unordered_ref
         return true;
     }
 
-    // Stripe lock of home group g (bounded wait with back-off; false when it gave up).
-    __device__ bool
-    lock_group(int64_t g) const
-    {
-        unsigned int* l = v.insert_locks + (static_cast<uint64_t>(g) & static_cast<uint64_t>(v.lock_mask));
-        unsigned int backoff = 32;
-        for (long long polls = 0; polls < detail::kWaitLimit; ++polls)
-        {
-            if (atomicCAS(l, 0u, 1u) == 0u)
-            {
-                __threadfence();
-                return true;
-            }
-            __nanosleep(backoff);
-            backoff = backoff < 256 ? backoff * 2 : 256;
-        }
-        return false;
-    }
-
     __device__ void
     unlock_group(int64_t g) const
     {
@@ -306,6 +287,38 @@ struct unordered_ref
         return false;
     }
 
+    // The stripe lock of home group `home` for an insert of `key`: 1 when taken, 0 when the key turned up
+    // present while waiting (checked every 16 polls, so a crowd of inserts of one key drains as soon as the
+    // first is stored instead of queueing on the lock one by one), -1 when the bounded wait gave up.  The lock
+    // word is read before each compare-and-swap, so waiters load from L2 instead of all issuing atomics on one
+    // address.
+    __device__ int
+    lock_group_or_present(int64_t home, key_type key) const
+    {
+        unsigned int* l = v.insert_locks + (static_cast<uint64_t>(home) & static_cast<uint64_t>(v.lock_mask));
+        unsigned int backoff = 32;
+        for (long long polls = 0; polls < detail::kWaitLimit; ++polls)
+        {
+            if (*reinterpret_cast<volatile unsigned int*>(l) == 0u && atomicCAS(l, 0u, 1u) == 0u)
+            {
+                __threadfence();
+                return 1;
+            }
+            if ((polls & 15) == 15)
+            {
+                int64_t target = -1;
+                bool target_tomb = false;
+                if (scan_for_insert(key, home, target, target_tomb))
+                {
+                    return 0;
+                }
+            }
+            __nanosleep(backoff);
+            backoff = backoff < 256 ? backoff * 2 : 256;
+        }
+        return -1;
+    }
+
     // Insert under the home group's stripe lock: erased slots are reused.  Returns the slot, or -1 (present,
     // refused -- no free slot in the table --, or the lock wait gave up, which sets an error bit).  As the
     // reference checks contains() and full() before it locks (unordered_base_detail.cuh:708-720, :958-994),
@@ -328,7 +341,12 @@ struct unordered_ref
                 return -1;
             }
         }
-        if (!lock_group(home))
+        const int locked = lock_group_or_present(home, key);
+        if (locked == 0)
+        {
+            return -1; // present: inserted by another thread while this one waited
+        }
+        if (locked < 0)
         {
             atomicOr(&header()->error, detail::kErrRetry);
             return -1;

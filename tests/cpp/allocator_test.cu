@@ -164,6 +164,7 @@ all_found(const Table& t, const std::vector<Key>& keys)
 int
 main()
 {
+    std::setvbuf(stdout, nullptr, _IOLBF, 0); // each line out before a failure can end the program
     std::mt19937_64 rng(3);
     const long long lib_before = sg_live_device_allocations();
 

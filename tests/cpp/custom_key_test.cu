@@ -178,6 +178,7 @@ range_keys(stdgpu::detail::custom_range<vec3i16, void> r, vec3i16* out)
 int
 main()
 {
+    std::setvbuf(stdout, nullptr, _IOLBF, 0); // each line out before a failure can end the program
     std::mt19937 rng(7);
     std::uniform_int_distribution<int> coord(-60, 60);
     const int n = 200000;

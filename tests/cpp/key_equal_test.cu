@@ -210,6 +210,7 @@ count(const std::vector<std::uint8_t>& v)
 int
 main()
 {
+    std::setvbuf(stdout, nullptr, _IOLBF, 0); // each line out before a failure can end the program
     std::mt19937 rng(7);
     constexpr int kBlock = 256;
     auto grid = [](int n) { return (n + kBlock - 1) / kBlock; };

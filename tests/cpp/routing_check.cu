@@ -3,6 +3,7 @@
 // trivially copyable keys of at most 8 bytes with a 4/8-byte trivially copyable mapped type -> the word-keyed
 // custom path; everything else -> the wide tables, and so do keys compared by a user KeyEqual or whose bytes do
 // not decide equality (floating point, padding).  Builds to a program that does nothing.
+#include <cstdio>
 #include <cstdint>
 #include <type_traits>
 
@@ -121,5 +122,6 @@ static_assert(std::is_same<decltype(a1{}.get_allocator()), safe_device_allocator
 int
 main()
 {
+    std::setvbuf(stdout, nullptr, _IOLBF, 0); // each line out before a failure can end the program
     return 0;
 }

@@ -388,6 +388,7 @@ deque_sequence(stdgpu::deque<std::uint64_t> d, int n, std::uint64_t* out)
 int
 main()
 {
+    std::setvbuf(stdout, nullptr, _IOLBF, 0); // each line out before a failure can end the program
     const int N = 100000;
     const int threads = 256;
     const int blocks = (N + threads - 1) / threads;

@@ -657,6 +657,7 @@ refusal_when_full()
 int
 main()
 {
+    std::setvbuf(stdout, nullptr, _IOLBF, 0); // each line out before a failure can end the program
     clear_nontrivial();
     set_of_vec3int32();
     map_of_key128();
