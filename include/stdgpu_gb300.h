@@ -91,6 +91,13 @@ typedef struct sg_unordered_view
     uint32_t* insert_locks;  /* device stripe locks of the native device inserts, lock_mask + 1 of them (a power
                                 of two); nullable: device inserts then claim never-used slots only */
     int64_t lock_mask;
+    /* The reference's excess-list accounting (NULL: off).  The reference stores a new key in its bucket's own
+     * slot when that slot is free, else in a slot taken from its excess list, and refuses every insert once
+     * that list is empty (unordered_base_detail.cuh:708-809, 958-994); these fields track the same state. */
+    uint32_t* bucket_heads;  /* one bit per bucket: set while a key holds the bucket's own slot */
+    uint32_t* slot_heads;    /* one bit per slot (num_groups x slots per group, then the 2 out-of-band slots):
+                                set where the key holding its bucket's own slot is stored */
+    int64_t excess_count;    /* the excess list's length */
 } sg_unordered_view;
 
 /* ---------------- device memory ---------------- */
@@ -197,6 +204,22 @@ typedef enum sg_insert_mode
     SG_INSERT_PARTITIONED = 2
 } sg_insert_mode;
 SG_API sg_status sg_unordered_set_insert_mode(sg_unordered* table, int32_t mode);
+
+/* The reference's excess-list refusal.  The reference keeps a new key in its bucket's own slot when that is
+ * free, else in a slot of its excess list (excess_count slots), and its insert loop refuses every insert
+ * once that list is empty or the table is full (src/stdgpu/impl/unordered_base_detail.cuh:708-809, 958-994),
+ * which can happen below max_size().  With the accounting on (on = 1), a table tracks the same state --
+ * which buckets' own slots are taken and how many keys hold excess slots -- and refuses exactly then; bulk
+ * inserts and erases then run one thread per key under the stripe locks, and a call of at most 4096 keys
+ * that could reach the refusal takes its keys in input order, as the reference does on one thread.  Off
+ * (on = 0), a table takes keys until no slot is free, through the tile and partitioned kernels.  On by
+ * default for tables whose max_size() is at most 2^20; switched only on an empty table (size 0, else
+ * SG_ERR_BAD_ARG), starting from the reference's empty state.  Synchronises.  Kept by rehash and clear;
+ * the batched tables and the server's tables do not keep it. */
+SG_API sg_status sg_unordered_set_excess_accounting(sg_unordered* table, int32_t on, void* stream);
+/* Keys holding excess slots (the reference's excess_count minus its free excess slots), -1 with the
+ * accounting off.  Synchronises. */
+SG_API sg_status sg_unordered_excess_used(sg_unordered* table, void* stream, int64_t* out);
 
 /* erase(begin, end) over keys: src/stdgpu/impl/unordered_base_detail.cuh:1045-1066 (per key :1019-1043).
  * out_erased (nullable): per key 1 if this call erased it, else 0. */

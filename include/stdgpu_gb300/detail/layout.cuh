@@ -50,7 +50,8 @@ struct table_header
     unsigned int error;            // sticky error bits (kErr*)
     unsigned int pad0;
     unsigned long long count;      // per-call scratch counter (valid / range)
-    unsigned long long pad1[2];
+    unsigned long long scratch;    // per-call scratch counter (valid: violations)
+    unsigned long long excess_used; // keys holding one of the reference's excess slots (excess-list accounting)
 };
 
 constexpr unsigned int kErrRetry = 1u;      // a CAS retry loop gave up

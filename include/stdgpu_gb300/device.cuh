@@ -20,6 +20,11 @@
 //    table at the same time.
 //  * erase marks the slot erased (compare-and-swap key -> erased marker);
 //    exactly one of several concurrent erases of a key reports success.
+//  * With the reference's excess-list accounting on (v.bucket_heads), an
+//    insert also takes its bucket's own slot or one of the excess slots, and
+//    is refused once those run out, as the reference's insert loop refuses it
+//    (unordered_base_detail.cuh:980-981); erase then takes the stripe lock
+//    too, and gives the bucket's slot or the excess slot back.
 //  * insert writes the key and its mapped value with one compare-and-swap over
 //    the whole slot (up to 16 bytes), so a concurrent find sees either no key
 //    or the key with its value (the reference orders the two with its per-slot
@@ -95,8 +100,15 @@ struct unordered_ref
     }
 
     // Slot index of key, or -1.  Stops at the first group holding a never-used slot.
-    __device__ int64_t
+    __device__ __forceinline__ int64_t
     find_slot(key_type key) const
+    {
+        return find_slot_home(key, home_group(key));
+    }
+
+    // find_slot along the probe sequence of home group `home` (the key's own).
+    __device__ int64_t
+    find_slot_home(key_type key, int64_t home) const
     {
         if (is_special(key))
         {
@@ -104,7 +116,7 @@ struct unordered_ref
             unsigned st = *reinterpret_cast<volatile unsigned*>(&header()->special_state[s]);
             return st == 1u ? special_slot(key) : -1;
         }
-        int64_t g = home_group(key);
+        int64_t g = home;
         for (int64_t probes = 0; probes < v.num_groups; ++probes)
         {
             const uint4* p = group_ptr(g);
@@ -287,13 +299,13 @@ struct unordered_ref
         return false;
     }
 
-    // The stripe lock of home group `home` for an insert of `key`: 1 when taken, 0 when the key turned up
-    // present while waiting (checked every 16 polls, so a crowd of inserts of one key drains as soon as the
-    // first is stored instead of queueing on the lock one by one), -1 when the bounded wait gave up.  The lock
-    // word is read before each compare-and-swap, so waiters load from L2 instead of all issuing atomics on one
-    // address.
+    // The stripe lock of home group `home` for an insert (for_insert) or an erase of `key`: 1 when taken, 0
+    // when the call was settled while waiting -- the key turned up present (insert) or absent (erase), checked
+    // every 16 polls, so a crowd of calls on one key drains as soon as the first is done instead of passing
+    // the lock on one by one --, -1 when the bounded wait gave up.  The lock word is read before each
+    // compare-and-swap, so waiters load from L2 instead of all issuing atomics on one address.
     __device__ int
-    lock_group_or_present(int64_t home, key_type key) const
+    lock_or_settled(int64_t home, key_type key, bool for_insert) const
     {
         unsigned int* l = v.insert_locks + (static_cast<uint64_t>(home) & static_cast<uint64_t>(v.lock_mask));
         unsigned int backoff = 32;
@@ -304,19 +316,103 @@ struct unordered_ref
                 __threadfence();
                 return 1;
             }
-            if ((polls & 15) == 15)
+            if ((polls & 15) == 15 && (find_slot_home(key, home) >= 0) == for_insert)
             {
-                int64_t target = -1;
-                bool target_tomb = false;
-                if (scan_for_insert(key, home, target, target_tomb))
-                {
-                    return 0;
-                }
+                return 0;
             }
             __nanosleep(backoff);
             backoff = backoff < 256 ? backoff * 2 : 256;
         }
         return -1;
+    }
+
+    // ---- the reference's excess-list accounting (v.bucket_heads != nullptr) ----
+    // The reference stores a new key in its bucket's own slot when that slot is free, else in a slot taken
+    // from its excess list; its insert loop refuses every insert once the table is full or that list is
+    // empty (unordered_base_detail.cuh:708-809, 958-994), and an erase frees the bucket's slot or gives the
+    // excess slot back (:811-913).  The view keeps the same state: bucket_heads (a bit per bucket: a key holds
+    // the bucket's own slot), slot_heads (a bit per slot: the key stored there is that key) and the header's
+    // excess_used.  Every change for a key of bucket b happens under the stripe lock of b's home group, which
+    // all keys of b share.
+    __device__ __forceinline__ bool
+    accounting() const
+    {
+        return v.bucket_heads != nullptr;
+    }
+
+    // the reference's loop guard (:980-981): full(), or no excess slot left
+    __device__ __forceinline__ bool
+    refuses_all() const
+    {
+        return *reinterpret_cast<volatile unsigned long long*>(&header()->excess_used) >=
+                       static_cast<unsigned long long>(v.excess_count) ||
+               *reinterpret_cast<volatile unsigned long long*>(&header()->size) >=
+                       static_cast<unsigned long long>(v.total_count);
+    }
+
+    // For a new key of bucket b: 1 = it takes the bucket's own slot, 0 = an excess slot, -1 = refused.  With
+    // may_take_bucket false the key takes an excess slot even when the bucket's own is free (a bulk call in
+    // which an earlier new key of the same bucket takes that slot).
+    __device__ int
+    take_bucket_or_excess(int64_t b, bool may_take_bucket = true) const
+    {
+        if (refuses_all())
+        {
+            return -1;
+        }
+        const unsigned bit = 1u << (b & 31);
+        if (may_take_bucket && (atomicOr(v.bucket_heads + (b >> 5), bit) & bit) == 0u)
+        {
+            return 1;
+        }
+        if (atomicAdd(&header()->excess_used, 1ull) < static_cast<unsigned long long>(v.excess_count))
+        {
+            return 0;
+        }
+        atomicAdd(&header()->excess_used, ~0ull);
+        return -1;
+    }
+
+    // Undoes take_bucket_or_excess(b) == held for an insert that stored nothing.
+    __device__ void
+    give_back(int64_t b, int held) const
+    {
+        if (held == 1)
+        {
+            atomicAnd(v.bucket_heads + (b >> 5), ~(1u << (b & 31)));
+        }
+        else if (held == 0)
+        {
+            atomicAdd(&header()->excess_used, ~0ull);
+        }
+    }
+
+    __device__ __forceinline__ void
+    mark_bucket_slot(int64_t slot) const
+    {
+        atomicOr(v.slot_heads + (slot >> 5), 1u << (slot & 31));
+    }
+
+    // Before the key of bucket b at `slot` is erased: clears the slot's bit and returns whether it was set.
+    __device__ __forceinline__ bool
+    unmark_bucket_slot(int64_t slot) const
+    {
+        const unsigned bit = 1u << (slot & 31);
+        return (atomicAnd(v.slot_heads + (slot >> 5), ~bit) & bit) != 0u;
+    }
+
+    // After that key is erased: the bucket's own slot becomes free, or its excess slot goes back.
+    __device__ void
+    release(int64_t b, bool was_bucket_slot) const
+    {
+        if (was_bucket_slot)
+        {
+            atomicAnd(v.bucket_heads + (b >> 5), ~(1u << (b & 31)));
+        }
+        else
+        {
+            atomicAdd(&header()->excess_used, ~0ull);
+        }
     }
 
     // Insert under the home group's stripe lock: erased slots are reused.  Returns the slot, or -1 (present,
@@ -325,9 +421,9 @@ struct unordered_ref
     // a key found present, or a table with no free slot along the key's probe sequence, is decided by one
     // scan without the lock, so inserts of present keys and inserts into a full table do not queue on it.
     __device__ int64_t
-    insert_slot_locked(key_type key, mapped_type mapped) const
+    insert_slot_locked(key_type key, mapped_type mapped, int64_t b, bool may_take_bucket = true) const
     {
-        const int64_t home = home_group(key);
+        const int64_t home = detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups);
         {
             int64_t target = -1;
             bool target_tomb = false;
@@ -335,13 +431,13 @@ struct unordered_ref
             {
                 return -1; // present
             }
-            if (target < 0)
+            if (target < 0 || (accounting() && refuses_all()))
             {
                 atomicAdd(&header()->refused, 1ull);
                 return -1;
             }
         }
-        const int locked = lock_group_or_present(home, key);
+        const int locked = lock_or_settled(home, key, true);
         if (locked == 0)
         {
             return -1; // present: inserted by another thread while this one waited
@@ -353,6 +449,7 @@ struct unordered_ref
         }
         int64_t result = -1;
         bool refused = false;
+        int held = -1; // accounting: what take_bucket_or_excess gave this key
         for (int attempt = 0; attempt < 65536; ++attempt)
         {
             int64_t target = -1;
@@ -366,6 +463,15 @@ struct unordered_ref
             {
                 refused = true;
                 break;
+            }
+            if (accounting() && held < 0)
+            {
+                held = take_bucket_or_excess(b, may_take_bucket);
+                if (held < 0)
+                {
+                    refused = true;
+                    break;
+                }
             }
             uint32_t image[4];
             if (target_tomb)
@@ -388,6 +494,10 @@ struct unordered_ref
                 {
                     atomicAdd(&header()->tombstones, ~0ull);
                 }
+                if (held == 1)
+                {
+                    mark_bucket_slot(target);
+                }
                 result = target;
                 break;
             }
@@ -396,6 +506,10 @@ struct unordered_ref
                 break;
             }
             // another key took the slot: scan again
+        }
+        if (result < 0 && held >= 0)
+        {
+            give_back(b, held);
         }
         unlock_group(home);
         if (refused)
@@ -407,9 +521,78 @@ struct unordered_ref
 
     // insert(value) / emplace(key, mapped): the slot this call stored the key in, or -1 when the key
     // was already present or no free slot was left (the reference returns (end(), false)).
-    __device__ int64_t
+    __device__ __forceinline__ int64_t
     insert_slot(key_type key, mapped_type mapped = mapped_type{}) const
     {
+        return insert_slot_bucket(key, mapped, bucket(key));
+    }
+
+    // insert_slot for a key whose hash the caller computed (the reference's Hash applied by the caller).
+    __device__ __forceinline__ int64_t
+    insert_slot_hashed(key_type key, uint64_t hash, mapped_type mapped = mapped_type{}) const
+    {
+        return insert_slot_bucket(key, mapped, static_cast<int64_t>(detail::fibonacci_bucket(hash, v.bucket_bits)));
+    }
+
+    // An out-of-band key (stored outside the probe groups) under the accounting: the stripe lock of its home
+    // group orders it with the other keys of its bucket.
+    __device__ int64_t
+    insert_special_counted(key_type key, mapped_type mapped, int64_t b, bool may_take_bucket) const
+    {
+        const int s = key == C::empty_key ? 0 : 1;
+        if (*reinterpret_cast<volatile unsigned*>(&header()->special_state[s]) == 1u)
+        {
+            return -1;
+        }
+        if (refuses_all())
+        {
+            atomicAdd(&header()->refused, 1ull);
+            return -1;
+        }
+        const int64_t home = detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups);
+        const int locked = lock_or_settled(home, key, true);
+        if (locked <= 0)
+        {
+            if (locked < 0)
+            {
+                atomicOr(&header()->error, detail::kErrRetry);
+            }
+            return -1;
+        }
+        int64_t result = -1;
+        const int held = take_bucket_or_excess(b, may_take_bucket);
+        if (held < 0)
+        {
+            atomicAdd(&header()->refused, 1ull);
+        }
+        else if (atomicCAS(&header()->special_state[s], 0u, 2u) == 0u)
+        {
+            store_slot(special_slot(key), key, mapped);
+            __threadfence();
+            atomicExch(&header()->special_state[s], 1u);
+            atomicAdd(&header()->size, 1ull);
+            if (held == 1)
+            {
+                mark_bucket_slot(special_slot(key));
+            }
+            result = special_slot(key);
+        }
+        else
+        {
+            give_back(b, held);
+        }
+        unlock_group(home);
+        return result;
+    }
+
+    // insert_slot for a key of bucket b; may_take_bucket as in take_bucket_or_excess (accounting only).
+    __device__ int64_t
+    insert_slot_bucket(key_type key, mapped_type mapped, int64_t b, bool may_take_bucket = true) const
+    {
+        if (is_special(key) && accounting())
+        {
+            return insert_special_counted(key, mapped, b, may_take_bucket);
+        }
         if (is_special(key))
         {
             const int s = key == C::empty_key ? 0 : 1;
@@ -425,9 +608,9 @@ struct unordered_ref
         }
         if (v.insert_locks != nullptr)
         {
-            return insert_slot_locked(key, mapped);
+            return insert_slot_locked(key, mapped, b, may_take_bucket);
         }
-        int64_t g = home_group(key);
+        int64_t g = detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups);
         int64_t steps = 0;
         const int64_t limit = v.num_groups + 4096;
         while (steps++ < limit)
@@ -541,9 +724,75 @@ struct unordered_ref
     }
 
     // erase(key): 1 when this call removed the key, else 0.
-    __device__ int64_t
+    __device__ __forceinline__ int64_t
     erase(key_type key) const
     {
+        return erase_bucket(key, bucket(key));
+    }
+
+    // erase for a key whose hash the caller computed.
+    __device__ __forceinline__ int64_t
+    erase_hashed(key_type key, uint64_t hash) const
+    {
+        return erase_bucket(key, static_cast<int64_t>(detail::fibonacci_bucket(hash, v.bucket_bits)));
+    }
+
+    // erase under the accounting: the stripe lock of the key's home group, then the slot's bits.
+    __device__ int64_t
+    erase_counted(key_type key, int64_t b) const
+    {
+        const int64_t home = detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups);
+        if (find_slot_home(key, home) < 0)
+        {
+            return 0;
+        }
+        const int locked = lock_or_settled(home, key, false);
+        if (locked <= 0)
+        {
+            if (locked < 0)
+            {
+                atomicOr(&header()->error, detail::kErrRetry);
+            }
+            return 0;
+        }
+        int64_t r = 0;
+        const int64_t slot = find_slot_home(key, home);
+        if (slot >= 0)
+        {
+            // the bit goes before the slot can be reused by another bucket's key
+            const bool was_bucket_slot = unmark_bucket_slot(slot);
+            bool erased = false;
+            if (is_special(key))
+            {
+                erased = atomicCAS(&header()->special_state[key == C::empty_key ? 0 : 1], 1u, 0u) == 1u;
+            }
+            else if (cas_key(slot, key, C::tomb_key) == key)
+            {
+                atomicAdd(&header()->tombstones, 1ull);
+                erased = true;
+            }
+            if (erased)
+            {
+                atomicAdd(&header()->size, ~0ull);
+                release(b, was_bucket_slot);
+                r = 1;
+            }
+            else if (was_bucket_slot)
+            {
+                mark_bucket_slot(slot);
+            }
+        }
+        unlock_group(home);
+        return r;
+    }
+
+    __device__ int64_t
+    erase_bucket(key_type key, int64_t b) const
+    {
+        if (accounting())
+        {
+            return erase_counted(key, b);
+        }
         if (is_special(key))
         {
             const int s = key == C::empty_key ? 0 : 1;
@@ -554,7 +803,8 @@ struct unordered_ref
             }
             return 0;
         }
-        const int64_t slot = find_slot(key);
+        const int64_t slot = find_slot_home(
+                key, detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups));
         if (slot < 0)
         {
             return 0;

@@ -363,6 +363,17 @@ public:
         d._alloc = sg_allocator{};
     }
 
+    // Not in the reference: the excess-list accounting switch of an empty object
+    // (sg_unordered_set_excess_accounting; on by default up to max_size() 2^20).  Off, the object takes keys
+    // until no slot is free instead of refusing them where the reference's excess list runs out.  Copies made
+    // before the switch keep the old device view.
+    void
+    set_excess_accounting(bool on)
+    {
+        gb300_check(sg_unordered_set_excess_accounting(_handle, on ? 1 : 0, nullptr), "set_excess_accounting");
+        gb300_check(sg_unordered_view_of(_handle, &_view), "set_excess_accounting");
+    }
+
     // insert(begin, end) over value_type elements: unordered_base_detail.cuh:996-1017
     void
     insert(const value_type* begin, const value_type* end)

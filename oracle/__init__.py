@@ -153,13 +153,14 @@ def port_lib() -> ctypes.CDLL:
         L.port_create.restype = c_void_p
         L.port_create.argtypes = [c_int64]
         L.port_destroy.argtypes = [c_void_p]
-        for f in ("port_size", "port_bucket_count", "port_max_size", "port_range", "port_bucket",
+        for f in ("port_size", "port_bucket_count", "port_max_size", "port_excess_used", "port_range", "port_bucket",
                   "port_bucket_size", "port_fibonacci_hashing", "port_expected_collisions",
                   "port_vector_push_back", "port_deque_ops", "port_bitset_count"):
             getattr(L, f).restype = c_int64
         L.port_size.argtypes = [c_void_p]
         L.port_bucket_count.argtypes = [c_void_p]
         L.port_max_size.argtypes = [c_void_p]
+        L.port_excess_used.argtypes = [c_void_p]
         L.port_bucket.argtypes = [c_void_p, ctypes.c_uint64]
         L.port_bucket_size.argtypes = [c_void_p, c_int64]
         L.port_fibonacci_hashing.argtypes = [ctypes.c_uint64, c_int64]
@@ -322,6 +323,9 @@ class PortTable(_TableBase):
 
     def size(self) -> int:
         return int(self.L.port_size(self.h))
+
+    def excess_used(self) -> int:
+        return int(self.L.port_excess_used(self.h))
 
     def valid(self) -> bool:
         return bool(self.L.port_valid(self.h))

@@ -345,6 +345,8 @@ void port_find_bulk(const port_table* t, const uint64_t* keys, int64_t n, uint64
 int64_t port_size(const port_table* t) { return t->occupied_count; }
 int64_t port_bucket_count(const port_table* t) { return t->bucket_count; }
 int64_t port_max_size(const port_table* t) { return t->total_count; }
+/* slots taken from the excess list: excess_count minus _excess_list_positions.size() */
+int64_t port_excess_used(const port_table* t) { return t->excess_count - t->excess_size; }
 
 /* bucket_size(n): :566-593 */
 int64_t port_bucket_size(const port_table* t, int64_t n)

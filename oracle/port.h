@@ -53,6 +53,7 @@ void port_find_bulk_h(const port_table* t, const uint64_t* keys, const uint64_t*
 int64_t port_size(const port_table* t);
 int64_t port_bucket_count(const port_table* t);
 int64_t port_max_size(const port_table* t);
+int64_t port_excess_used(const port_table* t);
 int64_t port_bucket(const port_table* t, uint64_t key);
 int64_t port_bucket_size(const port_table* t, int64_t n);
 void port_clear(port_table* t);

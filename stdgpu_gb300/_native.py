@@ -52,6 +52,9 @@ class sg_unordered_view(ctypes.Structure):
         ("kind", c_int32),
         ("insert_locks", c_void_p),
         ("lock_mask", c_int64),
+        ("bucket_heads", c_void_p),
+        ("slot_heads", c_void_p),
+        ("excess_count", c_int64),
     ]
 
 
@@ -111,6 +114,8 @@ SIGNATURES = {
     "sg_unordered_bucket": (c_int32, [c_void_p, c_void_p, POINTER(c_int64)]),
     "sg_unordered_geometry": (c_int32, [c_void_p, POINTER(sg_geometry)]),
     "sg_unordered_view_of": (c_int32, [c_void_p, POINTER(sg_unordered_view)]),
+    "sg_unordered_set_excess_accounting": (c_int32, [c_void_p, c_int32, c_void_p]),
+    "sg_unordered_excess_used": (c_int32, [c_void_p, c_void_p, POINTER(c_int64)]),
     "sg_unordered_geometry_for": (c_int32, [c_int32, c_int64, POINTER(sg_geometry)]),
     "sg_stager_create": (c_int32, [c_int64, c_int32, POINTER(c_void_p)]),
     "sg_stager_destroy": (c_int32, [c_void_p]),

@@ -97,6 +97,8 @@ def time_plain(caps, d_keys, d_q, offsets, out, steps: int, warmup: int) -> tupl
     """Plain per-table C-ABI calls (clear, insert, contains per table) on the current stream, from a C++ loop
     (comparators.plain_tables_steps).  Returns (GPU ms per step, host ms per step)."""
     tables = [C.unordered_set.createDeviceObject(int(c), key="u64") for c in caps]
+    for t in tables:
+        t.set_excess_accounting(False)  # the batched object's semantics: keys until no slot is free
     st = torch.cuda.current_stream()
     P.plain_tables_steps(tables, d_keys, d_q, offsets, 8, out, warmup, st)
     gpu_ms, host_ms = P.plain_tables_steps(tables, d_keys, d_q, offsets, 8, out, steps, st)

@@ -319,6 +319,18 @@ class unordered_base:
         """Bulk-insert strategy: "auto", "direct" or "partitioned" (sg_unordered_set_insert_mode)."""
         N.check(N.load().sg_unordered_set_insert_mode(self._h, self.INSERT_MODES[mode]), "set_insert_mode")
 
+    def set_excess_accounting(self, on: bool, stream=None) -> None:
+        """The reference's refusal once its excess list is empty (sg_unordered_set_excess_accounting); on by
+        default up to max_size() 2^20; only on an empty table."""
+        N.check(N.load().sg_unordered_set_excess_accounting(self._h, int(bool(on)), _stream(stream)),
+                "set_excess_accounting")
+
+    def excess_used(self, stream=None) -> int:
+        """Keys holding the reference's excess slots; -1 with the accounting off."""
+        out = c_int64()
+        N.check(N.load().sg_unordered_excess_used(self._h, _stream(stream), byref(out)), "excess_used")
+        return out.value
+
     def valid(self, stream=None) -> bool:
         out = c_int32()
         N.check(N.load().sg_unordered_valid(self._h, _stream(stream), byref(out)), "valid")

@@ -529,11 +529,15 @@ pool_release(void* p, void* ctx)
 sg_status
 create_server_table(sg_server* srv, int64_t capacity, void* stream, sg_unordered** out)
 {
-    if (srv->pool == nullptr)
+    const sg_status st = srv->pool == nullptr
+                                 ? sg_unordered_create(srv->kind, capacity, stream, out)
+                                 : sg_unordered_create_with_allocator(srv->kind, capacity, 0, &srv->table_alloc, stream, out);
+    if (st == SG_OK)
     {
-        return sg_unordered_create(srv->kind, capacity, stream, out);
+        // the server's launches take keys until no slot is free
+        sg::detail::unordered_accounting_off(*out);
     }
-    return sg_unordered_create_with_allocator(srv->kind, capacity, 0, &srv->table_alloc, stream, out);
+    return st;
 }
 
 int64_t

@@ -16,6 +16,11 @@ namespace detail
 
 extern std::atomic<long long> g_launches;
 
+// Switches a table just created (empty, nothing queued on it but its initialisation) to take keys until
+// no slot is free, without the reference's excess-list accounting and without a synchronisation: the
+// server's tables (unordered.cu).
+void unordered_accounting_off(sg_unordered* table);
+
 inline void
 count_launch(long long n = 1)
 {

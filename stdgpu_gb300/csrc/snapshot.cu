@@ -6,7 +6,9 @@
 // and the geometry it implies, the byte counts that follow), then the device header of the table, then the
 // raw slot image -- every 128-byte probe group plus the out-of-band tail group.  Loading recreates the
 // table from the capacity, checks that the geometry matches, and copies the image back, so the restored
-// table is bit for bit the saved one (erased slots included), whatever the keys' hash function.
+// table is bit for bit the saved one (erased slots included), whatever the keys' hash function.  A table
+// with the reference's excess-list accounting on (format version 2) also stores its two bit arrays after the
+// image; a version-1 file loads with the accounting off.
 // Copies go through one pinned staging buffer in 64 MB pieces.
 #include <cuda_runtime.h>
 
@@ -23,7 +25,7 @@ namespace
 {
 
 constexpr char kMagic[8] = { 'S', 'G', 'G', 'B', '3', '0', '0', 'T' };
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2;
 constexpr size_t kPiece = size_t{ 64 } << 20;
 
 struct file_header
@@ -39,7 +41,9 @@ struct file_header
     int64_t num_groups;
     int64_t header_bytes; // device table header
     int64_t image_bytes;  // probe groups + tail group
-    uint8_t reserved[128 - 8 - 16 - 6 * 8];
+    int64_t bucket_heads_bytes; // excess-list accounting (version 2): 0 when off
+    int64_t slot_heads_bytes;
+    uint8_t reserved[128 - 8 - 16 - 8 * 8];
 };
 static_assert(sizeof(file_header) == 128, "128-byte file header");
 
@@ -141,6 +145,11 @@ sg_unordered_save(sg_unordered* t, const char* path, void* stream)
     h.num_groups = g.num_groups;
     h.header_bytes = static_cast<int64_t>(sizeof(sg::detail::table_header));
     h.image_bytes = (g.num_groups + 1) * sg::detail::kGroupBytes;
+    if (v.bucket_heads != nullptr)
+    {
+        h.bucket_heads_bytes = (v.bucket_count + 31) / 32 * 4;
+        h.slot_heads_bytes = (v.num_groups * g.slots_per_group + 2 + 31) / 32 * 4;
+    }
     file_closer fc{ std::fopen(path, "wb") };
     if (fc.f == nullptr)
     {
@@ -161,7 +170,16 @@ sg_unordered_save(sg_unordered* t, const char* path, void* stream)
     {
         return st;
     }
-    return device_to_file(v.slots, h.image_bytes, fc.f, s, buf);
+    st = device_to_file(v.slots, h.image_bytes, fc.f, s, buf);
+    if (st == SG_OK && v.bucket_heads != nullptr)
+    {
+        st = device_to_file(v.bucket_heads, h.bucket_heads_bytes, fc.f, s, buf);
+        if (st == SG_OK)
+        {
+            st = device_to_file(v.slot_heads, h.slot_heads_bytes, fc.f, s, buf);
+        }
+    }
+    return st;
 }
 
 sg_status
@@ -179,9 +197,14 @@ sg_unordered_load(const char* path, void* stream, sg_unordered** out)
     }
     file_header h{};
     if (std::fread(&h, sizeof(h), 1, fc.f) != 1 || std::memcmp(h.magic, kMagic, sizeof(kMagic)) != 0 ||
-        h.version != kVersion)
+        h.version < 1 || h.version > kVersion)
     {
         return SG_ERR_BAD_ARG;
+    }
+    if (h.version == 1)
+    {
+        h.bucket_heads_bytes = 0;
+        h.slot_heads_bytes = 0;
     }
     // the file must describe exactly the table that createDeviceObject(capacity) builds
     sg_geometry g{};
@@ -192,11 +215,23 @@ sg_unordered_load(const char* path, void* stream, sg_unordered** out)
     {
         return SG_ERR_BAD_ARG;
     }
+    const bool accounting = h.bucket_heads_bytes != 0;
+    if (accounting && (h.bucket_heads_bytes != (g.bucket_count + 31) / 32 * 4 ||
+                       h.slot_heads_bytes != (g.num_groups * g.slots_per_group + 2 + 31) / 32 * 4))
+    {
+        return SG_ERR_BAD_ARG;
+    }
     sg_unordered* t = nullptr;
     sg_status st = h.custom_hash != 0 ? sg_unordered_create_hashed(h.kind, h.capacity, stream, &t)
                                       : sg_unordered_create(h.kind, h.capacity, stream, &t);
     if (st != SG_OK)
     {
+        return st;
+    }
+    st = sg_unordered_set_excess_accounting(t, accounting ? 1 : 0, stream);
+    if (st != SG_OK)
+    {
+        sg_unordered_destroy(t);
         return st;
     }
     sg_unordered_view v{};
@@ -212,6 +247,14 @@ sg_unordered_load(const char* path, void* stream, sg_unordered** out)
     if (st == SG_OK)
     {
         st = file_to_device(v.slots, h.image_bytes, fc.f, s, buf);
+    }
+    if (st == SG_OK && accounting)
+    {
+        st = file_to_device(v.bucket_heads, h.bucket_heads_bytes, fc.f, s, buf);
+        if (st == SG_OK)
+        {
+            st = file_to_device(v.slot_heads, h.slot_heads_bytes, fc.f, s, buf);
+        }
     }
     if (st != SG_OK)
     {

@@ -35,6 +35,12 @@ namespace detail
 
 std::atomic<long long> g_launches{ 0 };
 
+SG_D bool
+bit_set(const uint32_t* words, int64_t i)
+{
+    return (__ldcg(words + (i >> 5)) >> (i & 31)) & 1u;
+}
+
 // ---------------------------------------------------------------- kernels
 
 // Fills every slot with the never-used marker and the slots at or above total_count with the erased
@@ -75,6 +81,7 @@ k_init(dview t)
         t.hdr->size = 0;
         t.hdr->refused = 0;
         t.hdr->tombstones = 0;
+        t.hdr->excess_used = 0;
         t.hdr->special_state[0] = 0;
         t.hdr->special_state[1] = 0;
         t.hdr->error = 0;
@@ -765,6 +772,124 @@ k_erase(dview t, const void* keys, int64_t n, uint8_t* out_flags, const uint64_t
     block_add<2>(v, dst);
 }
 
+// Bulk insert / erase of a table with the reference's excess-list accounting on: one thread per key through
+// the device calls (sg::unordered_ref), which order the keys of one bucket under its stripe lock -- the
+// reference's per-key path (insert_value / erase_from_key, unordered_base_detail.cuh:470-522).  The result
+// is the reference's on one thread, which takes the keys in input order:
+//  * k_counted_candidates first finds, per bucket, the smallest input index of a key not stored yet -- in
+//    input order the first new key of that bucket, the one that takes the bucket's own slot if it is free;
+//    every other new key takes an excess slot (and a later pass resets the candidates);
+//  * a call of at most kCountedInOrderMax keys runs as one block, and when it could reach the refusal (the
+//    excess list or the table could run out within it), one thread takes its keys in input order, so which
+//    keys are refused is the same too.  A larger call that could reach it refuses keys in launch order.
+constexpr int64_t kCountedInOrderMax = 4096;
+constexpr uint32_t kNoCandidate = 0xFFFFFFFFu;
+
+template <int KIND>
+SG_D int64_t
+counted_bucket(const sg_unordered_view& v, typename kind_consts<KIND>::K key, const uint64_t* hashes, int64_t i)
+{
+    const uint64_t h = hashes != nullptr ? __ldg(hashes + i) : identity_word_hash{}(key);
+    return static_cast<int64_t>(fibonacci_bucket(h, v.bucket_bits));
+}
+
+// reset false: candidate per bucket (atomic minimum of the input indices of keys not stored); true: back to none.
+template <int KIND, bool AOS>
+__global__ void __launch_bounds__(kThreads)
+k_counted_candidates(sg_unordered_view v, const void* in0, const void* in1, int64_t n, const uint64_t* hashes,
+                     uint32_t* cand, bool reset)
+{
+    using C = kind_consts<KIND>;
+    const sg::unordered_ref<KIND> ref{ v };
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        typename C::K key;
+        typename C::V val;
+        load_input<KIND, AOS>(in0, in1, i, key, val);
+        const int64_t b = counted_bucket<KIND>(v, key, hashes, i);
+        if (reset)
+        {
+            cand[b] = kNoCandidate;
+        }
+        else if (ref.find_slot_home(key, group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups)) < 0)
+        {
+            atomicMin(cand + b, static_cast<uint32_t>(i));
+        }
+    }
+}
+
+template <int KIND, bool AOS>
+__global__ void __launch_bounds__(kThreads)
+k_insert_counted(sg_unordered_view v, const void* in0, const void* in1, int64_t n, uint8_t* out_flags,
+                 const uint64_t* hashes, const uint32_t* cand)
+{
+    using C = kind_consts<KIND>;
+    const sg::unordered_ref<KIND> ref{ v };
+    __shared__ int in_order;
+    int64_t first = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+    int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    if (gridDim.x == 1)
+    {
+        if (threadIdx.x == 0)
+        {
+            const unsigned long long used = *reinterpret_cast<volatile unsigned long long*>(&ref.header()->excess_used);
+            const unsigned long long size = *reinterpret_cast<volatile unsigned long long*>(&ref.header()->size);
+            in_order = used + static_cast<unsigned long long>(n) >= static_cast<unsigned long long>(v.excess_count) ||
+                       size + static_cast<unsigned long long>(n) >= static_cast<unsigned long long>(v.total_count);
+        }
+        __syncthreads();
+        if (in_order != 0)
+        {
+            if (threadIdx.x != 0)
+            {
+                return;
+            }
+            stride = 1;
+        }
+    }
+    for (int64_t i = first; i < n; i += stride)
+    {
+        typename C::K key;
+        typename C::V val;
+        load_input<KIND, AOS>(in0, in1, i, key, val);
+        const int64_t b = counted_bucket<KIND>(v, key, hashes, i);
+        // the bucket's own slot is for its candidate key (any copy of it)
+        const uint32_t c = cand[b];
+        bool first_new = false;
+        if (c != kNoCandidate)
+        {
+            typename C::K ck;
+            typename C::V cv;
+            load_input<KIND, AOS>(in0, in1, static_cast<int64_t>(c), ck, cv);
+            first_new = ck == key;
+        }
+        const int64_t slot = ref.insert_slot_bucket(key, val, b, first_new);
+        if (out_flags != nullptr)
+        {
+            out_flags[i] = static_cast<uint8_t>(slot >= 0);
+        }
+    }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kThreads)
+k_erase_counted(sg_unordered_view v, const void* keys, int64_t n, uint8_t* out_flags, const uint64_t* hashes)
+{
+    using K = typename kind_consts<KIND>::K;
+    const sg::unordered_ref<KIND> ref{ v };
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
+    {
+        const K key = __ldg(static_cast<const K*>(keys) + i);
+        const int64_t r = hashes != nullptr ? ref.erase_hashed(key, __ldg(hashes + i)) : ref.erase(key);
+        if (out_flags != nullptr)
+        {
+            out_flags[i] = static_cast<uint8_t>(r);
+        }
+    }
+}
+
 // Bulk find / contains (device-only find/contains in the reference, :619-706).
 template <int KIND, bool WANT_VALUES>
 __global__ void __launch_bounds__(kThreads, SG_FIND_MIN_BLOCKS)
@@ -908,6 +1033,62 @@ k_valid(dview t, sg_unordered_view v, unsigned long long* bad, bool check_reach)
     unsigned long long vv[2] = { live, wrong };
     unsigned long long* const dst[2] = { &t.hdr->count, bad };
     block_add<2>(vv, dst);
+}
+
+// valid() of the excess-list accounting: every set bit of slot_heads marks a stored key (and, with the
+// table's own hash, one whose bucket's bit is set); hdr->count gets the number of such keys, `bad` the
+// violations.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads)
+k_valid_heads(dview t, sg_unordered_view v, unsigned long long* bad, bool check_buckets)
+{
+    using C = kind_consts<KIND>;
+    using K = typename C::K;
+    constexpr int G = C::slots_per_group;
+    unordered_ref<KIND> ref{ v };
+    const int64_t nslots = static_cast<int64_t>(t.num_groups) * G;
+    const int64_t words = (nslots + 2 + 31) / 32;
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    unsigned long long heads = 0, wrong = 0;
+    for (int64_t w = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; w < words; w += stride)
+    {
+        unsigned bits = __ldcg(v.slot_heads + w);
+        heads += static_cast<unsigned long long>(__popc(bits));
+        while (bits != 0u)
+        {
+            const int64_t s = w * 32 + (__ffs(bits) - 1);
+            bits &= bits - 1u;
+            if (s >= nslots)
+            {
+                const int j = static_cast<int>(s - nslots);
+                const K k = j == 0 ? C::empty_key : C::tomb_key;
+                wrong += j > 1 || __ldcg(&t.hdr->special_state[j < 2 ? j : 0]) != 1u ||
+                         (check_buckets && !bit_set(v.bucket_heads, ref.bucket(k)));
+                continue;
+            }
+            const K k = __ldcg(reinterpret_cast<const K*>(t.slots + s * C::slot_bytes));
+            wrong += s >= t.total || k == C::empty_key || k == C::tomb_key ||
+                     (check_buckets && !bit_set(v.bucket_heads, ref.bucket(k)));
+        }
+    }
+    unsigned long long vv[2] = { heads, wrong };
+    unsigned long long* const dst[2] = { &t.hdr->count, bad };
+    block_add<2>(vv, dst);
+}
+
+// Set bits of a word array into *out.
+__global__ void __launch_bounds__(kThreads)
+k_popc_words(const uint32_t* w, int64_t n, unsigned long long* out)
+{
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    unsigned long long c = 0;
+    for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n; i += stride)
+    {
+        c += static_cast<unsigned long long>(__popc(__ldcg(w + i)));
+    }
+    unsigned long long vv[1] = { c };
+    unsigned long long* const dst[1] = { out };
+    block_add<1>(vv, dst);
 }
 
 // Compaction, pass 1: live slots per chunk of kRangeChunk slots.
@@ -1193,6 +1374,10 @@ struct sg_unordered
     int64_t lock_count;
     object_allocator oa;           // the table's own allocator (sg_unordered_create_with_allocator), or none
     void (*release_ctx)(void* ctx); // called with oa.ctx when the table is destroyed (nullable)
+    uint32_t* bucket_heads;        // the reference's excess-list accounting (sg_unordered_view), nullptr: off
+    uint32_t* slot_heads;
+    uint32_t* bucket_cand;         // a bulk insert's candidate per bucket (k_counted_candidates)
+    char* heads_block;             // their own block when switched on after creation, else nullptr (in `block`)
 };
 
 namespace
@@ -1223,7 +1408,41 @@ public_view(const sg_unordered* t)
     v.kind = t->kind;
     v.insert_locks = t->locks;
     v.lock_mask = t->lock_count - 1;
+    v.bucket_heads = t->bucket_heads;
+    v.slot_heads = t->slot_heads;
+    v.excess_count = t->excess_count;
     return v;
+}
+
+// The excess-list accounting's two bit arrays: one bit per bucket, one per slot (the two out-of-band slots
+// included), each rounded to 256 bytes.
+#ifndef SG_ACCOUNTING_DEFAULT_MAX
+#define SG_ACCOUNTING_DEFAULT_MAX (int64_t{ 1 } << 20) // on by default up to this max_size()
+#endif
+size_t
+bucket_heads_bytes(int64_t bucket_count)
+{
+    return static_cast<size_t>((bucket_count + 2047) / 2048 * 256);
+}
+
+size_t
+slot_heads_bytes(int64_t num_groups, int slot_bytes)
+{
+    const int64_t slots = num_groups * (kGroupBytes / slot_bytes) + 2;
+    return static_cast<size_t>((slots + 2047) / 2048 * 256);
+}
+
+// a bulk insert's candidate per bucket (k_counted_candidates)
+size_t
+bucket_cand_bytes(int64_t bucket_count)
+{
+    return static_cast<size_t>((bucket_count * 4 + 255) / 256 * 256);
+}
+
+size_t
+accounting_bytes(int64_t bucket_count, int64_t num_groups, int slot_bytes)
+{
+    return bucket_heads_bytes(bucket_count) + slot_heads_bytes(num_groups, slot_bytes) + bucket_cand_bytes(bucket_count);
 }
 
 // Stripe locks of the native device inserts: one per 16 probe groups, a power of two in [256, 2^22].
@@ -1255,6 +1474,10 @@ fill_geometry(int32_t kind, int64_t capacity, sg_geometry* g)
     const int64_t nchunks = (g->max_size + kRangeChunk - 1) / kRangeChunk;
     g->storage_bytes = (g->num_groups + 1) * kGroupBytes + static_cast<int64_t>(sizeof(table_header)) +
                        (nchunks + 1) * 4 + insert_lock_count(g->num_groups) * 4;
+    if (g->max_size <= SG_ACCOUNTING_DEFAULT_MAX)
+    {
+        g->storage_bytes += static_cast<int64_t>(accounting_bytes(b, g->num_groups, sb));
+    }
 }
 
 // Kernel dispatch over the six kinds.
@@ -1419,6 +1642,30 @@ use_partitioned_erase(const sg_unordered* t, int64_t n, const uint8_t* flags)
     return n >= (int64_t{ 1 } << 22) && bytes >= (int64_t{ 256 } << 20);
 }
 
+// Bulk insert of a table with the accounting on: candidates, the inserts, candidates reset.
+template <int KIND, bool AOS>
+sg_status
+insert_counted(sg_unordered* t, const void* in0, const void* in1, int64_t n, uint8_t* flags, cudaStream_t s,
+               const uint64_t* hashes)
+{
+    if (n >= (int64_t{ 1 } << 32) - 1)
+    {
+        return SG_ERR_BAD_ARG; // candidates are 32-bit input indices
+    }
+    const sg_unordered_view v = public_view(t);
+    static const int g_cand = persistent_grid(k_counted_candidates<KIND, AOS>, kThreads);
+    static const int g_ins = persistent_grid(k_insert_counted<KIND, AOS>, kThreads);
+    const int grid_cand = grid_for(n, kThreads, g_cand);
+    k_counted_candidates<KIND, AOS><<<grid_cand, kThreads, 0, s>>>(v, in0, in1, n, hashes, t->bucket_cand, false);
+    SG_LAUNCH_CHECK();
+    const int grid = n <= kCountedInOrderMax ? 1 : grid_for(n, kThreads, g_ins);
+    k_insert_counted<KIND, AOS><<<grid, kThreads, 0, s>>>(v, in0, in1, n, flags, hashes, t->bucket_cand);
+    SG_LAUNCH_CHECK();
+    k_counted_candidates<KIND, AOS><<<grid_cand, kThreads, 0, s>>>(v, in0, in1, n, hashes, t->bucket_cand, true);
+    SG_LAUNCH_CHECK();
+    return SG_OK;
+}
+
 template <int KIND>
 struct do_insert
 {
@@ -1426,6 +1673,11 @@ struct do_insert
     run(sg_unordered* t, const void* in0, const void* in1, bool aos, int64_t n, uint8_t* flags, cudaStream_t s,
         const uint64_t* hashes = nullptr)
     {
+        if (t->bucket_heads != nullptr)
+        {
+            return aos ? insert_counted<KIND, true>(t, in0, in1, n, flags, s, hashes)
+                       : insert_counted<KIND, false>(t, in0, in1, n, flags, s, hashes);
+        }
         part_layout pl{};
         unsigned long long* next_chunk = nullptr;
         sg_status st = SG_ERR_OOM;
@@ -1483,6 +1735,14 @@ struct do_erase
     static sg_status
     run(sg_unordered* t, const void* keys, int64_t n, uint8_t* flags, cudaStream_t s, const uint64_t* hashes = nullptr)
     {
+        if (t->bucket_heads != nullptr)
+        {
+            static const int max_grid = persistent_grid(k_erase_counted<KIND>, kThreads);
+            k_erase_counted<KIND><<<grid_for(n, kThreads, max_grid), kThreads, 0, s>>>(public_view(t), keys, n, flags,
+                                                                                      hashes);
+            SG_LAUNCH_CHECK();
+            return SG_OK;
+        }
         part_layout pl{};
         unsigned long long* next_chunk = nullptr;
         sg_status st = SG_ERR_OOM;
@@ -1576,6 +1836,21 @@ struct do_valid
 };
 
 template <int KIND>
+struct do_valid_heads
+{
+    static sg_status
+    run(sg_unordered* t, unsigned long long* bad, cudaStream_t s)
+    {
+        static const int max_grid = persistent_grid(k_valid_heads<KIND>, kThreads);
+        const int64_t words = (t->num_groups * (kGroupBytes / t->slot_bytes) + 2 + 31) / 32;
+        k_valid_heads<KIND><<<grid_for(words, kThreads, max_grid), kThreads, 0, s>>>(view_of(t), public_view(t), bad,
+                                                                                    !t->custom_hash);
+        SG_LAUNCH_CHECK();
+        return SG_OK;
+    }
+};
+
+template <int KIND>
 struct do_range
 {
     static sg_status
@@ -1625,6 +1900,20 @@ host_header(const sg_unordered* t)
 
 } // namespace
 
+namespace sg
+{
+namespace detail
+{
+void
+unordered_accounting_off(sg_unordered* t)
+{
+    t->bucket_heads = nullptr;
+    t->slot_heads = nullptr;
+    t->bucket_cand = nullptr;
+}
+} // namespace detail
+} // namespace sg
+
 extern "C" {
 
 sg_status
@@ -1669,6 +1958,31 @@ sg_unordered_geometry_for(int32_t kind, int64_t capacity, sg_geometry* out)
 namespace
 {
 
+// The accounting's arrays, carved from `base` (accounting_bytes of room).
+void
+place_accounting(sg_unordered* t, char* base)
+{
+    t->bucket_heads = reinterpret_cast<uint32_t*>(base);
+    t->slot_heads = reinterpret_cast<uint32_t*>(base + bucket_heads_bytes(t->bucket_count));
+    t->bucket_cand = reinterpret_cast<uint32_t*>(base + bucket_heads_bytes(t->bucket_count) +
+                                                 slot_heads_bytes(t->num_groups, t->slot_bytes));
+}
+
+// The accounting of an empty table: no bucket's own slot taken, no excess slot used, no candidates.
+sg_status
+reset_accounting(sg_unordered* t, cudaStream_t s)
+{
+    if (t->bucket_heads == nullptr)
+    {
+        return SG_OK;
+    }
+    SG_CUDA_TRY(cudaMemsetAsync(t->bucket_heads, 0, bucket_heads_bytes(t->bucket_count), s));
+    SG_CUDA_TRY(cudaMemsetAsync(t->slot_heads, 0, slot_heads_bytes(t->num_groups, t->slot_bytes), s));
+    SG_CUDA_TRY(cudaMemsetAsync(t->bucket_cand, 0xFF, bucket_cand_bytes(t->bucket_count), s));
+    SG_CUDA_TRY(cudaMemsetAsync(&t->hdr->excess_used, 0, sizeof(unsigned long long), s));
+    return SG_OK;
+}
+
 sg_status
 create_table(int32_t kind, int64_t capacity, const object_allocator& oa, void* stream, sg_unordered** out)
 {
@@ -1710,7 +2024,10 @@ create_table(int32_t kind, int64_t capacity, const object_allocator& oa, void* s
     const size_t off_hdr = up(static_cast<size_t>((t->num_groups + 1) * kGroupBytes));
     const size_t off_counts = off_hdr + up(sizeof(table_header));
     const size_t off_locks = off_counts + up(static_cast<size_t>(t->nchunks + 1) * sizeof(unsigned int));
-    const size_t block_bytes = off_locks + static_cast<size_t>(t->lock_count) * sizeof(unsigned int);
+    const bool accounting = t->total <= SG_ACCOUNTING_DEFAULT_MAX;
+    const size_t off_bheads = off_locks + up(static_cast<size_t>(t->lock_count) * sizeof(unsigned int));
+    const size_t block_bytes = accounting ? off_bheads + accounting_bytes(t->bucket_count, t->num_groups, t->slot_bytes)
+                                          : off_locks + static_cast<size_t>(t->lock_count) * sizeof(unsigned int);
     cudaError_t e = sg::detail::obj_malloc(t->oa, &t->block, block_bytes);
     if (e == cudaSuccess)
     {
@@ -1718,6 +2035,10 @@ create_table(int32_t kind, int64_t capacity, const object_allocator& oa, void* s
         t->hdr = reinterpret_cast<table_header*>(t->block + off_hdr);
         t->chunk_counts = reinterpret_cast<unsigned int*>(t->block + off_counts);
         t->locks = reinterpret_cast<unsigned int*>(t->block + off_locks);
+        if (accounting)
+        {
+            place_accounting(t, t->block + off_bheads);
+        }
         t->host_hdr = static_cast<unsigned long long*>(pinned_headers().get());
         if (t->host_hdr == nullptr)
         {
@@ -1727,6 +2048,10 @@ create_table(int32_t kind, int64_t capacity, const object_allocator& oa, void* s
     if (e == cudaSuccess)
     {
         e = cudaMemsetAsync(t->locks, 0, static_cast<size_t>(t->lock_count) * sizeof(unsigned int), as_stream(stream));
+    }
+    if (e == cudaSuccess && accounting && reset_accounting(t, as_stream(stream)) != SG_OK)
+    {
+        e = cudaErrorUnknown;
     }
     if (e != cudaSuccess)
     {
@@ -1742,6 +2067,44 @@ create_table(int32_t kind, int64_t capacity, const object_allocator& oa, void* s
     }
     *out = t;
     return SG_OK;
+}
+
+// Switches the accounting of an empty table on or off (no checks); the arrays of a table created without
+// them get their own block.
+sg_status
+set_accounting(sg_unordered* t, bool on, cudaStream_t s)
+{
+    if (!on)
+    {
+        t->bucket_heads = nullptr;
+        t->slot_heads = nullptr;
+        t->bucket_cand = nullptr;
+        return SG_OK;
+    }
+    if (t->bucket_heads == nullptr)
+    {
+        const auto up = [](size_t x) { return (x + 255) / 256 * 256; };
+        if (t->total <= SG_ACCOUNTING_DEFAULT_MAX)
+        {
+            // create_table placed them in the table's block, after the stripe locks
+            const size_t off_counts = up(static_cast<size_t>((t->num_groups + 1) * kGroupBytes)) + up(sizeof(table_header));
+            const size_t off_locks = off_counts + up(static_cast<size_t>(t->nchunks + 1) * sizeof(unsigned int));
+            place_accounting(t, t->block + off_locks + up(static_cast<size_t>(t->lock_count) * sizeof(unsigned int)));
+        }
+        else
+        {
+            if (t->heads_block == nullptr &&
+                sg::detail::obj_malloc(t->oa, &t->heads_block,
+                                       accounting_bytes(t->bucket_count, t->num_groups, t->slot_bytes)) != cudaSuccess)
+            {
+                t->heads_block = nullptr;
+                cudaGetLastError();
+                return SG_ERR_OOM;
+            }
+            place_accounting(t, t->heads_block);
+        }
+    }
+    return reset_accounting(t, s);
 }
 
 } // namespace
@@ -1791,6 +2154,10 @@ sg_unordered_destroy(sg_unordered* t)
     if (t->part_scratch != nullptr)
     {
         sg::detail::obj_free(t->oa, t->part_scratch);
+    }
+    if (t->heads_block != nullptr)
+    {
+        sg::detail::obj_free(t->oa, t->heads_block);
     }
     if (t->host_hdr != nullptr)
     {
@@ -1955,6 +2322,10 @@ sg_unordered_rehash(sg_unordered* t, int64_t new_capacity, void* stream)
     {
         st = create_table(t->kind, new_capacity, t->oa, stream, &fresh);
     }
+    if (st == SG_OK)
+    {
+        st = set_accounting(fresh, t->bucket_heads != nullptr, s);
+    }
     if (st == SG_OK && copied > 0)
     {
         st = dispatch<do_insert>(fresh->kind, fresh, buf, mb > 0 ? buf + kbytes : nullptr, false, copied, nullptr, s);
@@ -2090,7 +2461,50 @@ sg_unordered_clear(sg_unordered* t, void* stream)
     {
         return SG_ERR_BAD_ARG;
     }
-    return dispatch<do_init>(t->kind, t, as_stream(stream));
+    const sg_status st = reset_accounting(t, as_stream(stream));
+    return st != SG_OK ? st : dispatch<do_init>(t->kind, t, as_stream(stream));
+}
+
+sg_status
+sg_unordered_set_excess_accounting(sg_unordered* t, int32_t on, void* stream)
+{
+    if (t == nullptr || (on != 0 && on != 1))
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    cudaStream_t s = as_stream(stream);
+    sg_status st = read_header(t, s);
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    const table_header& h = host_header(t);
+    if (h.size != 0)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    return set_accounting(t, on != 0, s);
+}
+
+sg_status
+sg_unordered_excess_used(sg_unordered* t, void* stream, int64_t* out)
+{
+    if (t == nullptr || out == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (t->bucket_heads == nullptr)
+    {
+        *out = -1;
+        return SG_OK;
+    }
+    sg_status st = read_header(t, as_stream(stream));
+    if (st != SG_OK)
+    {
+        return st;
+    }
+    *out = static_cast<int64_t>(host_header(t).excess_used);
+    return SG_OK;
 }
 
 sg_status
@@ -2101,9 +2515,9 @@ sg_unordered_valid(sg_unordered* t, void* stream, int32_t* out_valid)
         return SG_ERR_BAD_ARG;
     }
     cudaStream_t s = as_stream(stream);
-    // hdr->count accumulates live slots; pad1[0] accumulates violations
-    SG_CUDA_TRY(cudaMemsetAsync(&t->hdr->count, 0, 3 * sizeof(unsigned long long), s));
-    sg_status st = dispatch<do_valid>(t->kind, t, &t->hdr->pad1[0], s);
+    // hdr->count accumulates live slots; hdr->scratch accumulates violations
+    SG_CUDA_TRY(cudaMemsetAsync(&t->hdr->count, 0, 2 * sizeof(unsigned long long), s));
+    sg_status st = dispatch<do_valid>(t->kind, t, &t->hdr->scratch, s);
     if (st != SG_OK)
     {
         return st;
@@ -2121,7 +2535,36 @@ sg_unordered_valid(sg_unordered* t, void* stream, int32_t* out_valid)
         ok = ok && (h.special_state[sp] <= 1u);
         specials += (h.special_state[sp] == 1u);
     }
-    ok = ok && h.pad1[0] == 0 && (h.count + specials == h.size);
+    ok = ok && h.scratch == 0 && (h.count + specials == h.size);
+    if (ok && t->bucket_heads != nullptr)
+    {
+        // the accounting: keys marked as holding their bucket's own slot, as many as buckets marked taken,
+        // and with the keys in excess slots they make up the size
+        const unsigned long long size = h.size, used = h.excess_used;
+        SG_CUDA_TRY(cudaMemsetAsync(&t->hdr->count, 0, 2 * sizeof(unsigned long long), s));
+        st = dispatch<do_valid_heads>(t->kind, t, &t->hdr->scratch, s);
+        if (st == SG_OK)
+        {
+            st = read_header(t, s);
+        }
+        if (st != SG_OK)
+        {
+            return st;
+        }
+        const unsigned long long heads = h.count;
+        ok = h.scratch == 0 && used <= static_cast<unsigned long long>(t->excess_count) && heads + used == size;
+        SG_CUDA_TRY(cudaMemsetAsync(&t->hdr->count, 0, sizeof(unsigned long long), s));
+        const int64_t words = (t->bucket_count + 31) / 32;
+        static const int max_grid = persistent_grid(k_popc_words, kThreads);
+        k_popc_words<<<grid_for(words, kThreads, max_grid), kThreads, 0, s>>>(t->bucket_heads, words, &t->hdr->count);
+        SG_LAUNCH_CHECK();
+        st = read_header(t, s);
+        if (st != SG_OK)
+        {
+            return st;
+        }
+        ok = ok && h.count == heads;
+    }
     *out_valid = ok ? 1 : 0;
     return SG_OK;
 }

@@ -103,6 +103,8 @@ def run_serial(caps, staged, arrivals=None, sync_each: bool = True, kernel_times
     the loop rehashes a table before an insert that needs room, by the server's policy (the tables then
     start at the admitted capacities); without it the tables must already be large enough."""
     tables = [C.unordered_map.createDeviceObject(int(c), key="u64", mapped="u64") for c in caps]
+    for t in tables:
+        t.set_excess_accounting(False)  # the server's tables: keys until no slot is free, tile kernels
     reqs = [N.sg_request(t, op, k.numel(), k.data_ptr(), v.data_ptr() if v is not None else None,
                          ov.data_ptr() if ov is not None else None, of.data_ptr())
             for t, op, k, v, ov, of in staged]

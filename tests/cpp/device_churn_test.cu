@@ -4,8 +4,10 @@
 // keys of a small key set with several threads per key; inserts and erases of different keys share a
 // launch.  After every launch the per-key outcomes and size() match a std::unordered_set /
 // std::unordered_map model, and no insert of an absent key is refused while the table holds fewer than
-// max_size() keys.  A second part races inserts and erases of the same keys in one launch and checks the
-// invariants that hold for any interleaving; a third fills the table to max_size() through churn.
+// max_size() keys (part 1 keeps fewer live keys than the reference's excess list has slots; parts 1b and 3
+// switch the excess-list accounting off, so their tables take keys up to max_size()).  A second part races
+// inserts and erases of the same keys in one launch and checks the invariants that hold for any
+// interleaving; a third fills the table to max_size() through churn.
 //
 // usage: device_churn_test [out_dir]  -- with out_dir, the launches of the first part (keys and per-thread
 // outcomes) are written there for a replay on the oracle.  Prints one line per check and "ALL PASS".
@@ -263,6 +265,7 @@ main(int argc, char** argv)
     // ---- part 1b: the same churn on unordered_map<uint64_t, uint32_t>: a re-inserted key takes its new value
     {
         map_t m = map_t::createDeviceObject(100);
+        m.set_excess_accounting(false); // keys until no slot is free: up to max_size() - 2 live keys
         const int max_size = m.max_size();
         std::vector<std::uint64_t> universe;
         for (int i = 0; i < max_size - 2; ++i)
@@ -418,6 +421,7 @@ main(int argc, char** argv)
     // ---- part 3: churn until the table is full, then refusal exactly at max_size()
     {
         set_t s = set_t::createDeviceObject(32);
+        s.set_excess_accounting(false); // keys until no slot is free, the reference's excess list aside
         const int max_size = s.max_size();
         std::vector<std::uint64_t> keys;
         for (int i = 0; i < 4 * max_size; ++i)

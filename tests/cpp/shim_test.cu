@@ -479,6 +479,30 @@ main()
         set_t::destroyDeviceObject(s);
     }
 
+    // insert_while_excess_empty below max_size(): capacity 3 has 7 slots, but the reference refuses once its
+    // excess list (3 slots) is empty.  Keys and outcomes recorded from the reference (tests/golden/refusal.npz,
+    // capacity 3), one device insert per launch in that order; then 10^5 device inserts of a new key are all
+    // refused.
+    {
+        const std::uint64_t keys3[16] = { 1638364144ull,   1070330891283ull, 328095614449ull,  345231260195ull,
+                                          980446690571ull, 643393456553ull,  518210457150ull,  850227063600ull,
+                                          33365788281ull,  777316343105ull,  411485446533ull,  99893614912ull,
+                                          726227504283ull, 1024155339141ull, 227809098477ull,  692791501211ull };
+        const int expect3[16] = { 1, 1, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0 };
+        set_t s = set_t::createDeviceObject(3);
+        check(s.max_size() == 7, "capacity 3 geometry");
+        bool same = true;
+        for (int i = 0; i < 16; ++i)
+        {
+            k_insert_same<<<1, 1>>>(s, keys3[i], 1, flags);
+            same = same && to_host(flags, 1)[0] == expect3[i];
+        }
+        check(same && s.size() == 6 && !s.full() && s.valid(), "insert_while_excess_empty (device inserts, capacity 3)");
+        k_insert_same<<<blocks, threads>>>(s, 1ull << 40, N, flags);
+        check(sum_of(flags, N) == 0 && s.size() == 6 && s.valid(), "insert_parallel_while_excess_empty");
+        set_t::destroyDeviceObject(s);
+    }
+
     // vector push_back from a user kernel (tests/stdgpu/vector.inc:404-512)
     {
         stdgpu::vector<std::uint32_t> v = stdgpu::vector<std::uint32_t>::createDeviceObject(N);

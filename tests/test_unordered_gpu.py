@@ -158,16 +158,25 @@ def test_capacity_one_refuses_like_reference():
     t.close()
 
 
-def test_refusal_when_full_matches_reference(golden):
-    """Sequential inserts into tiny tables, at capacities where the reference refuses because it is full."""
+@pytest.mark.parametrize("one_call", [False, True])
+def test_refusal_matches_reference(golden, one_call):
+    """Inserts into tiny tables until the reference refuses: at capacities 1, 2 and 8 because the table is
+    full, at 3, 4 and 5 because its excess list is empty below max_size() (the excess-list accounting, on by
+    default at these sizes).  Key by key, and as one bulk call (the reference on one thread)."""
     g = golden("refusal.npz")
-    for cap in [1, 2, 8]:
-        assert int(g[f"size_{cap}"]) == int(g[f"max_size_{cap}"])  # full-table refusals only
+    for cap in [1, 2, 3, 4, 5, 8]:
         t = Table(O.SET_U64, cap)
         keys = g[f"keys_{cap}"]
-        flags = [int(t.insert(keys[i:i + 1])[0]) for i in range(len(keys))]
+        if one_call:
+            flags = t.insert(keys).tolist()
+        else:
+            flags = [int(t.insert(keys[i:i + 1])[0]) for i in range(len(keys))]
         assert flags == g[f"flags_{cap}"].tolist(), cap
         assert t.size() == int(g[f"size_{cap}"]) and t.valid()
+        assert t.t.max_size() == int(g[f"max_size_{cap}"])
+        P = O.PortTable(O.SET_U64, cap)
+        P.insert(keys, flags=True)
+        assert t.t.excess_used() == P.excess_used()
         t.close()
 
 
