@@ -15,8 +15,11 @@
 // src/stdgpu/impl/unordered_base_detail.cuh:56-85, :547-564, scaled onto the groups) are those of the
 // library's own tables, and so are the slot rules: a never-used word is all ones, an erased word all ones
 // minus one; a key lives in the first group of its probe chain that had a never-used slot when it was
-// inserted, so a lookup stops at the first group with a never-used slot; a bulk insert may take an erased
-// slot of that group, a device insert only never-used slots (it may run beside device erases).
+// inserted, so a lookup stops at the first group with a never-used slot; an insert may take an erased slot
+// of that group (or, once no never-used slot is left anywhere, the first erased slot of its chain).  Device
+// inserts, which may run beside device erases, hold the stripe lock of the key's home group while they scan
+// and claim, so two device inserts of one key are ordered (the reference locks the bucket,
+// src/stdgpu/impl/unordered_base_detail.cuh:708-809).
 //
 // Keys compare with KeyEqual, as the reference compares them on every probe
 // (src/stdgpu/impl/unordered_base_detail.cuh:661, :673): a probe accepts a stored key when KeyEqual holds for
@@ -240,6 +243,8 @@ struct wide_ref
     W* keys = nullptr;
     value_store* values = nullptr;
     wide_header* hdr = nullptr;
+    unsigned int* locks = nullptr; // stripe locks of the device inserts, lock_mask + 1 of them
+    std::int64_t lock_mask = 0;
     std::int64_t max_size = 0;
     std::int64_t num_groups = 0;
     std::int64_t bucket_count = 0;
@@ -490,43 +495,107 @@ struct wide_ref
         {
             return special_insert(sp, mapped);
         }
-        std::int64_t g = home(hash);
-        for (std::int64_t n = 0; n < num_groups; ++n)
+        for (int attempt = 0; attempt < kWideRetry; ++attempt)
         {
-            for (int tries = 0;; ++tries)
+            std::int64_t g = home(hash);
+            std::int64_t first_tomb = -1; // the chain's first erased slot, for a table without never-used slots
+            for (std::int64_t n = 0; n < num_groups; ++n)
             {
-                const group_masks m = scan(g, [&](const W& x) { return same(x, w); });
-                if (m.match != 0u)
+                for (int tries = 0;; ++tries)
                 {
-                    return { g * G + (__ffs(m.match) - 1), false };
+                    const group_masks m = scan(g, [&](const W& x) { return same(x, w); });
+                    if (m.match != 0u)
+                    {
+                        return { g * G + (__ffs(m.match) - 1), false };
+                    }
+                    if (m.free == 0u)
+                    {
+                        if (first_tomb < 0 && m.tomb != 0u)
+                        {
+                            first_tomb = g * G + (__ffs(m.tomb) - 1);
+                        }
+                        break; // the chain goes on
+                    }
+                    if (tries >= kWideRetry)
+                    {
+                        atomicOr(&hdr->error, sg::detail::kErrRetry);
+                        return { -1, false };
+                    }
+                    const bool take_tomb = reuse_tombs && m.tomb != 0u;
+                    const std::int64_t slot = g * G + (__ffs(take_tomb ? m.tomb : m.free) - 1);
+                    const W expected = take_tomb ? WW::tomb() : WW::empty();
+                    const W old = WW::cas(keys + slot, expected, w);
+                    if (old == expected)
+                    {
+                        construct(slot, mapped);
+                        return { slot, true };
+                    }
+                    if (old != WW::empty() && old != WW::tomb() && same(old, w))
+                    {
+                        return { slot, false };
+                    }
+                    // another key took the slot: read the group again
                 }
-                if (m.free == 0u)
-                {
-                    break; // the chain goes on
-                }
-                if (tries >= kWideRetry)
-                {
-                    atomicOr(&hdr->error, sg::detail::kErrRetry);
-                    return { -1, false };
-                }
-                const bool take_tomb = reuse_tombs && m.tomb != 0u;
-                const std::int64_t slot = g * G + (__ffs(take_tomb ? m.tomb : m.free) - 1);
-                const W expected = take_tomb ? WW::tomb() : WW::empty();
-                const W old = WW::cas(keys + slot, expected, w);
-                if (old == expected)
-                {
-                    construct(slot, mapped);
-                    return { slot, true };
-                }
-                if (old != WW::empty() && old != WW::tomb() && same(old, w))
-                {
-                    return { slot, false };
-                }
-                // another key took the slot: read the group again
+                g = g + 1 == num_groups ? 0 : g + 1;
             }
-            g = g + 1 == num_groups ? 0 : g + 1;
+            // no never-used slot left anywhere: the chain's first erased slot (every slot was read, so the key
+            // is absent), else refused
+            if (!reuse_tombs || first_tomb < 0)
+            {
+                return { -1, false };
+            }
+            const W old = WW::cas(keys + first_tomb, WW::tomb(), w);
+            if (old == WW::tomb())
+            {
+                construct(first_tomb, mapped);
+                return { first_tomb, true };
+            }
+            if (old != WW::empty() && same(old, w))
+            {
+                return { first_tomb, false };
+            }
+            // another key took that slot meanwhile: read the chain again
         }
-        return { -1, false }; // no never-used slot left anywhere: refused
+        atomicOr(&hdr->error, sg::detail::kErrRetry);
+        return { -1, false };
+    }
+
+    // Device insert (insert / emplace, unordered_base_detail.cuh:958-994) under the stripe lock of the key's
+    // home group: erased slots are reused beside device erases.  A key found present without the lock, or
+    // stored by another thread while this one waits, decides the call without it.
+    __device__ wide_insert_result
+    insert_word_locked(const W& w, std::uint64_t hash, const value_store* mapped) const
+    {
+        if (special_of(w) >= 0 || locks == nullptr)
+        {
+            return insert_word(w, hash, false, mapped);
+        }
+        std::int64_t slot = find_word(w, hash);
+        if (slot >= 0)
+        {
+            return { slot, false };
+        }
+        unsigned int* l = locks + (static_cast<std::uint64_t>(home(hash)) & static_cast<std::uint64_t>(lock_mask));
+        unsigned int backoff = 32;
+        for (long long polls = 0; polls < sg::detail::kWaitLimit; ++polls)
+        {
+            if (*reinterpret_cast<volatile unsigned int*>(l) == 0u && atomicCAS(l, 0u, 1u) == 0u)
+            {
+                __threadfence();
+                const wide_insert_result r = insert_word(w, hash, true, mapped);
+                __threadfence();
+                atomicExch(l, 0u);
+                return r;
+            }
+            if ((polls & 15) == 15 && (slot = find_word(w, hash)) >= 0)
+            {
+                return { slot, false };
+            }
+            __nanosleep(backoff);
+            backoff = backoff < 256 ? backoff * 2 : 256;
+        }
+        atomicOr(&hdr->error, sg::detail::kErrRetry);
+        return { -1, false };
     }
 
     // Erase of key word w (try_erase, src/stdgpu/impl/unordered_base_detail.cuh:811-913); the caller counts it.
@@ -920,8 +989,15 @@ public:
             ++t.bucket_bits;
         }
         const std::int64_t slots = t.end_slot();
+        std::int64_t nlocks = 256; // one per 16 probe groups, a power of two in [256, 2^22]
+        while (nlocks < t.num_groups / 16 && nlocks < (std::int64_t{ 1 } << 22))
+        {
+            nlocks <<= 1;
+        }
+        t.lock_mask = nlocks - 1;
         bool ok = d.block(&t.keys, sizeof(W) * slots) && d.block(&t.hdr, sizeof(wide_header)) &&
-                  d.block(&d._range, sizeof(std::int32_t) * (geo.max_size + 2));
+                  d.block(&d._range, sizeof(std::int32_t) * (geo.max_size + 2)) &&
+                  d.block(&t.locks, sizeof(unsigned int) * nlocks);
         if (ok && ref_type::has_values)
         {
             ok = d.block(&t.values, sizeof(value_store) * slots);
@@ -934,6 +1010,7 @@ public:
         }
         const bool set = cudaMemsetAsync(t.keys, 0xff, sizeof(W) * slots, policy.stream) == cudaSuccess &&
                          cudaMemsetAsync(t.hdr, 0, sizeof(wide_header), policy.stream) == cudaSuccess &&
+                         cudaMemsetAsync(t.locks, 0, sizeof(unsigned int) * nlocks, policy.stream) == cudaSuccess &&
                          cudaStreamSynchronize(policy.stream) == cudaSuccess;
         gb300_check(set ? SG_OK : SG_ERR_CUDA, "createDeviceObject");
         return d;
@@ -1211,6 +1288,7 @@ protected:
         d.unblock(d._t.values);
         d.unblock(d._t.hdr);
         d.unblock(d._range);
+        d.unblock(d._t.locks);
         if (d._alloc.release_ctx != nullptr)
         {
             d._alloc.release_ctx(d._alloc.ctx);
@@ -1241,13 +1319,13 @@ protected:
         return iterator{ _t.keys + slot, ref_type::has_values ? _t.values + slot : nullptr };
     }
 
-    // insert(value) / emplace (unordered_base_detail.cuh:958-994); never-used slots only, so it may run
-    // beside device erases
+    // insert(value) / emplace (unordered_base_detail.cuh:958-994) under the key's stripe lock, so erased
+    // slots are reused beside device erases
     __device__ pair<iterator, bool>
     insert_impl(const key_type& key, const value_store* mapped) const
     {
         const wide_insert_result r =
-                _t.insert_word(to_wide<W>(key), static_cast<std::uint64_t>(Hash{}(key)), false, mapped);
+                _t.insert_word_locked(to_wide<W>(key), static_cast<std::uint64_t>(Hash{}(key)), mapped);
         if (!r.inserted)
         {
             return pair<iterator, bool>(end(), false);

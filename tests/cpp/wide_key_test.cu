@@ -654,6 +654,144 @@ refusal_when_full()
     cudaFree(d_n);
 }
 
+template <typename Table>
+__global__ void
+k_churn(Table t, const vec3int32* keys, const std::uint8_t* is_insert, int n, std::uint8_t* ok)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n)
+    {
+        ok[i] = is_insert[i] != 0 ? (t.insert(keys[i]).second ? 1 : 0) : (t.erase(keys[i]) == 1 ? 1 : 0);
+    }
+}
+
+// Device-only insert / erase churn of 12-byte keys (the reference's voxel-block pattern): every launch
+// inserts some keys of a small set and erases others, three threads per key, in shuffled thread order.
+// After every launch the per-key outcomes and size() equal a std::unordered_set model: erased slots are
+// reused, so no insert is refused below max_size().  Then blocks of max_size() keys are inserted and erased
+// until no never-used slot is left, and the table still fills to exactly max_size().
+static void
+device_churn_reuses_erased_slots()
+{
+    std::mt19937 rng(77);
+    nontrivial_set s = nontrivial_set::createDeviceObject(64);
+    const int max_size = static_cast<int>(s.max_size());
+    std::vector<vec3int32> universe;
+    for (int i = 0; i < 40; ++i)
+    {
+        universe.push_back(vec3int32(i * 7 - 100, i % 5, -i));
+    }
+    std::unordered_set<int> present;
+    bool same = true;
+    for (int l = 0; l < 300; ++l)
+    {
+        std::vector<vec3int32> keys;
+        std::vector<std::uint8_t> ins;
+        std::vector<int> which;
+        for (int k = 0; k < 40; ++k)
+        {
+            const int r = static_cast<int>(rng() % 3); // 0 nothing, 1 insert, 2 erase
+            for (int c = 0; r != 0 && c < 3; ++c)
+            {
+                keys.push_back(universe[k]);
+                ins.push_back(r == 1 ? 1 : 0);
+                which.push_back(k);
+            }
+        }
+        std::vector<int> order(keys.size());
+        for (size_t i = 0; i < order.size(); ++i)
+        {
+            order[i] = static_cast<int>(i);
+        }
+        std::shuffle(order.begin(), order.end(), rng);
+        std::vector<vec3int32> k2;
+        std::vector<std::uint8_t> i2;
+        std::vector<int> w2;
+        for (int o : order)
+        {
+            k2.push_back(keys[o]);
+            i2.push_back(ins[o]);
+            w2.push_back(which[o]);
+        }
+        const int n = static_cast<int>(k2.size());
+        if (n == 0)
+        {
+            continue;
+        }
+        vec3int32* dk = to_device(k2);
+        std::uint8_t* di = to_device(i2);
+        std::uint8_t* dok = nullptr;
+        cudaMalloc(&dok, n);
+        k_churn<<<(n + 127) / 128, 128>>>(s, dk, di, n, dok);
+        const std::vector<std::uint8_t> ok = to_host(dok, n);
+        std::vector<int> wins(40, 0);
+        for (int i = 0; i < n; ++i)
+        {
+            wins[w2[i]] += ok[i];
+        }
+        for (int k = 0; k < 40; ++k)
+        {
+            bool inserted = false, erased = false;
+            for (int i = 0; i < n; ++i)
+            {
+                inserted |= w2[i] == k && i2[i] == 1;
+                erased |= w2[i] == k && i2[i] == 0;
+            }
+            if (inserted)
+            {
+                same = same && wins[k] == (present.count(k) ? 0 : 1);
+                present.insert(k);
+            }
+            else if (erased)
+            {
+                same = same && wins[k] == (present.count(k) ? 1 : 0);
+                present.erase(k);
+            }
+        }
+        same = same && s.size() == static_cast<stdgpu::index_t>(present.size());
+        cudaFree(dk);
+        cudaFree(di);
+        cudaFree(dok);
+    }
+    check(same && s.valid(), "wide device churn: per-key outcomes and size() equal the model after every launch");
+    // clear the rest, then blocks of max_size() keys in and out until every slot has been used
+    nontrivial_set::destroyDeviceObject(s);
+    s = nontrivial_set::createDeviceObject(64);
+    bool filled = true;
+    for (int b = 0; b < 4; ++b)
+    {
+        std::vector<vec3int32> blk;
+        std::vector<std::uint8_t> one(max_size, 1), zero(max_size, 0);
+        for (int i = 0; i < max_size; ++i)
+        {
+            blk.push_back(vec3int32(1000 * b + i, b, i));
+        }
+        vec3int32* dk = to_device(blk);
+        std::uint8_t* d1 = to_device(one);
+        std::uint8_t* d0 = to_device(zero);
+        std::uint8_t* dok = nullptr;
+        cudaMalloc(&dok, max_size);
+        k_churn<<<(max_size + 127) / 128, 128>>>(s, dk, d1, max_size, dok);
+        int c = 0;
+        for (auto x : to_host(dok, max_size))
+        {
+            c += x;
+        }
+        filled = filled && c == max_size && s.size() == max_size;
+        if (b < 3)
+        {
+            k_churn<<<(max_size + 127) / 128, 128>>>(s, dk, d0, max_size, dok);
+            filled = filled && s.size() == 0;
+        }
+        cudaFree(dk);
+        cudaFree(d1);
+        cudaFree(d0);
+        cudaFree(dok);
+    }
+    check(filled && s.valid(), "wide device churn: erased slots refill the table to exactly max_size()");
+    nontrivial_set::destroyDeviceObject(s);
+}
+
 int
 main()
 {
@@ -664,6 +802,7 @@ main()
     u64_keys_with_payload();
     mapped_destructors();
     refusal_when_full();
+    device_churn_reuses_erased_slots();
     const cudaError_t e = cudaDeviceSynchronize();
     check(e == cudaSuccess, "no CUDA error");
     if (failures == 0)

@@ -31,9 +31,12 @@ def test_save_load_round_trip(tmp_path):
     path = tmp_path / "map.sgt"
     t.save(path)
     g = t.geometry()
-    assert path.stat().st_size == 128 + 64 + (g.num_groups + 1) * 128
+    # header, device header, slot image, then the excess-list accounting's bit arrays (on at this size)
+    assert t.excess_used() >= 0
+    acct = (g.bucket_count + 31) // 32 * 4 + (g.num_groups * g.slots_per_group + 2 + 31) // 32 * 4
+    assert path.stat().st_size == 128 + 64 + (g.num_groups + 1) * 128 + acct
     u = sg.unordered_map.load(path)
-    assert u.kind == t.kind and u.size() == t.size() and u.valid()
+    assert u.kind == t.kind and u.size() == t.size() and u.valid() and u.excess_used() == t.excess_used()
     assert u.max_size() == t.max_size() and u.bucket_count() == t.bucket_count()
     # same slots, in the same order
     assert torch.equal(u.device_range(), t.device_range())
