@@ -54,6 +54,15 @@ struct table_header
     unsigned long long excess_used; // keys holding one of the reference's excess slots (excess-list accounting)
 };
 
+// Changes to a table's header counters that a bulk kernel's thread accumulates and its block adds once.
+struct call_counts
+{
+    long long size = 0;
+    long long tombs = 0;
+    long long refused = 0;
+    long long excess = 0;
+};
+
 constexpr unsigned int kErrRetry = 1u;      // a CAS retry loop gave up
 constexpr unsigned int kErrIndex = 2u;      // an index outside the table was computed (never expected)
 

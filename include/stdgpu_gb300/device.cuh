@@ -54,6 +54,61 @@ struct unordered_ref
     static constexpr int SPL = C::slots_per_lane;
 
     sg_unordered_view v;
+    // A bulk kernel's per-thread counts: the header counters' changes accumulate here, to be added once per
+    // block, instead of one atomic per key on each counter (nullptr: every call updates the header).
+    detail::call_counts* defer = nullptr;
+
+    __device__ __forceinline__ void
+    add_size(long long d) const
+    {
+        if (defer != nullptr)
+        {
+            defer->size += d;
+        }
+        else
+        {
+            atomicAdd(&header()->size, static_cast<unsigned long long>(d));
+        }
+    }
+
+    __device__ __forceinline__ void
+    add_tombs(long long d) const
+    {
+        if (defer != nullptr)
+        {
+            defer->tombs += d;
+        }
+        else
+        {
+            atomicAdd(&header()->tombstones, static_cast<unsigned long long>(d));
+        }
+    }
+
+    __device__ __forceinline__ void
+    add_refused() const
+    {
+        if (defer != nullptr)
+        {
+            defer->refused += 1;
+        }
+        else
+        {
+            atomicAdd(&header()->refused, 1ull);
+        }
+    }
+
+    __device__ __forceinline__ void
+    add_excess(long long d) const
+    {
+        if (defer != nullptr)
+        {
+            defer->excess += d;
+        }
+        else
+        {
+            atomicAdd(&header()->excess_used, static_cast<unsigned long long>(d));
+        }
+    }
 
     __device__ __forceinline__ detail::table_header*
     header() const
@@ -365,6 +420,11 @@ struct unordered_ref
         {
             return 1;
         }
+        if (defer != nullptr)
+        {
+            defer->excess += 1; // a bulk call that cannot reach the end of the list: counted at its end
+            return 0;
+        }
         if (atomicAdd(&header()->excess_used, 1ull) < static_cast<unsigned long long>(v.excess_count))
         {
             return 0;
@@ -383,7 +443,7 @@ struct unordered_ref
         }
         else if (held == 0)
         {
-            atomicAdd(&header()->excess_used, ~0ull);
+            add_excess(-1);
         }
     }
 
@@ -411,7 +471,7 @@ struct unordered_ref
         }
         else
         {
-            atomicAdd(&header()->excess_used, ~0ull);
+            add_excess(-1);
         }
     }
 
@@ -433,7 +493,7 @@ struct unordered_ref
             }
             if (target < 0 || (accounting() && refuses_all()))
             {
-                atomicAdd(&header()->refused, 1ull);
+                add_refused();
                 return -1;
             }
         }
@@ -489,10 +549,10 @@ struct unordered_ref
             key_type old;
             if (detail::claim_slot_image<KIND>(slot_ptr(target), image, key, mapped, old))
             {
-                atomicAdd(&header()->size, 1ull);
+                add_size(1);
                 if (target_tomb)
                 {
-                    atomicAdd(&header()->tombstones, ~0ull);
+                    add_tombs(-1);
                 }
                 if (held == 1)
                 {
@@ -514,7 +574,7 @@ struct unordered_ref
         unlock_group(home);
         if (refused)
         {
-            atomicAdd(&header()->refused, 1ull);
+            add_refused();
         }
         return result;
     }
@@ -546,7 +606,7 @@ struct unordered_ref
         }
         if (refuses_all())
         {
-            atomicAdd(&header()->refused, 1ull);
+            add_refused();
             return -1;
         }
         const int64_t home = detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups);
@@ -563,14 +623,14 @@ struct unordered_ref
         const int held = take_bucket_or_excess(b, may_take_bucket);
         if (held < 0)
         {
-            atomicAdd(&header()->refused, 1ull);
+            add_refused();
         }
         else if (atomicCAS(&header()->special_state[s], 0u, 2u) == 0u)
         {
             store_slot(special_slot(key), key, mapped);
             __threadfence();
             atomicExch(&header()->special_state[s], 1u);
-            atomicAdd(&header()->size, 1ull);
+            add_size(1);
             if (held == 1)
             {
                 mark_bucket_slot(special_slot(key));
@@ -583,6 +643,89 @@ struct unordered_ref
         }
         unlock_group(home);
         return result;
+    }
+
+    // Insert of a bulk call with the accounting on that cannot reach the refusal (the caller checked that the
+    // size and the keys in excess slots stay below their limits whatever the call does) and runs no erase:
+    // no lock, as in the bulk kernels -- only free slots disappear during the launch, and each insert reads
+    // every slot before the one it claims, so a key is stored once.  The stored copy then takes its bucket's
+    // own slot when it is the bucket's first new key (first_new) and the slot is free, else an excess slot.
+    __device__ int64_t
+    insert_slot_quiet(key_type key, mapped_type mapped, int64_t b, bool first_new) const
+    {
+        int64_t slot = -1;
+        if (is_special(key))
+        {
+            const int s = key == C::empty_key ? 0 : 1;
+            if (atomicCAS(&header()->special_state[s], 0u, 2u) != 0u)
+            {
+                return -1;
+            }
+            store_slot(special_slot(key), key, mapped);
+            __threadfence();
+            atomicExch(&header()->special_state[s], 1u);
+            slot = special_slot(key);
+        }
+        else
+        {
+            const int64_t home = detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups);
+            for (int attempt = 0; attempt < 65536 && slot < 0; ++attempt)
+            {
+                int64_t target = -1;
+                bool target_tomb = false;
+                if (scan_for_insert(key, home, target, target_tomb))
+                {
+                    return -1; // present
+                }
+                if (target < 0)
+                {
+                    add_refused();
+                    return -1;
+                }
+                uint32_t image[4];
+                if (target_tomb)
+                {
+                    read_slot(target, image);
+                    if (detail::key_in_lane<KIND>(make_uint4(image[0], image[1], image[2], image[3]), 0) != C::tomb_key)
+                    {
+                        continue; // taken since the scan
+                    }
+                }
+                else
+                {
+                    image[0] = image[1] = image[2] = image[3] = ~0u;
+                }
+                key_type old;
+                if (detail::claim_slot_image<KIND>(slot_ptr(target), image, key, mapped, old))
+                {
+                    if (target_tomb)
+                    {
+                        add_tombs(-1);
+                    }
+                    slot = target;
+                }
+                else if (old == key)
+                {
+                    return -1;
+                }
+            }
+            if (slot < 0)
+            {
+                atomicOr(&header()->error, detail::kErrRetry);
+                return -1;
+            }
+        }
+        add_size(1);
+        const unsigned bit = 1u << (b & 31);
+        if (first_new && (atomicOr(v.bucket_heads + (b >> 5), bit) & bit) == 0u)
+        {
+            mark_bucket_slot(slot);
+        }
+        else
+        {
+            add_excess(1);
+        }
+        return slot;
     }
 
     // insert_slot for a key of bucket b; may_take_bucket as in take_bucket_or_excess (accounting only).
@@ -603,7 +746,7 @@ struct unordered_ref
             store_slot(special_slot(key), key, mapped);
             __threadfence();
             atomicExch(&header()->special_state[s], 1u);
-            atomicAdd(&header()->size, 1ull);
+            add_size(1);
             return special_slot(key);
         }
         if (v.insert_locks != nullptr)
@@ -648,7 +791,7 @@ struct unordered_ref
             const uint32_t never_used[4] = { ~0u, ~0u, ~0u, ~0u };
             if (detail::claim_slot_image<KIND>(slot_ptr(target), never_used, key, mapped, old))
             {
-                atomicAdd(&header()->size, 1ull);
+                add_size(1);
                 return target;
             }
             if (old == key)
@@ -657,7 +800,7 @@ struct unordered_ref
             }
             // lost the slot to another key: rescan the same group
         }
-        atomicAdd(&header()->refused, 1ull);
+        add_refused();
         return -1;
     }
 
@@ -737,6 +880,43 @@ struct unordered_ref
         return erase_bucket(key, static_cast<int64_t>(detail::fibonacci_bucket(hash, v.bucket_bits)));
     }
 
+    // Erase of a bulk erase call with the accounting on: no insert runs in the launch, so no lock -- the slot's
+    // bit is read after the swap that erased the key, which only one erase of a key wins.
+    __device__ int64_t
+    erase_quiet(key_type key, int64_t b) const
+    {
+        const int64_t slot =
+                find_slot_home(key, detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups));
+        if (slot < 0)
+        {
+            return 0;
+        }
+        if (is_special(key))
+        {
+            if (atomicCAS(&header()->special_state[key == C::empty_key ? 0 : 1], 1u, 0u) != 1u)
+            {
+                return 0;
+            }
+        }
+        else if (cas_key(slot, key, C::tomb_key) == key)
+        {
+            add_tombs(1);
+        }
+        else
+        {
+            return 0;
+        }
+        add_size(-1);
+        release(b, unmark_bucket_slot(slot));
+        return 1;
+    }
+
+    __device__ __forceinline__ int64_t
+    erase_quiet_hashed(key_type key, uint64_t hash) const
+    {
+        return erase_quiet(key, static_cast<int64_t>(detail::fibonacci_bucket(hash, v.bucket_bits)));
+    }
+
     // erase under the accounting: the stripe lock of the key's home group, then the slot's bits.
     __device__ int64_t
     erase_counted(key_type key, int64_t b) const
@@ -768,12 +948,12 @@ struct unordered_ref
             }
             else if (cas_key(slot, key, C::tomb_key) == key)
             {
-                atomicAdd(&header()->tombstones, 1ull);
+                add_tombs(1);
                 erased = true;
             }
             if (erased)
             {
-                atomicAdd(&header()->size, ~0ull);
+                add_size(-1);
                 release(b, was_bucket_slot);
                 r = 1;
             }
@@ -798,7 +978,7 @@ struct unordered_ref
             const int s = key == C::empty_key ? 0 : 1;
             if (atomicCAS(&header()->special_state[s], 1u, 0u) == 1u)
             {
-                atomicAdd(&header()->size, ~0ull);
+                add_size(-1);
                 return 1;
             }
             return 0;
@@ -811,8 +991,8 @@ struct unordered_ref
         }
         if (cas_key(slot, key, C::tomb_key) == key)
         {
-            atomicAdd(&header()->size, ~0ull);
-            atomicAdd(&header()->tombstones, 1ull);
+            add_size(-1);
+            add_tombs(1);
             return 1;
         }
         return 0;

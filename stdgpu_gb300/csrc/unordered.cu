@@ -802,6 +802,7 @@ k_counted_candidates(sg_unordered_view v, const void* in0, const void* in1, int6
     using C = kind_consts<KIND>;
     const sg::unordered_ref<KIND> ref{ v };
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    unsigned long long absent = 0, heads = 0;
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
     {
         typename C::K key;
@@ -814,9 +815,31 @@ k_counted_candidates(sg_unordered_view v, const void* in0, const void* in1, int6
         }
         else if (ref.find_slot_home(key, group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups)) < 0)
         {
-            atomicMin(cand + b, static_cast<uint32_t>(i));
+            // bounds for k_insert_counted: keys not stored (copies counted each), buckets that get a first new
+            // key while their own slot is free
+            ++absent;
+            if (atomicMin(cand + b, static_cast<uint32_t>(i)) == kNoCandidate && !bit_set(v.bucket_heads, b))
+            {
+                ++heads;
+            }
         }
     }
+    if (!reset)
+    {
+        unsigned long long c[2] = { absent, heads };
+        unsigned long long* const dst[2] = { &ref.header()->count, &ref.header()->scratch };
+        block_add<2>(c, dst);
+    }
+}
+
+// The header counters' changes of a block's threads, added once.
+SG_D void
+flush_counts(table_header* h, const call_counts& c)
+{
+    unsigned long long v[4] = { static_cast<unsigned long long>(c.size), static_cast<unsigned long long>(c.tombs),
+                                static_cast<unsigned long long>(c.refused), static_cast<unsigned long long>(c.excess) };
+    unsigned long long* const dst[4] = { &h->size, &h->tombstones, &h->refused, &h->excess_used };
+    block_add<4>(v, dst);
 }
 
 template <int KIND, bool AOS>
@@ -825,28 +848,37 @@ k_insert_counted(sg_unordered_view v, const void* in0, const void* in1, int64_t 
                  const uint64_t* hashes, const uint32_t* cand)
 {
     using C = kind_consts<KIND>;
-    const sg::unordered_ref<KIND> ref{ v };
-    __shared__ int in_order;
+    sg::unordered_ref<KIND> ref{ v };
+    // quiet: the call cannot reach the refusal -- it adds at most `absent` keys (k_counted_candidates), of which
+    // at least `heads` take their buckets' own slots -- so it needs no lock and adds the counters at each
+    // block's end (a block that starts after another block's flush sees larger counters and may take the
+    // immediate path, which is always right)
+    __shared__ int mode; // 0 quiet, 1 immediate, 2 in input order (one thread)
+    if (threadIdx.x == 0)
+    {
+        const table_header* h = ref.header();
+        const unsigned long long used = *reinterpret_cast<const volatile unsigned long long*>(&h->excess_used);
+        const unsigned long long size = *reinterpret_cast<const volatile unsigned long long*>(&h->size);
+        const unsigned long long absent = h->count, heads = h->scratch;
+        const bool quiet = used + (absent - heads) < static_cast<unsigned long long>(v.excess_count) &&
+                           size + absent < static_cast<unsigned long long>(v.total_count);
+        mode = quiet ? 0 : (gridDim.x == 1 ? 2 : 1);
+    }
+    __syncthreads();
     int64_t first = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x;
     int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    if (gridDim.x == 1)
+    call_counts counts;
+    if (mode == 0)
     {
-        if (threadIdx.x == 0)
+        ref.defer = &counts;
+    }
+    if (mode == 2)
+    {
+        if (threadIdx.x != 0)
         {
-            const unsigned long long used = *reinterpret_cast<volatile unsigned long long*>(&ref.header()->excess_used);
-            const unsigned long long size = *reinterpret_cast<volatile unsigned long long*>(&ref.header()->size);
-            in_order = used + static_cast<unsigned long long>(n) >= static_cast<unsigned long long>(v.excess_count) ||
-                       size + static_cast<unsigned long long>(n) >= static_cast<unsigned long long>(v.total_count);
+            return;
         }
-        __syncthreads();
-        if (in_order != 0)
-        {
-            if (threadIdx.x != 0)
-            {
-                return;
-            }
-            stride = 1;
-        }
+        stride = 1;
     }
     for (int64_t i = first; i < n; i += stride)
     {
@@ -864,11 +896,16 @@ k_insert_counted(sg_unordered_view v, const void* in0, const void* in1, int64_t 
             load_input<KIND, AOS>(in0, in1, static_cast<int64_t>(c), ck, cv);
             first_new = ck == key;
         }
-        const int64_t slot = ref.insert_slot_bucket(key, val, b, first_new);
+        const int64_t slot = mode == 0 ? ref.insert_slot_quiet(key, val, b, first_new)
+                                       : ref.insert_slot_bucket(key, val, b, first_new);
         if (out_flags != nullptr)
         {
             out_flags[i] = static_cast<uint8_t>(slot >= 0);
         }
+    }
+    if (mode == 0)
+    {
+        flush_counts(ref.header(), counts);
     }
 }
 
@@ -877,17 +914,23 @@ __global__ void __launch_bounds__(kThreads)
 k_erase_counted(sg_unordered_view v, const void* keys, int64_t n, uint8_t* out_flags, const uint64_t* hashes)
 {
     using K = typename kind_consts<KIND>::K;
-    const sg::unordered_ref<KIND> ref{ v };
+    // an erase-only launch: no lock (erase_quiet), and no insert reads the counters meanwhile, so they are
+    // added at the block's end
+    call_counts counts;
+    sg::unordered_ref<KIND> ref{ v };
+    ref.defer = &counts;
     const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
     for (int64_t i = static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride)
     {
         const K key = __ldg(static_cast<const K*>(keys) + i);
-        const int64_t r = hashes != nullptr ? ref.erase_hashed(key, __ldg(hashes + i)) : ref.erase(key);
+        const int64_t r = hashes != nullptr ? ref.erase_quiet_hashed(key, __ldg(hashes + i))
+                                            : ref.erase_quiet(key, ref.bucket(key));
         if (out_flags != nullptr)
         {
             out_flags[i] = static_cast<uint8_t>(r);
         }
     }
+    flush_counts(ref.header(), counts);
 }
 
 // Bulk find / contains (device-only find/contains in the reference, :619-706).
@@ -1656,6 +1699,7 @@ insert_counted(sg_unordered* t, const void* in0, const void* in1, int64_t n, uin
     static const int g_cand = persistent_grid(k_counted_candidates<KIND, AOS>, kThreads);
     static const int g_ins = persistent_grid(k_insert_counted<KIND, AOS>, kThreads);
     const int grid_cand = grid_for(n, kThreads, g_cand);
+    SG_CUDA_TRY(cudaMemsetAsync(&t->hdr->count, 0, 2 * sizeof(unsigned long long), s));
     k_counted_candidates<KIND, AOS><<<grid_cand, kThreads, 0, s>>>(v, in0, in1, n, hashes, t->bucket_cand, false);
     SG_LAUNCH_CHECK();
     const int grid = n <= kCountedInOrderMax ? 1 : grid_for(n, kThreads, g_ins);
