@@ -74,7 +74,7 @@ def parse_args(argv=None):
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-other-configs", action="store_true",
                    help="skip the small / batched / served configurations that follow the voxel step")
-    p.add_argument("--workload", choices=["voxel", "batched", "serve", "large", "small"], default="voxel",
+    p.add_argument("--workload", choices=["voxel", "batched", "serve", "large", "small", "device"], default="voxel",
                    help="voxel: the headline map workload; batched: 4096 small sets, batched vs plain calls; "
                         "serve: request stream over 256 resident maps, continuous batching vs serial calls; "
                         "large: capacity-2^30 map at 0.5/0.75/0.9 load plus vector / deque / bitset; "
@@ -612,12 +612,13 @@ def other_configs(args) -> dict:
     """The other benchmark configurations, each run once on this GPU after the voxel step, so that one
     invocation records them all: the L2-resident small set (with the reference's CPU time of the same
     configuration), the 4096 many-small-tables step (batched and graph forms against the plain per-table
-    calls from a C++ loop), the served request stream (server against serial plain calls), and the large
-    mixed workload (capacity-2^30 map at three loads, vector, deque, bitset).  A part that fails reports why
-    instead of its numbers."""
+    calls from a C++ loop), the served request stream (server against serial plain calls), the large
+    mixed workload (capacity-2^30 map at three loads, vector, deque, bitset), and the device calls and custom
+    key types through the C++ API (one thread per key inside a caller's kernel).  A part that fails reports
+    why instead of its numbers."""
     import torch
 
-    from stdgpu_gb300 import batch_bench, large_bench, serve_bench, small_bench
+    from stdgpu_gb300 import batch_bench, device_bench, large_bench, serve_bench, small_bench
 
     def small():
         r = small_bench.run(steps=20, warmup=5)
@@ -656,8 +657,18 @@ def other_configs(args) -> dict:
         return {"value": r["map"][-2]["find_mops"], "unit": UNIT, "detail": r,
                 "note": "value: find M keys/s of the capacity-2^30 map at 0.9 load; per part in detail"}
 
+    def device_calls():
+        r = device_bench.run(keys_log2=24)
+        if not r["checks_pass"]:
+            raise RuntimeError(f"device_bench checks failed: {json.dumps(r)[:300]}")
+        m = r["parts"][0]
+        return {"value": m["find_gkeys_s"] * 1e3, "unit": UNIT, "detail": r["parts"],
+                "note": "value: device find M keys/s of unordered_map<uint64_t,uint32_t> with 2^24 keys, capacity "
+                        "2^25 (one thread per key in the caller's kernel); custom-key voxel sets in detail"}
+
     out = {}
-    for name, fn in (("small", small), ("batched", batched), ("serve", serve), ("large", large)):
+    for name, fn in (("small", small), ("batched", batched), ("serve", serve), ("large", large),
+                     ("device_calls", device_calls)):
         t0 = time.perf_counter()
         try:
             out[name] = fn()
@@ -724,10 +735,27 @@ def small_arm(args):
     print(json.dumps(line), flush=True)
 
 
+def device_arm(args):
+    """Device calls (one thread per key in a caller's kernel) and custom key types, through the C++ API."""
+    from stdgpu_gb300 import device_bench
+    r = device_bench.run(keys_log2=args.keys_log2 if args.keys_log2 <= 26 else 26)
+    m = r["parts"][0] if r["parts"] else {}
+    line = {"metric": "device-call find M keys/s", "value": m.get("find_gkeys_s", 0.0) * 1e3, "unit": UNIT, "n_gpus": 1,
+            "steps": 1, "warmup": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic",
+            "config": {"workload": "device insert / find / erase of unordered_map<uint64_t,uint32_t> (distinct random "
+                                   "keys, capacity 2 x keys); 3 x int16 and 3 x int32 voxel sets with the spatial hash: "
+                                   "bulk insert, device contains (hits, misses), device insert, bulk erase"},
+            "device_calls": r}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.workload == "device":
+        device_arm(args)
     elif args.workload == "large":
         large_arm(args)
     elif args.workload == "small":

@@ -241,6 +241,16 @@ struct identity_word_hash
     }
 };
 
+#if defined(__CUDACC__)
+// Acquire-release fence at device scope: a lock's acquire after the compare-and-swap that took it, its release
+// before the store that frees it (lighter than __threadfence's sequentially consistent fence).
+__device__ __forceinline__ void
+fence_acq_rel_gpu()
+{
+    asm volatile("fence.acq_rel.gpu;" ::: "memory");
+}
+#endif
+
 // ---- deque ring state, shared by the library's bulk kernels and the device-side calls of
 // stdgpu_gb300/stdgpu.cuh.  A deque of capacity c is a ring of c slots plus one 32-bit turn word per slot:
 // push k and pop k use slot (ticket k) mod c; the k-th push waits for turn k, writes, and sets k + 1; the

@@ -58,8 +58,24 @@ struct unordered_ref
     // block, instead of one atomic per key on each counter (nullptr: every call updates the header).
     detail::call_counts* defer = nullptr;
 
+    // d (+-1) added to a header counter by the lanes of the warp that run this call together: one atomic
+    // per group of converged lanes instead of one per lane on the same address (the counters' updates are
+    // what bounds many device calls of one launch otherwise).
+    __device__ __forceinline__ static void
+    warp_add(unsigned long long* counter, int d)
+    {
+        const unsigned m = __activemask();
+        unsigned lane;
+        asm("mov.u32 %0, %%laneid;" : "=r"(lane));
+        const int sum = static_cast<int>(__reduce_add_sync(m, static_cast<unsigned>(d)));
+        if (lane == static_cast<unsigned>(__ffs(m) - 1) && sum != 0)
+        {
+            atomicAdd(counter, static_cast<unsigned long long>(static_cast<long long>(sum)));
+        }
+    }
+
     __device__ __forceinline__ void
-    add_size(long long d) const
+    add_size(int d) const
     {
         if (defer != nullptr)
         {
@@ -67,12 +83,12 @@ struct unordered_ref
         }
         else
         {
-            atomicAdd(&header()->size, static_cast<unsigned long long>(d));
+            warp_add(&header()->size, d);
         }
     }
 
     __device__ __forceinline__ void
-    add_tombs(long long d) const
+    add_tombs(int d) const
     {
         if (defer != nullptr)
         {
@@ -80,7 +96,7 @@ struct unordered_ref
         }
         else
         {
-            atomicAdd(&header()->tombstones, static_cast<unsigned long long>(d));
+            warp_add(&header()->tombstones, d);
         }
     }
 
@@ -93,7 +109,7 @@ struct unordered_ref
         }
         else
         {
-            atomicAdd(&header()->refused, 1ull);
+            warp_add(&header()->refused, 1);
         }
     }
 
@@ -158,7 +174,127 @@ struct unordered_ref
     __device__ __forceinline__ int64_t
     find_slot(key_type key) const
     {
-        return find_slot_home(key, home_group(key));
+        return find_slot_warp(key, home_group(key), nullptr);
+    }
+
+    // Key and mapped value of sub-slot s of a lane's 32-byte sector w.
+    __device__ __forceinline__ static key_type
+    sector_key(const uint32_t (&w)[8], int s)
+    {
+        const int h = s / SPL;
+        return detail::key_in_lane<KIND>(make_uint4(w[4 * h], w[4 * h + 1], w[4 * h + 2], w[4 * h + 3]), s % SPL);
+    }
+
+    __device__ __forceinline__ static mapped_type
+    sector_value(const uint32_t (&w)[8], int s)
+    {
+        const int h = s / SPL;
+        return detail::value_in_lane<KIND>(make_uint4(w[4 * h], w[4 * h + 1], w[4 * h + 2], w[4 * h + 3]), s % SPL);
+    }
+
+    // find_slot (and, with out, the mapped value) for the keys of a whole warp that calls together -- the
+    // usual shape of a caller's kernel, one key per thread: the warp reads each key's home group as one
+    // 128-byte request, 4 lanes taking 32 bytes each (the layout the bulk kernels read), instead of each
+    // thread issuing eight 16-byte loads per group, which holds a table in DRAM to about a third of the
+    // memory's random-read rate.  A key not decided in its home group (the group full of other keys), an
+    // out-of-band key, and the lanes of a partial warp go on alone.
+    __device__ int64_t
+    find_slot_warp(key_type key, int64_t home, mapped_type* out) const
+    {
+        constexpr int S = 32 / C::slot_bytes; // slots per 32-byte sector
+        constexpr bool is_map = detail::kind_traits<KIND>::is_map;
+        int64_t slot = -1;
+        bool read_value = true; // found alone: the value is read from the slot
+        mapped_type val{};
+        const bool probe = !is_special(key);
+        if (__activemask() == 0xffffffffu)
+        {
+            unsigned lane;
+            asm("mov.u32 %0, %%laneid;" : "=r"(lane));
+            const int tbase = static_cast<int>(lane & ~3u);
+            const int q = static_cast<int>(lane & 3u);
+            const long long my_home = probe ? static_cast<long long>(home) : 0ll;
+            long long hr[4];
+            uint32_t w[4][8];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+            {
+                hr[r] = __shfl_sync(0xffffffffu, my_home, tbase + r);
+                const char* p = static_cast<const char*>(v.slots) + hr[r] * detail::kGroupBytes + 32 * q;
+                asm volatile("ld.global.cg.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                             : "=r"(w[r][0]), "=r"(w[r][1]), "=r"(w[r][2]), "=r"(w[r][3]), "=r"(w[r][4]),
+                               "=r"(w[r][5]), "=r"(w[r][6]), "=r"(w[r][7])
+                             : "l"(p));
+            }
+            int64_t my_slot = -1;
+            bool my_more = false;
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+            {
+                const key_type kr = __shfl_sync(0xffffffffu, key, tbase + r);
+                unsigned mm = 0u, me = 0u;
+#pragma unroll
+                for (int s2 = 0; s2 < S; ++s2)
+                {
+                    const key_type k = sector_key(w[r], s2);
+                    mm |= static_cast<unsigned>(k == kr) << s2;
+                    me |= static_cast<unsigned>(k == C::empty_key) << s2;
+                }
+                const unsigned tm = (__ballot_sync(0xffffffffu, mm != 0u) >> tbase) & 0xFu;
+                const unsigned te = (__ballot_sync(0xffffffffu, me != 0u) >> tbase) & 0xFu;
+                const int owner = tm != 0u ? __ffs(tm) - 1 : 0;
+                const unsigned om = __shfl_sync(0xffffffffu, mm, tbase + owner);
+                mapped_type vr{};
+                if constexpr (is_map)
+                {
+                    // the first matching slot's value, selected over constant indices (the sector stays in registers)
+                    const int first = mm != 0u ? __ffs(mm) - 1 : 0;
+                    mapped_type mine{};
+#pragma unroll
+                    for (int s2 = 0; s2 < S; ++s2)
+                    {
+                        if (s2 == first)
+                        {
+                            mine = sector_value(w[r], s2);
+                        }
+                    }
+                    vr = __shfl_sync(0xffffffffu, mine, tbase + owner);
+                }
+                if (q == r)
+                {
+                    my_slot = tm != 0u ? hr[r] * G + owner * S + (__ffs(om) - 1) : -1;
+                    my_more = tm == 0u && te == 0u;
+                    val = vr;
+                }
+            }
+            if (!probe)
+            {
+                slot = find_slot_home(key, home);
+            }
+            else if (my_more)
+            {
+                slot = find_slot_home(key, detail::next_group(home, v.num_groups));
+            }
+            else
+            {
+                slot = my_slot;
+                read_value = false;
+            }
+        }
+        else
+        {
+            slot = find_slot_home(key, home);
+        }
+        if constexpr (is_map)
+        {
+            if (out != nullptr && slot >= 0)
+            {
+                *out = read_value ? __ldcg(reinterpret_cast<const mapped_type*>(slot_ptr(slot) +
+                                                                              detail::kind_traits<KIND>::val_offset))
+                                  : val;
+            }
+        }
+        return slot;
     }
 
     // find_slot along the probe sequence of home group `home` (the key's own).
@@ -262,25 +398,13 @@ struct unordered_ref
     __device__ bool
     find(key_type key, mapped_type* out) const
     {
-        const int64_t s = find_slot(key);
-        if (s < 0)
-        {
-            return false;
-        }
-        if constexpr (detail::kind_traits<KIND>::is_map)
-        {
-            if (out != nullptr)
-            {
-                *out = __ldcg(reinterpret_cast<const mapped_type*>(slot_ptr(s) + detail::kind_traits<KIND>::val_offset));
-            }
-        }
-        return true;
+        return find_slot_warp(key, home_group(key), out) >= 0;
     }
 
     __device__ void
     unlock_group(int64_t g) const
     {
-        __threadfence();
+        detail::fence_acq_rel_gpu();
         atomicExch(v.insert_locks + (static_cast<uint64_t>(g) & static_cast<uint64_t>(v.lock_mask)), 0u);
     }
 
@@ -312,12 +436,19 @@ struct unordered_ref
     // The key along its probe sequence from group home, up to the first group holding a never-used slot:
     // true when present; else target = the first free slot on the way (erased below max_size(), or never
     // used; -1 when there is none) and whether it is an erased one.
-    __device__ bool
+    __device__ __forceinline__ bool
     scan_for_insert(key_type key, int64_t home, int64_t& target, bool& target_tomb) const
     {
-        int64_t g = home;
         target = -1;
         target_tomb = false;
+        return scan_for_insert_from(key, home, target, target_tomb);
+    }
+
+    // scan_for_insert from group g0 on, with target / target_tomb as found before g0 (target -1: none yet).
+    __device__ bool
+    scan_for_insert_from(key_type key, int64_t g0, int64_t& target, bool& target_tomb) const
+    {
+        int64_t g = g0;
         for (int64_t probes = 0; probes < v.num_groups; ++probes)
         {
             const uint4* p = group_ptr(g);
@@ -354,6 +485,80 @@ struct unordered_ref
         return false;
     }
 
+    // scan_for_insert for the keys of a whole warp that calls together: the home groups are read as in
+    // find_slot_warp (one 128-byte request per key); a key whose home group is full of other keys, and the
+    // lanes of a partial warp, go on alone.
+    __device__ bool
+    scan_for_insert_warp(key_type key, int64_t home, int64_t& target, bool& target_tomb) const
+    {
+        constexpr int S = 32 / C::slot_bytes;
+        if (__activemask() != 0xffffffffu)
+        {
+            return scan_for_insert(key, home, target, target_tomb);
+        }
+        unsigned lane;
+        asm("mov.u32 %0, %%laneid;" : "=r"(lane));
+        const int tbase = static_cast<int>(lane & ~3u);
+        const int q = static_cast<int>(lane & 3u);
+        long long hr[4];
+        uint32_t w[4][8];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+        {
+            hr[r] = __shfl_sync(0xffffffffu, static_cast<long long>(home), tbase + r);
+            const char* p = static_cast<const char*>(v.slots) + hr[r] * detail::kGroupBytes + 32 * q;
+            asm volatile("ld.global.cg.v8.u32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                         : "=r"(w[r][0]), "=r"(w[r][1]), "=r"(w[r][2]), "=r"(w[r][3]), "=r"(w[r][4]), "=r"(w[r][5]),
+                           "=r"(w[r][6]), "=r"(w[r][7])
+                         : "l"(p));
+        }
+        bool present = false, any_empty = false;
+        target = -1;
+        target_tomb = false;
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+        {
+            const key_type kr = __shfl_sync(0xffffffffu, key, tbase + r);
+            const int64_t first_slot = hr[r] * G + q * S;
+            unsigned mm = 0u, me = 0u, mt = 0u;
+#pragma unroll
+            for (int s2 = 0; s2 < S; ++s2)
+            {
+                const key_type k = sector_key(w[r], s2);
+                mm |= static_cast<unsigned>(k == kr) << s2;
+                me |= static_cast<unsigned>(k == C::empty_key) << s2;
+                mt |= static_cast<unsigned>(k == C::tomb_key && first_slot + s2 < v.total_count) << s2;
+            }
+            const unsigned tm = (__ballot_sync(0xffffffffu, mm != 0u) >> tbase) & 0xFu;
+            const unsigned te = (__ballot_sync(0xffffffffu, me != 0u) >> tbase) & 0xFu;
+            const unsigned tf = (__ballot_sync(0xffffffffu, (me | mt) != 0u) >> tbase) & 0xFu;
+            // the group's first free slot, erased or never used, in slot order
+            const int fo = tf != 0u ? __ffs(tf) - 1 : 0;
+            const unsigned ff = __shfl_sync(0xffffffffu, me | mt, tbase + fo);
+            const unsigned ft = __shfl_sync(0xffffffffu, mt, tbase + fo);
+            if (q == r)
+            {
+                present = tm != 0u;
+                any_empty = te != 0u;
+                if (tf != 0u)
+                {
+                    const int sl = __ffs(ff) - 1;
+                    target = hr[r] * G + fo * S + sl;
+                    target_tomb = ((ft >> sl) & 1u) != 0u;
+                }
+            }
+        }
+        if (present)
+        {
+            return true;
+        }
+        if (any_empty)
+        {
+            return false;
+        }
+        return scan_for_insert_from(key, detail::next_group(home, v.num_groups), target, target_tomb);
+    }
+
     // The stripe lock of home group `home` for an insert (for_insert) or an erase of `key`: 1 when taken, 0
     // when the call was settled while waiting -- the key turned up present (insert) or absent (erase), checked
     // every 16 polls, so a crowd of calls on one key drains as soon as the first is done instead of passing
@@ -368,7 +573,7 @@ struct unordered_ref
         {
             if (*reinterpret_cast<volatile unsigned int*>(l) == 0u && atomicCAS(l, 0u, 1u) == 0u)
             {
-                __threadfence();
+                detail::fence_acq_rel_gpu();
                 return 1;
             }
             if ((polls & 15) == 15 && (find_slot_home(key, home) >= 0) == for_insert)
@@ -487,7 +692,7 @@ struct unordered_ref
         {
             int64_t target = -1;
             bool target_tomb = false;
-            if (scan_for_insert(key, home, target, target_tomb))
+            if (scan_for_insert_warp(key, home, target, target_tomb))
             {
                 return -1; // present
             }
@@ -885,8 +1090,8 @@ struct unordered_ref
     __device__ int64_t
     erase_quiet(key_type key, int64_t b) const
     {
-        const int64_t slot =
-                find_slot_home(key, detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups));
+        const int64_t slot = find_slot_warp(
+                key, detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups), nullptr);
         if (slot < 0)
         {
             return 0;
@@ -922,7 +1127,7 @@ struct unordered_ref
     erase_counted(key_type key, int64_t b) const
     {
         const int64_t home = detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups);
-        if (find_slot_home(key, home) < 0)
+        if (find_slot_warp(key, home, nullptr) < 0)
         {
             return 0;
         }
@@ -983,8 +1188,8 @@ struct unordered_ref
             }
             return 0;
         }
-        const int64_t slot = find_slot_home(
-                key, detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups));
+        const int64_t slot = find_slot_warp(
+                key, detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups), nullptr);
         if (slot < 0)
         {
             return 0;

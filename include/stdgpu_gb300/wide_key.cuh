@@ -401,6 +401,103 @@ struct wide_ref
         return -1;
     }
 
+    // Broadcast of a key word from lane src (full warp).
+    __device__ static W
+    shfl_word(const W& w, int src)
+    {
+        if constexpr (sizeof(W) == 16)
+        {
+            return W{ __shfl_sync(0xffffffffu, w.lo, src), __shfl_sync(0xffffffffu, w.hi, src) };
+        }
+        else
+        {
+            return __shfl_sync(0xffffffffu, w, src);
+        }
+    }
+
+    // find_word for the keys of a whole warp that calls together (one key per thread, the shape of a
+    // caller's kernel): each key's home group is read as one 128-byte request, 4 lanes taking 32 bytes
+    // each, instead of each thread issuing eight 16-byte loads per group.  A key not decided in its home
+    // group, an out-of-band key, and the lanes of a partial warp go on alone.
+    __device__ std::int64_t
+    find_word_warp(const W& w, std::uint64_t hash) const
+    {
+        constexpr int WPS = 32 / static_cast<int>(sizeof(W)); // words per 32-byte sector
+        if (__activemask() != 0xffffffffu)
+        {
+            return find_word(w, hash);
+        }
+        unsigned lane;
+        asm("mov.u32 %0, %%laneid;" : "=r"(lane));
+        const int tbase = static_cast<int>(lane & ~3u);
+        const int q = static_cast<int>(lane & 3u);
+        const bool probe = special_of(w) < 0;
+        const long long my_home = probe ? static_cast<long long>(home(hash)) : 0ll;
+        long long hr[4];
+        unsigned long long d[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+        {
+            hr[r] = __shfl_sync(0xffffffffu, my_home, tbase + r);
+            const char* p = reinterpret_cast<const char*>(keys + hr[r] * G) + 32 * q;
+            asm volatile("ld.global.cg.v4.u64 {%0,%1,%2,%3}, [%4];"
+                         : "=l"(d[r][0]), "=l"(d[r][1]), "=l"(d[r][2]), "=l"(d[r][3])
+                         : "l"(p));
+        }
+        std::int64_t my_slot = -1;
+        bool my_more = false;
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+        {
+            const W wr = shfl_word(w, tbase + r);
+            const std::int64_t first = hr[r] * G + q * WPS;
+            unsigned mm = 0u, me = 0u;
+#pragma unroll
+            for (int j = 0; j < WPS; ++j)
+            {
+                // word j of the sector: 16-byte load pair j / (WPS / 2), word j % (WPS / 2) of it
+                constexpr int per = WPS / 2;
+                const W x = word_in<W>(d[r][2 * (j / per)], d[r][2 * (j / per) + 1], j % per);
+                const bool live = first + j < max_size;
+                mm |= static_cast<unsigned>(live && x != WW::empty() && x != WW::tomb() && same(x, wr)) << j;
+                me |= static_cast<unsigned>(live && x == WW::empty()) << j;
+            }
+            const unsigned tm = (__ballot_sync(0xffffffffu, mm != 0u) >> tbase) & 0xFu;
+            const unsigned te = (__ballot_sync(0xffffffffu, me != 0u) >> tbase) & 0xFu;
+            const int owner = tm != 0u ? __ffs(tm) - 1 : 0;
+            const unsigned om = __shfl_sync(0xffffffffu, mm, tbase + owner);
+            if (q == r)
+            {
+                my_slot = tm != 0u ? hr[r] * G + owner * WPS + (__ffs(om) - 1) : -1;
+                my_more = tm == 0u && te == 0u;
+            }
+        }
+        if (!probe)
+        {
+            return find_word(w, hash);
+        }
+        if (!my_more)
+        {
+            return my_slot;
+        }
+        // the home group is full of other keys: the rest of the chain alone
+        std::int64_t g = static_cast<std::int64_t>(my_home) + 1 == num_groups ? 0 : static_cast<std::int64_t>(my_home) + 1;
+        for (std::int64_t n = 1; n < num_groups; ++n)
+        {
+            const group_masks m = scan(g, [&](const W& x) { return same(x, w); });
+            if (m.match != 0u)
+            {
+                return g * G + (__ffs(m.match) - 1);
+            }
+            if (m.free != 0u)
+            {
+                return -1;
+            }
+            g = g + 1 == num_groups ? 0 : g + 1;
+        }
+        return -1;
+    }
+
     __device__ std::int64_t
     find_word(const W& w, std::uint64_t hash) const
     {
@@ -570,7 +667,7 @@ struct wide_ref
         {
             return insert_word(w, hash, false, mapped);
         }
-        std::int64_t slot = find_word(w, hash);
+        std::int64_t slot = find_word_warp(w, hash);
         if (slot >= 0)
         {
             return { slot, false };
@@ -581,9 +678,9 @@ struct wide_ref
         {
             if (*reinterpret_cast<volatile unsigned int*>(l) == 0u && atomicCAS(l, 0u, 1u) == 0u)
             {
-                __threadfence();
+                sg::detail::fence_acq_rel_gpu();
                 const wide_insert_result r = insert_word(w, hash, true, mapped);
-                __threadfence();
+                sg::detail::fence_acq_rel_gpu();
                 atomicExch(l, 0u);
                 return r;
             }
@@ -668,6 +765,21 @@ struct wide_ref
 };
 
 #if defined(__CUDACC__)
+// d (+-1) added to a counter by the lanes of the warp that run the call together: one atomic per group of
+// converged lanes (device calls of one launch otherwise queue on the counter's address).
+__device__ inline void
+wide_converged_add(unsigned long long* counter, int d)
+{
+    const unsigned m = __activemask();
+    unsigned lane;
+    asm("mov.u32 %0, %%laneid;" : "=r"(lane));
+    const int sum = static_cast<int>(__reduce_add_sync(m, static_cast<unsigned>(d)));
+    if (lane == static_cast<unsigned>(__ffs(m) - 1) && sum != 0)
+    {
+        atomicAdd(counter, static_cast<unsigned long long>(static_cast<long long>(sum)));
+    }
+}
+
 // One warp's sum of per-lane deltas added to a counter (every lane of a full warp calls it).
 __device__ inline void
 wide_flush(unsigned long long* counter, long long delta)
@@ -1186,7 +1298,7 @@ public:
     __device__ iterator
     find(const key_type& key) const
     {
-        return at(_t.find_word(to_wide<W>(key), static_cast<std::uint64_t>(Hash{}(key))));
+        return at(_t.find_word_warp(to_wide<W>(key), static_cast<std::uint64_t>(Hash{}(key))));
     }
 
     __device__ bool
@@ -1234,7 +1346,7 @@ public:
         {
             return 0;
         }
-        atomicAdd(&_t.hdr->size, ~0ull);
+        wide_converged_add(&_t.hdr->size, -1);
         return 1;
     }
 #endif
@@ -1330,7 +1442,7 @@ protected:
         {
             return pair<iterator, bool>(end(), false);
         }
-        atomicAdd(&_t.hdr->size, 1ull);
+        wide_converged_add(&_t.hdr->size, 1);
         return pair<iterator, bool>(at(r.slot), true);
     }
 #endif
