@@ -1,8 +1,12 @@
 // Native device-side calls on a table, for use inside a caller's own kernels
 // (the reference's device member functions find / contains / count / insert /
 // emplace / erase, src/stdgpu/impl/unordered_base_detail.cuh:619-706, 958-994,
-// 1019-1043).  One calling thread per key; each call reads whole 128-byte probe
-// groups with 16-byte loads through L2.
+// 1019-1043).  One calling thread per key.  When a whole warp calls together
+// (the usual shape: one key per thread), lookups -- and the lock-free scans of
+// insert and erase -- read each key's home group as one 128-byte request, four
+// lanes taking 32 bytes each; a partial warp, and a key that goes on past its
+// home group, read alone.  The header counters (size, erased slots, refusals)
+// take one atomic per group of lanes that call together.
 //
 // Concurrency within one launch:
 //  * insert / emplace take the stripe lock of the key's home group (the
@@ -10,7 +14,10 @@
 //    key up to the first group holding a never-used slot, and claim the first
 //    free slot -- erased or never used -- with a compare-and-swap over the
 //    whole slot.  All inserts of one key share the lock, so they never scan and
-//    claim at the same time: a key is stored at most once and exactly one of
+//    claim at the same time (the lock word carries a version that each release
+//    advances: an insert that takes the lock at the version it read before its
+//    lock-free scan knows no insert of its stripe finished in between and claims
+//    the slot that scan found): a key is stored at most once and exactly one of
 //    several concurrent inserts of an absent key reports success, while erases
 //    (which take no lock) run in the same launch and free slots that the next
 //    inserts reuse -- as the reference's device insert, which locks the bucket
@@ -405,7 +412,15 @@ struct unordered_ref
     unlock_group(int64_t g) const
     {
         detail::fence_acq_rel_gpu();
-        atomicExch(v.insert_locks + (static_cast<uint64_t>(g) & static_cast<uint64_t>(v.lock_mask)), 0u);
+        // held (bit 0 set) -> free with the next version: word + 1
+        atomicAdd(v.insert_locks + (static_cast<uint64_t>(g) & static_cast<uint64_t>(v.lock_mask)), 1u);
+    }
+
+    // The stripe lock word of home group g: bit 0 held, bits 1-31 a version that every release advances.
+    __device__ __forceinline__ unsigned int*
+    lock_word(int64_t g) const
+    {
+        return v.insert_locks + (static_cast<uint64_t>(g) & static_cast<uint64_t>(v.lock_mask));
     }
 
     // The slot's current bytes as four words (unused words all ones).
@@ -567,11 +582,12 @@ struct unordered_ref
     __device__ int
     lock_or_settled(int64_t home, key_type key, bool for_insert) const
     {
-        unsigned int* l = v.insert_locks + (static_cast<uint64_t>(home) & static_cast<uint64_t>(v.lock_mask));
+        unsigned int* l = lock_word(home);
         unsigned int backoff = 32;
         for (long long polls = 0; polls < detail::kWaitLimit; ++polls)
         {
-            if (*reinterpret_cast<volatile unsigned int*>(l) == 0u && atomicCAS(l, 0u, 1u) == 0u)
+            const unsigned int x = *reinterpret_cast<volatile unsigned int*>(l);
+            if ((x & 1u) == 0u && atomicCAS(l, x, x | 1u) == x)
             {
                 detail::fence_acq_rel_gpu();
                 return 1;
@@ -689,20 +705,36 @@ struct unordered_ref
     insert_slot_locked(key_type key, mapped_type mapped, int64_t b, bool may_take_bucket = true) const
     {
         const int64_t home = detail::group_of_bucket(static_cast<uint64_t>(b), v.bucket_bits, v.num_groups);
+        // the lock's version before the lock-free scan: taking the lock at that same version means no insert
+        // of this stripe -- no insert of this key -- completed since, so the scan's answer still holds (erases
+        // take no lock, but they only turn keys into erased slots)
+        unsigned int* l = lock_word(home);
+        unsigned int v0;
+        // an acquire load: the scan's reads come after it, so a release seen here is seen by the scan too
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v0) : "l"(l) : "memory");
+        int64_t pre_target = -1;
+        bool pre_tomb = false;
+        if (scan_for_insert_warp(key, home, pre_target, pre_tomb))
         {
-            int64_t target = -1;
-            bool target_tomb = false;
-            if (scan_for_insert_warp(key, home, target, target_tomb))
-            {
-                return -1; // present
-            }
-            if (target < 0 || (accounting() && refuses_all()))
-            {
-                add_refused();
-                return -1;
-            }
+            return -1; // present
         }
-        const int locked = lock_or_settled(home, key, true);
+        if (pre_target < 0 || (accounting() && refuses_all()))
+        {
+            add_refused();
+            return -1;
+        }
+        bool scanned = false; // the prescan's target is current
+        int locked;
+        if ((v0 & 1u) == 0u && atomicCAS(l, v0, v0 | 1u) == v0)
+        {
+            detail::fence_acq_rel_gpu();
+            locked = 1;
+            scanned = true;
+        }
+        else
+        {
+            locked = lock_or_settled(home, key, true);
+        }
         if (locked == 0)
         {
             return -1; // present: inserted by another thread while this one waited
@@ -717,13 +749,16 @@ struct unordered_ref
         int held = -1; // accounting: what take_bucket_or_excess gave this key
         for (int attempt = 0; attempt < 65536; ++attempt)
         {
-            int64_t target = -1;
-            bool target_tomb = false;
-            const bool present = scan_for_insert(key, home, target, target_tomb);
-            if (present)
+            int64_t target = pre_target;
+            bool target_tomb = pre_tomb;
+            if (!scanned)
             {
-                break;
+                if (scan_for_insert(key, home, target, target_tomb))
+                {
+                    break; // present
+                }
             }
+            scanned = false; // a lost claim below reads the chain again
             if (target < 0)
             {
                 refused = true;
