@@ -409,9 +409,12 @@ struct unordered_ref
     }
 
     __device__ void
-    unlock_group(int64_t g) const
+    unlock_group(int64_t g, bool fence = true) const
     {
-        detail::fence_acq_rel_gpu();
+        if (fence)
+        {
+            detail::fence_acq_rel_gpu();
+        }
         // held (bit 0 set) -> free with the next version: word + 1
         atomicAdd(v.insert_locks + (static_cast<uint64_t>(g) & static_cast<uint64_t>(v.lock_mask)), 1u);
     }
@@ -727,7 +730,8 @@ struct unordered_ref
         int locked;
         if ((v0 & 1u) == 0u && atomicCAS(l, v0, v0 | 1u) == v0)
         {
-            detail::fence_acq_rel_gpu();
+            // no fence: nothing is read under the lock on this path, and the claim below waits for this
+            // compare-and-swap's answer
             locked = 1;
             scanned = true;
         }
@@ -811,7 +815,9 @@ struct unordered_ref
         {
             give_back(b, held);
         }
-        unlock_group(home);
+        // the claim's compare-and-swap has answered, so the next holder sees the key; the accounting's bit
+        // updates are not waited for, and need the fence
+        unlock_group(home, accounting());
         if (refused)
         {
             add_refused();

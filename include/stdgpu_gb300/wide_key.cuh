@@ -415,43 +415,42 @@ struct wide_ref
         }
     }
 
-    // find_word for the keys of a whole warp that calls together (one key per thread, the shape of a
-    // caller's kernel): each key's home group is read as one 128-byte request, 4 lanes taking 32 bytes
-    // each, instead of each thread issuing eight 16-byte loads per group.  A key not decided in its home
-    // group, an out-of-band key, and the lanes of a partial warp go on alone.
-    __device__ std::int64_t
-    find_word_warp(const W& w, std::uint64_t hash) const
+    // The home group of each key of a whole warp that calls together (one key per thread, the shape of a
+    // caller's kernel and of the bulk kernels), read as one 128-byte request per key -- 4 lanes taking 32
+    // bytes each -- instead of each thread issuing eight 16-byte loads per group.  For this lane's key: the
+    // slot holding it (or -1), the group's first never-used and first erased slot (or -1).  The caller makes
+    // sure the whole warp is converged (every lane calls).
+    struct home_view
+    {
+        std::int64_t match, first_free, first_tomb;
+    };
+
+    __device__ home_view
+    warp_home_scan(const W& w, std::int64_t my_home) const
     {
         constexpr int WPS = 32 / static_cast<int>(sizeof(W)); // words per 32-byte sector
-        if (__activemask() != 0xffffffffu)
-        {
-            return find_word(w, hash);
-        }
         unsigned lane;
         asm("mov.u32 %0, %%laneid;" : "=r"(lane));
         const int tbase = static_cast<int>(lane & ~3u);
         const int q = static_cast<int>(lane & 3u);
-        const bool probe = special_of(w) < 0;
-        const long long my_home = probe ? static_cast<long long>(home(hash)) : 0ll;
         long long hr[4];
         unsigned long long d[4][4];
 #pragma unroll
         for (int r = 0; r < 4; ++r)
         {
-            hr[r] = __shfl_sync(0xffffffffu, my_home, tbase + r);
+            hr[r] = __shfl_sync(0xffffffffu, static_cast<long long>(my_home), tbase + r);
             const char* p = reinterpret_cast<const char*>(keys + hr[r] * G) + 32 * q;
             asm volatile("ld.global.cg.v4.u64 {%0,%1,%2,%3}, [%4];"
                          : "=l"(d[r][0]), "=l"(d[r][1]), "=l"(d[r][2]), "=l"(d[r][3])
                          : "l"(p));
         }
-        std::int64_t my_slot = -1;
-        bool my_more = false;
+        home_view out{ -1, -1, -1 };
 #pragma unroll
         for (int r = 0; r < 4; ++r)
         {
             const W wr = shfl_word(w, tbase + r);
             const std::int64_t first = hr[r] * G + q * WPS;
-            unsigned mm = 0u, me = 0u;
+            unsigned mm = 0u, me = 0u, mt = 0u;
 #pragma unroll
             for (int j = 0; j < WPS; ++j)
             {
@@ -459,29 +458,53 @@ struct wide_ref
                 constexpr int per = WPS / 2;
                 const W x = word_in<W>(d[r][2 * (j / per)], d[r][2 * (j / per) + 1], j % per);
                 const bool live = first + j < max_size;
-                mm |= static_cast<unsigned>(live && x != WW::empty() && x != WW::tomb() && same(x, wr)) << j;
-                me |= static_cast<unsigned>(live && x == WW::empty()) << j;
+                const bool empty = x == WW::empty(), tomb = x == WW::tomb();
+                mm |= static_cast<unsigned>(live && !empty && !tomb && same(x, wr)) << j;
+                me |= static_cast<unsigned>(live && empty) << j;
+                mt |= static_cast<unsigned>(live && tomb) << j;
             }
             const unsigned tm = (__ballot_sync(0xffffffffu, mm != 0u) >> tbase) & 0xFu;
             const unsigned te = (__ballot_sync(0xffffffffu, me != 0u) >> tbase) & 0xFu;
-            const int owner = tm != 0u ? __ffs(tm) - 1 : 0;
-            const unsigned om = __shfl_sync(0xffffffffu, mm, tbase + owner);
+            const unsigned tt = (__ballot_sync(0xffffffffu, mt != 0u) >> tbase) & 0xFu;
+            const int om_l = tm != 0u ? __ffs(tm) - 1 : 0;
+            const int oe_l = te != 0u ? __ffs(te) - 1 : 0;
+            const int ot_l = tt != 0u ? __ffs(tt) - 1 : 0;
+            const unsigned om = __shfl_sync(0xffffffffu, mm, tbase + om_l);
+            const unsigned oe = __shfl_sync(0xffffffffu, me, tbase + oe_l);
+            const unsigned ot = __shfl_sync(0xffffffffu, mt, tbase + ot_l);
             if (q == r)
             {
-                my_slot = tm != 0u ? hr[r] * G + owner * WPS + (__ffs(om) - 1) : -1;
-                my_more = tm == 0u && te == 0u;
+                const std::int64_t g0 = hr[r] * G;
+                out.match = tm != 0u ? g0 + om_l * WPS + (__ffs(om) - 1) : -1;
+                out.first_free = te != 0u ? g0 + oe_l * WPS + (__ffs(oe) - 1) : -1;
+                out.first_tomb = tt != 0u ? g0 + ot_l * WPS + (__ffs(ot) - 1) : -1;
             }
         }
+        return out;
+    }
+
+    // find_word for the keys of a whole warp that calls together (warp_home_scan); a key not decided in its
+    // home group, an out-of-band key, and the lanes of a partial warp go on alone.
+    __device__ std::int64_t
+    find_word_warp(const W& w, std::uint64_t hash) const
+    {
+        if (__activemask() != 0xffffffffu)
+        {
+            return find_word(w, hash);
+        }
+        const bool probe = special_of(w) < 0;
+        const std::int64_t my_home = probe ? home(hash) : 0;
+        const home_view h = warp_home_scan(w, my_home);
         if (!probe)
         {
             return find_word(w, hash);
         }
-        if (!my_more)
+        if (h.match >= 0 || h.first_free >= 0)
         {
-            return my_slot;
+            return h.match;
         }
         // the home group is full of other keys: the rest of the chain alone
-        std::int64_t g = static_cast<std::int64_t>(my_home) + 1 == num_groups ? 0 : static_cast<std::int64_t>(my_home) + 1;
+        std::int64_t g = my_home + 1 == num_groups ? 0 : my_home + 1;
         for (std::int64_t n = 1; n < num_groups; ++n)
         {
             const group_masks m = scan(g, [&](const W& x) { return same(x, w); });
@@ -496,6 +519,48 @@ struct wide_ref
             g = g + 1 == num_groups ? 0 : g + 1;
         }
         return -1;
+    }
+
+    // A bulk insert's first try for the keys of a whole warp (insert-only launch: free slots only disappear):
+    // present in the home group, or one claim of the home group's first erased slot (reuse_tombs) or first
+    // never-used slot when the group has a never-used slot -- the slot the per-thread insert_word would pick.
+    // {-2, false} when the key needs insert_word (claim lost, home group full, out-of-band key, partial warp).
+    __device__ wide_insert_result
+    insert_word_warp_try(const W& w, std::uint64_t hash, bool reuse_tombs, const value_store* mapped) const
+    {
+        if (__activemask() != 0xffffffffu)
+        {
+            return { -2, false };
+        }
+        const bool probe = special_of(w) < 0;
+        const std::int64_t my_home = probe ? home(hash) : 0;
+        const home_view h = warp_home_scan(w, my_home);
+        if (!probe)
+        {
+            return { -2, false };
+        }
+        if (h.match >= 0)
+        {
+            return { h.match, false };
+        }
+        if (h.first_free < 0)
+        {
+            return { -2, false };
+        }
+        const bool take_tomb = reuse_tombs && h.first_tomb >= 0;
+        const std::int64_t slot = take_tomb ? h.first_tomb : h.first_free;
+        const W expected = take_tomb ? WW::tomb() : WW::empty();
+        const W old = WW::cas(keys + slot, expected, w);
+        if (old == expected)
+        {
+            construct(slot, mapped);
+            return { slot, true };
+        }
+        if (old != WW::empty() && old != WW::tomb() && same(old, w))
+        {
+            return { slot, false };
+        }
+        return { -2, false };
     }
 
     __device__ std::int64_t
@@ -711,7 +776,7 @@ struct wide_ref
             atomicExch(&hdr->special_state[sp], 0u);
             return true;
         }
-        const std::int64_t slot = find_if(hash, [&](const W& x) { return same(x, w); });
+        const std::int64_t slot = find_word_warp(w, hash);
         if (slot < 0)
         {
             return false;
@@ -806,9 +871,13 @@ k_wide_insert(Ref t, const Value* in, std::int64_t n)
     {
         const Value& v = in[i];
         const Key key = Ref::key_of(v);
-        const wide_insert_result r = t.insert_word(to_wide<typename Ref::W>(key),
-                                                   static_cast<std::uint64_t>(typename Ref::hasher{}(key)), true,
-                                                   Ref::mapped_of(v));
+        const typename Ref::W w = to_wide<typename Ref::W>(key);
+        const std::uint64_t h = static_cast<std::uint64_t>(typename Ref::hasher{}(key));
+        wide_insert_result r = t.insert_word_warp_try(w, h, true, Ref::mapped_of(v));
+        if (r.slot == -2)
+        {
+            r = t.insert_word(w, h, true, Ref::mapped_of(v));
+        }
         added += r.inserted ? 1 : 0;
     }
     wide_flush(&t.hdr->size, added);
