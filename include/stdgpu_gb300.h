@@ -221,6 +221,13 @@ SG_API sg_status sg_unordered_set_excess_accounting(sg_unordered* table, int32_t
  * accounting off.  Synchronises. */
 SG_API sg_status sg_unordered_excess_used(sg_unordered* table, void* stream, int64_t* out);
 
+/* A device buffer of at least `bytes` owned by the table, for a caller that stages a bulk call's inputs
+ * (the C++ API's custom-key calls turn keys into key words and hashes there): no allocation per call.  Valid
+ * until the next call of this function on the table (a larger request replaces the buffer, after a device
+ * synchronisation) or the table's destruction; calls on one table are stream-ordered, so one call's staging
+ * is not overwritten by the next before it is read.  Allocated with the table's allocator. */
+SG_API sg_status sg_unordered_call_scratch(sg_unordered* table, int64_t bytes, void* stream, void** out);
+
 /* erase(begin, end) over keys: src/stdgpu/impl/unordered_base_detail.cuh:1045-1066 (per key :1019-1043).
  * out_erased (nullable): per key 1 if this call erased it, else 0. */
 SG_API sg_status sg_unordered_erase(sg_unordered* table, const void* keys, int64_t n, uint8_t* out_erased, void* stream);

@@ -183,6 +183,16 @@ struct scratch
     scratch& operator=(const scratch&) = delete;
 };
 
+// The table's own staging buffer for a bulk call (sg_unordered_call_scratch): no allocation per call.
+struct table_scratch
+{
+    void* p = nullptr;
+    table_scratch(sg_unordered* h, std::size_t bytes, cudaStream_t s)
+    {
+        gb300_check(sg_unordered_call_scratch(h, static_cast<std::int64_t>(bytes), s, &p), "scratch");
+    }
+};
+
 inline std::size_t
 align256(std::size_t x)
 {
@@ -375,7 +385,7 @@ public:
         }
         const std::size_t wb = align256(sizeof(W) * n);
         const std::size_t mb = std::is_same<T, void>::value ? 0 : align256(sizeof(std::uint64_t) * n);
-        scratch s(wb + mb + sizeof(std::uint64_t) * n, policy.stream);
+        table_scratch s(_handle, wb + mb + sizeof(std::uint64_t) * n, policy.stream);
         char* base = static_cast<char*>(s.p);
         auto* words = reinterpret_cast<W*>(base);
         auto* mapped = reinterpret_cast<M*>(base + wb);
@@ -403,7 +413,7 @@ public:
             return;
         }
         const std::size_t wb = align256(sizeof(W) * n);
-        scratch s(wb + sizeof(std::uint64_t) * n, policy.stream);
+        table_scratch s(_handle, wb + sizeof(std::uint64_t) * n, policy.stream);
         auto* words = reinterpret_cast<W*>(s.p);
         auto* hashes = reinterpret_cast<std::uint64_t*>(static_cast<char*>(s.p) + wb);
         k_prepare_keys<Key, Hash><<<grid_of(n), 256, 0, policy.stream>>>(begin, n, words, hashes, false);
@@ -483,7 +493,7 @@ public:
         const std::int64_t cap = _view.total_count + 2;
         const std::size_t wb = align256(sizeof(W) * cap);
         const std::size_t hb = align256(sizeof(std::uint64_t) * cap);
-        scratch s(wb + hb + align256(cap) + 256, policy.stream);
+        table_scratch s(_handle, wb + hb + align256(cap) + 256, policy.stream);
         char* base = static_cast<char*>(s.p);
         auto* words = reinterpret_cast<W*>(base);
         auto* hashes = reinterpret_cast<std::uint64_t*>(base + wb);

@@ -116,6 +116,7 @@ SIGNATURES = {
     "sg_unordered_view_of": (c_int32, [c_void_p, POINTER(sg_unordered_view)]),
     "sg_unordered_set_excess_accounting": (c_int32, [c_void_p, c_int32, c_void_p]),
     "sg_unordered_excess_used": (c_int32, [c_void_p, c_void_p, POINTER(c_int64)]),
+    "sg_unordered_call_scratch": (c_int32, [c_void_p, c_int64, c_void_p, POINTER(c_void_p)]),
     "sg_unordered_geometry_for": (c_int32, [c_int32, c_int64, POINTER(sg_geometry)]),
     "sg_stager_create": (c_int32, [c_int64, c_int32, POINTER(c_void_p)]),
     "sg_stager_destroy": (c_int32, [c_void_p]),

@@ -1421,6 +1421,8 @@ struct sg_unordered
     uint32_t* slot_heads;
     uint32_t* bucket_cand;         // a bulk insert's candidate per bucket (k_counted_candidates)
     char* heads_block;             // their own block when switched on after creation, else nullptr (in `block`)
+    char* call_scratch;            // sg_unordered_call_scratch: the caller-side staging of the C++ API's bulk calls
+    int64_t call_scratch_bytes;
 };
 
 namespace
@@ -2203,6 +2205,10 @@ sg_unordered_destroy(sg_unordered* t)
     {
         sg::detail::obj_free(t->oa, t->heads_block);
     }
+    if (t->call_scratch != nullptr)
+    {
+        sg::detail::obj_free(t->oa, t->call_scratch);
+    }
     if (t->host_hdr != nullptr)
     {
         pinned_headers().put(t->host_hdr);
@@ -2528,6 +2534,37 @@ sg_unordered_set_excess_accounting(sg_unordered* t, int32_t on, void* stream)
         return SG_ERR_BAD_ARG;
     }
     return set_accounting(t, on != 0, s);
+}
+
+sg_status
+sg_unordered_call_scratch(sg_unordered* t, int64_t bytes, void* stream, void** out)
+{
+    if (t == nullptr || bytes < 0 || out == nullptr)
+    {
+        return SG_ERR_BAD_ARG;
+    }
+    if (bytes > t->call_scratch_bytes)
+    {
+        if (t->call_scratch != nullptr)
+        {
+            // a call queued earlier may still read the old buffer
+            SG_CUDA_TRY(cudaDeviceSynchronize());
+            sg::detail::obj_free(t->oa, t->call_scratch);
+            t->call_scratch = nullptr;
+            t->call_scratch_bytes = 0;
+        }
+        const int64_t want = (bytes + (int64_t{ 1 } << 20) - 1) & ~((int64_t{ 1 } << 20) - 1);
+        if (sg::detail::obj_malloc(t->oa, &t->call_scratch, static_cast<size_t>(want)) != cudaSuccess)
+        {
+            t->call_scratch = nullptr;
+            cudaGetLastError();
+            return SG_ERR_OOM;
+        }
+        t->call_scratch_bytes = want;
+    }
+    (void)stream;
+    *out = t->call_scratch;
+    return SG_OK;
 }
 
 sg_status
