@@ -9,6 +9,7 @@
 #include <set>
 #include <string>
 #include <unordered_set>
+#include <unordered_map>
 #include <vector>
 
 #include <stdgpu_gb300/stdgpu.cuh>
@@ -129,6 +130,25 @@ k_find_values(map_t m, const std::uint64_t* keys, int n, int* ok)
     {
         auto it = m.find(keys[i]);
         ok[i] = (it != m.end() && it->first == keys[i] && it->second == static_cast<std::uint32_t>(i)) ? 1 : 0;
+    }
+}
+
+// find from a warp whose lanes call in different shapes: every lane (a full warp, the cooperative read),
+// odd lanes only (a partial warp), and full warps in which some lanes hold the out-of-band keys or keys that
+// are absent.  want[i]: the expected value + 1, or 0 when absent.
+__global__ void
+k_find_shapes(map_t m, const std::uint64_t* keys, const std::uint32_t* want, int n, int mode, int* bad)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || (mode == 1 && (threadIdx.x & 1) == 0))
+    {
+        return;
+    }
+    auto it = m.find(keys[i]);
+    const std::uint32_t got = it != m.end() ? it->second + 1u : 0u;
+    if (got != want[i] || m.contains(keys[i]) != (want[i] != 0u))
+    {
+        atomicAdd(bad, 1);
     }
 }
 
@@ -454,6 +474,58 @@ main()
         m.erase(d_keys, d_keys + N / 2);
         check(m.size() == N - N / 2 && m.valid(), "bulk erase(begin, end)");
         cudaFree(d_values);
+        map_t::destroyDeviceObject(m);
+    }
+
+    // device find in every call shape against the host model: full warps, odd lanes only, out-of-band and
+    // absent keys mixed into full warps
+    {
+        const int n = 4096;
+        map_t m = map_t::createDeviceObject(n);
+        std::vector<std::uint64_t> k(n);
+        std::vector<std::uint32_t> want(n, 0u);
+        std::vector<stdgpu::pair<const std::uint64_t, std::uint32_t>> stored;
+        for (int i = 0; i < n; ++i)
+        {
+            k[i] = i % 97 == 5 ? ~0ull : (i % 89 == 7 ? ~0ull - 1 : keys[i]);
+            if (i % 3 != 0) // two keys in three are stored, with value i
+            {
+                want[i] = static_cast<std::uint32_t>(i) + 1u;
+            }
+        }
+        // the out-of-band keys are stored once each, with the value of their first stored occurrence
+        std::unordered_map<std::uint64_t, std::uint32_t> first;
+        for (int i = 0; i < n; ++i)
+        {
+            if (want[i] != 0u && first.emplace(k[i], static_cast<std::uint32_t>(i)).second)
+            {
+                stored.emplace_back(k[i], static_cast<std::uint32_t>(i));
+            }
+        }
+        for (int i = 0; i < n; ++i)
+        {
+            auto f = first.find(k[i]);
+            want[i] = f != first.end() ? f->second + 1u : 0u;
+        }
+        auto* dv = to_device(stored);
+        m.insert(dv, dv + stored.size());
+        auto* dk = to_device(k);
+        auto* dw = to_device(want);
+        int* dbad = nullptr;
+        cudaMalloc(&dbad, sizeof(int));
+        bool ok = true;
+        for (int mode = 0; mode < 2; ++mode)
+        {
+            cudaMemset(dbad, 0, sizeof(int));
+            k_find_shapes<<<(n + 127) / 128, 128>>>(m, dk, dw, n, mode, dbad);
+            ok = ok && to_host(dbad, 1)[0] == 0;
+        }
+        check(ok && m.size() == static_cast<stdgpu::index_t>(stored.size()),
+              "device find: full warps, half warps, out-of-band and absent keys");
+        cudaFree(dv);
+        cudaFree(dk);
+        cudaFree(dw);
+        cudaFree(dbad);
         map_t::destroyDeviceObject(m);
     }
 
