@@ -648,11 +648,12 @@ load_homes(const dview& t, const tile_lanes& L, uint64_t hash, bool probe, uint3
 // by the key's own lane with one compare-and-swap -- 32 claims in flight per warp.
 // The step over keys already in registers (key / val of lane element i, meaningful when valid; hashes as
 // in the loading steps below).
-template <int KIND>
+// GIVEN: the caller passes the key's hash in given_hash (a staged element that carries it).
+template <int KIND, bool GIVEN = false>
 SG_D void
 insert_kv_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K key,
                typename kind_consts<KIND>::V val, int64_t i, bool valid, uint8_t* out_flags, step_counts& c,
-               const uint64_t* hashes = nullptr)
+               const uint64_t* hashes = nullptr, uint64_t given_hash = 0)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
@@ -669,7 +670,8 @@ insert_kv_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::
     const bool probe = valid && !special;
     uint32_t hr[kTile];
     uint32_t pre[kTile][8];
-    const uint64_t hash = hashes != nullptr && probe ? __ldcs(hashes + i) : static_cast<uint64_t>(key);
+    const uint64_t hash = GIVEN ? given_hash
+                                : (hashes != nullptr && probe ? __ldcs(hashes + i) : static_cast<uint64_t>(key));
     load_homes<KIND>(t, L, hash, probe, hr, pre);
     int my_state = 0; // 0 present, 1 claim my_target, 2 decided beyond the home group
     uint32_t my_target = 0;
@@ -857,10 +859,10 @@ locate_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K k
 }
 
 // Erase step: every lane locates its key, then swaps its slot to the erased marker.
-template <int KIND>
+template <int KIND, bool GIVEN = false>
 SG_D void
 erase_key_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::K key, int64_t i, bool valid,
-               uint8_t* out_flags, step_counts& c, const uint64_t* hashes = nullptr)
+               uint8_t* out_flags, step_counts& c, const uint64_t* hashes = nullptr, uint64_t given_hash = 0)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
@@ -878,7 +880,8 @@ erase_key_step(const dview& t, const tile_lanes& L, typename kind_consts<KIND>::
     }
     const bool probe = valid && !special;
     V dummy{};
-    const uint64_t hash = hashes != nullptr && probe ? __ldcs(hashes + i) : static_cast<uint64_t>(key);
+    const uint64_t hash = GIVEN ? given_hash
+                                : (hashes != nullptr && probe ? __ldcs(hashes + i) : static_cast<uint64_t>(key));
     const int32_t my_slot = locate_step<KIND, false>(t, L, key, hash, probe, dummy);
     if (my_slot >= 0)
     {

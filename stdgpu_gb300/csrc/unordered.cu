@@ -171,6 +171,15 @@ struct slot_image
                                                                      unsigned int>::type>::type;
 };
 
+// A partitioned element of a table whose buckets come from caller-supplied hashes: the element's bytes and
+// its key's hash, so the ordered kernels need not read the hash array at random positions.
+template <typename E>
+struct with_hash
+{
+    E e;
+    uint64_t h;
+};
+
 // value_type bytes of (key, mapped); padding bytes are zero.
 template <int KIND>
 SG_D typename slot_image<KIND>::type
@@ -229,14 +238,16 @@ struct part_layout
 // has no room for), sorts the elements by partition in shared memory and writes each partition's run with
 // consecutive threads, so stores reach L2 as whole lines rather than one request per element (random small
 // writes cost as many requests as random line reads).
-template <int KIND, bool AOS, int PER>
+template <int KIND, bool AOS, int PER, bool HASHED = false>
 __global__ void __launch_bounds__(kThreads, 6)
-k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, part_layout pl, void* out)
+k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, part_layout pl, void* out,
+               const uint64_t* hashes = nullptr)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
     using V = typename C::V;
-    using E = typename slot_image<KIND>::type;
+    using E = typename std::conditional<HASHED, with_hash<typename slot_image<KIND>::type>,
+                                        typename slot_image<KIND>::type>::type;
     constexpr int kTileElems = PER * kThreads;
     __shared__ E stage[kTileElems];
     __shared__ uint8_t spid[kTileElems];
@@ -268,8 +279,17 @@ k_part_scatter(const void* in0, const void* in1, int64_t n, int bits, part_layou
                 K key;
                 V val;
                 load_input<KIND, AOS>(in0, in1, i, key, val);
-                elem[j] = pack_element<KIND>(key, val);
-                pid[j] = part_of<KIND>(key, bits, pl.shift);
+                if constexpr (HASHED)
+                {
+                    const uint64_t h = __ldcs(hashes + i);
+                    elem[j] = E{ pack_element<KIND>(key, val), h };
+                    pid[j] = static_cast<uint32_t>(fibonacci_bucket(h, bits)) >> pl.shift;
+                }
+                else
+                {
+                    elem[j] = pack_element<KIND>(key, val);
+                    pid[j] = part_of<KIND>(key, bits, pl.shift);
+                }
                 rank[j] = atomicAdd(&cnt[pid[j]], 1u);
             }
         }
@@ -578,6 +598,10 @@ struct staged_elem
     using type = typename std::conditional<ERASE, typename kind_consts<KIND>::K, typename slot_image<KIND>::type>::type;
 };
 
+// The set kind holding the key type of KIND (erase partitions bare keys).
+template <int KIND>
+constexpr int keys_kind = sizeof(typename kind_consts<KIND>::K) == 8 ? SG_SET_U64 : SG_SET_U32;
+
 // key / mapped value of a value_type image (padding ignored)
 template <int KIND>
 SG_D void
@@ -608,14 +632,17 @@ unpack_element(const typename slot_image<KIND>::type& e, typename kind_consts<KI
 #ifndef SG_ERASE_MIN_BLOCKS
 #define SG_ERASE_MIN_BLOCKS 5
 #endif
-template <int KIND, bool ERASE, int CHUNK>
+template <int KIND, bool ERASE, int CHUNK, bool HASHED = false>
 __global__ void __launch_bounds__(kThreads, ERASE ? SG_ERASE_MIN_BLOCKS : SG_ORDERED_MIN_BLOCKS)
 k_ordered_staged(dview t, const void* in, part_layout pl, unsigned long long* next_chunk)
 {
     using C = kind_consts<KIND>;
     using K = typename C::K;
     using V = typename C::V;
-    using E = typename staged_elem<KIND, ERASE>::type;
+    // with caller-supplied hashes the staged elements carry them (with_hash, written by k_part_scatter)
+    using E = typename std::conditional<
+            HASHED, with_hash<typename slot_image<ERASE ? keys_kind<KIND> : KIND>::type>,
+            typename staged_elem<KIND, ERASE>::type>::type;
     static_assert(2 * CHUNK * sizeof(E) <= 40 * 1024, "staging buffers exceed the static shared memory budget");
     __shared__ __align__(128) E buf[2][CHUNK];
     __shared__ __align__(8) uint64_t full[2];
@@ -708,9 +735,26 @@ k_ordered_staged(dview t, const void* in, part_layout pl, unsigned long long* ne
             const bool valid = i < last;
             K key = C::empty_key;
             V val{};
+            uint64_t h = 0;
             if (valid)
             {
-                if constexpr (ERASE)
+                if constexpr (HASHED)
+                {
+                    const E& x = buf[b][i - first];
+                    h = x.h;
+                    if constexpr (ERASE)
+                    {
+                        typename kind_consts<keys_kind<KIND>>::K k2;
+                        typename kind_consts<keys_kind<KIND>>::V v2;
+                        unpack_element<keys_kind<KIND>>(x.e, k2, v2);
+                        key = static_cast<K>(k2);
+                    }
+                    else
+                    {
+                        unpack_element<KIND>(x.e, key, val);
+                    }
+                }
+                else if constexpr (ERASE)
                 {
                     key = buf[b][i - first];
                 }
@@ -719,7 +763,18 @@ k_ordered_staged(dview t, const void* in, part_layout pl, unsigned long long* ne
                     unpack_element<KIND>(buf[b][i - first], key, val);
                 }
             }
-            if constexpr (ERASE)
+            if constexpr (HASHED)
+            {
+                if constexpr (ERASE)
+                {
+                    erase_key_step<KIND, true>(t, L, key, i, valid, nullptr, c, nullptr, h);
+                }
+                else
+                {
+                    insert_kv_step<KIND, true>(t, L, key, val, i, valid, nullptr, c, nullptr, h);
+                }
+            }
+            else if constexpr (ERASE)
             {
 #if SG_ERASE_DEFER
                 erase_key_step_deferred<KIND>(t, L, key, valid, c, pend);
@@ -1638,11 +1693,13 @@ ensure_part_scratch(sg_unordered* t, int64_t bytes)
 // gives bare keys), in one pass: each partition gets room for its mean share plus 1/16 and two chunks, the
 // overflow region n/16 plus one scatter tile.  Returns the layout and the ordered kernel's chunk counter,
 // both zeroed.
-template <int PKIND, bool AOS, int CHUNK>
+template <int PKIND, bool AOS, int CHUNK, bool HASHED = false>
 sg_status
 partition_into_scratch(sg_unordered* t, const void* in0, const void* in1, int64_t n, cudaStream_t s, part_layout* pl,
-                       unsigned long long** next_chunk)
+                       unsigned long long** next_chunk, const uint64_t* hashes = nullptr)
 {
+    using E = typename std::conditional<HASHED, with_hash<typename slot_image<PKIND>::type>,
+                                        typename slot_image<PKIND>::type>::type;
     const int parts = partitions_for(t);
     int shift = t->bits;
     for (int p = parts; p > 1; p >>= 1)
@@ -1654,7 +1711,7 @@ partition_into_scratch(sg_unordered* t, const void* in0, const void* in1, int64_
     const int64_t cap = round_up(mean + mean / 16 + 2 * CHUNK, CHUNK);
     constexpr int PER = part_per<PKIND>;
     const int64_t ocap = round_up(n / 16 + PER * kThreads, CHUNK);
-    const int64_t ebytes = round_up((parts * cap + ocap) * kind_consts<PKIND>::slot_bytes, 256);
+    const int64_t ebytes = round_up((parts * cap + ocap) * static_cast<int64_t>(sizeof(E)), 256);
     constexpr int64_t kControlBytes = 2048; // fill[kPartMax], ofill, lost, then the 8-byte chunk counter
     sg_status st = ensure_part_scratch(t, ebytes + kControlBytes);
     if (st != SG_OK)
@@ -1666,16 +1723,12 @@ partition_into_scratch(sg_unordered* t, const void* in0, const void* in1, int64_
     *pl = part_layout{ parts,   shift,          static_cast<unsigned int>(cap), static_cast<unsigned int>(ocap),
                        control, control + kPartMax, control + kPartMax + 1 };
     *next_chunk = reinterpret_cast<unsigned long long*>(control + kPartMax + 2);
-    static const int g_scatter = persistent_grid(k_part_scatter<PKIND, AOS, PER>, kThreads);
-    k_part_scatter<PKIND, AOS, PER><<<grid_for(n, kThreads * PER, g_scatter), kThreads, 0, s>>>(
-            in0, in1, n, t->bits, *pl, t->part_scratch);
+    static const int g_scatter = persistent_grid(k_part_scatter<PKIND, AOS, PER, HASHED>, kThreads);
+    k_part_scatter<PKIND, AOS, PER, HASHED><<<grid_for(n, kThreads * PER, g_scatter), kThreads, 0, s>>>(
+            in0, in1, n, t->bits, *pl, t->part_scratch, hashes);
     SG_LAUNCH_CHECK();
     return SG_OK;
 }
-
-// The set kind holding the key type of KIND (erase partitions bare keys).
-template <int KIND>
-constexpr int keys_kind = sizeof(typename kind_consts<KIND>::K) == 8 ? SG_SET_U64 : SG_SET_U32;
 
 bool
 use_partitioned_erase(const sg_unordered* t, int64_t n, const uint8_t* flags)
@@ -1733,10 +1786,20 @@ struct do_insert
         unsigned long long* next_chunk = nullptr;
         sg_status st = SG_ERR_OOM;
         constexpr int kChunk = SG_ORDERED_STAGE ? kStageChunk : kOrderedChunk;
-        if (hashes == nullptr && use_partitioned_insert(t, n, flags))
+        constexpr int kChunkH = 512; // elements that carry their hash (with_hash): 32 bytes for 16-byte pairs
+        if (use_partitioned_insert(t, n, flags) && (hashes == nullptr || SG_ORDERED_STAGE))
         {
-            st = aos ? partition_into_scratch<KIND, true, kChunk>(t, in0, in1, n, s, &pl, &next_chunk)
-                     : partition_into_scratch<KIND, false, kChunk>(t, in0, in1, n, s, &pl, &next_chunk);
+            if (hashes == nullptr)
+            {
+                st = aos ? partition_into_scratch<KIND, true, kChunk>(t, in0, in1, n, s, &pl, &next_chunk)
+                         : partition_into_scratch<KIND, false, kChunk>(t, in0, in1, n, s, &pl, &next_chunk);
+            }
+            else
+            {
+                st = aos ? partition_into_scratch<KIND, true, kChunkH, true>(t, in0, in1, n, s, &pl, &next_chunk, hashes)
+                         : partition_into_scratch<KIND, false, kChunkH, true>(t, in0, in1, n, s, &pl, &next_chunk,
+                                                                               hashes);
+            }
             if (st != SG_OK && st != SG_ERR_OOM)
             {
                 return st;
@@ -1745,7 +1808,18 @@ struct do_insert
         // the direct kernel: without room for the scratch array it does the whole insert; after a partitioned
         // insert it is gated on the scatter having left elements out
         const unsigned int* gate = nullptr;
-        if (st == SG_OK)
+        if (st == SG_OK && hashes != nullptr)
+        {
+            if constexpr (SG_ORDERED_STAGE)
+            {
+                static const int max_grid = persistent_grid(k_ordered_staged<KIND, false, kChunkH, true>, kThreads);
+                k_ordered_staged<KIND, false, kChunkH, true><<<grid_for(n, kChunkH, max_grid), kThreads, 0, s>>>(
+                        view_of(t), t->part_scratch, pl, next_chunk);
+            }
+            SG_LAUNCH_CHECK();
+            gate = pl.lost;
+        }
+        else if (st == SG_OK)
         {
             if constexpr (SG_ORDERED_STAGE)
             {
@@ -1797,16 +1871,31 @@ struct do_erase
         part_layout pl{};
         unsigned long long* next_chunk = nullptr;
         sg_status st = SG_ERR_OOM;
-        if (hashes == nullptr && use_partitioned_erase(t, n, flags))
+        if (use_partitioned_erase(t, n, flags) && (hashes == nullptr || SG_ORDERED_STAGE))
         {
-            st = partition_into_scratch<keys_kind<KIND>, false, kEraseChunk>(t, keys, nullptr, n, s, &pl, &next_chunk);
+            st = hashes == nullptr
+                         ? partition_into_scratch<keys_kind<KIND>, false, kEraseChunk>(t, keys, nullptr, n, s, &pl,
+                                                                                      &next_chunk)
+                         : partition_into_scratch<keys_kind<KIND>, false, kEraseChunk, true>(t, keys, nullptr, n, s,
+                                                                                            &pl, &next_chunk, hashes);
             if (st != SG_OK && st != SG_ERR_OOM)
             {
                 return st;
             }
         }
         const unsigned int* gate = nullptr;
-        if (st == SG_OK)
+        if (st == SG_OK && hashes != nullptr)
+        {
+            if constexpr (SG_ORDERED_STAGE)
+            {
+                static const int g_ordered = persistent_grid(k_ordered_staged<KIND, true, kEraseChunk, true>, kThreads);
+                k_ordered_staged<KIND, true, kEraseChunk, true><<<grid_for(n, kEraseChunk, g_ordered), kThreads, 0, s>>>(
+                        view_of(t), t->part_scratch, pl, next_chunk);
+            }
+            SG_LAUNCH_CHECK();
+            gate = pl.lost;
+        }
+        else if (st == SG_OK)
         {
             if constexpr (SG_ORDERED_STAGE)
             {

@@ -179,3 +179,49 @@ def test_mode_rejects_unknown_value():
     t = sg.unordered_set.createDeviceObject(1024, key="u32")
     assert sg.load().sg_unordered_set_insert_mode(t._h, 3) == N.SG_ERR_BAD_ARG
     sg.unordered_base.destroyDeviceObject(t)
+
+
+@pytest.mark.parametrize("kind,key,mapped", [(O.SET_U64, "u64", None), (O.MAP_U64_U32, "u64", "u32"),
+                                             (O.SET_U32, "u32", None), (O.MAP_U32_U64, "u32", "u64")])
+def test_partitioned_with_caller_hashes(kind, key, mapped):
+    """Tables whose buckets come from caller-supplied hashes (custom key types): the partitioned insert and
+    erase carry each key's hash in the staged element; contents, sizes and find answers equal the oracle's
+    on the same hashes, with duplicates, out-of-band keys and erased slots reused."""
+    rng = np.random.default_rng(300 + kind)
+    cap = 1 << 16
+    if mapped is None:
+        t = sg.unordered_set.createDeviceObject(cap, key=key, custom_hash=True)
+    else:
+        t = sg.unordered_map.createDeviceObject(cap, key=key, mapped=mapped, custom_hash=True)
+    t.set_excess_accounting(False)  # the tile and partitioned kernels
+    t.set_insert_mode("partitioned")
+    P = O.PortTable(kind, cap)
+    kd = O.KEY_DTYPE[kind]
+    mix = lambda k: (k.astype(np.uint64) * np.uint64(0xD6E8FEB86659FD93)) ^ np.uint64(0x5555)  # the caller's hash
+    for rnd in range(3):
+        k = keys_for(kind, rng, 40000)
+        v = vals_for(kind, k)
+        h = mix(k)
+        P.insert(k, v, hashes=h)
+        t.insert(dev(k), dev(v) if v is not None else None, hashes=dev(h))
+        assert t.size() == P.size() and t.valid()
+        e = np.concatenate([k[rng.random(len(k)) < 0.5], keys_for(kind, rng, 4000)])
+        he = mix(e)
+        P.erase(e, hashes=he)
+        t.erase(dev(e), hashes=dev(he))
+        assert t.size() == P.size() and t.valid()
+        gk, gv = contents(t, kind)
+        pk, pv = P.range()
+        order = np.argsort(pk, kind="stable")
+        assert np.array_equal(gk, pk[order])
+        if pv is not None:
+            assert np.array_equal(gv, pv[order])
+        q = np.concatenate([k, keys_for(kind, rng, 4000)])
+        hq = mix(q)
+        pvals, pfound = P.find(q, hashes=hq)
+        gvals, gfound = t.find(dev(q), hashes=dev(hq))
+        gfound = gfound.cpu().numpy()
+        assert np.array_equal(gfound, pfound)
+        if pvals is not None and gvals is not None:
+            assert np.array_equal(host(gvals, O.VAL_DTYPE[kind])[pfound == 1], pvals[pfound == 1])
+    sg.unordered_base.destroyDeviceObject(t)
