@@ -919,7 +919,9 @@ struct unordered_ref
             {
                 int64_t target = -1;
                 bool target_tomb = false;
-                if (scan_for_insert(key, home, target, target_tomb))
+                // the first read with the warp (all lanes arrive here together in a bulk kernel's step)
+                if (attempt == 0 ? scan_for_insert_warp(key, home, target, target_tomb)
+                                 : scan_for_insert(key, home, target, target_tomb))
                 {
                     return -1; // present
                 }
