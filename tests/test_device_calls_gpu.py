@@ -6,9 +6,16 @@ of keys outside the cube, device insert of new keys, bulk erase; sizes and valid
 
 import pytest
 
-pytestmark = pytest.mark.gpu
+
+def test_device_bench_program_compiles_for_sm103a():
+    """CPU part: the program builds against the library for sm_103a (no device needed)."""
+    import stdgpu_gb300
+    from stdgpu_gb300 import device_bench
+    stdgpu_gb300.load()
+    assert device_bench.build().exists()
 
 
+@pytest.mark.gpu
 @pytest.mark.parametrize("keys_log2", [12, 18])
 def test_device_calls_and_custom_keys(keys_log2):
     from stdgpu_gb300 import device_bench
